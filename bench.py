@@ -1,0 +1,318 @@
+"""Benchmark of the GB300 P3 step (prints ONE JSON line on rank 0).
+
+Workload (headline): P3 precision form, ncol=345,600 x nlev=128, dt=300 s,
+state carried across steps, FP32-bulk (process rates and table interpolation
+in FP32, FP64 state / residuals / fluxes).  The plain FP64 form is timed on
+the same workload and reported beside it.  A "step" is one p3_main call over
+all columns.  Inputs (15.9 GB per step) are larger than L2, so no flush is
+needed between steps.
+
+  value       column-levels/s of the FP32-bulk step, inputs resident in HBM
+  e2e         the same step through the public API with pinned HOST buffers:
+              every step copies the 23 input fields host->device and the
+              20 per-level outputs + 2 interface fluxes + 2 surface fields back
+  roofline    HBM roofline of the column kernel at 360 algorithmic bytes per
+              column-level (23 FP64 inputs read, 22 FP64 outputs written)
+  cpu_baseline  the CPU oracle (a C++/OpenMP restatement of the reference
+              p3_main) on a bounded sample, all host cores
+
+--impl reference times the CPU oracle alone (the reference itself cannot be
+built: its EKAT/Kokkos submodules are empty).  Multi-GPU (torchrun): each rank
+runs its own 345,600 columns (weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+NCOL, NLEV, DT = 345_600, 128, 300.0
+ALG_BYTES_PER_CL = 360.0
+SEED = 1002  # config 2 seed (1000 + config index)
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def _traffic_per_cl(kernel_tag):
+    """DRAM bytes per column-level of the column kernel from the committed ncu
+    summary (profiles/), or None."""
+    f = ROOT / "profiles" / "p3_column_kernel_traffic.txt"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith(kernel_tag + " dram_bytes_per_cl"):
+            return float(line.split()[-1])
+    return None
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = max(smax, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(seconds_target=15.0, nlev=NLEV):
+    """CPU oracle on a bounded sample of the same workload (all host cores)."""
+    import numpy as np
+    from scream_gb300 import _lib as L
+    from scream_gb300.p3 import generate_inputs
+    from oracle import p3_oracle as O
+    tab = L.host_tables()
+    cores = os.cpu_count() or 1
+    ncol = max(256, 64 * cores)
+    inp = generate_inputs(1, SEED, ncol, nlev)
+    st = {k: np.array(v, copy=True) for k, v in inp.items()}
+    st.update(O.empty_outputs(ncol, nlev))
+    O.p3_main(st, tab, DT, nthreads=cores)  # warm-up step
+    total_us, steps = 0.0, 0
+    t_end = time.time() + seconds_target
+    while time.time() < t_end or steps < 2:
+        err, us = O.p3_main(st, tab, DT, it=steps + 2, nthreads=cores)
+        total_us += us
+        steps += 1
+    value = ncol * nlev * steps / (total_us * 1e-6)
+    return {"value": value, "unit": "column-levels/s", "cores": cores, "kind": "port",
+            "sample": f"{ncol} columns x {nlev} levels (RH-stress workload, config-2 distributions), "
+                      f"{steps} steps, oracle p3_main with OpenMP over columns"}
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    cb = cpu_baseline(seconds_target=max(5.0, 2.0 * args.steps))
+    line = {"metric": "P3 column-levels/sec at nlev=128", "value": cb["value"], "unit": "column-levels/s",
+            "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded standard-atmosphere columns)",
+            "config": {"workload": f"P3 p3_main ncol={NCOL} nlev={NLEV} dt={DT} (sampled on CPU)"},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "column-levels/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+    import scream_gb300 as p3
+    from scream_gb300 import _lib as L
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    ncol = args.ncol or NCOL
+    ctx = p3.P3Context()
+    inputs = p3.generate_inputs(1, SEED + 7919 * rank, ncol, NLEV)
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed_device(precision, steps, warmup):
+        f = p3.P3Fields.from_inputs(inputs)
+        for s in range(warmup):
+            ctx.p3_main(f, DT, precision, it=s + 1, sync=False)
+        ctx.check()
+        barrier()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        t0 = time.perf_counter()
+        for s in range(steps):
+            ev[s][0].record(stream)
+            ctx.p3_main(f, DT, precision, it=warmup + s + 1, sync=False)
+            ev[s][1].record(stream)
+        barrier()
+        wall = time.perf_counter() - t0
+        ctx.check()
+        kms = [a.elapsed_time(b) for a, b in ev]
+        del f
+        torch.cuda.empty_cache()
+        return wall, kms
+
+    # FP64 plain form (reported beside the headline)
+    wall64, k64 = timed_device(L.P3X_FP64, args.steps, args.warmup)
+    # FP32-bulk headline, with clocks sampled during the timed region
+    with ClockSampler(local) as clk:
+        wall32, k32 = timed_device(L.P3X_FP32_BULK, args.steps, args.warmup)
+    clocks = clk.summary()
+
+    def maxr(x):
+        if ws > 1:
+            import torch.distributed as dist
+            t = torch.tensor([x], dtype=torch.float64, device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            return float(t.item())
+        return x
+
+    wall32 = maxr(wall32)
+    wall64 = maxr(wall64)
+    cl_step = ncol * NLEV
+    value = ws * cl_step * args.steps / wall32
+    value64 = ws * cl_step * args.steps / wall64
+
+    # e2e: pinned host buffers through the public API
+    h2d_fields = L.INPUT_FIELDS
+    d2h_fields = [n for n in L.ALL_FIELDS if n not in L.DIAG_IN_FIELDS]
+    f = p3.P3Fields.allocate(ncol, NLEV)
+    host_in = {n: torch.from_numpy(np.ascontiguousarray(inputs[n])).pin_memory() for n in h2d_fields}
+    host_out = {n: torch.empty(f.t[n].shape, dtype=torch.float64).pin_memory() for n in d2h_fields}
+    h2d_bytes = sum(v.numel() * 8 for v in host_in.values())
+    d2h_bytes = sum(v.numel() * 8 for v in host_out.values())
+
+    def e2e_step(it):
+        for n in h2d_fields:
+            f.t[n].copy_(host_in[n], non_blocking=True)
+        ctx.p3_main(f, DT, L.P3X_FP32_BULK, it=it, sync=False)
+        for n in d2h_fields:
+            host_out[n].copy_(f.t[n], non_blocking=True)
+
+    e2e_steps = max(2, min(args.steps, 5))
+    for s in range(min(args.warmup, 2)):
+        e2e_step(s + 1)
+    barrier()
+    t0 = time.perf_counter()
+    for s in range(e2e_steps):
+        e2e_step(s + 1)
+    barrier()
+    e2e_wall = maxr(time.perf_counter() - t0)
+    ctx.check()
+    e2e_value = ws * cl_step * e2e_steps / e2e_wall
+    del f, host_in, host_out
+    torch.cuda.empty_cache()
+
+    if rank != 0:
+        return 0
+    hbm_peak, peak_kind = _peaks()
+    kmean32 = sum(k32) / len(k32) * 1e-3
+    achieved = ALG_BYTES_PER_CL * cl_step / kmean32 / 1e9
+    tpc = _traffic_per_cl("fp32")
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved / hbm_peak, "peak_source": peak_kind,
+            "traffic": (tpc * cl_step if tpc is not None else None),
+            "kernel": "p3_main_kernel<float> (fused part1/part2/sedimentation/part3)",
+            "alg_bytes_per_cl": ALG_BYTES_PER_CL}
+    kmean64 = sum(k64) / len(k64) * 1e-3
+    cb = cpu_baseline(seconds_target=args.cpu_seconds) if not args.no_cpu else None
+    line = {
+        "metric": "P3 column-levels/sec at nlev=128 (FP32-bulk; FP64 beside it)",
+        "value": value, "unit": "column-levels/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": wall32 / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32-bulk (f64 state/residuals/fluxes)",
+        "data": "synthetic (seeded standard-atmosphere columns, RH~U(0.9,1.05) in even columns)",
+        "config": {"workload": f"P3 p3_main ncol={ncol} nlev={NLEV} dt={DT}s, state carried",
+                   "l2": "inputs 15.9 GB/step > L2 (no flush needed)", "columns_per_gpu": ncol},
+        "fp64": {"value": value64, "unit": "column-levels/s", "ms_per_step": wall64 / args.steps * 1e3,
+                 "kernel_ms": kmean64 * 1e3,
+                 "hbm_gbs_alg": ALG_BYTES_PER_CL * cl_step / kmean64 / 1e9,
+                 "fp32_bulk_speedup": value / value64},
+        "roofline": roof,
+        "e2e": {"value": e2e_value, "unit": "column-levels/s", "h2d_bytes_per_step": h2d_bytes,
+                "d2h_bytes_per_step": d2h_bytes, "steps": e2e_steps,
+                "path": "pinned host tensors -> P3Context.p3_main (libp3x C ABI) -> pinned host"},
+        "gpu_launches": args.steps,
+        "clocks": clocks,
+        "cpu_baseline": cb,
+    }
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--ncol", type=int, default=0)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

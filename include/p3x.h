@@ -1,0 +1,327 @@
+/*
+ * p3x -- GB300-native P3 microphysics step behind the EAMxx P3 call surface.
+ *
+ * C ABI (no C++ or torch types).  Every entry point returns P3X_OK (0) or a
+ * negative status.  Unless stated otherwise, field pointers are DEVICE
+ * pointers to FP64 arrays laid out (ncol, nlev) row-major: level k of
+ * column i is at ptr[i*ld + k], level 0 is the model top.  This is EAMxx's
+ * view_2d<Spack> with a pack size of 1, the layout the reference uses on GPU.
+ * Interface fields (precip_liq_flux, precip_ice_flux) hold nlev+1 values per
+ * column with their own leading dimension.
+ *
+ * Reference interfaces replaced (paths relative to components/eamxx/src/):
+ *   p3x_runtime ............ P3Runtime              physics/p3/p3_functions.hpp:112-157
+ *   p3x_prognostic_state ... P3PrognosticState      physics/p3/p3_functions.hpp:159-182
+ *   p3x_diagnostic_inputs .. P3DiagnosticInputs     physics/p3/p3_functions.hpp:184-213
+ *   p3x_diagnostic_outputs . P3DiagnosticOutputs    physics/p3/p3_functions.hpp:215-241
+ *   p3x_infrastructure ..... P3Infrastructure       physics/p3/p3_functions.hpp:243-263
+ *   p3x_history_only ....... P3HistoryOnly          physics/p3/p3_functions.hpp:265-275
+ *   p3x_context_create ..... p3_init + P3LookupTables
+ *                            physics/p3/p3_f90.cpp:103-113,
+ *                            physics/p3/impl/p3_table_ice_impl.hpp:16-78,
+ *                            physics/p3/impl/p3_table3_impl.hpp:85-148
+ *   p3x_main ............... Functions<Real,Device>::p3_main
+ *                            physics/p3/p3_functions.hpp:1355-1369,
+ *                            physics/p3/impl/p3_main_impl.hpp:333-372
+ *   p3x_main_f ............. p3_main_c (Fortran-callable, host arrays,
+ *                            (its:ite,kts:kte) column-fastest layout)
+ *                            physics/p3/p3_iso_c.f90:132-183,
+ *                            physics/p3/p3_main_wrap.cpp:11-24
+ */
+#ifndef P3X_H
+#define P3X_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* Status codes                                                        */
+/* ------------------------------------------------------------------ */
+#define P3X_OK 0
+#define P3X_EINVAL (-1)   /* bad argument (null pointer, nlev <= 0, dt <= 0, ...) */
+#define P3X_ENOMEM (-2)   /* device allocation failed or budget exceeded          */
+#define P3X_ENUMERIC (-3) /* T <= 0 or NaN met in a saturation evaluation          */
+#define P3X_ETIMEOUT (-4) /* sedimentation substep cap or a bounded wait ran out   */
+#define P3X_ECUDA (-5)    /* a CUDA runtime call failed                            */
+#define P3X_ETABLE (-6)   /* lookup table file missing / malformed / wrong version */
+
+/* p3_init info codes (physics/p3/p3_iso_c.f90:43-130 returns 0 or -1..-6). */
+
+/* Precision forms. */
+#define P3X_FP64 0      /* FP64 everywhere                                            */
+#define P3X_FP32_BULK 1 /* process rates + table interpolation in FP32; saturation    */
+                        /* residuals, state updates, sedimentation flux accumulation  */
+                        /* and column budgets in FP64                                 */
+
+/* P3Runtime, p3_functions.hpp:112-133 (same names, same defaults). */
+typedef struct p3x_runtime {
+  double max_total_ni;
+  double autoconversion_prefactor;
+  double autoconversion_qc_exponent;
+  double autoconversion_nc_exponent;
+  double autoconversion_radius;
+  double accretion_prefactor;
+  double accretion_qc_exponent;
+  double accretion_qr_exponent;
+  double rain_selfcollection_prefactor;
+  double rain_selfcollection_breakup_diameter;
+  double constant_mu_rain;
+  double spa_ccn_to_nc_factor;
+  double cldliq_to_ice_collection_factor;
+  double rain_to_ice_collection_factor;
+  double min_rime_rho;
+  double max_rime_rho;
+  double immersion_freezing_exponent;
+  double deposition_nucleation_exponent;
+  double ice_sedimentation_factor;
+  int32_t do_ice_production;
+  int32_t pad_;
+} p3x_runtime;
+
+/* P3PrognosticState, p3_functions.hpp:159-182 (in/out). */
+typedef struct p3x_prognostic_state {
+  double *qc, *nc, *qr, *nr, *qi, *qm, *ni, *bm, *qv, *th;
+} p3x_prognostic_state;
+
+/* P3DiagnosticInputs, p3_functions.hpp:184-213 (read only). */
+typedef struct p3x_diagnostic_inputs {
+  const double *nc_nuceat_tend, *nccn, *ni_activated, *inv_qc_relvar, *cld_frac_i,
+      *cld_frac_l, *cld_frac_r, *pres, *dz, *dpres, *inv_exner, *qv_prev, *t_prev;
+} p3x_diagnostic_inputs;
+
+/* P3DiagnosticOutputs, p3_functions.hpp:215-241.  precip_liq_surf and
+ * precip_ice_surf have one value per column; precip_liq_flux and
+ * precip_ice_flux have nlev+1 per column. */
+typedef struct p3x_diagnostic_outputs {
+  double *qv2qi_depos_tend, *precip_liq_surf, *precip_ice_surf, *diag_eff_radius_qc,
+      *diag_eff_radius_qi, *diag_eff_radius_qr, *rho_qi, *precip_liq_flux, *precip_ice_flux,
+      *precip_total_tend, *nevapr;
+} p3x_diagnostic_outputs;
+
+/* P3Infrastructure, p3_functions.hpp:243-263.  its/ite/kts/kte are kept for
+ * the Fortran-style entry; col_location may be NULL (debug output only). */
+typedef struct p3x_infrastructure {
+  double dt;
+  int32_t it, its, ite, kts, kte;
+  int32_t predictNc, prescribedCCN;
+  const double* col_location;
+} p3x_infrastructure;
+
+/* P3HistoryOnly, p3_functions.hpp:265-275.  The reference requires the
+ * caller to zero these before p3_main (eamxx_p3_run.cpp:27-29); p3x zeroes
+ * them itself, so callers may but need not. */
+typedef struct p3x_history_only {
+  double *liq_ice_exchange, *vap_liq_exchange, *vap_ice_exchange;
+} p3x_history_only;
+
+/* Leading dimensions in elements; 0 selects the dense value (nlev, nlev+1). */
+typedef struct p3x_layout {
+  int64_t ld;
+  int64_t ld_int;
+} p3x_layout;
+
+/* Launch configuration (chosen by p3x_autotune or set by hand). */
+typedef struct p3x_launch_config {
+  int32_t lanes_per_column;  /* 8, 16 or 32                                    */
+  int32_t columns_per_block; /* columns handled concurrently by one CTA        */
+  int32_t table_staging;     /* 0: tables read through L1/L2; 1: staged into   */
+                             /*    shared memory by bulk copies (cp.async.bulk) */
+  int32_t blocks_per_sm;     /* persistent grid = blocks_per_sm x SM count (0 = auto) */
+} p3x_launch_config;
+
+typedef struct p3x_context p3x_context;
+
+void p3x_runtime_defaults(p3x_runtime* rt);
+
+/* Creates the lookup tables (the official text file when table_file is not
+ * NULL, otherwise generated in-process) and uploads them to the current
+ * device.  *info receives 0 or the negative P3X_* code of the failure. */
+int p3x_context_create(const char* table_file, p3x_context** out, int* info);
+int p3x_context_destroy(p3x_context* ctx);
+
+/* Host copies of the P3LookupTables of a context (for checking / oracles).
+ * Sizes: ice 5*4*50*12, collect 5*4*50*30*2, vn/vm/revap 300*10, mu_r 150,
+ * dnu 16.  Any pointer may be NULL. */
+int p3x_context_get_tables(const p3x_context* ctx, double* ice, double* collect, double* vn,
+                           double* vm, double* revap, double* mu_r, double* dnu);
+
+/* Host-only: fills caller-provided HOST arrays with the generated
+ * P3LookupTables (same sizes as p3x_context_get_tables); when table_file is
+ * not NULL the ice / collection tables are read from it instead.  Touches no
+ * GPU. */
+int p3x_tables_generate(const char* table_file, double* ice, double* collect, double* vn, double* vm,
+                        double* revap, double* mu_r, double* dnu);
+
+/* Regularised upper incomplete gamma function Q(a, x) used by the ice-table
+ * generator (series for x < a+1, Legendre continued fraction otherwise). */
+double p3x_incomplete_gamma_q(double a, double x);
+
+/* Writes the generated ice / collection table in the official text format. */
+int p3x_write_ice_table(const char* path, const char* version);
+
+/* Functions<Real,Device>::p3_main: one P3 step over nj columns of nk levels,
+ * device pointers, synchronous on `stream` (a cudaStream_t, NULL = legacy
+ * default stream).  *elapsed_us (may be NULL) receives the step time in
+ * microseconds measured with CUDA events, like the reference's return value. */
+int p3x_main(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_state* prog,
+             const p3x_diagnostic_inputs* din, const p3x_diagnostic_outputs* dout,
+             const p3x_infrastructure* infra, const p3x_history_only* hist, int32_t nj, int32_t nk,
+             const p3x_layout* layout, int32_t precision, void* stream, double* elapsed_us);
+
+/* Same, stream-ordered and asynchronous: no host synchronisation, no
+ * allocation.  Device-side error bits accumulate in the context; read them
+ * with p3x_context_check. */
+int p3x_main_async(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_state* prog,
+                   const p3x_diagnostic_inputs* din, const p3x_diagnostic_outputs* dout,
+                   const p3x_infrastructure* infra, const p3x_history_only* hist, int32_t nj,
+                   int32_t nk, const p3x_layout* layout, int32_t precision, void* stream);
+
+/* Synchronises `stream`, returns and clears the accumulated device status. */
+int p3x_context_check(p3x_context* ctx, void* stream);
+
+/* Overrides the launch configuration used by p3x_main for a precision form. */
+int p3x_set_launch_config(p3x_context* ctx, int32_t precision, const p3x_launch_config* cfg);
+int p3x_get_launch_config(const p3x_context* ctx, int32_t precision, p3x_launch_config* cfg);
+
+/* p3_main_c (physics/p3/p3_iso_c.f90:132-183), same argument order and
+ * meaning: HOST arrays in the Fortran (its:ite, kts:kte) layout (column index
+ * fastest), precip fluxes (its:ite, kts:kte+1).  Uses the default context
+ * created by p3x_init.  Runs FP64 on the current device.  elapsed_s receives
+ * the step time in seconds. */
+int p3x_init(const char* table_file, int* info);
+int p3x_finalize(void);
+int p3x_main_f(double* qc, double* nc, double* qr, double* nr, double* th_atm, double* qv,
+               double dt, double* qi, double* qm, double* ni, double* bm, double* pres,
+               double* dz, double* nc_nuceat_tend, double* nccn_prescribed, double* ni_activated,
+               double* inv_qc_relvar, int32_t it, double* precip_liq_surf,
+               double* precip_ice_surf, int32_t its, int32_t ite, int32_t kts, int32_t kte,
+               double* diag_eff_radius_qc, double* diag_eff_radius_qi,
+               double* diag_eff_radius_qr, double* rho_qi, int32_t do_predict_nc,
+               int32_t do_prescribed_CCN, double* dpres, double* inv_exner,
+               double* qv2qi_depos_tend, double* precip_liq_flux, double* precip_ice_flux,
+               double* cld_frac_r, double* cld_frac_l, double* cld_frac_i,
+               double* liq_ice_exchange, double* vap_liq_exchange, double* vap_ice_exchange,
+               double* qv_prev, double* t_prev, double* elapsed_s);
+
+/* ------------------------------------------------------------------ */
+/* Batched form: many independent instances in one persistent launch   */
+/* ------------------------------------------------------------------ */
+typedef struct p3x_instance_desc {
+  p3x_prognostic_state prog;
+  p3x_diagnostic_inputs din;
+  p3x_diagnostic_outputs dout;
+  p3x_history_only hist;
+  p3x_layout layout;
+  int32_t ncol, nlev;
+  double dt;
+  int32_t it;
+  int32_t predictNc, prescribedCCN;
+  int32_t precision;
+} p3x_instance_desc;
+
+typedef struct p3x_batch p3x_batch;
+
+/* Builds the device work list (one item per column of every instance,
+ * heaviest first) for n instances.  Allocates once, here. */
+int p3x_batch_create(p3x_context* ctx, const p3x_runtime* rt, const p3x_instance_desc* descs,
+                     int32_t n, p3x_batch** out);
+/* One persistent launch over the work list on `stream` (no host sync). */
+int p3x_batch_run(p3x_batch* b, void* stream);
+/* Captures the batch launch into a CUDA graph; later p3x_batch_run calls
+ * replay the graph. */
+int p3x_batch_capture_graph(p3x_batch* b, void* stream);
+int p3x_batch_set_launch_config(p3x_batch* b, const p3x_launch_config* cfg);
+int p3x_batch_destroy(p3x_batch* b);
+
+/* Autotuner: times candidate launch configurations (lanes per column x
+ * columns per CTA x table staging x blocks per SM) on the given batch and
+ * stores the fastest in *best (and in the batch).  ms_best may be NULL. */
+int p3x_autotune_batch(p3x_batch* b, void* stream, int32_t reps, p3x_launch_config* best,
+                       double* ms_best);
+
+/* ------------------------------------------------------------------ */
+/* Synthetic workload (seeded standard-atmosphere columns)             */
+/* ------------------------------------------------------------------ */
+/* Field order of the 23 P3 inputs handled by the generator and the
+ * serving loop: the 10 prognostic fields then the 13 diagnostic inputs. */
+enum {
+  P3X_F_QC = 0, P3X_F_NC, P3X_F_QR, P3X_F_NR, P3X_F_QI, P3X_F_QM, P3X_F_NI, P3X_F_BM,
+  P3X_F_QV, P3X_F_TH, P3X_F_NC_NUCEAT_TEND, P3X_F_NCCN, P3X_F_NI_ACTIVATED,
+  P3X_F_INV_QC_RELVAR, P3X_F_CLD_FRAC_I, P3X_F_CLD_FRAC_L, P3X_F_CLD_FRAC_R, P3X_F_PRES,
+  P3X_F_DZ, P3X_F_DPRES, P3X_F_INV_EXNER, P3X_F_QV_PREV, P3X_F_T_PREV, P3X_NUM_INPUTS
+};
+
+/* Fills columns [col0, col0+ncol) of a workload (HOST arrays, (ncol, nlev)
+ * row-major with leading dimension ld).  kind 0: RH ~ U(0.3, 1.05);
+ * kind 1: RH ~ U(0.9, 1.05) in even-indexed columns (supersaturation
+ * stress); kind 2: the reference's "mixed" test case
+ * (physics/p3/p3_ic_cases.cpp:11-120).  Column i draws from its own stream
+ * seeded by (seed, i), so any column range is reproducible on its own. */
+int p3x_workload_generate(int32_t kind, uint64_t seed, int32_t col0, int32_t ncol, int32_t nlev,
+                          double* const* fields, int64_t ld);
+
+/* Column budgets in FP64 (share/property_checks/
+ * mass_and_energy_column_conservation_check.cpp:281-347): total water
+ * W = sum_k (qv+qc+qr+qi) dpres/g and energy-like
+ * E = sum_k (cp T + (Lv+Lf) qv + Lf (qc+qr)) dpres/g, per column, device
+ * arrays.  T is th/inv_exner.  Asynchronous on `stream`. */
+int p3x_column_budgets(const p3x_prognostic_state* prog, const double* dpres,
+                       const double* inv_exner, int32_t ncol, int32_t nlev, int64_t ld,
+                       double* water_out, double* energy_out, void* stream);
+
+/* ------------------------------------------------------------------ */
+/* Serving: continuous batching of P3 steps under a memory budget      */
+/* ------------------------------------------------------------------ */
+typedef struct p3x_server p3x_server;
+
+typedef struct p3x_serve_stats {
+  int64_t completed;
+  int64_t rejected;        /* larger than the whole budget               */
+  double p50_ms, p90_ms, p99_ms, max_ms, mean_ms;
+  double wall_s;
+  double column_levels_per_s;
+  double offered_rate_hz;
+  int64_t peak_bytes;
+  int32_t peak_inflight;
+} p3x_serve_stats;
+
+/* budget_bytes: device memory the server may hold for resident instances.
+ * max_inflight: concurrent steps (one CUDA stream each). */
+int p3x_server_create(p3x_context* ctx, const p3x_runtime* rt, int64_t budget_bytes,
+                      int32_t max_inflight, p3x_server** out);
+int p3x_server_destroy(p3x_server* s);
+
+/* Submits a request: instance `instance_id` (created on first use with a
+ * synthetic workload of ncol x nlev from `seed`, kept resident until its
+ * last step) advances by one step.  arrival_s is the request's arrival time
+ * on the server clock.  Non-blocking. */
+int p3x_server_submit(p3x_server* s, int64_t instance_id, int32_t ncol, int32_t nlev,
+                      int32_t precision, int32_t total_steps, uint64_t seed, double dt,
+                      double arrival_s);
+
+/* Runs an open-loop Poisson load: n requests drawn from a seeded generator
+ * (ncol log-uniform in [1, max_ncol], nlev from {72,128}, FP64 / FP32-bulk
+ * 50/50, 1..20 steps per instance), arriving at rate_hz. */
+int p3x_server_run_poisson(p3x_server* s, double rate_hz, int32_t n_requests,
+                           int32_t max_ncol, uint64_t seed, p3x_serve_stats* stats);
+
+/* Copies one prognostic field (P3X_F_QC..P3X_F_TH) or a surface precip
+ * field (-1: precip_liq_surf, -2: precip_ice_surf) of a resident instance to
+ * host memory (for result checks). */
+int p3x_server_read_field(p3x_server* s, int64_t instance_id, int32_t field, double* host_out,
+                          int64_t n);
+/* Waits until every submitted request has finished. */
+int p3x_server_drain(p3x_server* s, p3x_serve_stats* stats);
+
+/* Version string of the library build. */
+const char* p3x_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* P3X_H */

@@ -1,0 +1,794 @@
+/*
+ * C ABI of libp3x (declared in include/p3x.h): lookup-table contexts, the
+ * p3_main drop-in (device pointers), the p3_main_c drop-in (host arrays in the
+ * Fortran layout), the batched persistent form with CUDA-graph capture and
+ * its autotuner, synthetic workloads and column budgets.
+ */
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "p3x.h"
+#include "p3x_internal.hpp"
+#include "p3x_launch.hpp"
+
+struct p3x_context {
+  int device = 0;
+  int num_sms = 0;
+  p3x::HostTables host;
+  /* device tables, FP64 and FP32 copies */
+  double *d_ice = nullptr, *d_coll = nullptr, *d_vn = nullptr, *d_vm = nullptr, *d_revap = nullptr;
+  float *f_ice = nullptr, *f_coll = nullptr, *f_vn = nullptr, *f_vm = nullptr, *f_revap = nullptr;
+  /* Table3 two-column slices for every possible mu index (1..9):
+   * [9][3][300][2] */
+  double* d_t3slices = nullptr;
+  float* f_t3slices = nullptr;
+  uint32_t* d_err = nullptr;
+  p3x_launch_config cfg[2];
+  /* scratch of the Fortran-layout entry (grown on demand) */
+  std::vector<double*> fbuf;
+  int64_t fbuf_elems = 0;
+  double* fstage = nullptr;
+  int64_t fstage_elems = 0;
+};
+
+namespace p3x {
+namespace {
+
+int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return P3X_OK;
+  if (e == cudaErrorMemoryAllocation) return P3X_ENOMEM;
+  return P3X_ECUDA;
+}
+#define P3X_CUDA(x)                         \
+  do {                                      \
+    const cudaError_t e_ = (x);             \
+    if (e_ != cudaSuccess) return cuda_status(e_); \
+  } while (0)
+
+int status_from_bits(uint32_t bits) {
+  if (bits & dev::kErrNumeric) return P3X_ENUMERIC;
+  if (bits & (dev::kErrSubstep | dev::kErrWait)) return P3X_ETIMEOUT;
+  return P3X_OK;
+}
+
+std::mutex g_tables_mu;
+std::unique_ptr<HostTables> g_generated;
+
+/* Generated tables are built once per process (the ice-table generation
+ * integrates ~1e9 PSD bins). */
+const HostTables& generated_tables() {
+  std::lock_guard<std::mutex> lk(g_tables_mu);
+  if (!g_generated) {
+    auto t = std::make_unique<HostTables>();
+    build_rain_tables(*t, 1.0);
+    build_ice_tables(*t);
+    g_generated = std::move(t);
+  }
+  return *g_generated;
+}
+
+template <class T>
+int upload(T** dst, const std::vector<double>& src) {
+  std::vector<T> tmp(src.begin(), src.end());
+  P3X_CUDA(cudaMalloc(reinterpret_cast<void**>(dst), sizeof(T) * tmp.size()));
+  P3X_CUDA(cudaMemcpy(*dst, tmp.data(), sizeof(T) * tmp.size(), cudaMemcpyHostToDevice));
+  return P3X_OK;
+}
+
+dev::RuntimeDev make_runtime(const p3x_runtime& r) {
+  dev::RuntimeDev d;
+  d.max_total_ni = r.max_total_ni;
+  d.autoconversion_prefactor = r.autoconversion_prefactor;
+  d.autoconversion_qc_exponent = r.autoconversion_qc_exponent;
+  d.autoconversion_nc_exponent = r.autoconversion_nc_exponent;
+  d.autoconversion_radius = r.autoconversion_radius;
+  d.accretion_prefactor = r.accretion_prefactor;
+  d.accretion_qc_exponent = r.accretion_qc_exponent;
+  d.accretion_qr_exponent = r.accretion_qr_exponent;
+  d.rain_selfcollection_prefactor = r.rain_selfcollection_prefactor;
+  d.rain_selfcollection_breakup_diameter = r.rain_selfcollection_breakup_diameter;
+  d.constant_mu_rain = r.constant_mu_rain;
+  d.spa_ccn_to_nc_factor = r.spa_ccn_to_nc_factor;
+  d.cldliq_to_ice_collection_factor = r.cldliq_to_ice_collection_factor;
+  d.rain_to_ice_collection_factor = r.rain_to_ice_collection_factor;
+  d.min_rime_rho = r.min_rime_rho;
+  d.max_rime_rho = r.max_rime_rho;
+  d.immersion_freezing_exponent = r.immersion_freezing_exponent;
+  d.deposition_nucleation_exponent = r.deposition_nucleation_exponent;
+  d.ice_sedimentation_factor = r.ice_sedimentation_factor;
+  d.do_ice_production = r.do_ice_production;
+  /* p3/impl/p3_autoconversion_impl.hpp:27-32 */
+  if (r.autoconversion_radius == 25.0e-6) {
+    d.cons3 = dev::C::CONS3;
+  } else {
+    d.cons3 = 1.0 / (dev::C::CONS2 * std::pow(r.autoconversion_radius, 3.0));
+  }
+  /* p3/impl/p3_table3_impl.hpp:52-62 with the constant mu_r */
+  double rdumjj = r.constant_mu_rain + 1;
+  rdumjj = std::max(rdumjj, 1.);
+  rdumjj = std::min(rdumjj, 10.);
+  int dumjj = static_cast<int>(rdumjj);
+  dumjj = std::max(dumjj, 1);
+  dumjj = std::min(dumjj, 9);
+  d.t3_rdumjj = rdumjj;
+  d.t3_dumjj = dumjj;
+  return d;
+}
+
+bool valid_runtime(const p3x_runtime& r) {
+  return std::isfinite(r.constant_mu_rain) && r.max_rime_rho > 0 && r.min_rime_rho > 0 &&
+         std::isfinite(r.max_total_ni) && r.autoconversion_radius > 0;
+}
+
+LaunchSpec spec_of(const p3x_launch_config& c) {
+  LaunchSpec s;
+  s.lanes = c.lanes_per_column;
+  s.groups_per_block = c.columns_per_block;
+  s.staged = c.table_staging;
+  s.blocks_per_sm = c.blocks_per_sm;
+  return s;
+}
+
+int sm_stride_for(int nlev_max) {
+  int s = nlev_max + 1;
+  return (s + 1) & ~1;
+}
+
+bool spec_fits(int precision, const LaunchSpec& ls, int stride) {
+  if (ls.lanes != 8 && ls.lanes != 16 && ls.lanes != 32) return false;
+  if (ls.groups_per_block <= 0 || ls.groups_per_block * ls.lanes > 256) return false;
+  const size_t smem = precision == P3X_FP32_BULK ? p3_smem_bytes<float>(ls, stride) : p3_smem_bytes<double>(ls, stride);
+  return smem <= size_t(227 * 1024);
+}
+
+/* Falls back to tables in global memory and then to fewer columns per CTA
+ * when a configuration does not fit in shared memory (very deep columns). */
+LaunchSpec fit_spec(int precision, LaunchSpec ls, int stride) {
+  if (spec_fits(precision, ls, stride)) return ls;
+  ls.staged = 0;
+  while (ls.groups_per_block > 1 && !spec_fits(precision, ls, stride)) ls.groups_per_block /= 2;
+  return ls;
+}
+
+template <class TR>
+dev::KParams<TR> make_kparams(p3x_context* ctx, const dev::RuntimeDev& rtd);
+
+template <>
+dev::KParams<double> make_kparams<double>(p3x_context* ctx, const dev::RuntimeDev& rtd) {
+  dev::KParams<double> kp{};
+  kp.rt = rtd;
+  kp.ice = ctx->d_ice;
+  kp.collect = ctx->d_coll;
+  kp.vn = ctx->d_vn;
+  kp.vm = ctx->d_vm;
+  kp.revap = ctx->d_revap;
+  kp.t3slice = ctx->d_t3slices + size_t(rtd.t3_dumjj - 1) * dev::kT3SliceElems;
+  kp.err = ctx->d_err;
+  return kp;
+}
+template <>
+dev::KParams<float> make_kparams<float>(p3x_context* ctx, const dev::RuntimeDev& rtd) {
+  dev::KParams<float> kp{};
+  kp.rt = rtd;
+  kp.ice = ctx->f_ice;
+  kp.collect = ctx->f_coll;
+  kp.vn = ctx->f_vn;
+  kp.vm = ctx->f_vm;
+  kp.revap = ctx->f_revap;
+  kp.t3slice = ctx->f_t3slices + size_t(rtd.t3_dumjj - 1) * dev::kT3SliceElems;
+  kp.err = ctx->d_err;
+  return kp;
+}
+
+int fill_inst(const p3x_prognostic_state* prog, const p3x_diagnostic_inputs* din,
+              const p3x_diagnostic_outputs* dout, const p3x_history_only* hist, const p3x_layout* layout,
+              int32_t nj, int32_t nk, double dt, int predictNc, int prescribedCCN, int precision,
+              dev::Inst& in) {
+  if (!prog || !din || !dout || !hist) return P3X_EINVAL;
+  if (nj < 0 || nk <= 0 || !(dt > 0)) return P3X_EINVAL;
+  if (precision != P3X_FP64 && precision != P3X_FP32_BULK) return P3X_EINVAL;
+  in.qc = prog->qc; in.nc = prog->nc; in.qr = prog->qr; in.nr = prog->nr; in.qi = prog->qi;
+  in.qm = prog->qm; in.ni = prog->ni; in.bm = prog->bm; in.qv = prog->qv; in.th = prog->th;
+  in.nc_nuceat_tend = din->nc_nuceat_tend; in.nccn = din->nccn; in.ni_activated = din->ni_activated;
+  in.inv_qc_relvar = din->inv_qc_relvar; in.cld_frac_i = din->cld_frac_i; in.cld_frac_l = din->cld_frac_l;
+  in.cld_frac_r = din->cld_frac_r; in.pres = din->pres; in.dz = din->dz; in.dpres = din->dpres;
+  in.inv_exner = din->inv_exner; in.qv_prev = din->qv_prev; in.t_prev = din->t_prev;
+  in.qv2qi_depos_tend = dout->qv2qi_depos_tend; in.precip_liq_surf = dout->precip_liq_surf;
+  in.precip_ice_surf = dout->precip_ice_surf; in.diag_eff_radius_qc = dout->diag_eff_radius_qc;
+  in.diag_eff_radius_qi = dout->diag_eff_radius_qi; in.diag_eff_radius_qr = dout->diag_eff_radius_qr;
+  in.rho_qi = dout->rho_qi; in.precip_liq_flux = dout->precip_liq_flux; in.precip_ice_flux = dout->precip_ice_flux;
+  in.precip_total_tend = dout->precip_total_tend; in.nevapr = dout->nevapr;
+  in.liq_ice_exchange = hist->liq_ice_exchange; in.vap_liq_exchange = hist->vap_liq_exchange;
+  in.vap_ice_exchange = hist->vap_ice_exchange;
+  const void* ptrs[] = {in.qc, in.nc, in.qr, in.nr, in.qi, in.qm, in.ni, in.bm, in.qv, in.th,
+                        in.nc_nuceat_tend, in.nccn, in.ni_activated, in.inv_qc_relvar, in.cld_frac_i,
+                        in.cld_frac_l, in.cld_frac_r, in.pres, in.dz, in.dpres, in.inv_exner, in.qv_prev,
+                        in.t_prev, in.qv2qi_depos_tend, in.precip_liq_surf, in.precip_ice_surf,
+                        in.diag_eff_radius_qc, in.diag_eff_radius_qi, in.diag_eff_radius_qr, in.rho_qi,
+                        in.precip_liq_flux, in.precip_ice_flux, in.precip_total_tend, in.nevapr,
+                        in.liq_ice_exchange, in.vap_liq_exchange, in.vap_ice_exchange};
+  if (nj > 0)
+    for (const void* p : ptrs)
+      if (!p) return P3X_EINVAL;
+  in.ld = (layout && layout->ld > 0) ? layout->ld : nk;
+  in.ld_int = (layout && layout->ld_int > 0) ? layout->ld_int : nk + 1;
+  if (in.ld < nk || in.ld_int < nk + 1) return P3X_EINVAL;
+  in.ncol = nj;
+  in.nlev = nk;
+  in.dt = dt;
+  in.predictNc = predictNc ? 1 : 0;
+  in.prescribedCCN = prescribedCCN ? 1 : 0;
+  in.precision = precision;
+  in.pad_ = 0;
+  return P3X_OK;
+}
+
+int launch_single(p3x_context* ctx, const p3x_runtime* rt, const dev::Inst& in, cudaStream_t st) {
+  if (in.ncol == 0) return P3X_OK;
+  const dev::RuntimeDev rtd = make_runtime(*rt);
+  const int stride = sm_stride_for(in.nlev);
+  const LaunchSpec ls = fit_spec(in.precision, spec_of(ctx->cfg[in.precision]), stride);
+  if (!spec_fits(in.precision, ls, stride)) return P3X_EINVAL;
+  cudaError_t e;
+  if (in.precision == P3X_FP32_BULK) {
+    dev::KParams<float> kp = make_kparams<float>(ctx, rtd);
+    kp.sm_stride = stride;
+    kp.nwork = in.ncol;
+    kp.work = nullptr;
+    kp.insts = nullptr;
+    e = launch_p3<float>(in, kp, ls, ctx->num_sms, st);
+  } else {
+    dev::KParams<double> kp = make_kparams<double>(ctx, rtd);
+    kp.sm_stride = stride;
+    kp.nwork = in.ncol;
+    kp.work = nullptr;
+    kp.insts = nullptr;
+    e = launch_p3<double>(in, kp, ls, ctx->num_sms, st);
+  }
+  return cuda_status(e);
+}
+
+int read_and_clear_err(p3x_context* ctx, cudaStream_t st) {
+  uint32_t bits = 0;
+  P3X_CUDA(cudaMemcpyAsync(&bits, ctx->d_err, sizeof(bits), cudaMemcpyDeviceToHost, st));
+  P3X_CUDA(cudaStreamSynchronize(st));
+  if (bits) P3X_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(uint32_t), st));
+  P3X_CUDA(cudaStreamSynchronize(st));
+  return status_from_bits(bits);
+}
+
+p3x_context* g_default_ctx = nullptr;
+
+}  // namespace
+}  // namespace p3x
+
+using namespace p3x;
+
+extern "C" {
+
+const char* p3x_version(void) { return "p3x 0.1 (sm_103a)"; }
+
+void p3x_runtime_defaults(p3x_runtime* rt) {
+  if (!rt) return;
+  rt->max_total_ni = 740.0e3;
+  rt->autoconversion_prefactor = 1350.0;
+  rt->autoconversion_qc_exponent = 2.47;
+  rt->autoconversion_nc_exponent = 1.79;
+  rt->autoconversion_radius = 25.0e-6;
+  rt->accretion_prefactor = 67.0;
+  rt->accretion_qc_exponent = 1.15;
+  rt->accretion_qr_exponent = 1.15;
+  rt->rain_selfcollection_prefactor = 5.78;
+  rt->rain_selfcollection_breakup_diameter = 0.00028;
+  rt->constant_mu_rain = 1.0;
+  rt->spa_ccn_to_nc_factor = 1.0;
+  rt->cldliq_to_ice_collection_factor = 0.5;
+  rt->rain_to_ice_collection_factor = 1.0;
+  rt->min_rime_rho = 50.0;
+  rt->max_rime_rho = 900.0;
+  rt->immersion_freezing_exponent = 0.65;
+  rt->deposition_nucleation_exponent = 0.304;
+  rt->ice_sedimentation_factor = 1.0;
+  rt->do_ice_production = 1;
+  rt->pad_ = 0;
+}
+
+int p3x_tables_generate(const char* table_file, double* ice, double* collect, double* vn, double* vm,
+                        double* revap, double* mu_r, double* dnu) {
+  HostTables t;
+  if (table_file) {
+    if (read_ice_table_file(table_file, "4.1.1", t) != 0) return P3X_ETABLE;
+    build_rain_tables(t, 1.0);
+  } else {
+    t = generated_tables();
+  }
+  if (ice) std::copy(t.ice.begin(), t.ice.end(), ice);
+  if (collect) std::copy(t.collect.begin(), t.collect.end(), collect);
+  if (vn) std::copy(t.vn.begin(), t.vn.end(), vn);
+  if (vm) std::copy(t.vm.begin(), t.vm.end(), vm);
+  if (revap) std::copy(t.revap.begin(), t.revap.end(), revap);
+  if (mu_r) std::copy(t.mu_r.begin(), t.mu_r.end(), mu_r);
+  if (dnu) std::copy(t.dnu.begin(), t.dnu.end(), dnu);
+  return P3X_OK;
+}
+
+double p3x_incomplete_gamma_q(double a, double x) { return incomplete_gamma_q(a, x); }
+
+int p3x_write_ice_table(const char* path, const char* version) {
+  if (!path) return P3X_EINVAL;
+  return write_ice_table_file(path, version ? version : "4.1.1") == 0 ? P3X_OK : P3X_ETABLE;
+}
+
+int p3x_context_create(const char* table_file, p3x_context** out, int* info) {
+  if (info) *info = 0;
+  if (!out) return P3X_EINVAL;
+  *out = nullptr;
+  auto ctx = std::make_unique<p3x_context>();
+  if (table_file) {
+    HostTables t;
+    const int rc = read_ice_table_file(table_file, "4.1.1", t);
+    if (rc != 0) {
+      if (info) *info = P3X_ETABLE;
+      return P3X_ETABLE;
+    }
+    build_rain_tables(t, 1.0);
+    ctx->host = std::move(t);
+  } else {
+    ctx->host = generated_tables();
+  }
+  int st;
+  if (cudaGetDevice(&ctx->device) != cudaSuccess) {
+    if (info) *info = P3X_ECUDA;
+    return P3X_ECUDA;
+  }
+  cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  const HostTables& H = ctx->host;
+  if ((st = upload(&ctx->d_ice, H.ice)) || (st = upload(&ctx->d_coll, H.collect)) ||
+      (st = upload(&ctx->d_vn, H.vn)) || (st = upload(&ctx->d_vm, H.vm)) ||
+      (st = upload(&ctx->d_revap, H.revap)) || (st = upload(&ctx->f_ice, H.ice)) ||
+      (st = upload(&ctx->f_coll, H.collect)) || (st = upload(&ctx->f_vn, H.vn)) ||
+      (st = upload(&ctx->f_vm, H.vm)) || (st = upload(&ctx->f_revap, H.revap))) {
+    if (info) *info = st;
+    p3x_context_destroy(ctx.release());
+    return st;
+  }
+  /* Table3 slices for mu index j = 1..9: columns (j-1, j) of vn, vm, revap */
+  std::vector<double> sl(size_t(9) * dev::kT3SliceElems);
+  for (int j = 1; j <= 9; ++j) {
+    double* s = &sl[size_t(j - 1) * dev::kT3SliceElems];
+    const std::vector<double>* tabs[3] = {&H.vn, &H.vm, &H.revap};
+    for (int t = 0; t < 3; ++t)
+      for (int i = 0; i < kVT0; ++i)
+        for (int c = 0; c < 2; ++c) s[t * 600 + i * 2 + c] = (*tabs[t])[size_t(i) * kVT1 + (j - 1 + c)];
+  }
+  if ((st = upload(&ctx->d_t3slices, sl)) || (st = upload(&ctx->f_t3slices, sl))) {
+    if (info) *info = st;
+    p3x_context_destroy(ctx.release());
+    return st;
+  }
+  if (cudaMalloc(&ctx->d_err, sizeof(uint32_t)) != cudaSuccess ||
+      cudaMemset(ctx->d_err, 0, sizeof(uint32_t)) != cudaSuccess) {
+    if (info) *info = P3X_ENOMEM;
+    p3x_context_destroy(ctx.release());
+    return P3X_ENOMEM;
+  }
+  ctx->cfg[P3X_FP64] = p3x_launch_config{32, 8, 1, 0};
+  ctx->cfg[P3X_FP32_BULK] = p3x_launch_config{32, 8, 1, 0};
+  *out = ctx.release();
+  return P3X_OK;
+}
+
+int p3x_context_destroy(p3x_context* ctx) {
+  if (!ctx) return P3X_EINVAL;
+  void* ptrs[] = {ctx->d_ice, ctx->d_coll, ctx->d_vn, ctx->d_vm, ctx->d_revap, ctx->f_ice, ctx->f_coll,
+                  ctx->f_vn, ctx->f_vm, ctx->f_revap, ctx->d_t3slices, ctx->f_t3slices, ctx->d_err,
+                  ctx->fstage};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  for (double* p : ctx->fbuf)
+    if (p) cudaFree(p);
+  delete ctx;
+  return P3X_OK;
+}
+
+int p3x_context_get_tables(const p3x_context* ctx, double* ice, double* collect, double* vn, double* vm,
+                           double* revap, double* mu_r, double* dnu) {
+  if (!ctx) return P3X_EINVAL;
+  const HostTables& H = ctx->host;
+  if (ice) std::copy(H.ice.begin(), H.ice.end(), ice);
+  if (collect) std::copy(H.collect.begin(), H.collect.end(), collect);
+  if (vn) std::copy(H.vn.begin(), H.vn.end(), vn);
+  if (vm) std::copy(H.vm.begin(), H.vm.end(), vm);
+  if (revap) std::copy(H.revap.begin(), H.revap.end(), revap);
+  if (mu_r) std::copy(H.mu_r.begin(), H.mu_r.end(), mu_r);
+  if (dnu) std::copy(H.dnu.begin(), H.dnu.end(), dnu);
+  return P3X_OK;
+}
+
+int p3x_set_launch_config(p3x_context* ctx, int32_t precision, const p3x_launch_config* cfg) {
+  if (!ctx || !cfg || (precision != P3X_FP64 && precision != P3X_FP32_BULK)) return P3X_EINVAL;
+  const LaunchSpec ls = spec_of(*cfg);
+  if (!spec_fits(precision, ls, sm_stride_for(1))) return P3X_EINVAL;
+  ctx->cfg[precision] = *cfg;
+  return P3X_OK;
+}
+
+int p3x_get_launch_config(const p3x_context* ctx, int32_t precision, p3x_launch_config* cfg) {
+  if (!ctx || !cfg || (precision != P3X_FP64 && precision != P3X_FP32_BULK)) return P3X_EINVAL;
+  *cfg = ctx->cfg[precision];
+  return P3X_OK;
+}
+
+int p3x_main_async(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_state* prog,
+                   const p3x_diagnostic_inputs* din, const p3x_diagnostic_outputs* dout,
+                   const p3x_infrastructure* infra, const p3x_history_only* hist, int32_t nj, int32_t nk,
+                   const p3x_layout* layout, int32_t precision, void* stream) {
+  if (!ctx || !rt || !infra || !valid_runtime(*rt)) return P3X_EINVAL;
+  dev::Inst in;
+  const int st = fill_inst(prog, din, dout, hist, layout, nj, nk, infra->dt, infra->predictNc,
+                           infra->prescribedCCN, precision, in);
+  if (st) return st;
+  return launch_single(ctx, rt, in, static_cast<cudaStream_t>(stream));
+}
+
+int p3x_context_check(p3x_context* ctx, void* stream) {
+  if (!ctx) return P3X_EINVAL;
+  return read_and_clear_err(ctx, static_cast<cudaStream_t>(stream));
+}
+
+int p3x_main(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_state* prog,
+             const p3x_diagnostic_inputs* din, const p3x_diagnostic_outputs* dout,
+             const p3x_infrastructure* infra, const p3x_history_only* hist, int32_t nj, int32_t nk,
+             const p3x_layout* layout, int32_t precision, void* stream, double* elapsed_us) {
+  if (!ctx || !rt || !infra || !valid_runtime(*rt)) return P3X_EINVAL;
+  dev::Inst in;
+  int st = fill_inst(prog, din, dout, hist, layout, nj, nk, infra->dt, infra->predictNc, infra->prescribedCCN,
+                     precision, in);
+  if (st) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaEvent_t e0, e1;
+  P3X_CUDA(cudaEventCreate(&e0));
+  P3X_CUDA(cudaEventCreate(&e1));
+  cudaEventRecord(e0, s);
+  st = launch_single(ctx, rt, in, s);
+  cudaEventRecord(e1, s);
+  const cudaError_t se = cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  if (se != cudaSuccess) return cuda_status(se);
+  if (elapsed_us) *elapsed_us = double(ms) * 1000.0;
+  return read_and_clear_err(ctx, s);
+}
+
+/* ------------------------------------------------------------------ */
+/* Fortran-layout entry (p3_main_c)                                    */
+/* ------------------------------------------------------------------ */
+int p3x_init(const char* table_file, int* info) {
+  if (g_default_ctx) return P3X_OK;
+  return p3x_context_create(table_file, &g_default_ctx, info);
+}
+
+int p3x_finalize(void) {
+  if (!g_default_ctx) return P3X_OK;
+  const int st = p3x_context_destroy(g_default_ctx);
+  g_default_ctx = nullptr;
+  return st;
+}
+
+int p3x_main_f(double* qc, double* nc, double* qr, double* nr, double* th_atm, double* qv, double dt,
+               double* qi, double* qm, double* ni, double* bm, double* pres, double* dz,
+               double* nc_nuceat_tend, double* nccn_prescribed, double* ni_activated, double* inv_qc_relvar,
+               int32_t it, double* precip_liq_surf, double* precip_ice_surf, int32_t its, int32_t ite,
+               int32_t kts, int32_t kte, double* diag_eff_radius_qc, double* diag_eff_radius_qi,
+               double* diag_eff_radius_qr, double* rho_qi, int32_t do_predict_nc, int32_t do_prescribed_CCN,
+               double* dpres, double* inv_exner, double* qv2qi_depos_tend, double* precip_liq_flux,
+               double* precip_ice_flux, double* cld_frac_r, double* cld_frac_l, double* cld_frac_i,
+               double* liq_ice_exchange, double* vap_liq_exchange, double* vap_ice_exchange, double* qv_prev,
+               double* t_prev, double* elapsed_s) {
+  (void)it;
+  if (!g_default_ctx) {
+    int info = 0;
+    const int st = p3x_init(nullptr, &info);
+    if (st) return st;
+  }
+  p3x_context* ctx = g_default_ctx;
+  if (!(dt > 0) || ite < its || kte < kts) return P3X_EINVAL;
+  const int ncol = ite - its + 1, nlev = kte - kts + 1;
+  /* fields in order: 23 inputs (P3X_F_*), then outputs */
+  double* host[] = {qc, nc, qr, nr, qi, qm, ni, bm, qv, th_atm, nc_nuceat_tend, nccn_prescribed, ni_activated,
+                    inv_qc_relvar, cld_frac_i, cld_frac_l, cld_frac_r, pres, dz, dpres, inv_exner, qv_prev,
+                    t_prev,
+                    /* 23.. outputs (mid levels) */
+                    qv2qi_depos_tend, diag_eff_radius_qc, diag_eff_radius_qi, diag_eff_radius_qr, rho_qi,
+                    liq_ice_exchange, vap_liq_exchange, vap_ice_exchange};
+  constexpr int nin = P3X_NUM_INPUTS, nmid = nin + 8;
+  for (double* p : host)
+    if (!p) return P3X_EINVAL;
+  if (!precip_liq_surf || !precip_ice_surf || !precip_liq_flux || !precip_ice_flux) return P3X_EINVAL;
+  /* device buffers: nmid mid-level fields + 2 hidden mid (precip_total_tend,
+   * nevapr) + 2 interface fields + 2 surface fields */
+  const int64_t ld = nlev, ldi = nlev + 1;
+  const int64_t mid = int64_t(ncol) * ld, itf = int64_t(ncol) * ldi;
+  const int nbuf = nmid + 2 + 2 + 2;
+  const int64_t need = std::max<int64_t>(mid, itf);
+  if (int64_t(ctx->fbuf.size()) != nbuf || ctx->fbuf_elems < need) {
+    for (double* p : ctx->fbuf)
+      if (p) cudaFree(p);
+    ctx->fbuf.assign(nbuf, nullptr);
+    for (int b = 0; b < nbuf; ++b) P3X_CUDA(cudaMalloc(&ctx->fbuf[b], sizeof(double) * need));
+    ctx->fbuf_elems = need;
+  }
+  if (ctx->fstage_elems < need) {
+    if (ctx->fstage) cudaFree(ctx->fstage);
+    P3X_CUDA(cudaMalloc(&ctx->fstage, sizeof(double) * need));
+    ctx->fstage_elems = need;
+  }
+  cudaStream_t s = 0;
+  /* host (its:ite, kts:kte) column-fastest -> device (ncol, nlev) */
+  for (int f = 0; f < nin; ++f) {
+    P3X_CUDA(cudaMemcpyAsync(ctx->fstage, host[f], sizeof(double) * mid, cudaMemcpyHostToDevice, s));
+    P3X_CUDA(launch_transpose_to_levels(ctx->fstage, ctx->fbuf[f], ncol, nlev, ld, s));
+  }
+  double** B = ctx->fbuf.data();
+  p3x_prognostic_state prog{B[0], B[1], B[2], B[3], B[4], B[5], B[6], B[7], B[8], B[9]};
+  p3x_diagnostic_inputs din{B[10], B[11], B[12], B[13], B[14], B[15], B[16], B[17], B[18], B[19], B[20], B[21], B[22]};
+  p3x_diagnostic_outputs dout{B[23], B[nmid + 4], B[nmid + 5], B[24], B[25], B[26], B[27],
+                              B[nmid + 2], B[nmid + 3], B[nmid], B[nmid + 1]};
+  p3x_history_only hist{B[28], B[29], B[30]};
+  p3x_infrastructure infra{dt, it, its, ite, kts, kte, do_predict_nc, do_prescribed_CCN, nullptr};
+  p3x_layout lay{ld, ldi};
+  p3x_runtime rt;
+  p3x_runtime_defaults(&rt);
+  double us = 0;
+  int st = p3x_main(ctx, &rt, &prog, &din, &dout, &infra, &hist, ncol, nlev, &lay, P3X_FP64, s, &us);
+  if (st) return st;
+  if (elapsed_s) *elapsed_s = us * 1e-6;
+  /* copy back in/out and out fields */
+  auto back = [&](const double* dsrc, double* hdst, int nl, int64_t ldx) -> int {
+    P3X_CUDA(launch_transpose_to_columns(dsrc, ctx->fstage, ncol, nl, ldx, s));
+    P3X_CUDA(cudaMemcpyAsync(hdst, ctx->fstage, sizeof(double) * int64_t(ncol) * nl, cudaMemcpyDeviceToHost, s));
+    return P3X_OK;
+  };
+  for (int f = 0; f < P3X_F_TH + 1; ++f)
+    if ((st = back(B[f], host[f], nlev, ld))) return st;
+  for (int f = nin; f < nmid; ++f)
+    if ((st = back(B[f], host[f], nlev, ld))) return st;
+  if ((st = back(B[nmid + 2], precip_liq_flux, nlev + 1, ldi))) return st;
+  if ((st = back(B[nmid + 3], precip_ice_flux, nlev + 1, ldi))) return st;
+  P3X_CUDA(cudaMemcpyAsync(precip_liq_surf, B[nmid + 4], sizeof(double) * ncol, cudaMemcpyDeviceToHost, s));
+  P3X_CUDA(cudaMemcpyAsync(precip_ice_surf, B[nmid + 5], sizeof(double) * ncol, cudaMemcpyDeviceToHost, s));
+  P3X_CUDA(cudaStreamSynchronize(s));
+  return P3X_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* workload / budgets                                                  */
+/* ------------------------------------------------------------------ */
+int p3x_workload_generate(int32_t kind, uint64_t seed, int32_t col0, int32_t ncol, int32_t nlev,
+                          double* const* fields, int64_t ld) {
+  return workload_generate(kind, seed, col0, ncol, nlev, fields, ld);
+}
+
+int p3x_column_budgets(const p3x_prognostic_state* prog, const double* dpres, const double* inv_exner,
+                       int32_t ncol, int32_t nlev, int64_t ld, double* water_out, double* energy_out,
+                       void* stream) {
+  if (!prog || !dpres || !inv_exner || ncol < 0 || nlev <= 0) return P3X_EINVAL;
+  if (ld <= 0) ld = nlev;
+  return cuda_status(launch_budgets(prog->qv, prog->qc, prog->qr, prog->qi, prog->th, dpres, inv_exner, ncol,
+                                    nlev, ld, water_out, energy_out, static_cast<cudaStream_t>(stream)));
+}
+
+}  // extern "C"
+
+/* ------------------------------------------------------------------ */
+/* batched form                                                        */
+/* ------------------------------------------------------------------ */
+struct p3x_batch {
+  p3x_context* ctx = nullptr;
+  dev::RuntimeDev rtd{};
+  dev::Inst* insts_d = nullptr;
+  struct Group {
+    int precision = 0;
+    dev::WorkItem* work_d = nullptr;
+    int nwork = 0;
+    int nlev_max = 0;
+    LaunchSpec ls{32, 8, 1, 0};
+  } groups[2];
+  int ngroups = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace p3x {
+namespace {
+int batch_launch(p3x_batch* b, cudaStream_t st) {
+  dev::Inst dummy{};
+  for (int g = 0; g < b->ngroups; ++g) {
+    auto& G = b->groups[g];
+    if (G.nwork == 0) continue;
+    const int stride = sm_stride_for(G.nlev_max);
+    const LaunchSpec ls = fit_spec(G.precision, G.ls, stride);
+    cudaError_t e;
+    if (G.precision == P3X_FP32_BULK) {
+      dev::KParams<float> kp = make_kparams<float>(b->ctx, b->rtd);
+      kp.sm_stride = stride;
+      kp.nwork = G.nwork;
+      kp.work = G.work_d;
+      kp.insts = b->insts_d;
+      e = launch_p3<float>(dummy, kp, ls, b->ctx->num_sms, st);
+    } else {
+      dev::KParams<double> kp = make_kparams<double>(b->ctx, b->rtd);
+      kp.sm_stride = stride;
+      kp.nwork = G.nwork;
+      kp.work = G.work_d;
+      kp.insts = b->insts_d;
+      e = launch_p3<double>(dummy, kp, ls, b->ctx->num_sms, st);
+    }
+    if (e != cudaSuccess) return cuda_status(e);
+  }
+  return P3X_OK;
+}
+void drop_graph(p3x_batch* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+}
+}  // namespace
+}  // namespace p3x
+
+extern "C" {
+
+int p3x_batch_create(p3x_context* ctx, const p3x_runtime* rt, const p3x_instance_desc* descs, int32_t n,
+                     p3x_batch** out) {
+  if (!ctx || !rt || !descs || n <= 0 || !out || !valid_runtime(*rt)) return P3X_EINVAL;
+  *out = nullptr;
+  std::vector<dev::Inst> insts(n);
+  for (int i = 0; i < n; ++i) {
+    const p3x_instance_desc& d = descs[i];
+    const int st = fill_inst(&d.prog, &d.din, &d.dout, &d.hist, &d.layout, d.ncol, d.nlev, d.dt, d.predictNc,
+                             d.prescribedCCN, d.precision, insts[i]);
+    if (st) return st;
+  }
+  auto b = std::make_unique<p3x_batch>();
+  b->ctx = ctx;
+  b->rtd = make_runtime(*rt);
+  P3X_CUDA(cudaMalloc(&b->insts_d, sizeof(dev::Inst) * n));
+  P3X_CUDA(cudaMemcpy(b->insts_d, insts.data(), sizeof(dev::Inst) * n, cudaMemcpyHostToDevice));
+  for (int p = 0; p < 2; ++p) {
+    /* deeper columns first, then interleave instances so that neighbouring
+     * work items belong to different instances */
+    std::vector<int> idx;
+    for (int i = 0; i < n; ++i)
+      if (insts[i].precision == p) idx.push_back(i);
+    if (idx.empty()) continue;
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int c) { return insts[a].nlev > insts[c].nlev; });
+    std::vector<dev::WorkItem> work;
+    int nlev_max = 0;
+    for (int i : idx) {
+      nlev_max = std::max(nlev_max, insts[i].nlev);
+      for (int c = 0; c < insts[i].ncol; ++c) work.push_back(dev::WorkItem{i, c});
+    }
+    auto& G = b->groups[b->ngroups++];
+    G.precision = p;
+    G.nwork = int(work.size());
+    G.nlev_max = nlev_max;
+    G.ls = spec_of(ctx->cfg[p]);
+    if (!work.empty()) {
+      P3X_CUDA(cudaMalloc(&G.work_d, sizeof(dev::WorkItem) * work.size()));
+      P3X_CUDA(cudaMemcpy(G.work_d, work.data(), sizeof(dev::WorkItem) * work.size(), cudaMemcpyHostToDevice));
+    }
+  }
+  *out = b.release();
+  return P3X_OK;
+}
+
+int p3x_batch_run(p3x_batch* b, void* stream) {
+  if (!b) return P3X_EINVAL;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (b->exec) return cuda_status(cudaGraphLaunch(b->exec, st));
+  return batch_launch(b, st);
+}
+
+int p3x_batch_capture_graph(p3x_batch* b, void* stream) {
+  if (!b) return P3X_EINVAL;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (st == nullptr) return P3X_EINVAL; /* the legacy stream cannot be captured */
+  drop_graph(b);
+  P3X_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  const int rc = batch_launch(b, st);
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(st, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_status(e);
+  b->graph = g;
+  P3X_CUDA(cudaGraphInstantiate(&b->exec, g, 0));
+  return P3X_OK;
+}
+
+int p3x_batch_set_launch_config(p3x_batch* b, const p3x_launch_config* cfg) {
+  if (!b || !cfg) return P3X_EINVAL;
+  for (int g = 0; g < b->ngroups; ++g) {
+    const LaunchSpec ls = spec_of(*cfg);
+    if (!spec_fits(b->groups[g].precision, ls, sm_stride_for(1))) return P3X_EINVAL;
+    b->groups[g].ls = ls;
+  }
+  drop_graph(b);
+  return P3X_OK;
+}
+
+int p3x_batch_destroy(p3x_batch* b) {
+  if (!b) return P3X_EINVAL;
+  drop_graph(b);
+  if (b->insts_d) cudaFree(b->insts_d);
+  for (int g = 0; g < b->ngroups; ++g)
+    if (b->groups[g].work_d) cudaFree(b->groups[g].work_d);
+  delete b;
+  return P3X_OK;
+}
+
+/* Times every candidate configuration on the batch (each run advances the
+ * batch's instances by one step) and keeps the fastest. */
+int p3x_autotune_batch(p3x_batch* b, void* stream, int32_t reps, p3x_launch_config* best, double* ms_best) {
+  if (!b || reps <= 0) return P3X_EINVAL;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  drop_graph(b);
+  const int lanes_c[] = {8, 16, 32};
+  const int groups_c[] = {2, 4, 8};
+  const int staged_c[] = {0, 1};
+  const int bps_c[] = {0, 1};
+  p3x_launch_config best_cfg{32, 8, 1, 0};
+  double best_ms = 1e300;
+  cudaEvent_t e0, e1;
+  P3X_CUDA(cudaEventCreate(&e0));
+  P3X_CUDA(cudaEventCreate(&e1));
+  for (int L : lanes_c)
+    for (int G : groups_c)
+      for (int S : staged_c)
+        for (int B : bps_c) {
+          const int groups = G * (32 / L); /* keep the CTA size in warps comparable across lane counts */
+          if (groups * L > 256) continue;
+          p3x_launch_config c{L, groups, S, B};
+          bool ok = true;
+          for (int g = 0; g < b->ngroups; ++g) {
+            const LaunchSpec ls = spec_of(c);
+            if (!spec_fits(b->groups[g].precision, ls, sm_stride_for(b->groups[g].nlev_max))) ok = false;
+          }
+          if (!ok) continue;
+          for (int g = 0; g < b->ngroups; ++g) b->groups[g].ls = spec_of(c);
+          if (batch_launch(b, st) != P3X_OK) continue; /* warm-up */
+          cudaEventRecord(e0, st);
+          int rc = P3X_OK;
+          for (int r = 0; r < reps && rc == P3X_OK; ++r) rc = batch_launch(b, st);
+          cudaEventRecord(e1, st);
+          if (cudaEventSynchronize(e1) != cudaSuccess || rc != P3X_OK) continue;
+          float ms = 0;
+          cudaEventElapsedTime(&ms, e0, e1);
+          const double per = double(ms) / reps;
+          if (per < best_ms) {
+            best_ms = per;
+            best_cfg = c;
+          }
+        }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (int g = 0; g < b->ngroups; ++g) b->groups[g].ls = spec_of(best_cfg);
+  if (best) *best = best_cfg;
+  if (ms_best) *ms_best = best_ms;
+  const int st_err = read_and_clear_err(b->ctx, st);
+  return best_ms < 1e300 ? st_err : P3X_ECUDA;
+}
+
+}  // extern "C"

@@ -1,0 +1,102 @@
+/*
+ * Auxiliary device kernels of libp3x: layout transposes for the
+ * Fortran-layout entry point, and the FP64 column water / energy budgets
+ * (share/property_checks/mass_and_energy_column_conservation_check.cpp:281-347).
+ */
+#include "p3x_launch.hpp"
+
+namespace p3x {
+
+namespace {
+
+/* src[k*ncol + i] (column fastest) -> dst[i*ld + k] (level contiguous), via a
+ * 32x33 shared tile so that both sides are coalesced. */
+__global__ void transpose_to_levels(const double* __restrict__ src, double* __restrict__ dst, int ncol,
+                                    int nlev, int64_t ld) {
+  __shared__ double tile[32][33];
+  const int i0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int k = k0 + r, i = i0 + threadIdx.x;
+    if (k < nlev && i < ncol) tile[r][threadIdx.x] = src[int64_t(k) * ncol + i];
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int i = i0 + r, k = k0 + threadIdx.x;
+    if (k < nlev && i < ncol) dst[int64_t(i) * ld + k] = tile[threadIdx.x][r];
+  }
+}
+
+__global__ void transpose_to_columns(const double* __restrict__ src, double* __restrict__ dst, int ncol,
+                                     int nlev, int64_t ld) {
+  __shared__ double tile[32][33];
+  const int i0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int i = i0 + r, k = k0 + threadIdx.x;
+    if (k < nlev && i < ncol) tile[r][threadIdx.x] = src[int64_t(i) * ld + k];
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int k = k0 + r, i = i0 + threadIdx.x;
+    if (k < nlev && i < ncol) dst[int64_t(k) * ncol + i] = tile[threadIdx.x][r];
+  }
+}
+
+/* One warp per column; lanes stride the levels; shuffle reduction. */
+__global__ void column_budgets(const double* __restrict__ qv, const double* __restrict__ qc,
+                               const double* __restrict__ qr, const double* __restrict__ qi,
+                               const double* __restrict__ th, const double* __restrict__ dpres,
+                               const double* __restrict__ inv_exner, int ncol, int nlev, int64_t ld,
+                               double* __restrict__ water, double* __restrict__ energy) {
+  constexpr double g = 9.80616, cp = 1004.64, Lv = 2501000.0, Lf = 333700.0;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= ncol) return;
+  const int64_t o = int64_t(warp) * ld;
+  double w = 0, e = 0;
+  for (int k = lane; k < nlev; k += 32) {
+    const double dp = dpres[o + k];
+    const double T = th[o + k] / inv_exner[o + k];
+    w += (qv[o + k] + qc[o + k] + qi[o + k] + qr[o + k]) * dp / g;
+    e += (T * cp + (Lv + Lf) * qv[o + k] + Lf * (qc[o + k] + qr[o + k])) * dp / g;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    w += __shfl_xor_sync(0xffffffffu, w, off);
+    e += __shfl_xor_sync(0xffffffffu, e, off);
+  }
+  if (lane == 0) {
+    if (water) water[warp] = w;
+    if (energy) energy[warp] = e;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_transpose_to_levels(const double* src, double* dst, int ncol, int nlev, int64_t ld,
+                                       cudaStream_t st) {
+  if (ncol <= 0 || nlev <= 0) return cudaSuccess;
+  dim3 grid((ncol + 31) / 32, (nlev + 31) / 32), block(32, 8);
+  transpose_to_levels<<<grid, block, 0, st>>>(src, dst, ncol, nlev, ld);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_transpose_to_columns(const double* src, double* dst, int ncol, int nlev, int64_t ld,
+                                        cudaStream_t st) {
+  if (ncol <= 0 || nlev <= 0) return cudaSuccess;
+  dim3 grid((ncol + 31) / 32, (nlev + 31) / 32), block(32, 8);
+  transpose_to_columns<<<grid, block, 0, st>>>(src, dst, ncol, nlev, ld);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_budgets(const double* qv, const double* qc, const double* qr, const double* qi,
+                           const double* th, const double* dpres, const double* inv_exner, int ncol,
+                           int nlev, int64_t ld, double* water, double* energy, cudaStream_t st) {
+  if (ncol <= 0) return cudaSuccess;
+  const int threads = 256;
+  const long long blocks = (int64_t(ncol) * 32 + threads - 1) / threads;
+  column_budgets<<<unsigned(blocks), threads, 0, st>>>(qv, qc, qr, qi, th, dpres, inv_exner, ncol, nlev, ld,
+                                                       water, energy);
+  return cudaGetLastError();
+}
+
+}  // namespace p3x

@@ -1,0 +1,937 @@
+/*
+ * The fused P3 column kernel.
+ *
+ * One group of LANES threads (8, 16 or 32; a warp or part of one) owns one
+ * column at a time; lane l owns levels l, l+LANES, l+2*LANES, ...  Inputs
+ * are level-contiguous (EAMxx layout), so a group's loads of one field are
+ * coalesced.  Per column the kernel runs, in the reference's stage order
+ * (p3/impl/p3_main_impl.hpp:108-325):
+ *
+ *   1. p3_main_init + p3_main_part1 (level-parallel); the column-wide early
+ *      exit of p3_main_impl.hpp:237-239 is a group ballot.
+ *   2. p3_main_part2 (level-parallel) with the second early exit (:260).
+ *   3. cloud, rain and ice sedimentation: CFL substeps with the Courant
+ *      maximum as a group shuffle reduction and the upwind flux divergence
+ *      walked down the levels chunk by chunk with a shuffle-up and a carry
+ *      (p3_upwind_impl.hpp:14-116).  Substep loops are capped.
+ *   4. homogeneous freezing + p3_main_part3 (level-parallel).
+ *
+ * Between phases, per-level quantities live in shared memory (13 FP64
+ * arrays per column); prognostic fields are written back to their global
+ * arrays after each phase and re-read from L2 by the next.  Lookup tables
+ * are read from global memory (L1/L2) or staged into shared memory once per
+ * CTA with cp.async.bulk + mbarrier (tiny Table3 slices for the runtime's
+ * constant rain shape parameter, plus the whole ice table).
+ */
+#pragma once
+
+#include "p3x_physics.cuh"
+
+namespace p3x {
+namespace dev {
+
+/* Arguments of one instance (device pointers, (ncol, nlev) row-major). */
+struct Inst {
+  double *qc, *nc, *qr, *nr, *qi, *qm, *ni, *bm, *qv, *th;
+  const double *nc_nuceat_tend, *nccn, *ni_activated, *inv_qc_relvar, *cld_frac_i, *cld_frac_l,
+      *cld_frac_r, *pres, *dz, *dpres, *inv_exner, *qv_prev, *t_prev;
+  double *qv2qi_depos_tend, *precip_liq_surf, *precip_ice_surf, *diag_eff_radius_qc,
+      *diag_eff_radius_qi, *diag_eff_radius_qr, *rho_qi, *precip_liq_flux, *precip_ice_flux,
+      *precip_total_tend, *nevapr;
+  double *liq_ice_exchange, *vap_liq_exchange, *vap_ice_exchange;
+  int64_t ld, ld_int;
+  int32_t ncol, nlev;
+  double dt;
+  int32_t predictNc, prescribedCCN, precision, pad_;
+};
+
+/* Work item of the batched form: (instance, column). */
+struct WorkItem {
+  int32_t inst, col;
+};
+
+template <class TR>
+struct KParams {
+  RuntimeDev rt;
+  /* global tables in the rate precision */
+  const TR* ice;
+  const TR* collect;
+  const TR* vn;
+  const TR* vm;
+  const TR* revap;
+  const TR* t3slice; /* [3][300][2] = vn, vm, revap columns (t3_dumjj-1, t3_dumjj) */
+  int staged;        /* stage ice table + Table3 slices into shared memory */
+  int sm_stride;     /* doubles per per-level shared array (>= nlev_max + 1, even) */
+  int groups_per_block;
+  int nwork;         /* number of columns (single) or work items (batched) */
+  const WorkItem* work;
+  const Inst* insts;
+  uint32_t* err;
+};
+
+constexpr int kIceTableElems = kDensize * kRimsize * kIsize * kIceCols; /* 12000 */
+constexpr int kT3SliceElems = 3 * 300 * 2;
+constexpr int kMaxSubsteps = 100000;
+constexpr long long kWaitSpinLimit = 1ll << 26;
+constexpr uint64_t kWaitNanosLimit = 2000000000ull; /* 2 s */
+
+/* shared arrays of one column group */
+enum {
+  A_TATM = 0, A_RHO, A_RHOFACR, A_RHOFACI, A_ACN, A_INVDZ, A_QVSL, A_QVSI, A_QVSSI,
+  A_R0, A_R1, A_R2, A_R3, A_NARR,
+  /* sedimentation re-uses the part2-only arrays */
+  A_V1 = A_QVSL, A_V2 = A_QVSI, A_PFLUX = A_QVSSI
+};
+
+template <class TR>
+__host__ __device__ constexpr size_t table_smem_bytes() {
+  return ((sizeof(TR) * (kIceTableElems + kT3SliceElems) + 15) / 16) * 16 + 16;
+}
+
+/* ------------------------------------------------------------------ */
+/* group primitives                                                    */
+/* ------------------------------------------------------------------ */
+template <int LANES>
+__device__ __forceinline__ unsigned group_mask() {
+  if (LANES == 32) return 0xffffffffu;
+  const unsigned lw = threadIdx.x & 31u;
+  return (0xffffffffu >> (32 - LANES)) << (lw & ~unsigned(LANES - 1));
+}
+template <int LANES>
+__device__ __forceinline__ bool group_any(unsigned mask, bool p) {
+  return __ballot_sync(mask, p) != 0u;
+}
+template <int LANES>
+__device__ __forceinline__ double group_max(unsigned mask, double v) {
+#pragma unroll
+  for (int o = LANES / 2; o > 0; o >>= 1) v = vmax(v, __shfl_xor_sync(mask, v, o, LANES));
+  return v;
+}
+template <int LANES>
+__device__ __forceinline__ int group_min_int(unsigned mask, int v) {
+#pragma unroll
+  for (int o = LANES / 2; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(mask, v, o, LANES));
+  return v;
+}
+template <int LANES>
+__device__ __forceinline__ int group_max_int(unsigned mask, int v) {
+#pragma unroll
+  for (int o = LANES / 2; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(mask, v, o, LANES));
+  return v;
+}
+
+/* ------------------------------------------------------------------ */
+/* bulk copy of the tables into shared memory                          */
+/* ------------------------------------------------------------------ */
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+/* Thread 0 arms an mbarrier with the byte count and issues the bulk copies;
+ * every thread then waits on the barrier's phase with a bounded spin.
+ * Returns false (and sets kErrWait) if the wait gave up. */
+template <class TR>
+__device__ bool stage_tables(const KParams<TR>& kp, TR* s_ice, TR* s_t3, uint64_t* mbar, uint32_t& err) {
+  const uint32_t bar = smem_u32(mbar);
+  const uint32_t ice_bytes = uint32_t(sizeof(TR) * kIceTableElems);
+  const uint32_t t3_bytes = uint32_t(sizeof(TR) * kT3SliceElems);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(1) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                 "r"(ice_bytes + t3_bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(s_ice)),
+        "l"(kp.ice), "r"(ice_bytes), "r"(bar)
+        : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(s_t3)),
+        "l"(kp.t3slice), "r"(t3_bytes), "r"(bar)
+        : "memory");
+  }
+  bool done = false;
+  uint64_t t0;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  for (long long spin = 0; spin < kWaitSpinLimit; ++spin) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(0)
+        : "memory");
+    if (ok) {
+      done = true;
+      break;
+    }
+    uint64_t t1;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+    if (t1 - t0 > kWaitNanosLimit) break;
+  }
+  if (!done) err |= kErrWait;
+  return done;
+}
+
+/* Applies a rate-precision DSD adjustment of a number concentration to the
+ * FP64 value only when the DSD routine changed it (exact for FP64). */
+template <class TR>
+__device__ __forceinline__ void apply_n_adjust(double& n_d, TR n_in, TR n_out) {
+  if (n_out != n_in) n_d = double(n_out);
+}
+
+/* ------------------------------------------------------------------ */
+/* one column                                                          */
+/* ------------------------------------------------------------------ */
+template <class TR, int LANES>
+__device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, const Tabs<TR>& tb,
+                          double* __restrict__ sm, const double esat0, uint32_t& err) {
+  const RuntimeDev& rt = kp.rt;
+  const unsigned mask = group_mask<LANES>();
+  const int lane = threadIdx.x & (LANES - 1);
+  const int nk = in.nlev;
+  const int S = kp.sm_stride;
+  const int64_t co = int64_t(col) * in.ld;
+  const int64_t ci = int64_t(col) * in.ld_int;
+  const double dt = in.dt;
+  const double inv_dt = 1 / dt;
+  const bool predictNc = in.predictNc != 0, prescribedCCN = in.prescribedCCN != 0;
+  const bool do_ice = rt.do_ice_production != 0;
+  const int kbot = nk - 1, ktop = 0;
+  (void)ktop;
+#define SMA(a, k) sm[(a)*S + (k)]
+
+  /* ---------------- phase 1: p3_main_init + p3_main_part1 ---------------- */
+  bool nucl = false, hydro = false;
+  for (int k = lane; k < nk; k += LANES) {
+    const int64_t o = co + k;
+    const double cld_l = in.cld_frac_l[o];
+    const double inv_exner = in.inv_exner[o];
+    double th = in.th[o];
+    const double dz = in.dz[o];
+    double qv = in.qv[o];
+    const double pres = in.pres[o];
+    const double dpres = in.dpres[o];
+    double qc = in.qc[o], nc = in.nc[o], qr = in.qr[o], nr = in.nr[o];
+    double qi = in.qi[o], ni = in.ni[o], qm = in.qm[o], bm = in.bm[o];
+
+    in.diag_eff_radius_qc[o] = 10.e-6;
+    in.diag_eff_radius_qi[o] = 25.e-6;
+    in.diag_eff_radius_qr[o] = 500.e-6;
+    in.rho_qi[o] = 0;
+    in.qv2qi_depos_tend[o] = 0;
+    in.precip_total_tend[o] = 0;
+    in.nevapr[o] = 0;
+    in.liq_ice_exchange[o] = 0;
+    in.vap_liq_exchange[o] = 0;
+    in.vap_ice_exchange[o] = 0;
+
+    const double inv_cld_l = 1 / cld_l;
+    const double exner = 1 / inv_exner;
+    double T = th * exner;
+    qv = vmax(qv, 0.);
+    const double inv_dz = 1 / dz;
+
+    const double rho = dpres / dz / C::gravit;
+    const double inv_rho = 1 / rho;
+    const double qvsl = qv_sat_dry<TR>(T, pres, false, err);
+    const double qvsi = qv_sat_dry<TR>(T, pres, true, err);
+    const double qvssi = qv / qvsi - 1;
+    const TR rhofacr = m_pow(TR(C::RHO_1000MB) * TR(inv_rho), TR(.54));
+    const TR rhofaci = m_pow(TR(C::RHO_600MB) * TR(inv_rho), TR(.54));
+    const TR dum = TR(1.496e-6) * m_pow(TR(T), TR(1.5)) / (TR(T) + TR(120));
+    const TR acn = TR(C::gravit) * TR(C::RHO_H2O) / (TR(18) * dum);
+    if (T < C::T_zerodegc && qvssi >= -0.05) nucl = true;
+
+    if (qc < C::QSMALL) {
+      qv = qv + qc;
+      th = th - inv_exner * qc * C::LatVap * C::INV_CP;
+      qc = 0;
+      nc = 0;
+    } else {
+      hydro = true;
+      if (prescribedCCN) {
+        nc = vmax(nc, rt.spa_ccn_to_nc_factor * in.nccn[o] / inv_cld_l);
+      } else if (predictNc) {
+        nc = vmax(nc + in.nc_nuceat_tend[o] * dt, 0.0);
+      } else {
+        nc = C::NCCNST * inv_rho;
+      }
+    }
+    if (qr < C::QSMALL) {
+      qv = qv + qr;
+      th = th - inv_exner * qr * C::LatVap * C::INV_CP;
+      qr = 0;
+      nr = 0;
+    } else {
+      hydro = true;
+    }
+    if (qi < C::QSMALL || (qi < 1.e-8 && qvssi < -0.1)) {
+      qv = qv + qi;
+      th = th - inv_exner * qi * (C::LatVap + C::LatIce) * C::INV_CP;
+      qi = 0; ni = 0; qm = 0; bm = 0;
+    } else {
+      hydro = true;
+    }
+    if (qi >= C::QSMALL && qi < 1.e-8 && T >= C::T_zerodegc) {
+      qr = qr + qi;
+      th = th - inv_exner * qi * C::LatIce * C::INV_CP;
+      qi = 0; ni = 0; qm = 0; bm = 0;
+    }
+    T = th * exner;
+
+    in.qc[o] = qc; in.nc[o] = nc; in.qr[o] = qr; in.nr[o] = nr;
+    in.qi[o] = qi; in.ni[o] = ni; in.qm[o] = qm; in.bm[o] = bm;
+    in.qv[o] = qv; in.th[o] = th;
+    SMA(A_TATM, k) = T;
+    SMA(A_RHO, k) = rho;
+    SMA(A_RHOFACR, k) = double(rhofacr);
+    SMA(A_RHOFACI, k) = double(rhofaci);
+    SMA(A_ACN, k) = double(acn);
+    SMA(A_INVDZ, k) = inv_dz;
+    SMA(A_QVSL, k) = qvsl;
+    SMA(A_QVSI, k) = qvsi;
+    SMA(A_QVSSI, k) = qvssi;
+  }
+  for (int k = lane; k <= nk; k += LANES) {
+    in.precip_liq_flux[ci + k] = 0;
+    in.precip_ice_flux[ci + k] = 0;
+  }
+  double precip_liq_surf = 0, precip_ice_surf = 0;
+  if (lane == 0) {
+    in.precip_liq_surf[col] = 0;
+    in.precip_ice_surf[col] = 0;
+  }
+  if (!group_any<LANES>(mask, nucl || hydro)) return;
+
+  /* ---------------- phase 2: p3_main_part2 ---------------- */
+  hydro = false;
+  for (int k = lane; k < nk; k += LANES) {
+    const int64_t o = co + k;
+    State s;
+    s.qc = in.qc[o]; s.nc = in.nc[o]; s.qr = in.qr[o]; s.nr = in.nr[o];
+    s.qi = in.qi[o]; s.qm = in.qm[o]; s.ni = in.ni[o]; s.bm = in.bm[o];
+    s.qv = in.qv[o]; s.th = in.th[o];
+    const double T = SMA(A_TATM, k);
+    const double qvssi = SMA(A_QVSSI, k);
+    if (s.qc < C::QSMALL && s.qr < C::QSMALL && s.qi < C::QSMALL && T < C::T_zerodegc && qvssi < -0.05)
+      continue;
+
+    const double pres = in.pres[o];
+    const double cld_i = in.cld_frac_i[o], cld_l = in.cld_frac_l[o], cld_r = in.cld_frac_r[o];
+    const double inv_exner = in.inv_exner[o];
+    const double rho = SMA(A_RHO, k);
+    const double inv_rho = 1 / rho;
+    const double qvsl = SMA(A_QVSL, k), qvsi = SMA(A_QVSI, k);
+    const double rhofaci = SMA(A_RHOFACI, k);
+    const double acn = SMA(A_ACN, k);
+    Incld inc;
+    calc_incloud(s.qc, s.qr, s.qi, s.qm, s.nc, s.nr, s.ni, s.bm, 1 / cld_l, 1 / cld_i, 1 / cld_r, inc);
+
+    Rates<TR> r;
+    r.zero();
+    PhysVars<TR> v;
+    v.mu = v.dv = v.sc = v.dqsdt = v.dqsidt = v.ab = v.abi = v.kap = v.eii = TR(0);
+    TR tv_fallspd = 0, tv_selfcol = 0, tv_qc2qi = 0, tv_melt = 0, tv_nr = 0, tv_qr2qi = 0,
+       tv_lammax = 0, tv_lammin = 0, tv_vent = 0;
+    TR mu_c = 0, lamc = 0, cdist = 0, cdist1 = 0, mu_r = 0, lamr = 0, cdistr = 0, logn0r = 0;
+    TR epsi = 0, epsr = 0, epsc = 0, epsi_tot = 0;
+    TR rho_qm_cloud = TR(400);
+    bool wet = false;
+    (void)epsc;
+
+    const bool skip_micro = !(inc.qc >= C::QSMALL || inc.qr >= C::QSMALL || inc.qi >= C::QSMALL);
+    if (!skip_micro) {
+      const TR T_r = TR(T), rho_r = TR(rho), rhofaci_r = TR(rhofaci);
+      get_time_space_phys_variables<TR>(T_r, TR(pres), rho_r, TR(qvsl), TR(qvsi), v);
+      {
+        const TR n_in = TR(inc.nc);
+        TR n_out = n_in;
+        get_cloud_dsd2<TR>(TR(inc.qc), n_out, mu_c, rho_r, lamc, cdist, cdist1);
+        apply_n_adjust(inc.nc, n_in, n_out);
+      }
+      s.nc = inc.nc * cld_l;
+      {
+        const TR n_in = TR(inc.nr);
+        TR n_out = n_in;
+        get_rain_dsd2<TR>(TR(inc.qr), n_out, mu_r, lamr, rt);
+        apply_n_adjust(inc.nr, n_in, n_out);
+        if (inc.qr >= C::QSMALL) {
+          cdistr = TR(inc.nr) / m_tgamma(mu_r + TR(1));
+          logn0r = m_log10(cdistr) + (mu_r + TR(1)) * m_log10(lamr);
+        }
+      }
+      s.nr = inc.nr * cld_r;
+      impose_max_total_ni(inc.ni, rt.max_total_ni, inv_rho);
+      if (inc.qi >= C::QSMALL) {
+        inc.ni = vmax(inc.ni, C::NSMALL);
+        inc.nr = vmax(inc.nr, C::NSMALL);
+        const double rhop = calc_bulk_rho_rime(inc.qi, inc.qm, inc.bm, rt);
+        s.qm = inc.qm * cld_i;
+        s.bm = inc.bm * cld_i;
+        TableIce<TR> ti;
+        lookup_ice<TR>(TR(inc.qi), TR(inc.ni), TR(inc.qm), TR(rhop), ti);
+        TableRain<TR> trn;
+        lookup_rain<TR>(TR(inc.qr), TR(inc.nr), trn);
+        tv_fallspd = apply_table_ice<TR>(1, tb, ti);
+        tv_selfcol = apply_table_ice<TR>(2, tb, ti);
+        tv_qc2qi = apply_table_ice<TR>(3, tb, ti);
+        tv_melt = apply_table_ice<TR>(4, tb, ti);
+        tv_lammax = apply_table_ice<TR>(6, tb, ti);
+        tv_lammin = apply_table_ice<TR>(7, tb, ti);
+        tv_vent = apply_table_ice<TR>(9, tb, ti);
+        if (inc.qr >= C::QSMALL) {
+          tv_nr = apply_table_coll<TR>(0, tb, ti, trn);
+          tv_qr2qi = apply_table_coll<TR>(1, tb, ti, trn);
+        }
+        inc.ni = vmin(inc.ni, double(tv_lammax) * inc.ni);
+        inc.ni = vmax(inc.ni, double(tv_lammin) * inc.ni);
+      }
+      const TR qi_r = TR(inc.qi), qc_r = TR(inc.qc), ni_r = TR(inc.ni), nc_r = TR(inc.nc), qr_r = TR(inc.qr);
+      const TR qsat0 = TR(C::ep_2 * esat0 / vmax(pres, 1.e-3));
+      if (do_ice) {
+        ice_cldliq_collection<TR>(rho_r, T_r, rhofaci_r, tv_qc2qi, qi_r, qc_r, ni_r, nc_r, r, rt);
+        ice_rain_collection<TR>(rho_r, T_r, rhofaci_r, logn0r, tv_nr, tv_qr2qi, qi_r, ni_r, qr_r, r, rt);
+        ice_self_collection<TR>(rho_r, rhofaci_r, tv_selfcol, v.eii, TR(inc.qm), qi_r, ni_r, r);
+      }
+      ice_melting<TR>(rho_r, T_r, qsat0, rhofaci_r, tv_melt, tv_vent, v, TR(s.qv), qi_r, ni_r, r);
+      if (do_ice) {
+        wet = ice_cldliq_wet_growth<TR>(rho_r, T_r, qsat0, rhofaci_r, tv_melt, tv_vent, v, TR(s.qv), qc_r,
+                                        qi_r, ni_r, qr_r, r);
+      }
+      /* ice_relaxation_timescale, p3_ice_relaxation_timescale_impl.hpp:9-37 */
+      if (inc.qi >= C::QSMALL && T < C::Tmelt) {
+        epsi = ((tv_melt + tv_vent * m_cbrt(v.sc) * m_sqrt(rhofaci_r * rho_r / v.mu)) * TR(2.0) * TR(C::Pi) *
+                rho_r * v.dv) * ni_r;
+        epsi_tot = epsi_tot + epsi;
+      } else {
+        epsi = TR(0);
+      }
+      rho_qm_cloud = calc_rime_density<TR>(T_r, rhofaci_r, tv_fallspd, TR(acn), lamc, mu_c, qc_r,
+                                           r.qc2qi_collect_tend);
+      if (do_ice) {
+        cldliq_immersion_freezing<TR>(T_r, lamc, mu_c, cdist1, qc_r, r, rt);
+        rain_immersion_freezing<TR>(T_r, lamr, mu_r, cdistr, qr_r, r, rt);
+      }
+      /* calc_liq_relaxation_timescale, p3_calc_liq_relaxation_timescale_impl.hpp:13-43 */
+      if (inc.qr >= C::QSMALL) {
+        Table3<TR> t3;
+        lookup3<TR>(mu_r, lamr, rt, t3);
+        epsr = TR(2) * TR(C::Pi) * cdistr * rho_r * v.dv *
+               (TR(C::f1r) * m_tgamma(mu_r + TR(2)) / lamr +
+                TR(C::f2r) * m_sqrt(rho_r / v.mu) * m_cbrt(v.sc) * apply_table3<TR>(tb, tb.revap, t3));
+      }
+      {
+        double evap, nevap;
+        evaporate_rain(inc.qr, inc.qc, inc.nr, inc.qi, cld_l, cld_r, s.qv, in.qv_prev[o], qvsl, qvsi,
+                       double(v.ab), double(v.abi), double(epsr), double(epsi_tot), T, in.t_prev[o],
+                       double(v.dqsdt), dt, evap, nevap);
+        r.qr2qv_evap_tend = TR(evap);
+        r.nr_evap_tend = TR(nevap);
+      }
+      if (do_ice) {
+        double vd, sb, nsb, bg;
+        ice_deposition_sublimation(inc.qi, inc.ni, T, qvsl, qvsi, double(epsi), double(v.abi), s.qv, inv_dt,
+                                   vd, sb, nsb, bg);
+        r.qv2qi_vapdep_tend = TR(vd);
+        r.qi2qv_sublim_tend = TR(sb);
+        r.ni_sublim_tend = TR(nsb);
+        r.qc2qi_berg_tend = TR(bg);
+      }
+    }
+    if (do_ice) {
+      ice_nucleation<TR>(TR(T), TR(inv_rho), TR(s.ni), TR(in.ni_activated[o]), qvssi, TR(inv_dt), predictNc,
+                         prescribedCCN, r, rt);
+    }
+    cloud_water_autoconversion<TR>(TR(rho), TR(inc.qc), TR(inc.nc), r, rt);
+    if (inc.qc >= C::QSMALL) r.nc_selfcollect_tend = TR(0);
+    cloud_rain_accretion<TR>(TR(inc.qc), TR(inc.nc), TR(inc.qr), r, rt);
+    rain_self_collection<TR>(TR(rho), TR(inc.qr), TR(inc.nr), r, rt);
+    back_to_cell_average<TR>(TR(cld_l), TR(cld_r), TR(cld_i), r);
+
+    Rates<double> rd = to_double(r);
+    water_conservation(s.qc, s.qr, s.qi, dt, rd);
+    number_conservation(s.nc, s.nr, s.ni, dt, rd);
+    ice_supersat_conservation(rd, cld_i, s.qv, qvsi, s.th / inv_exner, dt);
+    prevent_liq_supersaturation<TR>(pres, T, s.qv, dt, rd, err);
+    update_prognostics(rd, inv_exner, predictNc, prescribedCCN, wet, dt, double(rho_qm_cloud), inv_rho, s);
+
+    in.qv2qi_depos_tend[o] = rd.qv2qi_vapdep_tend - rd.qi2qv_sublim_tend + rd.qv2qi_nucleat_tend;
+    in.precip_total_tend[o] = rd.qc2qr_accret_tend + rd.qc2qr_autoconv_tend + rd.qc2qr_ice_shed_tend + rd.qc2qi_collect_tend;
+    in.nevapr[o] = rd.qi2qv_sublim_tend + rd.qr2qv_evap_tend;
+    in.vap_ice_exchange[o] = rd.qv2qi_vapdep_tend - rd.qi2qv_sublim_tend + rd.qv2qi_nucleat_tend;
+    in.vap_liq_exchange[o] = -rd.qr2qv_evap_tend;
+    in.liq_ice_exchange[o] = rd.qc2qi_hetero_freeze_tend + rd.qr2qi_immers_freeze_tend - rd.qi2qr_melt_tend +
+                             rd.qc2qi_berg_tend + rd.qc2qi_collect_tend + rd.qr2qi_collect_tend;
+
+    if (s.qc < C::QSMALL) {
+      s.qv = s.qv + s.qc;
+      s.th = s.th - inv_exner * s.qc * C::LatVap * C::INV_CP;
+      s.qc = 0;
+      s.nc = 0;
+    } else {
+      hydro = true;
+    }
+    if (s.qr < C::QSMALL) {
+      s.qv = s.qv + s.qr;
+      s.th = s.th - inv_exner * s.qr * C::LatVap * C::INV_CP;
+      s.qr = 0;
+      s.nr = 0;
+    } else {
+      hydro = true;
+    }
+    if (s.qi < C::QSMALL) {
+      s.qv = s.qv + s.qi;
+      s.th = s.th - inv_exner * s.qi * (C::LatVap + C::LatIce) * C::INV_CP;
+      s.qi = 0; s.ni = 0; s.qm = 0; s.bm = 0;
+    } else {
+      hydro = true;
+    }
+    {
+      double ni_incld = s.ni / cld_i;
+      impose_max_total_ni(ni_incld, rt.max_total_ni, inv_rho);
+      s.ni = ni_incld * cld_i;
+    }
+    in.qc[o] = s.qc; in.nc[o] = s.nc; in.qr[o] = s.qr; in.nr[o] = s.nr;
+    in.qi[o] = s.qi; in.qm[o] = s.qm; in.ni[o] = s.ni; in.bm[o] = s.bm;
+    in.qv[o] = s.qv; in.th[o] = s.th;
+  }
+  if (!group_any<LANES>(mask, hydro)) return;
+
+  /* ---------------- phase 3: sedimentation ---------------- */
+  double* const V1 = &SMA(A_V1, 0);
+  double* const V2 = &SMA(A_V2, 0);
+  double* const PF = &SMA(A_PFLUX, 0);
+  double* const R0 = &SMA(A_R0, 0);
+  double* const R1 = &SMA(A_R1, 0);
+  double* const R2 = &SMA(A_R2, 0);
+  double* const R3 = &SMA(A_R3, 0);
+
+#pragma unroll 1
+  for (int sp = 0; sp < 3; ++sp) {
+    double* g0 = sp == 0 ? in.qc : (sp == 1 ? in.qr : in.qi);
+    double* g1 = sp == 0 ? in.nc : (sp == 1 ? in.nr : in.ni);
+    const double* cldp = sp == 0 ? in.cld_frac_l : (sp == 1 ? in.cld_frac_r : in.cld_frac_i);
+    const int nfield = sp == 0 ? (predictNc ? 2 : 1) : (sp == 1 ? 2 : 4);
+
+    /* load the species into shared memory; find top / bottom (p3_find_impl.hpp) */
+    int my_top = 1 << 30, my_bot = -1;
+    for (int k = lane; k < nk; k += LANES) {
+      const double q = g0[co + k];
+      R0[k] = q;
+      R1[k] = g1[co + k];
+      if (sp == 2) {
+        R2[k] = in.qm[co + k];
+        R3[k] = in.bm[co + k];
+      }
+      if (q >= C::QSMALL) {
+        my_top = min(my_top, k);
+        my_bot = max(my_bot, k);
+      }
+    }
+    if (sp == 1) {
+      for (int k = lane; k <= nk; k += LANES) PF[k] = 0;
+    }
+    const int k_qxtop = group_min_int<LANES>(mask, my_top);
+    int k_qxbot = group_max_int<LANES>(mask, my_bot);
+    __syncwarp(mask);
+    if (k_qxbot < 0) continue; /* species absent */
+
+    double dt_left = dt, prt_accum = 0.0;
+    bool first = true;
+    int nsub = 0;
+    while (dt_left > C::dt_left_tol) {
+      if (++nsub > kMaxSubsteps) {
+        err |= kErrSubstep;
+        break;
+      }
+      /* fall speeds on [k_qxtop, k_qxbot] and the Courant maximum */
+      double lmax = 0.0;
+      for (int k = lane; k < nk; k += LANES) {
+        V1[k] = 0;
+        V2[k] = 0;
+        if (k < k_qxtop || k > k_qxbot) continue;
+        const int64_t o = co + k;
+        const double cld = cldp[o];
+        double v1 = 0, v2 = 0;
+        if (sp == 0) {
+          double qc_incld, nc_incld;
+          if (first) {
+            const double inv_cld = 1 / cld;
+            if (R0[k] >= C::QSMALL) {
+              qc_incld = R0[k] * inv_cld;
+              nc_incld = vmax(R1[k] * inv_cld, 0.);
+            } else {
+              qc_incld = 0;
+              nc_incld = 0;
+            }
+            qc_incld = vmin(qc_incld, C::incloud_limit);
+          } else {
+            qc_incld = R0[k] / cld;
+            nc_incld = R1[k] / cld;
+          }
+          if (qc_incld > C::QSMALL) {
+            TR mu_c, lamc, cdist, cdist1;
+            const TR n_in = TR(nc_incld);
+            TR n_out = n_in;
+            get_cloud_dsd2<TR>(TR(qc_incld), n_out, mu_c, TR(SMA(A_RHO, k)), lamc, cdist, cdist1);
+            apply_n_adjust(nc_incld, n_in, n_out);
+            R1[k] = nc_incld * cld;
+            const TR dum = TR(1) / m_pow(lamc, TR(C::bcn));
+            const TR acn = TR(SMA(A_ACN, k));
+            v1 = double(acn * m_tgamma(TR(4) + TR(C::bcn) + mu_c) * dum / m_tgamma(mu_c + TR(4)));
+            if (predictNc) v2 = double(acn * m_tgamma(TR(1) + TR(C::bcn) + mu_c) * dum / m_tgamma(mu_c + TR(1)));
+            lmax = vmax(lmax, v1 * dt_left * SMA(A_INVDZ, k));
+          }
+        } else if (sp == 1) {
+          double qr_incld, nr_incld;
+          if (first) {
+            const double inv_cld = 1 / cld;
+            if (R0[k] >= C::QSMALL) {
+              qr_incld = R0[k] * inv_cld;
+              nr_incld = vmax(R1[k] * inv_cld, 0.);
+            } else {
+              qr_incld = 0;
+              nr_incld = 0;
+            }
+            qr_incld = vmin(qr_incld, C::precip_limit);
+          } else {
+            qr_incld = R0[k] / cld;
+            nr_incld = R1[k] / cld;
+          }
+          if (qr_incld > C::QSMALL) {
+            TR mu_r = 0, lamr;
+            const TR n_in = TR(nr_incld);
+            TR n_out = n_in;
+            get_rain_dsd2<TR>(TR(qr_incld), n_out, mu_r, lamr, rt);
+            apply_n_adjust(nr_incld, n_in, n_out);
+            Table3<TR> t3;
+            lookup3<TR>(mu_r, lamr, rt, t3);
+            const TR rhofacr = TR(SMA(A_RHOFACR, k));
+            v1 = double(apply_table3<TR>(tb, tb.vm, t3) * rhofacr);
+            v2 = double(apply_table3<TR>(tb, tb.vn, t3) * rhofacr);
+            R1[k] = nr_incld * cld;
+            lmax = vmax(lmax, v1 * dt_left * SMA(A_INVDZ, k));
+          }
+        } else {
+          double qi_incld, ni_incld, qm_incld, bm_incld;
+          if (first) {
+            const double inv_cld = 1 / cld;
+            const double inv_cld_l = 1 / in.cld_frac_l[o];
+            if (R0[k] >= C::QSMALL) {
+              qi_incld = R0[k] * inv_cld;
+              ni_incld = vmax(R1[k] * inv_cld, 0.);
+            } else {
+              qi_incld = 0;
+              ni_incld = 0;
+            }
+            if (R0[k] >= C::QSMALL && R2[k] >= C::QSMALL) {
+              qm_incld = R2[k] * inv_cld;
+              bm_incld = vmax(R3[k] * inv_cld_l, 0.);
+            } else {
+              qm_incld = 0;
+              bm_incld = 0;
+            }
+            qi_incld = vmin(qi_incld, C::incloud_limit);
+            bm_incld = vmin(bm_incld, C::incloud_limit);
+          } else {
+            qi_incld = R0[k] / cld;
+            ni_incld = R1[k] / cld;
+            qm_incld = R2[k] / cld;
+            bm_incld = R3[k] / cld;
+          }
+          if (qi_incld > C::QSMALL) {
+            ni_incld = vmax(ni_incld, C::NSMALL);
+            const double rhop = calc_bulk_rho_rime(qi_incld, qm_incld, bm_incld, rt);
+            R2[k] = qm_incld * cld;
+            R3[k] = bm_incld * cld;
+            TableIce<TR> ti;
+            lookup_ice<TR>(TR(qi_incld), TR(ni_incld), TR(qm_incld), TR(rhop), ti);
+            const TR tv_n = apply_table_ice<TR>(0, tb, ti);
+            const TR tv_q = apply_table_ice<TR>(1, tb, ti);
+            const TR tv_lmax = apply_table_ice<TR>(6, tb, ti);
+            const TR tv_lmin = apply_table_ice<TR>(7, tb, ti);
+            ni_incld = vmin(ni_incld, double(tv_lmax) * ni_incld);
+            ni_incld = vmax(ni_incld, double(tv_lmin) * ni_incld);
+            R1[k] = ni_incld * cld;
+            const TR rhofaci = TR(SMA(A_RHOFACI, k));
+            v1 = double(TR(rt.ice_sedimentation_factor) * tv_q * rhofaci);
+            v2 = double(TR(rt.ice_sedimentation_factor) * tv_n * rhofaci);
+            lmax = vmax(lmax, v1 * dt_left * SMA(A_INVDZ, k));
+          }
+        }
+        V1[k] = v1;
+        V2[k] = v2;
+      }
+      const double Co_max = group_max<LANES>(mask, lmax);
+      __syncwarp(mask);
+      if (!(Co_max >= 0) || Co_max > 2.0e9) {
+        err |= kErrNumeric;
+        break;
+      }
+
+      /* generalized_sedimentation + calc_first_order_upwind_step (kdir = -1) */
+      const int tmpint1 = static_cast<int>(Co_max + 1);
+      const double dt_sub = dt_left / tmpint1;
+      const int k_temp = (k_qxbot == kbot) ? k_qxbot : k_qxbot + 1;
+      double carry0 = 0, carry1 = 0, carry2 = 0, carry3 = 0, flux_bot = 0;
+      for (int base = k_qxtop; base <= k_temp; base += LANES) {
+        const int k = base + lane;
+        const bool act = k <= k_temp;
+        double f0 = 0, f1 = 0, f2 = 0, f3 = 0;
+        double rho = 0, invdz = 0, v1 = 0, v2 = 0;
+        if (act) {
+          rho = SMA(A_RHO, k);
+          invdz = SMA(A_INVDZ, k);
+          v1 = V1[k];
+          v2 = V2[k];
+          f0 = v1 * R0[k] * rho;
+          if (nfield > 1) f1 = v2 * R1[k] * rho;
+          if (nfield > 2) {
+            f2 = v1 * R2[k] * rho;
+            f3 = v1 * R3[k] * rho;
+          }
+        }
+        double u0 = __shfl_up_sync(mask, f0, 1, LANES);
+        double u1 = __shfl_up_sync(mask, f1, 1, LANES);
+        double u2 = __shfl_up_sync(mask, f2, 1, LANES);
+        double u3 = __shfl_up_sync(mask, f3, 1, LANES);
+        if (lane == 0) {
+          u0 = carry0; u1 = carry1; u2 = carry2; u3 = carry3;
+        }
+        if (act) {
+          const double irho = 1 / rho;
+          R0[k] += ((u0 - f0) * invdz) * dt_sub * irho;
+          if (nfield > 1) R1[k] += ((u1 - f1) * invdz) * dt_sub * irho;
+          if (nfield > 2) {
+            R2[k] += ((u2 - f2) * invdz) * dt_sub * irho;
+            R3[k] += ((u3 - f3) * invdz) * dt_sub * irho;
+          }
+          if (sp == 1) PF[k + 1] += f0;
+          if (k == kbot) flux_bot = f0;
+        }
+        carry0 = __shfl_sync(mask, f0, LANES - 1, LANES);
+        carry1 = __shfl_sync(mask, f1, LANES - 1, LANES);
+        carry2 = __shfl_sync(mask, f2, LANES - 1, LANES);
+        carry3 = __shfl_sync(mask, f3, LANES - 1, LANES);
+      }
+      if (k_qxbot == kbot) {
+        const int owner = (kbot - k_qxtop) % LANES;
+        const double fb = __shfl_sync(mask, flux_bot, owner, LANES);
+        prt_accum += fb * dt_sub;
+      } else {
+        k_qxbot += 1;
+      }
+      dt_left -= dt_sub;
+      first = false;
+      __syncwarp(mask);
+    }
+    if (sp == 0) precip_liq_surf = prt_accum * C::INV_RHO_H2O * inv_dt;
+    else if (sp == 1) precip_liq_surf += prt_accum * C::INV_RHO_H2O * inv_dt;
+    else precip_ice_surf += prt_accum * C::INV_RHO_H2O * inv_dt;
+
+    for (int k = lane; k < nk; k += LANES) {
+      g0[co + k] = R0[k];
+      g1[co + k] = R1[k];
+      if (sp == 2) {
+        in.qm[co + k] = R2[k];
+        in.bm[co + k] = R3[k];
+      }
+    }
+    if (sp == 1) {
+      for (int k = lane; k <= nk; k += LANES) in.precip_liq_flux[ci + k] = PF[k];
+    }
+    __syncwarp(mask);
+  }
+  if (lane == 0) {
+    in.precip_liq_surf[col] = precip_liq_surf;
+    in.precip_ice_surf[col] = precip_ice_surf;
+  }
+
+  /* ---------------- phase 4: homogeneous freezing + p3_main_part3 ---------------- */
+  for (int k = lane; k < nk; k += LANES) {
+    const int64_t o = co + k;
+    State s;
+    s.qc = in.qc[o]; s.nc = in.nc[o]; s.qr = in.qr[o]; s.nr = in.nr[o];
+    s.qi = in.qi[o]; s.qm = in.qm[o]; s.ni = in.ni[o]; s.bm = in.bm[o];
+    s.qv = in.qv[o]; s.th = in.th[o];
+    const double inv_exner = in.inv_exner[o];
+    const double cld_l = in.cld_frac_l[o], cld_r = in.cld_frac_r[o], cld_i = in.cld_frac_i[o];
+    const double rho = SMA(A_RHO, k);
+    const double inv_rho = 1 / rho;
+    double vap_liq = in.vap_liq_exchange[o];
+    double eff_qc = in.diag_eff_radius_qc[o], eff_qr = in.diag_eff_radius_qr[o], eff_qi = in.diag_eff_radius_qi[o];
+    double rho_qi = 0;
+
+    /* homogeneous_freezing, p3/impl/p3_ice_sed_impl.hpp:207-270 */
+    if (do_ice && SMA(A_TATM, k) < C::T_homogfrz) {
+      const double Qc_nuc = s.qc, Qr_nuc = s.qr;
+      const double Nc_nuc = vmax(s.nc, C::NSMALL), Nr_nuc = vmax(s.nr, C::NSMALL);
+      const bool qc_ge = s.qc >= C::QSMALL, qr_ge = s.qr >= C::QSMALL;
+      if (qc_ge) {
+        s.qm = s.qm + Qc_nuc;
+        s.qi = s.qi + Qc_nuc;
+        s.bm = s.bm + Qc_nuc * C::INV_RHO_RIMEMAX;
+        s.ni = s.ni + Nc_nuc;
+        s.th = s.th + inv_exner * Qc_nuc * C::LatIce * C::INV_CP;
+      }
+      if (qr_ge) {
+        s.qm = s.qm + Qr_nuc;
+        s.qi = s.qi + Qr_nuc;
+        s.bm = s.bm + Qr_nuc * C::INV_RHO_RIMEMAX;
+        s.ni = s.ni + Nr_nuc;
+        s.th = s.th + inv_exner * Qr_nuc * C::LatIce * C::INV_CP;
+      }
+      if (qc_ge) { s.qc = 0; s.nc = 0; }
+      if (qr_ge) { s.qr = 0; s.nr = 0; }
+    }
+
+    /* part3: cloud */
+    if (s.qc >= C::QSMALL) {
+      const double qc_incld = s.qc / cld_l;
+      double nc_incld = s.nc / cld_l;
+      TR mu_c, lamc, cd, cd1;
+      const TR n_in = TR(nc_incld);
+      TR n_out = n_in;
+      get_cloud_dsd2<TR>(TR(qc_incld), n_out, mu_c, TR(rho), lamc, cd, cd1);
+      apply_n_adjust(nc_incld, n_in, n_out);
+      s.nc = nc_incld * cld_l;
+      eff_qc = double(TR(0.5) * (mu_c + TR(3)) / lamc);
+    } else {
+      s.qv = s.qv + s.qc;
+      s.th = s.th - inv_exner * s.qc * C::LatVap * C::INV_CP;
+      vap_liq = vap_liq - s.qc;
+      s.qc = 0;
+      s.nc = 0;
+    }
+    /* part3: rain */
+    if (s.qr >= C::QSMALL) {
+      const double qr_incld = s.qr / cld_r;
+      double nr_incld = s.nr / cld_r;
+      TR mu_r = 0, lamr;
+      const TR n_in = TR(nr_incld);
+      TR n_out = n_in;
+      get_rain_dsd2<TR>(TR(qr_incld), n_out, mu_r, lamr, rt);
+      apply_n_adjust(nr_incld, n_in, n_out);
+      s.nr = nr_incld * cld_r;
+      eff_qr = double(TR(1.5) / lamr);
+    } else {
+      s.qv = s.qv + s.qr;
+      s.th = s.th - inv_exner * s.qr * C::LatVap * C::INV_CP;
+      vap_liq = vap_liq - s.qr;
+      s.qr = 0;
+      s.nr = 0;
+    }
+    /* part3: ice */
+    {
+      const bool qi_gt_small = s.qi >= C::QSMALL;
+      s.ni = vmax(s.ni, C::NSMALL);
+      const double qi_incld = s.qi / cld_i;
+      double ni_incld = s.ni / cld_i;
+      double qm_incld = s.qm / cld_i;
+      double bm_incld = s.bm / cld_i;
+      double rhop = 0;
+      if (qi_gt_small) {
+        rhop = calc_bulk_rho_rime(qi_incld, qm_incld, bm_incld, rt);
+        s.qm = qm_incld * cld_i;
+        s.bm = bm_incld * cld_i;
+      }
+      impose_max_total_ni(ni_incld, rt.max_total_ni, inv_rho);
+      if (qi_gt_small) {
+        TableIce<TR> ti;
+        lookup_ice<TR>(TR(qi_incld), TR(ni_incld), TR(qm_incld), TR(rhop), ti);
+        const TR tv_eff = apply_table_ice<TR>(5, tb, ti);
+        const TR tv_lmax = apply_table_ice<TR>(6, tb, ti);
+        const TR tv_lmin = apply_table_ice<TR>(7, tb, ti);
+        const TR tv_dens = apply_table_ice<TR>(11, tb, ti);
+        ni_incld = vmin(ni_incld, double(tv_lmax) * ni_incld);
+        ni_incld = vmax(ni_incld, double(tv_lmin) * ni_incld);
+        eff_qi = double(tv_eff);
+        rho_qi = double(tv_dens);
+      }
+      s.ni = ni_incld * cld_i;
+      if (s.qm < C::QSMALL && qi_gt_small) {
+        s.qm = 0;
+        s.bm = 0;
+      }
+      if (!qi_gt_small) {
+        s.qv = s.qv + s.qi;
+        s.th = s.th - inv_exner * s.qi * (C::LatVap + C::LatIce) * C::INV_CP;
+        s.qi = 0; s.ni = 0; s.qm = 0; s.bm = 0;
+      }
+    }
+    if (s.qr < C::QSMALL) s.nr = 0;
+
+    in.qc[o] = s.qc; in.nc[o] = s.nc; in.qr[o] = s.qr; in.nr[o] = s.nr;
+    in.qi[o] = s.qi; in.qm[o] = s.qm; in.ni[o] = s.ni; in.bm[o] = s.bm;
+    in.qv[o] = s.qv; in.th[o] = s.th;
+    in.vap_liq_exchange[o] = vap_liq;
+    in.diag_eff_radius_qc[o] = eff_qc;
+    in.diag_eff_radius_qr[o] = eff_qr;
+    in.diag_eff_radius_qi[o] = eff_qi;
+    in.rho_qi[o] = rho_qi;
+  }
+#undef SMA
+}
+
+/* ------------------------------------------------------------------ */
+/* kernel                                                              */
+/* ------------------------------------------------------------------ */
+template <class TR, int LANES>
+__global__ void __launch_bounds__(256) p3_main_kernel(const Inst inst0, const KParams<TR> kp) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint32_t err = 0;
+  double* group_base;
+  Tabs<TR> tb;
+  tb.collect = kp.collect;
+  if (kp.staged) {
+    TR* s_ice = reinterpret_cast<TR*>(smem_raw);
+    TR* s_t3 = s_ice + kIceTableElems;
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw + table_smem_bytes<TR>() - 16);
+    const bool ok = stage_tables<TR>(kp, s_ice, s_t3, mbar, err);
+    if (!ok) {
+      if (threadIdx.x == 0) atomicOr(kp.err, err);
+      return;
+    }
+    tb.ice = s_ice;
+    tb.vn = s_t3;
+    tb.vm = s_t3 + 600;
+    tb.revap = s_t3 + 1200;
+    tb.t3_stride = 2;
+    tb.t3_j0 = kp.rt.t3_dumjj - 1;
+    group_base = reinterpret_cast<double*>(smem_raw + table_smem_bytes<TR>());
+  } else {
+    tb.ice = kp.ice;
+    tb.vn = kp.vn;
+    tb.vm = kp.vm;
+    tb.revap = kp.revap;
+    tb.t3_stride = kVT1;
+    tb.t3_j0 = 0;
+    group_base = reinterpret_cast<double*>(smem_raw);
+  }
+  const int g_in_block = threadIdx.x / LANES;
+  double* sm = group_base + size_t(g_in_block) * A_NARR * kp.sm_stride;
+  /* liquid saturation vapour pressure at 0 C (qsat0 of ice_melting and
+   * ice_cldliq_wet_growth), evaluated once */
+  const double esat0 = double(murphy_koop_svp<TR>(TR(C::Tmelt), false, err));
+
+  const int groups_total = gridDim.x * kp.groups_per_block;
+  for (int w = blockIdx.x * kp.groups_per_block + g_in_block; w < kp.nwork; w += groups_total) {
+    if (kp.work) {
+      const WorkItem wi = kp.work[w];
+      p3_column<TR, LANES>(kp.insts[wi.inst], wi.col, kp, tb, sm, esat0, err);
+    } else {
+      p3_column<TR, LANES>(inst0, w, kp, tb, sm, esat0, err);
+    }
+  }
+  if (err) atomicOr(kp.err, err);
+}
+
+}  // namespace dev
+}  // namespace p3x

@@ -1,0 +1,7 @@
+/* Column kernel instantiation: rate type double, 8 lanes per column. */
+#include "p3x_kernels_impl.cuh"
+
+namespace p3x {
+template cudaError_t launch_p3_lanes<double, 8>(const dev::Inst&, const dev::KParams<double>&,
+                                                  const LaunchSpec&, int, cudaStream_t);
+}  // namespace p3x

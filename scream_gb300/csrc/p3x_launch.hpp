@@ -1,0 +1,55 @@
+/* Host-side launch interface of the device kernels (internal to libp3x). */
+#ifndef P3X_LAUNCH_HPP
+#define P3X_LAUNCH_HPP
+
+#include <cuda_runtime.h>
+
+#include "p3x_column.cuh"
+
+namespace p3x {
+
+struct LaunchSpec {
+  int lanes;            /* 8, 16, 32 */
+  int groups_per_block; /* columns per CTA */
+  int staged;           /* tables in shared memory */
+  int blocks_per_sm;    /* 0: as many as fit */
+};
+
+/* Shared-memory bytes of one CTA. */
+template <class TR>
+inline size_t p3_smem_bytes(const LaunchSpec& ls, int sm_stride) {
+  const size_t tables = ls.staged ? dev::table_smem_bytes<TR>() : 0;
+  return tables + size_t(ls.groups_per_block) * dev::A_NARR * size_t(sm_stride) * sizeof(double);
+}
+
+/* Persistent launch of the column kernel for one lane count (defined in
+ * p3x_kernels_impl.cuh, instantiated in p3x_k_*.cu).  kp.nwork, kp.work,
+ * kp.insts and kp.sm_stride are set by the caller. */
+template <class TR, int LANES>
+cudaError_t launch_p3_lanes(const dev::Inst& inst0, const dev::KParams<TR>& kp, const LaunchSpec& ls,
+                            int num_sms, cudaStream_t stream);
+
+template <class TR>
+inline cudaError_t launch_p3(const dev::Inst& inst0, const dev::KParams<TR>& kp, const LaunchSpec& ls,
+                             int num_sms, cudaStream_t stream) {
+  switch (ls.lanes) {
+    case 8: return launch_p3_lanes<TR, 8>(inst0, kp, ls, num_sms, stream);
+    case 16: return launch_p3_lanes<TR, 16>(inst0, kp, ls, num_sms, stream);
+    case 32: return launch_p3_lanes<TR, 32>(inst0, kp, ls, num_sms, stream);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+/* (nlev, ncol) column-fastest <-> (ncol, ld) level-contiguous transposes. */
+cudaError_t launch_transpose_to_levels(const double* src, double* dst, int ncol, int nlev, int64_t ld,
+                                       cudaStream_t st);
+cudaError_t launch_transpose_to_columns(const double* src, double* dst, int ncol, int nlev, int64_t ld,
+                                        cudaStream_t st);
+
+cudaError_t launch_budgets(const double* qv, const double* qc, const double* qr, const double* qi,
+                           const double* th, const double* dpres, const double* inv_exner, int ncol,
+                           int nlev, int64_t ld, double* water, double* energy, cudaStream_t st);
+
+}  // namespace p3x
+
+#endif

@@ -1,0 +1,964 @@
+/*
+ * Device physics of the P3 step, templated on the process-rate type TR
+ * (double: plain form; float: FP32-bulk form).  State (mixing ratios,
+ * numbers, theta, qv), saturation residuals, conservation limiters and the
+ * prognostic updates are always FP64.
+ *
+ * Each routine states the same formula as the reference routine it names
+ * (paths relative to components/eamxx/src/physics/), in the same order of
+ * operations, so the FP64 form differs from the CPU reference only by the
+ * rounding of the math library and fused multiply-adds.
+ */
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace p3x {
+namespace dev {
+
+/* share/physics_constants.hpp:27-102 */
+namespace C {
+constexpr double Cpair = 1004.64, Rair = 287.042, RH2O = 461.505, RV = RH2O;
+constexpr double RHO_H2O = 1000.0, INV_RHO_H2O = 1.0 / RHO_H2O;
+constexpr double ep_2 = 18.016 / 28.966;
+constexpr double gravit = 9.80616, LatVap = 2501000.0, LatIce = 333700.0, CpLiq = 4188.0;
+constexpr double Tmelt = 273.15, T_zerodegc = Tmelt, T_homogfrz = Tmelt - 40, T_rainfrz = Tmelt - 4;
+constexpr double Pi = 3.14159265358979323;
+constexpr double INV_RHO_RIMEMAX = 1.0 / 900.0;
+constexpr double THIRD = 1.0 / 3.0, SXTH = 1.0 / 6.0, PIOV3 = Pi * THIRD, PIOV6 = Pi * SXTH;
+constexpr double BIMM = 2.0, CONS1 = PIOV6 * RHO_H2O, CONS2 = 4. * PIOV3 * RHO_H2O;
+constexpr double CONS3 = 1.0 / (CONS2 * 1.562500000000000e-14);
+constexpr double CONS5 = PIOV6 * BIMM, CONS6 = PIOV6 * PIOV6 * RHO_H2O * BIMM;
+constexpr double QSMALL = 1.e-14, QTENDSMALL = 1e-20, BSMALL = 1.e-15, NSMALL = 1.e-16;
+constexpr double P0 = 100000.0, RD = Rair;
+constexpr double RHO_1000MB = P0 / (RD * Tmelt), RHO_600MB = 60000 / (RD * 253.15);
+constexpr double CP = Cpair, INV_CP = 1.0 / CP;
+constexpr double dt_left_tol = 1.e-4, bcn = 2., dropmass = 5.2e-7, NCCNST = 200.0e+6;
+constexpr double incloud_limit = 5.1e-3, precip_limit = 1.0e-2, f1r = 0.78, f2r = 0.32;
+constexpr double nmltratio = 1.0;
+constexpr double lookup_table_1a_dum1_c = 4.135985029041767e+00;
+}  // namespace C
+
+constexpr int kDensize = 5, kRimsize = 4, kIsize = 50, kIceCols = 12, kRcollsize = 30,
+              kCollCols = 2, kVT1 = 10;
+
+/* status bits accumulated on the device */
+enum : uint32_t { kErrNumeric = 1u, kErrSubstep = 2u, kErrWait = 4u };
+
+/* Runtime options, P3Runtime (p3/p3_functions.hpp:112-133). */
+struct RuntimeDev {
+  double max_total_ni, autoconversion_prefactor, autoconversion_qc_exponent,
+      autoconversion_nc_exponent, autoconversion_radius, accretion_prefactor,
+      accretion_qc_exponent, accretion_qr_exponent, rain_selfcollection_prefactor,
+      rain_selfcollection_breakup_diameter, constant_mu_rain, spa_ccn_to_nc_factor,
+      cldliq_to_ice_collection_factor, rain_to_ice_collection_factor, min_rime_rho, max_rime_rho,
+      immersion_freezing_exponent, deposition_nucleation_exponent, ice_sedimentation_factor;
+  int do_ice_production;
+  /* derived once on the host */
+  double cons3;       /* autoconversion CONS3 (p3_autoconversion_impl.hpp:27-32) */
+  int t3_dumjj;       /* Table3 mu index for the constant mu_r (p3_table3_impl.hpp:52-62) */
+  double t3_rdumjj;
+};
+
+/* ------------------------------------------------------------------ */
+/* math wrappers (explicit precision)                                  */
+/* ------------------------------------------------------------------ */
+__device__ __forceinline__ double m_exp(double x) { return exp(x); }
+__device__ __forceinline__ float m_exp(float x) { return expf(x); }
+__device__ __forceinline__ double m_log(double x) { return log(x); }
+__device__ __forceinline__ float m_log(float x) { return logf(x); }
+__device__ __forceinline__ double m_log10(double x) { return log10(x); }
+__device__ __forceinline__ float m_log10(float x) { return log10f(x); }
+__device__ __forceinline__ double m_pow(double x, double y) { return pow(x, y); }
+__device__ __forceinline__ float m_pow(float x, float y) { return powf(x, y); }
+__device__ __forceinline__ double m_cbrt(double x) { return cbrt(x); }
+__device__ __forceinline__ float m_cbrt(float x) { return cbrtf(x); }
+__device__ __forceinline__ double m_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float m_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double m_tgamma(double x) { return tgamma(x); }
+__device__ __forceinline__ float m_tgamma(float x) { return tgammaf(x); }
+__device__ __forceinline__ double m_expm1(double x) { return expm1(x); }
+__device__ __forceinline__ float m_expm1(float x) { return expm1f(x); }
+__device__ __forceinline__ double m_tanh(double x) { return tanh(x); }
+__device__ __forceinline__ float m_tanh(float x) { return tanhf(x); }
+__device__ __forceinline__ double m_fabs(double x) { return fabs(x); }
+__device__ __forceinline__ float m_fabs(float x) { return fabsf(x); }
+
+/* std::max / std::min semantics ((a < b) ? b : a), as the CPU reference. */
+template <class T> __device__ __forceinline__ T vmax(T a, T b) { return (a < b) ? b : a; }
+template <class T> __device__ __forceinline__ T vmin(T a, T b) { return (b < a) ? b : a; }
+template <class T> __device__ __forceinline__ T sq(T x) { return x * x; }
+
+/* ------------------------------------------------------------------ */
+/* Saturation (share/physics_saturation_impl.hpp)                      */
+/* ------------------------------------------------------------------ */
+
+/* MurphyKoop_svp, physics_saturation_impl.hpp:38-81.  T <= 0 or NaN sets the
+ * numeric status bit (the reference aborts the kernel there). */
+template <class TR>
+__device__ __forceinline__ TR murphy_koop_svp(TR t, bool ice, uint32_t& err) {
+  if (!(t > TR(0))) err |= kErrNumeric;
+  if (t < TR(C::Tmelt) && ice) {
+    return m_exp(TR(9.550426) - (TR(5723.265) / t) + (TR(3.53068) * m_log(t)) - (TR(0.00728332) * t));
+  }
+  const TR logt = m_log(t);
+  return m_exp(TR(54.842763) - (TR(6763.22) / t) - (TR(4.210) * logt) + (TR(0.000367) * t) +
+               (m_tanh(TR(0.0415) * (t - TR(218.8))) *
+                (TR(53.878) - (TR(1331.22) / t) - (TR(9.44523) * logt) + TR(0.014025) * t)));
+}
+
+/* qv_sat_dry (MurphyKoop), physics_saturation_impl.hpp:126-157.  The vapour
+ * pressure is evaluated in TR; the mixing ratio is formed in FP64. */
+template <class TR>
+__device__ __forceinline__ double qv_sat_dry(double t, double p, bool ice, uint32_t& err) {
+  const double e_pres = double(murphy_koop_svp<TR>(TR(t), ice, err));
+  return C::ep_2 * e_pres / vmax(p, 1.e-3);
+}
+
+/* ------------------------------------------------------------------ */
+/* Tables                                                              */
+/* ------------------------------------------------------------------ */
+/* Table pointers (global or staged shared memory; generic addresses).
+ * t3 tables may be the full [300][10] arrays (t3_stride = 10, t3_j0 = 0) or
+ * a staged two-column slice (t3_stride = 2, t3_j0 = first staged column). */
+template <class TR>
+struct Tabs {
+  const TR* ice;
+  const TR* collect;
+  const TR* vn;
+  const TR* vm;
+  const TR* revap;
+  int t3_stride, t3_j0;
+};
+
+template <class TR>
+__device__ __forceinline__ TR ice_at(const Tabs<TR>& t, int jj, int ii, int i, int idx) {
+  return t.ice[((jj * kRimsize + ii) * kIsize + i) * kIceCols + idx];
+}
+template <class TR>
+__device__ __forceinline__ TR coll_at(const Tabs<TR>& t, int jj, int ii, int i, int j, int idx) {
+  return __ldg(&t.collect[(((jj * kRimsize + ii) * kIsize + i) * kRcollsize + j) * kCollCols + idx]);
+}
+template <class TR>
+__device__ __forceinline__ TR t3_at(const Tabs<TR>& t, const TR* tab, int i, int j) {
+  return tab[i * t.t3_stride + (j - t.t3_j0)];
+}
+
+template <class TR>
+struct TableIce {
+  int dumi, dumjj, dumii;
+  TR dum1, dum4, dum5;
+};
+template <class TR>
+struct TableRain {
+  int dumj;
+  TR dum3;
+};
+template <class TR>
+struct Table3 {
+  int dumii, dumjj;
+  TR rdumii, rdumjj;
+};
+
+/* lookup_ice, p3/impl/p3_table_ice_impl.hpp:80-138 */
+template <class TR>
+__device__ __forceinline__ void lookup_ice(TR qi, TR ni, TR qm, TR rhop, TableIce<TR>& tab) {
+  tab.dum1 = (m_log10(qi / ni) + TR(18)) * TR(C::lookup_table_1a_dum1_c) - TR(10);
+  tab.dumi = static_cast<int>(tab.dum1);
+  tab.dum1 = vmin(tab.dum1, TR(kIsize));
+  tab.dum1 = vmax(tab.dum1, TR(1.));
+  tab.dumi = max(1, tab.dumi);
+  tab.dumi = min(kIsize - 1, tab.dumi);
+  tab.dum4 = (qm / qi) * TR(3) + TR(1);
+  tab.dumii = static_cast<int>(tab.dum4);
+  tab.dum4 = vmin(tab.dum4, TR(kRimsize));
+  tab.dum4 = vmax(tab.dum4, TR(1.));
+  tab.dumii = max(1, tab.dumii);
+  tab.dumii = min(kRimsize - 1, tab.dumii);
+  if (rhop <= TR(650)) {
+    tab.dum5 = (rhop - TR(50)) * TR(0.005) + TR(1);
+  } else {
+    tab.dum5 = (rhop - TR(650)) * TR(0.004) + TR(4);
+  }
+  tab.dumjj = static_cast<int>(tab.dum5);
+  tab.dum5 = vmin(tab.dum5, TR(kDensize));
+  tab.dum5 = vmax(tab.dum5, TR(1.));
+  tab.dumjj = max(1, tab.dumjj);
+  tab.dumjj = min(kDensize - 1, tab.dumjj);
+  tab.dumi -= 1;
+  tab.dumjj -= 1;
+  tab.dumii -= 1;
+}
+
+/* lookup_rain, p3_table_ice_impl.hpp:140-173 */
+template <class TR>
+__device__ __forceinline__ void lookup_rain(TR qr, TR nr, TableRain<TR>& tab) {
+  const bool gt_small = qr > TR(C::QSMALL) && nr > TR(0.0);
+  TR dumlr = TR(1);
+  if (gt_small) dumlr = m_cbrt(qr / (TR(C::Pi) * TR(C::RHO_H2O) * nr));
+  tab.dum3 = (m_log10(TR(1) * dumlr) + TR(5)) * TR(10.70415);
+  tab.dumj = static_cast<int>(tab.dum3);
+  tab.dum3 = vmin(tab.dum3, TR(kRcollsize));
+  tab.dum3 = vmax(tab.dum3, TR(1));
+  tab.dumj = max(1, tab.dumj);
+  tab.dumj = min(kRcollsize - 1, tab.dumj);
+  if (!gt_small) {
+    tab.dumj = 1;
+    tab.dum3 = TR(1);
+  }
+  tab.dumj -= 1;
+}
+
+/* apply_table_ice, p3_table_ice_impl.hpp:175-212 */
+template <class TR>
+__device__ __forceinline__ TR apply_table_ice(int idx, const Tabs<TR>& t, const TableIce<TR>& tab) {
+  const TR w1 = tab.dum1 - TR(tab.dumi) - TR(1);
+  const TR w4 = tab.dum4 - TR(tab.dumii) - TR(1);
+  const TR w5 = tab.dum5 - TR(tab.dumjj) - TR(1);
+  const TR a00 = ice_at(t, tab.dumjj, tab.dumii, tab.dumi, idx);
+  const TR a01 = ice_at(t, tab.dumjj, tab.dumii, tab.dumi + 1, idx);
+  const TR a10 = ice_at(t, tab.dumjj, tab.dumii + 1, tab.dumi, idx);
+  const TR a11 = ice_at(t, tab.dumjj, tab.dumii + 1, tab.dumi + 1, idx);
+  const TR b00 = ice_at(t, tab.dumjj + 1, tab.dumii, tab.dumi, idx);
+  const TR b01 = ice_at(t, tab.dumjj + 1, tab.dumii, tab.dumi + 1, idx);
+  const TR b10 = ice_at(t, tab.dumjj + 1, tab.dumii + 1, tab.dumi, idx);
+  const TR b11 = ice_at(t, tab.dumjj + 1, tab.dumii + 1, tab.dumi + 1, idx);
+  TR iproc1 = a00 + w1 * (a01 - a00);
+  TR gproc1 = a10 + w1 * (a11 - a10);
+  const TR tmp1 = iproc1 + w4 * (gproc1 - iproc1);
+  iproc1 = b00 + w1 * (b01 - b00);
+  gproc1 = b10 + w1 * (b11 - b10);
+  const TR tmp2 = iproc1 + w4 * (gproc1 - iproc1);
+  return tmp1 + w5 * (tmp2 - tmp1);
+}
+
+/* apply_table_coll, p3_table_ice_impl.hpp:214-297 */
+template <class TR>
+__device__ __forceinline__ TR apply_table_coll(int idx, const Tabs<TR>& t, const TableIce<TR>& ti,
+                                               const TableRain<TR>& tr) {
+  const TR w1 = ti.dum1 - TR(ti.dumi) - TR(1);
+  const TR w3 = tr.dum3 - TR(tr.dumj) - TR(1);
+  const TR w4 = ti.dum4 - TR(ti.dumii) - TR(1);
+  const TR w5 = ti.dum5 - TR(ti.dumjj) - TR(1);
+  TR tmp[2];
+#pragma unroll
+  for (int dj = 0; dj < 2; ++dj) {
+    const int jj = ti.dumjj + dj;
+    TR v[2];
+#pragma unroll
+    for (int di = 0; di < 2; ++di) {
+      const int ii = ti.dumii + di;
+      const TR c00 = coll_at(t, jj, ii, ti.dumi, tr.dumj, idx);
+      const TR c10 = coll_at(t, jj, ii, ti.dumi + 1, tr.dumj, idx);
+      const TR c01 = coll_at(t, jj, ii, ti.dumi, tr.dumj + 1, idx);
+      const TR c11 = coll_at(t, jj, ii, ti.dumi + 1, tr.dumj + 1, idx);
+      const TR dproc1 = c00 + w1 * (c10 - c00);
+      const TR dproc2 = c01 + w1 * (c11 - c01);
+      v[di] = dproc1 + w3 * (dproc2 - dproc1);
+    }
+    tmp[dj] = v[0] + w4 * (v[1] - v[0]);
+  }
+  return tmp[0] + w5 * (tmp[1] - tmp[0]);
+}
+
+/* lookup (Table3), p3_table3_impl.hpp:14-64.  The mu index is fixed by the
+ * constant rain shape parameter and precomputed (rt.t3_dumjj/t3_rdumjj). */
+template <class TR>
+__device__ __forceinline__ void lookup3(TR mu_r, TR lamr, const RuntimeDev& rt, Table3<TR>& tab) {
+  const TR dum1 = (mu_r + TR(1)) / lamr;
+  if (dum1 <= TR(195.e-6)) {
+    const TR inv_dum3 = TR(0.1);
+    TR rdumii = (dum1 * TR(1.e6) + TR(5)) * inv_dum3;
+    rdumii = vmax(rdumii, TR(1.0));
+    rdumii = vmin(rdumii, TR(20.0));
+    int dumii = static_cast<int>(rdumii);
+    dumii = max(dumii, 1);
+    dumii = min(dumii, 20);
+    tab.rdumii = rdumii;
+    tab.dumii = dumii;
+  } else {
+    const TR inv_dum3 = TR(C::THIRD * 0.1);
+    TR rdumii = (dum1 * TR(1.e+6) - TR(195)) * inv_dum3 + TR(20);
+    rdumii = vmax(rdumii, TR(20.0));
+    rdumii = vmin(rdumii, TR(300.0));
+    int dumii = static_cast<int>(rdumii);
+    dumii = max(dumii, 20);
+    dumii = min(dumii, 299);
+    tab.rdumii = rdumii;
+    tab.dumii = dumii;
+  }
+  tab.rdumjj = TR(rt.t3_rdumjj);
+  tab.dumjj = rt.t3_dumjj;
+}
+
+/* apply_table (Table3), p3_table3_impl.hpp:66-83 */
+template <class TR>
+__device__ __forceinline__ TR apply_table3(const Tabs<TR>& t, const TR* table, const Table3<TR>& t3) {
+  const TR rdumii_m_dumii = t3.rdumii - TR(t3.dumii);
+  const TR t_im1_jm1 = t3_at(t, table, t3.dumii - 1, t3.dumjj - 1);
+  const TR dum1 = (t_im1_jm1 + rdumii_m_dumii * (t3_at(t, table, t3.dumii, t3.dumjj - 1) - t_im1_jm1));
+  const TR t_im1_j = t3_at(t, table, t3.dumii - 1, t3.dumjj);
+  const TR dum2 = (t_im1_j + rdumii_m_dumii * (t3_at(t, table, t3.dumii, t3.dumjj) - t_im1_j));
+  return dum1 + (t3.rdumjj - TR(t3.dumjj)) * (dum2 - dum1);
+}
+
+/* ------------------------------------------------------------------ */
+/* In-cloud values and DSD                                              */
+/* ------------------------------------------------------------------ */
+
+/* calculate_incloud_mixingratios, p3/impl/p3_incloud_mixingratios_impl.hpp:12-69
+ * (bm_incld uses inv_cld_frac_l, line 49).  FP64. */
+struct Incld {
+  double qc, qr, qi, qm, nc, nr, ni, bm;
+};
+__device__ __forceinline__ void calc_incloud(double qc, double qr, double qi, double qm, double nc,
+                                             double nr, double ni, double bm, double inv_cld_l,
+                                             double inv_cld_i, double inv_cld_r, Incld& o) {
+  if (qc >= C::QSMALL) { o.qc = qc * inv_cld_l; o.nc = vmax(nc * inv_cld_l, 0.); }
+  else { o.qc = 0; o.nc = 0; }
+  if (qi >= C::QSMALL) { o.qi = qi * inv_cld_i; o.ni = vmax(ni * inv_cld_i, 0.); }
+  else { o.qi = 0; o.ni = 0; }
+  if (qi >= C::QSMALL && qm >= C::QSMALL) { o.qm = qm * inv_cld_i; o.bm = vmax(bm * inv_cld_l, 0.); }
+  else { o.qm = 0; o.bm = 0; }
+  if (qr >= C::QSMALL) { o.qr = qr * inv_cld_r; o.nr = vmax(nr * inv_cld_r, 0.); }
+  else { o.qr = 0; o.nr = 0; }
+  if (o.qc > C::incloud_limit || o.qi > C::incloud_limit || o.qr > C::precip_limit ||
+      o.bm > C::incloud_limit) {
+    o.qc = vmin(o.qc, C::incloud_limit);
+    o.qi = vmin(o.qi, C::incloud_limit);
+    o.bm = vmin(o.bm, C::incloud_limit);
+    o.qr = vmin(o.qr, C::precip_limit);
+  }
+}
+
+/* get_cloud_dsd2, p3/impl/p3_dsd2_impl.hpp:14-74 (iparam = 3) */
+template <class TR>
+__device__ __forceinline__ void get_cloud_dsd2(TR qc, TR& nc, TR& mu_c, TR rho, TR& lamc, TR& cdist,
+                                               TR& cdist1) {
+  lamc = 0; cdist = 0; cdist1 = 0; mu_c = 0;
+  if (qc >= TR(C::QSMALL)) {
+    nc = vmax(nc, TR(C::NSMALL));
+    TR mu = TR(0.0005714) * (nc * TR(1.e-6) * rho) + TR(0.2714);
+    mu = TR(1) / (mu * mu) - TR(1);
+    mu = vmax(mu, TR(2.));
+    mu = vmin(mu, TR(15.));
+    mu_c = mu;
+    lamc = m_cbrt(TR(C::CONS1) * nc * (mu_c + TR(3)) * (mu_c + TR(2)) * (mu_c + TR(1)) / qc);
+    const TR lammin = (mu_c + TR(1)) * TR(2.5e+4);
+    const TR lammax = (mu_c + TR(1)) * TR(1.e+6);
+    const bool lt = lamc < lammin, gt = lamc > lammax;
+    if (lt) lamc = lammin;
+    if (gt) lamc = lammax;
+    if (lt || gt) {
+      nc = TR(6) * (lamc * lamc * lamc) * qc /
+           (TR(C::Pi) * TR(C::RHO_H2O) * (mu_c + TR(3)) * (mu_c + TR(2)) * (mu_c + TR(1)));
+    }
+    cdist = nc * (mu_c + TR(1)) / lamc;
+    cdist1 = nc / m_tgamma(mu_c + TR(1));
+  }
+}
+
+/* get_rain_dsd2, p3_dsd2_impl.hpp:76-126 */
+template <class TR>
+__device__ __forceinline__ void get_rain_dsd2(TR qr, TR& nr, TR& mu_r, TR& lamr, const RuntimeDev& rt) {
+  lamr = 0;
+  if (qr >= TR(C::QSMALL)) {
+    const TR nr_lim = vmax(nr, TR(C::NSMALL));
+    mu_r = TR(rt.constant_mu_rain);
+    const TR f = TR(C::CONS1) * (mu_r + TR(3)) * (mu_r + TR(2)) * (mu_r + TR(1));
+    lamr = m_cbrt(f * nr_lim / qr);
+    const TR lammax = (mu_r + TR(1.)) * TR(1.e+5);
+    const TR lammin = (mu_r + TR(1.)) * TR(500);
+    const bool lt = lamr < lammin, gt = lamr > lammax;
+    nr = nr_lim;
+    if (lt || gt) {
+      if (lt) lamr = lammin;
+      if (gt) lamr = lammax;
+      nr = lamr * lamr * lamr * qr / f;
+    }
+  }
+}
+
+/* impose_max_total_ni, p3_impose_max_total_ni_impl.hpp:9-27 */
+template <class T>
+__device__ __forceinline__ void impose_max_total_ni(T& ni_local, double max_total_ni, T inv_rho_local) {
+  if (ni_local >= T(1e-20)) ni_local = ni_local * vmin(T(max_total_ni) * inv_rho_local / ni_local, T(1.));
+}
+
+/* calc_bulk_rho_rime, p3/impl/p3_ice_sed_impl.hpp:14-64 */
+template <class T>
+__device__ __forceinline__ T calc_bulk_rho_rime(T qi_tot, T& qi_rim, T& bi_rim, const RuntimeDev& rt) {
+  T rho_rime = 0;
+  const bool gt = bi_rim >= T(C::BSMALL);
+  const bool lt = bi_rim < T(C::BSMALL);
+  if (gt) rho_rime = qi_rim / bi_rim;
+  const bool rr_lt_min = rho_rime < T(rt.min_rime_rho);
+  const bool rr_gt_max = rho_rime > T(rt.max_rime_rho);
+  if (gt && rr_lt_min) rho_rime = T(rt.min_rime_rho);
+  if (gt && rr_gt_max) rho_rime = T(rt.max_rime_rho);
+  if (gt && (rr_gt_max || rr_lt_min)) bi_rim = qi_rim / rho_rime;
+  if (lt) { qi_rim = 0; bi_rim = 0; rho_rime = 0; }
+  if (qi_rim > qi_tot && rho_rime > T(0)) { qi_rim = qi_tot; bi_rim = qi_rim / rho_rime; }
+  if (qi_rim < T(C::QSMALL)) { qi_rim = 0; bi_rim = 0; }
+  return rho_rime;
+}
+
+/* ------------------------------------------------------------------ */
+/* Process rates (all in-cloud, TR)                                    */
+/* ------------------------------------------------------------------ */
+template <class TR>
+struct Rates {
+  TR qc2qr_accret_tend, qr2qv_evap_tend, qc2qr_autoconv_tend, nc_accret_tend, nc_selfcollect_tend,
+      nc2nr_autoconv_tend, nr_selfcollect_tend, nr_evap_tend, ncautr, qi2qv_sublim_tend,
+      nr_ice_shed_tend, qc2qi_hetero_freeze_tend, qr2qi_collect_tend, qc2qr_ice_shed_tend,
+      qi2qr_melt_tend, qc2qi_collect_tend, qr2qi_immers_freeze_tend, qv2qi_nucleat_tend,
+      ni2nr_melt_tend, nc_collect_tend, ncshdc, nc2ni_immers_freeze_tend, nr_collect_tend,
+      ni_selfcollect_tend, ni_nucleat_tend, qv2qi_vapdep_tend, qc2qi_berg_tend,
+      nr2ni_immers_freeze_tend, ni_sublim_tend;
+  __device__ __forceinline__ void zero() {
+    qc2qr_accret_tend = qr2qv_evap_tend = qc2qr_autoconv_tend = nc_accret_tend = nc_selfcollect_tend =
+        nc2nr_autoconv_tend = nr_selfcollect_tend = nr_evap_tend = ncautr = qi2qv_sublim_tend =
+            nr_ice_shed_tend = qc2qi_hetero_freeze_tend = qr2qi_collect_tend = qc2qr_ice_shed_tend =
+                qi2qr_melt_tend = qc2qi_collect_tend = qr2qi_immers_freeze_tend = qv2qi_nucleat_tend =
+                    ni2nr_melt_tend = nc_collect_tend = ncshdc = nc2ni_immers_freeze_tend =
+                        nr_collect_tend = ni_selfcollect_tend = ni_nucleat_tend = qv2qi_vapdep_tend =
+                            qc2qi_berg_tend = nr2ni_immers_freeze_tend = ni_sublim_tend = TR(0);
+  }
+};
+
+/* get_time_space_phys_variables, p3_get_time_space_phys_variables_impl.hpp:12-45 */
+template <class TR>
+struct PhysVars {
+  TR mu, dv, sc, dqsdt, dqsidt, ab, abi, kap, eii;
+};
+template <class TR>
+__device__ __forceinline__ void get_time_space_phys_variables(TR T_atm, TR pres, TR rho, TR qv_sat_l,
+                                                              TR qv_sat_i, PhysVars<TR>& v) {
+  v.mu = TR(1.496e-6) * m_pow(T_atm, TR(1.5)) / (T_atm + TR(120));
+  v.dv = TR(8.794e-5) * m_pow(T_atm, TR(1.81)) / pres;
+  v.sc = v.mu / (rho * v.dv);
+  const TR dum = TR(1) / (TR(C::RV) * sq(T_atm));
+  v.dqsdt = TR(C::LatVap) * qv_sat_l * dum;
+  v.dqsidt = TR(C::LatVap + C::LatIce) * qv_sat_i * dum;
+  v.ab = TR(1) + v.dqsdt * TR(C::LatVap) * TR(C::INV_CP);
+  v.abi = TR(1) + v.dqsidt * TR(C::LatVap + C::LatIce) * TR(C::INV_CP);
+  v.kap = TR(1.414e+3) * v.mu;
+  if (T_atm < TR(253.15)) {
+    v.eii = TR(0.001);
+  } else if (T_atm < TR(273.15)) {
+    v.eii = TR(0.001) + (T_atm - TR(253.15)) * (TR(0.3) - TR(0.001)) / TR(20);
+  } else {
+    v.eii = TR(0.3);
+  }
+}
+
+/* ice_cldliq_collection, p3/impl/p3_ice_collection_impl.hpp:9-52 */
+template <class TR>
+__device__ __forceinline__ void ice_cldliq_collection(TR rho, TR temp, TR rhofaci, TR tv, TR qi_incld,
+                                                      TR qc_incld, TR ni_incld, TR nc_incld,
+                                                      Rates<TR>& r, const RuntimeDev& rt) {
+  const bool t_neg = temp <= TR(C::Tmelt);
+  const bool both = qi_incld >= TR(C::QSMALL) && qc_incld >= TR(C::QSMALL);
+  const TR f = TR(rt.cldliq_to_ice_collection_factor);
+  if (both && t_neg) r.qc2qi_collect_tend = rhofaci * tv * qc_incld * f * rho * ni_incld;
+  if (both) r.nc_collect_tend = rhofaci * tv * nc_incld * f * rho * ni_incld;
+  if (both && !t_neg) {
+    r.qc2qr_ice_shed_tend = rhofaci * tv * qc_incld * f * rho * ni_incld;
+    r.nc_collect_tend = rhofaci * tv * nc_incld * f * rho * ni_incld;
+    r.ncshdc = r.qc2qr_ice_shed_tend * TR(1.0 / C::dropmass);
+  }
+}
+
+/* ice_rain_collection, p3_ice_collection_impl.hpp:54-101 */
+template <class TR>
+__device__ __forceinline__ void ice_rain_collection(TR rho, TR temp, TR rhofaci, TR logn0r, TR tv_nr,
+                                                    TR tv_qr, TR qi_incld, TR ni_incld, TR qr_incld,
+                                                    Rates<TR>& r, const RuntimeDev& rt) {
+  const bool t_neg = temp <= TR(C::Tmelt);
+  const bool both = qi_incld >= TR(C::QSMALL) && qr_incld >= TR(C::QSMALL);
+  const TR f = TR(rt.rain_to_ice_collection_factor);
+  if (both && t_neg) {
+    r.qr2qi_collect_tend = m_pow(TR(10.0), tv_qr + logn0r) * rho * rhofaci * f * ni_incld;
+    r.nr_collect_tend = m_pow(TR(10.0), tv_nr + logn0r) * rho * rhofaci * f * ni_incld;
+  }
+  if (both && !t_neg) r.nr_collect_tend = m_pow(TR(10.0), tv_nr + logn0r) * rho * rhofaci * f * ni_incld;
+}
+
+/* ice_self_collection, p3_ice_collection_impl.hpp:103-152 */
+template <class TR>
+__device__ __forceinline__ void ice_self_collection(TR rho, TR rhofaci, TR tv, TR eii, TR qm_incld,
+                                                    TR qi_incld, TR ni_incld, Rates<TR>& r) {
+  const bool qm_pos = qm_incld > TR(0);
+  if (qi_incld >= TR(C::QSMALL)) {
+    TR tmp1 = 0;
+    if (qm_pos) tmp1 = qm_incld / qi_incld;
+    TR Eii_fact = 0;
+    if (tmp1 < TR(0.6) && qm_pos) Eii_fact = TR(1);
+    if (tmp1 >= TR(0.6) && tmp1 < TR(0.9) && qm_pos) Eii_fact = TR(1) - (tmp1 - TR(0.6)) / TR(0.3);
+    if (tmp1 >= TR(0.9) && qm_pos) Eii_fact = TR(0);
+    if (!qm_pos) Eii_fact = TR(1);
+    r.ni_selfcollect_tend = tv * rho * eii * Eii_fact * rhofaci * ni_incld * ni_incld;
+  }
+}
+
+/* ice_melting, p3/impl/p3_ice_melting_impl.hpp:10-53 (max(...,0) inside the branch) */
+template <class TR>
+__device__ __forceinline__ void ice_melting(TR rho, TR T_atm, TR qsat0, TR rhofaci, TR tv_melt,
+                                            TR tv_vent, const PhysVars<TR>& v, TR qv, TR qi_incld,
+                                            TR ni_incld, Rates<TR>& r) {
+  if (qi_incld >= TR(C::QSMALL) && T_atm > TR(C::Tmelt)) {
+    TR t = ((tv_melt + tv_vent * m_cbrt(v.sc) * m_sqrt(rhofaci * rho / v.mu)) *
+            ((T_atm - TR(C::Tmelt)) * v.kap - rho * TR(C::LatVap) * v.dv * (qsat0 - qv)) * TR(2) *
+            TR(C::Pi) / TR(C::LatIce)) *
+           ni_incld;
+    t = vmax(t, TR(0.));
+    r.qi2qr_melt_tend = t;
+    r.ni2nr_melt_tend = t * (ni_incld / qi_incld);
+  }
+}
+
+/* ice_cldliq_wet_growth, p3/impl/p3_ice_cldliq_wet_growth_impl.hpp:12-80 */
+template <class TR>
+__device__ __forceinline__ bool ice_cldliq_wet_growth(TR rho, TR temp, TR qsat0, TR rhofaci, TR tv_melt,
+                                                      TR tv_vent, const PhysVars<TR>& v, TR qv,
+                                                      TR qc_incld, TR qi_incld, TR ni_incld, TR qr_incld,
+                                                      Rates<TR>& r) {
+  const bool t_neg = temp < TR(C::Tmelt);
+  const bool any_if = qi_incld >= TR(C::QSMALL) && (qc_incld + qr_incld) >= TR(1.0e-6) && t_neg;
+  const bool any_if_col = any_if && (r.qc2qi_collect_tend + r.qr2qi_collect_tend) >= TR(1.0e-10);
+  bool wet = false;
+  if (any_if) {
+    TR g = ((tv_melt + tv_vent * m_cbrt(v.sc) * m_sqrt(rhofaci * rho / v.mu)) * TR(C::Pi * 2) *
+            (rho * TR(C::LatVap) * v.dv * (qsat0 - qv) - (temp - TR(C::Tmelt)) * v.kap) /
+            (TR(C::LatIce) + TR(C::CpLiq) * (temp - TR(C::Tmelt)))) *
+           ni_incld;
+    g = vmax(g, TR(0.));
+    const TR dum = vmax(TR(0.), (r.qc2qi_collect_tend + r.qr2qi_collect_tend) - g);
+    const bool dum_ge_small = dum >= TR(1.0e-10);
+    if (dum_ge_small) {
+      r.nr_ice_shed_tend = r.nr_ice_shed_tend + dum * TR(1.923e+6);
+      const TR dum1 = TR(1.0) / (r.qc2qi_collect_tend + r.qr2qi_collect_tend);
+      if (any_if_col) {
+        r.qc2qr_ice_shed_tend = r.qc2qr_ice_shed_tend + dum * r.qc2qi_collect_tend * dum1;
+        r.qc2qi_collect_tend = vmax(TR(0.), r.qc2qi_collect_tend - dum * r.qc2qi_collect_tend * dum1);
+        r.qr2qi_collect_tend = vmax(TR(0.), r.qr2qi_collect_tend - dum * r.qr2qi_collect_tend * dum1);
+      }
+    }
+    wet = dum_ge_small;
+  }
+  return wet;
+}
+
+/* calc_rime_density, p3/impl/p3_calc_rime_density_impl.hpp:13-70 */
+template <class TR>
+__device__ __forceinline__ TR calc_rime_density(TR T_atm, TR rhofaci, TR tv_fallspd, TR acn, TR lamc,
+                                                TR mu_c, TR qc_incld, TR qc2qi_collect_tend) {
+  TR rho_qm_cloud = TR(400);
+  if (qc2qi_collect_tend >= TR(C::QSMALL) && T_atm < TR(C::T_zerodegc)) {
+    const TR vtrmi1 = tv_fallspd * rhofaci;
+    if (qc_incld >= TR(C::QSMALL)) {
+      const TR Vt_qc = acn * m_tgamma(TR(4) + TR(C::bcn) + mu_c) / (m_pow(lamc, TR(C::bcn)) * m_tgamma(TR(4) + mu_c));
+      const TR D_c = (TR(4) + mu_c) / lamc;
+      const TR V_impact = m_fabs(vtrmi1 - Vt_qc);
+      const TR inv_Tc = TR(1) / vmin(TR(-0.001), T_atm - TR(C::T_zerodegc));
+      const TR Ri = vmax(TR(1.), vmin(TR(-0.5e+6) * D_c * V_impact * inv_Tc, TR(12.)));
+      if (Ri <= TR(8.0)) {
+        rho_qm_cloud = (TR(0.051) + TR(0.114) * Ri - TR(0.0055) * sq(Ri)) * TR(1000);
+      } else {
+        rho_qm_cloud = TR(611.) + TR(72.25) * (Ri - TR(8));
+      }
+    }
+  }
+  return rho_qm_cloud;
+}
+
+/* cldliq_immersion_freezing, p3/impl/p3_cldliq_imm_freezing_impl.hpp:13-50 */
+template <class TR>
+__device__ __forceinline__ void cldliq_immersion_freezing(TR T_atm, TR lamc, TR mu_c, TR cdist1, TR qc_incld,
+                                                          Rates<TR>& r, const RuntimeDev& rt) {
+  if (qc_incld >= TR(C::QSMALL) && T_atm <= TR(C::T_rainfrz)) {
+    const TR expAimmDt = m_exp(TR(rt.immersion_freezing_exponent) * (TR(C::T_zerodegc) - T_atm));
+    const TR inv_lamc = TR(1) / lamc;
+    const TR inv_lamc3 = inv_lamc * inv_lamc * inv_lamc;
+    if constexpr (sizeof(TR) == sizeof(double)) {
+      r.qc2qi_hetero_freeze_tend = TR(C::CONS6) * cdist1 * m_tgamma(TR(7) + mu_c) * expAimmDt * sq(inv_lamc3);
+    } else {
+      /* (1/lamc)^6 underflows single precision: multiply it in twice */
+      r.qc2qi_hetero_freeze_tend = TR(C::CONS6) * cdist1 * m_tgamma(TR(7) + mu_c) * expAimmDt * inv_lamc3 * inv_lamc3;
+    }
+    r.nc2ni_immers_freeze_tend = TR(C::CONS5) * cdist1 * m_tgamma(TR(4.0) + mu_c) * expAimmDt * inv_lamc3;
+  }
+}
+
+/* rain_immersion_freezing, p3/impl/p3_rain_imm_freezing_impl.hpp:13-44 */
+template <class TR>
+__device__ __forceinline__ void rain_immersion_freezing(TR T_atm, TR lamr, TR mu_r, TR cdistr, TR qr_incld,
+                                                        Rates<TR>& r, const RuntimeDev& rt) {
+  if (qr_incld >= TR(C::QSMALL) && T_atm <= TR(C::T_rainfrz)) {
+    const TR e = m_exp(TR(rt.immersion_freezing_exponent) * (TR(C::T_zerodegc) - T_atm));
+    r.qr2qi_immers_freeze_tend =
+        TR(C::CONS6) * m_exp(m_log(cdistr) + m_log(m_tgamma(TR(7.) + mu_r)) - TR(6.) * m_log(lamr)) * e;
+    r.nr2ni_immers_freeze_tend =
+        TR(C::CONS5) * m_exp(m_log(cdistr) + m_log(m_tgamma(TR(4.) + mu_r)) - TR(3.) * m_log(lamr)) * e;
+  }
+}
+
+/* ice_nucleation, p3/impl/p3_ice_nucleation_impl.hpp:9-61 */
+template <class TR>
+__device__ __forceinline__ void ice_nucleation(TR temp, TR inv_rho, TR ni, TR ni_activated, double qv_supersat_i,
+                                               TR inv_dt, bool do_predict_nc, bool do_prescribed_CCN,
+                                               Rates<TR>& r, const RuntimeDev& rt) {
+  const TR mi0 = TR(4.0 * C::PIOV3 * 900.0 * 1.e-18);
+  const bool do_log = (!do_predict_nc || do_prescribed_CCN);
+  const bool base = temp < TR(C::Tmelt - 15.0) && qv_supersat_i >= 0.05;
+  if (base && do_log) {
+    TR dum = TR(0.005) * m_exp(TR(rt.deposition_nucleation_exponent) * (TR(C::Tmelt) - temp)) * TR(1.0e3) * inv_rho;
+    dum = vmin(dum, TR(1.0e5) * inv_rho);
+    const TR N_nuc = vmax(TR(0.), (dum - ni) * inv_dt);
+    if (N_nuc >= TR(C::NSMALL)) {
+      const TR Q_nuc = vmax(TR(0.), (dum - ni) * mi0 * inv_dt);
+      r.qv2qi_nucleat_tend = Q_nuc;
+      r.ni_nucleat_tend = N_nuc;
+    }
+  } else if (base && !do_log) {
+    r.ni_nucleat_tend = vmax(TR(0.), (ni_activated - ni) * inv_dt);
+    r.qv2qi_nucleat_tend = r.ni_nucleat_tend * mi0;
+  }
+}
+
+/* cloud_water_autoconversion, p3/impl/p3_autoconversion_impl.hpp:9-58 */
+template <class TR>
+__device__ __forceinline__ void cloud_water_autoconversion(TR rho, TR qc_incld, TR nc_incld, Rates<TR>& r,
+                                                           const RuntimeDev& rt) {
+  if (qc_incld >= TR(1e-8)) {
+    r.qc2qr_autoconv_tend = TR(rt.autoconversion_prefactor) * m_pow(qc_incld, TR(rt.autoconversion_qc_exponent)) *
+                            m_pow(nc_incld * TR(1.e-6) * rho, TR(-rt.autoconversion_nc_exponent));
+    r.ncautr = r.qc2qr_autoconv_tend * TR(rt.cons3);
+    r.nc2nr_autoconv_tend = r.qc2qr_autoconv_tend * nc_incld / qc_incld;
+  }
+  if (r.qc2qr_autoconv_tend == TR(0)) r.nc2nr_autoconv_tend = 0;
+  if (r.nc2nr_autoconv_tend == TR(0)) r.qc2qr_autoconv_tend = 0;
+}
+
+/* cloud_rain_accretion, p3/impl/p3_cloud_rain_acc_impl.hpp:14-55 */
+template <class TR>
+__device__ __forceinline__ void cloud_rain_accretion(TR qc_incld, TR nc_incld, TR qr_incld, Rates<TR>& r,
+                                                     const RuntimeDev& rt) {
+  if (qr_incld >= TR(C::QSMALL) && qc_incld >= TR(C::QSMALL)) {
+    if (rt.accretion_qc_exponent == rt.accretion_qr_exponent) {
+      r.qc2qr_accret_tend = TR(rt.accretion_prefactor) * m_pow(qc_incld * qr_incld, TR(rt.accretion_qr_exponent));
+    } else {
+      r.qc2qr_accret_tend = TR(rt.accretion_prefactor) * m_pow(qc_incld, TR(rt.accretion_qc_exponent)) *
+                            m_pow(qr_incld, TR(rt.accretion_qr_exponent));
+    }
+    r.nc_accret_tend = r.qc2qr_accret_tend * nc_incld / qc_incld;
+    if (r.nc_accret_tend == TR(0)) r.qc2qr_accret_tend = 0;
+    if (r.qc2qr_accret_tend == TR(0)) r.nc_accret_tend = 0;
+  }
+}
+
+/* rain_self_collection, p3/impl/p3_rain_self_collection_impl.hpp:9-56 */
+template <class TR>
+__device__ __forceinline__ void rain_self_collection(TR rho, TR qr_incld, TR nr_incld, Rates<TR>& r,
+                                                     const RuntimeDev& rt) {
+  if (qr_incld >= TR(C::QSMALL)) {
+    const TR dum2 = m_cbrt((qr_incld) / (TR(C::Pi) * TR(C::RHO_H2O) * nr_incld));
+    const TR dbr = TR(rt.rain_selfcollection_breakup_diameter);
+    const TR dum = (dum2 < dbr) ? TR(1) : TR(2) - m_exp(TR(2300) * (dum2 - dbr));
+    r.nr_selfcollect_tend = dum * TR(rt.rain_selfcollection_prefactor) * nr_incld * qr_incld * rho;
+  }
+}
+
+/* back_to_cell_average, p3/impl/p3_back_to_cell_average_impl.hpp:14-77 */
+template <class TR>
+__device__ __forceinline__ void back_to_cell_average(TR cld_l, TR cld_r, TR cld_i, Rates<TR>& r) {
+  const TR ir = vmin(cld_i, cld_r), il = vmin(cld_i, cld_l), lr = vmin(cld_l, cld_r);
+  r.qc2qr_accret_tend *= lr;
+  r.qr2qv_evap_tend *= cld_r;
+  r.qc2qr_autoconv_tend *= cld_l;
+  r.nc_accret_tend *= lr;
+  r.nc_selfcollect_tend *= cld_l;
+  r.nc2nr_autoconv_tend *= cld_l;
+  r.nr_selfcollect_tend *= cld_r;
+  r.nr_evap_tend *= cld_r;
+  r.ncautr *= lr;
+  r.qi2qv_sublim_tend *= cld_i;
+  r.nr_ice_shed_tend *= il;
+  r.qc2qi_hetero_freeze_tend *= il;
+  r.qr2qi_collect_tend *= ir;
+  r.qc2qr_ice_shed_tend *= il;
+  r.qi2qr_melt_tend *= cld_i;
+  r.qc2qi_collect_tend *= il;
+  r.qr2qi_immers_freeze_tend *= cld_r;
+  r.ni2nr_melt_tend *= cld_i;
+  r.nc_collect_tend *= il;
+  r.ncshdc *= il;
+  r.nc2ni_immers_freeze_tend *= cld_l;
+  r.nr_collect_tend *= ir;
+  r.ni_selfcollect_tend *= cld_i;
+  r.qv2qi_vapdep_tend *= cld_i;
+  r.nr2ni_immers_freeze_tend *= cld_r;
+  r.ni_sublim_tend *= cld_i;
+  r.qc2qi_berg_tend *= il;
+}
+
+/* Converts a rate set to FP64 (identity for the plain form). */
+template <class TR>
+__device__ __forceinline__ Rates<double> to_double(const Rates<TR>& a) {
+  Rates<double> b;
+  b.qc2qr_accret_tend = a.qc2qr_accret_tend; b.qr2qv_evap_tend = a.qr2qv_evap_tend;
+  b.qc2qr_autoconv_tend = a.qc2qr_autoconv_tend; b.nc_accret_tend = a.nc_accret_tend;
+  b.nc_selfcollect_tend = a.nc_selfcollect_tend; b.nc2nr_autoconv_tend = a.nc2nr_autoconv_tend;
+  b.nr_selfcollect_tend = a.nr_selfcollect_tend; b.nr_evap_tend = a.nr_evap_tend; b.ncautr = a.ncautr;
+  b.qi2qv_sublim_tend = a.qi2qv_sublim_tend; b.nr_ice_shed_tend = a.nr_ice_shed_tend;
+  b.qc2qi_hetero_freeze_tend = a.qc2qi_hetero_freeze_tend; b.qr2qi_collect_tend = a.qr2qi_collect_tend;
+  b.qc2qr_ice_shed_tend = a.qc2qr_ice_shed_tend; b.qi2qr_melt_tend = a.qi2qr_melt_tend;
+  b.qc2qi_collect_tend = a.qc2qi_collect_tend; b.qr2qi_immers_freeze_tend = a.qr2qi_immers_freeze_tend;
+  b.qv2qi_nucleat_tend = a.qv2qi_nucleat_tend; b.ni2nr_melt_tend = a.ni2nr_melt_tend;
+  b.nc_collect_tend = a.nc_collect_tend; b.ncshdc = a.ncshdc; b.nc2ni_immers_freeze_tend = a.nc2ni_immers_freeze_tend;
+  b.nr_collect_tend = a.nr_collect_tend; b.ni_selfcollect_tend = a.ni_selfcollect_tend;
+  b.ni_nucleat_tend = a.ni_nucleat_tend; b.qv2qi_vapdep_tend = a.qv2qi_vapdep_tend;
+  b.qc2qi_berg_tend = a.qc2qi_berg_tend; b.nr2ni_immers_freeze_tend = a.nr2ni_immers_freeze_tend;
+  b.ni_sublim_tend = a.ni_sublim_tend;
+  return b;
+}
+
+/* ------------------------------------------------------------------ */
+/* FP64 residual routines                                               */
+/* ------------------------------------------------------------------ */
+
+/* evaporate_rain, p3/impl/p3_evaporate_rain_impl.hpp:9-203.  The
+ * supersaturation residual and the A_c source term are FP64; the
+ * relaxation coefficients come in from the rate precision. */
+__device__ __forceinline__ void evaporate_rain(double qr_incld, double qc_incld, double nr_incld,
+                                               double qi_incld, double cld_frac_l, double cld_frac_r,
+                                               double qv, double qv_prev, double qv_sat_l, double qv_sat_i,
+                                               double ab, double abi, double epsr, double epsi_tot,
+                                               double t_atm, double t_atm_prev, double dqsdt, double dt,
+                                               double& qr2qv_evap_tend, double& nr_evap_tend) {
+  qr2qv_evap_tend = 0;
+  nr_evap_tend = 0;
+  const double inv_dt = 1 / dt;
+  const double inv_cp = 1 / C::Cpair;
+  const double ssat_r = qv - qv_sat_l;
+  const double cld_frac = ((qc_incld + qi_incld) < 1.e-6) ? 0.0 : cld_frac_l;
+  if (qr_incld >= C::QSMALL && ssat_r < 0 && cld_frac_r > cld_frac) {
+    const double tau_r = 1 / epsr;
+    double eps_eff, A_c;
+    if (t_atm < C::Tmelt) {
+      eps_eff = epsr + epsi_tot * (1 + (C::LatVap + C::LatIce) * inv_cp * dqsdt) / abi;
+      A_c = (qv - qv_prev) * inv_dt - dqsdt * (t_atm - t_atm_prev) * inv_dt -
+            (qv_sat_l - qv_sat_i) * (1 + (C::LatVap + C::LatIce) * inv_cp * dqsdt) / abi * epsi_tot;
+    } else {
+      eps_eff = epsr;
+      A_c = (qv - qv_prev) * inv_dt - dqsdt * (t_atm - t_atm_prev) * inv_dt;
+    }
+    if (eps_eff < 1e-20) eps_eff = 1e-20;
+    const double tau_eff = 1 / eps_eff;
+    if (qr_incld < 1e-12 && qv / qv_sat_l < 0.999) {
+      qr2qv_evap_tend = qr_incld * inv_dt;
+    } else {
+      const double dt_over_tau = dt / tau_eff;
+      const double w = -expm1(-dt_over_tau) / dt_over_tau;
+      const double equilib = -A_c / ab * tau_eff / tau_r;
+      const double instant = -ssat_r / (ab * tau_r);
+      qr2qv_evap_tend = instant * w + equilib * (1 - w);
+    }
+    if (qr2qv_evap_tend > -ssat_r * inv_dt / ab) qr2qv_evap_tend = -ssat_r * inv_dt / ab;
+    if (qr2qv_evap_tend < 0) qr2qv_evap_tend = 0;
+    if (qr2qv_evap_tend > qr_incld * inv_dt) qr2qv_evap_tend = qr_incld * inv_dt;
+    qr2qv_evap_tend = qr2qv_evap_tend * (cld_frac_r - cld_frac) / cld_frac_r;
+    nr_evap_tend = qr2qv_evap_tend * (nr_incld / qr_incld);
+  }
+}
+
+/* ice_deposition_sublimation, p3/impl/p3_ice_deposition_sublimation_impl.hpp:9-65
+ * (the vapour residual qv - qv_sat is FP64). */
+__device__ __forceinline__ void ice_deposition_sublimation(double qi_incld, double ni_incld, double T_atm,
+                                                           double qv_sat_l, double qv_sat_i, double epsi,
+                                                           double abi, double qv, double inv_dt,
+                                                           double& vapdep, double& sublim, double& ni_sublim,
+                                                           double& berg) {
+  berg = 0; vapdep = 0; sublim = 0; ni_sublim = 0;
+  if (qi_incld > C::QSMALL) {
+    const double qi_tend = vmin(epsi / abi, inv_dt) * (qv - qv_sat_i);
+    const bool neg = qi_tend < 0;
+    if (neg) {
+      sublim = -qi_tend;
+      ni_sublim = sublim * (ni_incld / qi_incld);
+    }
+    const bool T_lt_frz = T_atm < C::T_zerodegc;
+    if (T_lt_frz && !neg) vapdep = qi_tend;
+    if (T_lt_frz) berg = vmax(epsi / abi * (qv_sat_l - qv_sat_i), 0.);
+  }
+}
+
+/* cloud/rain/ice water conservation, p3/impl/p3_conservation_impl.hpp:9-98 */
+__device__ __forceinline__ void water_conservation(double qc, double qr, double qi, double dt, Rates<double>& r) {
+  {
+    const double sinks = (r.qc2qr_autoconv_tend + r.qc2qr_accret_tend + r.qc2qi_collect_tend +
+                          r.qc2qi_hetero_freeze_tend + r.qc2qr_ice_shed_tend + r.qc2qi_berg_tend) * dt;
+    const double sources = qc;
+    double ratio;
+    if (sinks > sources && sinks >= C::QTENDSMALL) {
+      ratio = sources / sinks;
+      r.qc2qr_autoconv_tend *= ratio;
+      r.qc2qr_accret_tend *= ratio;
+      r.qc2qi_collect_tend *= ratio;
+      r.qc2qi_hetero_freeze_tend *= ratio;
+      r.qc2qr_ice_shed_tend *= ratio;
+      r.qc2qi_berg_tend *= ratio;
+    } else {
+      ratio = 1;
+    }
+    if (sources > C::QTENDSMALL) {
+      r.qv2qi_vapdep_tend *= (1 - ratio);
+      r.qi2qv_sublim_tend *= (1 - ratio);
+    }
+  }
+  {
+    const double sinks = (r.qr2qv_evap_tend + r.qr2qi_collect_tend + r.qr2qi_immers_freeze_tend) * dt;
+    const double sources = qr + (r.qc2qr_autoconv_tend + r.qc2qr_accret_tend + r.qi2qr_melt_tend +
+                                 r.qc2qr_ice_shed_tend) * dt;
+    if (sinks > sources && sinks >= C::QTENDSMALL) {
+      const double ratio = sources / sinks;
+      r.qr2qv_evap_tend *= ratio;
+      r.qr2qi_collect_tend *= ratio;
+      r.qr2qi_immers_freeze_tend *= ratio;
+    }
+  }
+  {
+    const double sinks = (r.qi2qv_sublim_tend + r.qi2qr_melt_tend) * dt;
+    const double sources = qi + (r.qv2qi_vapdep_tend + r.qv2qi_nucleat_tend + r.qr2qi_collect_tend +
+                                 r.qc2qi_collect_tend + r.qr2qi_immers_freeze_tend +
+                                 r.qc2qi_hetero_freeze_tend + r.qc2qi_berg_tend) * dt;
+    if (sinks > sources && sinks >= C::QTENDSMALL) {
+      const double ratio = sources / sinks;
+      r.qi2qv_sublim_tend *= ratio;
+      r.qi2qr_melt_tend *= ratio;
+    }
+  }
+}
+
+/* nc/nr/ni conservation, p3/impl/p3_{nc,nr,ni}_conservation_impl.hpp */
+__device__ __forceinline__ void number_conservation(double nc, double nr, double ni, double dt, Rates<double>& r) {
+  {
+    const double sink = (r.nc_collect_tend + r.nc2ni_immers_freeze_tend + r.nc_accret_tend + r.nc2nr_autoconv_tend) * dt;
+    const double source = nc + r.nc_selfcollect_tend * dt;
+    if (sink > source) {
+      const double ratio = source / sink;
+      r.nc_collect_tend *= ratio;
+      r.nc2ni_immers_freeze_tend *= ratio;
+      r.nc_accret_tend *= ratio;
+      r.nc2nr_autoconv_tend *= ratio;
+    }
+  }
+  {
+    const double sink = (r.nr_collect_tend + r.nr2ni_immers_freeze_tend + r.nr_selfcollect_tend + r.nr_evap_tend) * dt;
+    const double source = nr + (r.ni2nr_melt_tend * C::nmltratio + r.nr_ice_shed_tend + r.ncshdc + r.nc2nr_autoconv_tend) * dt;
+    if (sink > source) {
+      const double ratio = source / sink;
+      r.nr_collect_tend *= ratio;
+      r.nr2ni_immers_freeze_tend *= ratio;
+      r.nr_selfcollect_tend *= ratio;
+      r.nr_evap_tend *= ratio;
+    }
+  }
+  {
+    const double sink = (r.ni2nr_melt_tend + r.ni_sublim_tend + r.ni_selfcollect_tend) * dt;
+    const double source = ni + (r.ni_nucleat_tend + r.nr2ni_immers_freeze_tend + r.nc2ni_immers_freeze_tend) * dt;
+    if (sink > source) {
+      const double ratio = source / sink;
+      r.ni2nr_melt_tend *= ratio;
+      r.ni_sublim_tend *= ratio;
+      r.ni_selfcollect_tend *= ratio;
+    }
+  }
+}
+
+/* ice_supersat_conservation, p3/impl/p3_ice_supersat_conservation_impl.hpp:12-40 */
+__device__ __forceinline__ void ice_supersat_conservation(Rates<double>& r, double cld_frac_i, double qv,
+                                                          double qv_sat_i, double t_atm, double dt) {
+  const double latsublim2 = (C::LatVap + C::LatIce) * (C::LatVap + C::LatIce);
+  const double qv_sink = r.qv2qi_vapdep_tend + r.qv2qi_nucleat_tend;
+  if (qv_sink > C::QSMALL && cld_frac_i > 1e-20) {
+    double qv_avail = (qv + (r.qi2qv_sublim_tend + r.qr2qv_evap_tend) * dt - qv_sat_i) /
+                      (1 + latsublim2 * qv_sat_i / (C::CP * C::RH2O * sq(t_atm))) / dt;
+    qv_avail = vmax(qv_avail, 0.);
+    if (qv_sink > qv_avail) {
+      const double fract = qv_avail / qv_sink;
+      r.qv2qi_nucleat_tend *= fract;
+      r.qv2qi_vapdep_tend *= fract;
+    }
+  }
+}
+
+/* prevent_liq_supersaturation, p3/impl/p3_prevent_liq_supersaturation_impl.hpp:12-79 */
+template <class TR>
+__device__ __forceinline__ void prevent_liq_supersaturation(double pres, double t_atm, double qv, double dt,
+                                                            Rates<double>& r, uint32_t& err) {
+  const double qv_sources = r.qi2qv_sublim_tend + r.qr2qv_evap_tend;
+  if (!(qv_sources >= C::QSMALL)) return;
+  const double qv_sinks = r.qv2qi_vapdep_tend + r.qv2qi_nucleat_tend;
+  const double T_endstep = t_atm + ((qv_sinks - r.qi2qv_sublim_tend) * (C::LatVap + C::LatIce) * C::INV_CP -
+                                    r.qr2qv_evap_tend * C::LatVap * C::INV_CP) * dt;
+  const double qsl = qv_sat_dry<TR>(T_endstep, pres, false, err);
+  const double A = C::LatVap * qsl * dt * C::INV_CP / (C::RV * T_endstep * T_endstep) *
+                   ((C::LatVap + C::LatIce) * r.qi2qv_sublim_tend + C::LatVap * r.qr2qv_evap_tend);
+  double frac = (qsl - qv + qv_sinks * dt + A) / (qv_sources * dt + A);
+  frac = vmax(0., frac);
+  frac = vmin(1., frac);
+  r.qi2qv_sublim_tend = frac * r.qi2qv_sublim_tend;
+  r.qr2qv_evap_tend = frac * r.qr2qv_evap_tend;
+}
+
+/* update_prognostic_ice / update_prognostic_liquid,
+ * p3/impl/p3_update_prognostics_impl.hpp:9-123 (IPARAM = 3). */
+struct State {
+  double qc, nc, qr, nr, qi, qm, ni, bm, qv, th;
+};
+__device__ __forceinline__ void update_prognostics(const Rates<double>& r, double inv_exner, bool predictNc,
+                                                   bool prescribedCCN, bool log_wetgrowth, double dt,
+                                                   double rho_qm_cloud, double inv_rho, State& s) {
+  s.qc = s.qc + (-r.qc2qi_hetero_freeze_tend - r.qc2qi_collect_tend - r.qc2qr_ice_shed_tend - r.qc2qi_berg_tend) * dt;
+  if (predictNc) s.nc = s.nc + (-r.nc_collect_tend - r.nc2ni_immers_freeze_tend) * dt;
+  s.qr = s.qr + (-r.qr2qi_collect_tend + r.qi2qr_melt_tend - r.qr2qi_immers_freeze_tend + r.qc2qr_ice_shed_tend) * dt;
+  s.nr = s.nr + (-r.nr_collect_tend - r.nr2ni_immers_freeze_tend + C::nmltratio * r.ni2nr_melt_tend +
+                 r.nr_ice_shed_tend + r.ncshdc) * dt;
+  if (s.qi >= C::QSMALL) {
+    s.bm = s.bm - ((r.qi2qv_sublim_tend + r.qi2qr_melt_tend) / s.qi) * dt * s.bm;
+    s.qm = s.qm - ((r.qi2qv_sublim_tend + r.qi2qr_melt_tend) * s.qm / s.qi) * dt;
+    s.qi = s.qi - (r.qi2qv_sublim_tend + r.qi2qr_melt_tend) * dt;
+  }
+  const double dum = (r.qr2qi_collect_tend + r.qc2qi_collect_tend + r.qr2qi_immers_freeze_tend +
+                      r.qc2qi_hetero_freeze_tend) * dt;
+  s.qi = s.qi + (r.qv2qi_vapdep_tend + r.qv2qi_nucleat_tend + r.qc2qi_berg_tend) * dt + dum;
+  s.qm = s.qm + dum;
+  s.bm = s.bm + (r.qr2qi_collect_tend * C::INV_RHO_RIMEMAX + r.qc2qi_collect_tend / rho_qm_cloud +
+                 (r.qr2qi_immers_freeze_tend + r.qc2qi_hetero_freeze_tend) * C::INV_RHO_RIMEMAX) * dt;
+  s.ni = s.ni + (r.ni_nucleat_tend - r.ni2nr_melt_tend - r.ni_sublim_tend - r.ni_selfcollect_tend +
+                 r.nr2ni_immers_freeze_tend + r.nc2ni_immers_freeze_tend) * dt;
+  if (s.qm < 0) { s.qm = 0; s.bm = 0; }
+  if (log_wetgrowth) { s.qm = s.qi; s.bm = s.qm * C::INV_RHO_RIMEMAX; }
+  s.qv = s.qv + (-r.qv2qi_vapdep_tend + r.qi2qv_sublim_tend - r.qv2qi_nucleat_tend) * dt;
+  s.th = s.th + inv_exner * ((r.qv2qi_vapdep_tend - r.qi2qv_sublim_tend + r.qv2qi_nucleat_tend) *
+                                 (C::LatVap + C::LatIce) * C::INV_CP +
+                             (r.qr2qi_collect_tend + r.qc2qi_collect_tend + r.qc2qi_hetero_freeze_tend +
+                              r.qr2qi_immers_freeze_tend - r.qi2qr_melt_tend + r.qc2qi_berg_tend) *
+                                 C::LatIce * C::INV_CP) * dt;
+  /* liquid */
+  s.qc = s.qc + (-r.qc2qr_accret_tend - r.qc2qr_autoconv_tend) * dt;
+  s.qr = s.qr + (r.qc2qr_accret_tend + r.qc2qr_autoconv_tend - r.qr2qv_evap_tend) * dt;
+  if (predictNc || prescribedCCN) {
+    s.nc = s.nc + (-r.nc_accret_tend - r.nc2nr_autoconv_tend + r.nc_selfcollect_tend) * dt;
+  } else {
+    s.nc = C::NCCNST * inv_rho;
+  }
+  s.nr = s.nr + (r.ncautr - r.nr_selfcollect_tend - r.nr_evap_tend) * dt;
+  s.qv = s.qv + r.qr2qv_evap_tend * dt;
+  s.th = s.th + inv_exner * (-r.qr2qv_evap_tend * C::LatVap * C::INV_CP) * dt;
+}
+
+}  // namespace dev
+}  // namespace p3x

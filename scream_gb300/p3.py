@@ -1,0 +1,275 @@
+"""Host-side mirror of the EAMxx P3 call surface over libp3x.
+
+``P3Context`` owns the lookup tables (``P3LookupTables`` + ``p3_init``,
+components/eamxx/src/physics/p3/p3_f90.cpp:103-113); ``P3Context.p3_main``
+is ``Functions<Real,Device>::p3_main`` (p3_functions.hpp:1355-1369) on
+device tensors; ``P3Microphysics`` mirrors the atmosphere-process plugin
+(components/eamxx/src/physics/p3/eamxx_p3_process_interface.hpp:22-444,
+eamxx_p3_run.cpp:5-45) for resident device state.
+
+Device memory and streams come from PyTorch; every computation is a CUDA
+kernel of libp3x.  There is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Dict, Optional
+
+import numpy as np
+
+from . import _lib as L
+
+try:  # torch is plumbing for device memory and streams
+    import torch
+except Exception:  # pragma: no cover - torch is present in every supported environment
+    torch = None
+
+
+def _ptr(t) -> int:
+    return 0 if t is None else int(t.data_ptr())
+
+
+def _stream_handle(stream=None) -> int:
+    if torch is None:
+        return 0
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return int(s.cuda_stream)
+
+
+def field_shape(name: str, ncol: int, nlev: int):
+    if name in L.SURFACE_FIELDS:
+        return (ncol,)
+    if name in L.INTERFACE_FIELDS:
+        return (ncol, nlev + 1)
+    return (ncol, nlev)
+
+
+def generate_inputs(kind: int, seed: int, ncol: int, nlev: int, col0: int = 0) -> Dict[str, np.ndarray]:
+    """Synthetic P3 inputs (host float64 arrays of shape (ncol, nlev)).
+
+    kind 0: standard-atmosphere columns with one cloud layer (RH ~ U(0.3, 1.05));
+    kind 1: same with RH ~ U(0.9, 1.05) in even columns; kind 2: the reference's
+    "mixed" test case.  Columns are generated independently from (seed, column).
+    """
+    lib = L.load()
+    arrs = {n: np.zeros((ncol, nlev), dtype=np.float64) for n in L.INPUT_FIELDS}
+    ptrs = (C.c_void_p * len(L.INPUT_FIELDS))(*[a.ctypes.data for a in arrs.values()])
+    L.check("p3x_workload_generate",
+            lib.p3x_workload_generate(kind, seed, col0, ncol, nlev, ptrs, nlev))
+    return arrs
+
+
+@dataclass
+class P3Fields:
+    """All arrays of one P3 call (device tensors, level-contiguous)."""
+    ncol: int
+    nlev: int
+    t: Dict[str, "torch.Tensor"] = field(default_factory=dict)
+
+    @classmethod
+    def allocate(cls, ncol: int, nlev: int, device="cuda"):
+        f = cls(ncol, nlev)
+        for n in L.ALL_FIELDS:
+            f.t[n] = torch.zeros(field_shape(n, ncol, nlev), dtype=torch.float64, device=device)
+        return f
+
+    @classmethod
+    def from_inputs(cls, inputs: Dict[str, np.ndarray], device="cuda"):
+        ncol, nlev = inputs["qc"].shape
+        f = cls.allocate(ncol, nlev, device)
+        for n in L.INPUT_FIELDS:
+            f.t[n].copy_(torch.from_numpy(np.ascontiguousarray(inputs[n])))
+        return f
+
+    def prog(self):
+        return L.PrognosticState(*[_ptr(self.t[n]) for n in L.PROG_FIELDS])
+
+    def din(self):
+        return L.DiagnosticInputs(*[_ptr(self.t[n]) for n in L.DIAG_IN_FIELDS])
+
+    def dout(self):
+        return L.DiagnosticOutputs(*[_ptr(self.t[n]) for n in L.DIAG_OUT_FIELDS])
+
+    def hist(self):
+        return L.HistoryOnly(*[_ptr(self.t[n]) for n in L.HIST_FIELDS])
+
+    def to_host(self) -> Dict[str, np.ndarray]:
+        return {n: v.detach().cpu().numpy() for n, v in self.t.items()}
+
+    def desc(self, dt: float, precision: int, predictNc=True, prescribedCCN=True, it=1):
+        return L.InstanceDesc(self.prog(), self.din(), self.dout(), self.hist(),
+                              L.Layout(self.nlev, self.nlev + 1), self.ncol, self.nlev, dt, it,
+                              int(predictNc), int(prescribedCCN), precision)
+
+
+class P3Context:
+    """Lookup tables on the device (generated in-process, or read from the
+    official ``p3_lookup_table_1.dat-v4.1.1`` text file)."""
+
+    def __init__(self, table_file: Optional[str] = None):
+        self.lib = L.load()
+        self.h = C.c_void_p()
+        info = C.c_int(0)
+        rc = self.lib.p3x_context_create(table_file.encode() if table_file else None,
+                                         C.byref(self.h), C.byref(info))
+        L.check("p3x_context_create", rc)
+
+    def close(self):
+        if self.h:
+            self.lib.p3x_context_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def tables(self) -> Dict[str, np.ndarray]:
+        shp = {"ice": (5, 4, 50, 12), "collect": (5, 4, 50, 30, 2), "vn": (300, 10), "vm": (300, 10),
+               "revap": (300, 10), "mu_r": (150,), "dnu": (16,)}
+        out = {k: np.zeros(s) for k, s in shp.items()}
+        args = [out[k].ctypes.data_as(L._dp) for k in shp]
+        L.check("p3x_context_get_tables", self.lib.p3x_context_get_tables(self.h, *args))
+        return out
+
+    def set_launch_config(self, precision: int, lanes=32, columns_per_block=8, table_staging=1,
+                          blocks_per_sm=0):
+        cfg = L.LaunchConfig(lanes, columns_per_block, table_staging, blocks_per_sm)
+        L.check("p3x_set_launch_config", self.lib.p3x_set_launch_config(self.h, precision, C.byref(cfg)))
+
+    def launch_config(self, precision: int) -> dict:
+        cfg = L.LaunchConfig()
+        L.check("p3x_get_launch_config", self.lib.p3x_get_launch_config(self.h, precision, C.byref(cfg)))
+        return cfg.as_dict()
+
+    def p3_main(self, f: P3Fields, dt: float, precision: int = L.P3X_FP64, runtime: L.Runtime = None,
+                predictNc=True, prescribedCCN=True, it=1, stream=None, sync=True) -> float:
+        """One P3 step in place on ``f``; returns the kernel time in microseconds
+        (sync) or 0.0 (async; errors then surface in :meth:`check`)."""
+        rt = runtime if runtime is not None else L.default_runtime()
+        infra = L.Infrastructure(dt, it, 1, f.ncol, 1, f.nlev, int(predictNc), int(prescribedCCN), None)
+        prog, din, dout, hist = f.prog(), f.din(), f.dout(), f.hist()
+        lay = L.Layout(f.nlev, f.nlev + 1)
+        sh = _stream_handle(stream)
+        if sync:
+            us = C.c_double(0)
+            rc = self.lib.p3x_main(self.h, C.byref(rt), C.byref(prog), C.byref(din), C.byref(dout),
+                                   C.byref(infra), C.byref(hist), f.ncol, f.nlev, C.byref(lay),
+                                   precision, sh, C.byref(us))
+            L.check("p3x_main", rc)
+            return us.value
+        rc = self.lib.p3x_main_async(self.h, C.byref(rt), C.byref(prog), C.byref(din), C.byref(dout),
+                                     C.byref(infra), C.byref(hist), f.ncol, f.nlev, C.byref(lay),
+                                     precision, sh)
+        L.check("p3x_main_async", rc)
+        return 0.0
+
+    def check(self, stream=None):
+        L.check("p3x_context_check", self.lib.p3x_context_check(self.h, _stream_handle(stream)))
+
+    def budgets(self, f: P3Fields, stream=None):
+        """Column total water and energy (FP64, device tensors of shape (ncol,))."""
+        w = torch.zeros(f.ncol, dtype=torch.float64, device=f.t["qc"].device)
+        e = torch.zeros_like(w)
+        prog = f.prog()
+        rc = self.lib.p3x_column_budgets(C.byref(prog), _ptr(f.t["dpres"]), _ptr(f.t["inv_exner"]),
+                                         f.ncol, f.nlev, f.nlev, _ptr(w), _ptr(e), _stream_handle(stream))
+        L.check("p3x_column_budgets", rc)
+        return w, e
+
+
+class P3Batch:
+    """Many instances advanced by one persistent launch (optionally a CUDA graph)."""
+
+    def __init__(self, ctx: P3Context, fields, dts, precision: int, runtime: L.Runtime = None,
+                 predictNc=True, prescribedCCN=True):
+        self.ctx = ctx
+        self.fields = list(fields)
+        rt = runtime if runtime is not None else L.default_runtime()
+        descs = (L.InstanceDesc * len(self.fields))(
+            *[f.desc(dt, precision, predictNc, prescribedCCN) for f, dt in zip(self.fields, dts)])
+        self.h = C.c_void_p()
+        L.check("p3x_batch_create", ctx.lib.p3x_batch_create(ctx.h, C.byref(rt), descs, len(self.fields),
+                                                             C.byref(self.h)))
+
+    def run(self, stream=None):
+        L.check("p3x_batch_run", self.ctx.lib.p3x_batch_run(self.h, _stream_handle(stream)))
+
+    def capture_graph(self, stream):
+        L.check("p3x_batch_capture_graph", self.ctx.lib.p3x_batch_capture_graph(self.h, _stream_handle(stream)))
+
+    def set_launch_config(self, lanes=32, columns_per_block=8, table_staging=1, blocks_per_sm=0):
+        cfg = L.LaunchConfig(lanes, columns_per_block, table_staging, blocks_per_sm)
+        L.check("p3x_batch_set_launch_config", self.ctx.lib.p3x_batch_set_launch_config(self.h, C.byref(cfg)))
+
+    def autotune(self, reps=3, stream=None):
+        cfg = L.LaunchConfig()
+        ms = C.c_double(0)
+        L.check("p3x_autotune_batch", self.ctx.lib.p3x_autotune_batch(self.h, _stream_handle(stream), reps,
+                                                                      C.byref(cfg), C.byref(ms)))
+        return cfg.as_dict(), ms.value
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.p3x_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class P3Microphysics:
+    """Mirror of the ``P3Microphysics`` atmosphere process for resident device
+    state: ``set_grids`` fixes (ncol, nlev), ``initialize`` creates the tables
+    and the fields, ``run(dt)`` advances the step counter and calls p3_main
+    (eamxx_p3_run.cpp:5-45), ``finalize`` releases everything."""
+
+    def __init__(self, params: Optional[dict] = None):
+        params = dict(params or {})
+        self.runtime = L.default_runtime()
+        for k in L.RUNTIME_FIELDS:
+            if k in params:
+                setattr(self.runtime, k, float(params[k]))
+        if "do_ice_production" in params:
+            self.runtime.do_ice_production = int(bool(params["do_ice_production"]))
+        self.predictNc = bool(params.get("do_predict_nc", True))
+        self.prescribedCCN = bool(params.get("do_prescribed_CCN", True))
+        self.precision = int(params.get("precision", L.P3X_FP64))
+        self.table_file = params.get("table_file")
+        self.ncol = self.nlev = None
+        self.ctx = None
+        self.fields = None
+        self.it = 0
+
+    def type(self):
+        return "Physics"
+
+    def name(self):
+        return "p3"
+
+    def set_grids(self, ncol: int, nlev: int):
+        self.ncol, self.nlev = int(ncol), int(nlev)
+
+    def initialize(self, inputs: Optional[Dict[str, np.ndarray]] = None):
+        self.ctx = P3Context(self.table_file)
+        if inputs is None:
+            self.fields = P3Fields.allocate(self.ncol, self.nlev)
+        else:
+            self.fields = P3Fields.from_inputs(inputs)
+        self.it = 0
+
+    def run(self, dt: float, stream=None) -> float:
+        self.it += 1
+        return self.ctx.p3_main(self.fields, dt, self.precision, self.runtime, self.predictNc,
+                                self.prescribedCCN, self.it, stream)
+
+    def finalize(self):
+        if self.ctx is not None:
+            self.ctx.close()
+        self.ctx = None
+        self.fields = None

@@ -1,0 +1,295 @@
+"""GPU parity of the P3 step against the CPU oracle, through the C ABI.
+
+How parity is judged.  P3 contains complete-depletion cancellations (e.g. a
+number-conservation limiter that sets ni + (sources - sinks) dt to a
+round-off residue) whose residue then feeds a table lookup on qi/ni.  A 1-ulp
+change of a single input moves the ice fields of the oracle itself by ~1e-2
+(rel-L2) after one step.  So:
+  * every stage is checked at tight FP64 tolerance under conditions that do
+    not trigger the amplification (ice sedimentation off; ice production off),
+    and liquid / vapour / heat fields are checked at 1e-10 in the full step;
+  * ice fields of the full step are checked against the oracle's own 1-ulp
+    perturbation envelope;
+  * conservation (column water, 1e-12 relative) and bitwise invariance across
+    launch configurations, batching, graphs and the Fortran-layout entry are
+    exact checks.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import column_water, oracle_state, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+LIQ = ["qc", "nc", "qr", "nr", "qv", "th", "precip_liq_surf", "precip_liq_flux", "diag_eff_radius_qc",
+       "diag_eff_radius_qr", "vap_liq_exchange", "precip_total_tend"]
+ICE = ["qi", "qm", "ni", "bm", "precip_ice_surf", "diag_eff_radius_qi", "rho_qi", "vap_ice_exchange",
+       "liq_ice_exchange", "qv2qi_depos_tend", "nevapr"]
+ALLF = LIQ + ICE
+
+
+def run_gpu(ctx, inputs, steps=1, precision=0, runtime=None, predictNc=True, prescribedCCN=True):
+    import scream_gb300 as p3
+    f = p3.P3Fields.from_inputs(inputs)
+    for s in range(steps):
+        ctx.p3_main(f, 300.0, precision, runtime=runtime, predictNc=predictNc, prescribedCCN=prescribedCCN,
+                    it=s + 1)
+    return f.to_host()
+
+
+def run_oracle(tables, inputs, steps=1, runtime=None, predictNc=True, prescribedCCN=True, perturb=None):
+    from oracle import p3_oracle as O
+    st = oracle_state(inputs)
+    if perturb:
+        st[perturb] = np.nextafter(st[perturb], np.inf)
+    for s in range(steps):
+        err, _ = O.p3_main(st, tables, 300.0, runtime=runtime, predictNc=predictNc, prescribedCCN=prescribedCCN,
+                           it=s + 1)
+        assert err == 0
+    return st
+
+
+def runtimes(**mods):
+    from scream_gb300 import _lib as L
+    from oracle import p3_oracle as O
+    rt, ort = L.default_runtime(), O.default_runtime()
+    for k, v in mods.items():
+        setattr(rt, k, v)
+        setattr(ort, k, v)
+    return rt, ort
+
+
+@pytest.fixture(scope="module")
+def case0(built):
+    from scream_gb300.p3 import generate_inputs
+    return generate_inputs(0, 1000, 64, 72)
+
+
+@pytest.mark.parametrize("mods", [{"ice_sedimentation_factor": 0.0}, {"do_ice_production": 0}])
+def test_fp64_stage_parity_tight(gpu_ctx, tables, case0, mods):
+    """With ice sedimentation off (part1/part2/part3, cloud+rain sedimentation)
+    or ice production off (everything else incl. ice sedimentation), every
+    field matches the oracle to FP64 round-off."""
+    rt, ort = runtimes(**mods)
+    g = run_gpu(gpu_ctx, case0, runtime=rt)
+    o = run_oracle(tables, case0, runtime=ort)
+    for n in ALLF:
+        tol = 1e-9 if n in ("ni", "nc", "nr") else 1e-10
+        assert rel_l2(g[n], o[n]) <= tol, (n, rel_l2(g[n], o[n]))
+
+
+def test_fp64_full_step_parity(gpu_ctx, tables, case0):
+    g = run_gpu(gpu_ctx, case0)
+    o = run_oracle(tables, case0)
+    for n in LIQ:
+        assert rel_l2(g[n], o[n]) <= 1e-10, (n, rel_l2(g[n], o[n]))
+    env = {n: 0.0 for n in ICE}
+    for p in ["th", "qv", "ni"]:
+        op = run_oracle(tables, case0, perturb=p)
+        for n in ICE:
+            env[n] = max(env[n], rel_l2(op[n], o[n]))
+    for n in ICE:
+        assert rel_l2(g[n], o[n]) <= 10 * env[n] + 1e-10, (n, rel_l2(g[n], o[n]), env[n])
+
+
+def test_fp64_conserves_column_water(gpu_ctx, built):
+    from scream_gb300.p3 import generate_inputs
+    inp = generate_inputs(1, 1002, 2048, 128)
+    w0 = column_water(inp)
+    g = run_gpu(gpu_ctx, inp)
+    p = (g["precip_liq_surf"] + g["precip_ice_surf"]) * 1000.0 * 300.0
+    assert np.max(np.abs(column_water(g) + p - w0) / w0) <= 1e-12
+
+
+def test_mixed_ic_six_steps(gpu_ctx, tables):
+    """The reference's p3_run_and_cmp case (mixed IC, 3 x 72, dt 300, 6 steps)."""
+    from scream_gb300.p3 import generate_inputs
+    inp = generate_inputs(2, 0, 3, 72)
+    for pn, pc in [(True, True), (False, False), (True, False)]:
+        g = run_gpu(gpu_ctx, inp, steps=6, predictNc=pn, prescribedCCN=pc)
+        o = run_oracle(tables, inp, steps=6, predictNc=pn, prescribedCCN=pc)
+        env = {}
+        for p in ["th", "qv"]:
+            op = run_oracle(tables, inp, steps=6, predictNc=pn, prescribedCCN=pc, perturb=p)
+            for n in ALLF:
+                env[n] = max(env.get(n, 0.0), rel_l2(op[n], o[n]))
+        for n in ALLF:
+            assert rel_l2(g[n], o[n]) <= 10 * env[n] + 1e-9, (pn, pc, n, rel_l2(g[n], o[n]), env[n])
+
+
+@pytest.mark.parametrize("nlev", [1, 2, 33, 97, 256])
+def test_ragged_level_counts(gpu_ctx, tables, nlev):
+    from scream_gb300.p3 import generate_inputs
+    inp = generate_inputs(0, 1100 + nlev, 24, nlev)
+    rt, ort = runtimes(ice_sedimentation_factor=0.0)
+    g = run_gpu(gpu_ctx, inp, runtime=rt)
+    o = run_oracle(tables, inp, runtime=ort)
+    for n in ALLF:
+        tol = 1e-9 if n in ("ni", "nc", "nr") else 1e-10
+        assert rel_l2(g[n], o[n]) <= tol, (nlev, n, rel_l2(g[n], o[n]))
+
+
+def test_empty_batch_is_noop(gpu_ctx):
+    import scream_gb300 as p3
+    f = p3.P3Fields.allocate(0, 72)
+    assert gpu_ctx.p3_main(f, 300.0) >= 0.0
+
+
+def test_outputs_are_fully_written(gpu_ctx, case0):
+    """History fields and every interface of the precip fluxes are written by
+    the kernel (callers need not zero them)."""
+    import scream_gb300 as p3
+    import torch
+    f = p3.P3Fields.from_inputs(case0)
+    for n in ["liq_ice_exchange", "vap_liq_exchange", "vap_ice_exchange", "precip_liq_flux", "precip_ice_flux",
+              "precip_liq_surf", "precip_ice_surf", "rho_qi", "nevapr", "precip_total_tend", "qv2qi_depos_tend"]:
+        f.t[n].fill_(float("nan"))
+    gpu_ctx.p3_main(f, 300.0)
+    h = f.to_host()
+    for n in ["liq_ice_exchange", "vap_liq_exchange", "vap_ice_exchange", "precip_liq_flux", "precip_ice_flux",
+              "precip_liq_surf", "precip_ice_surf", "rho_qi", "nevapr", "precip_total_tend", "qv2qi_depos_tend"]:
+        assert np.all(np.isfinite(h[n])), n
+    torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_launch_configs_bitwise_identical(gpu_ctx, case0, precision):
+    base = None
+    for lanes, cols, staged in [(32, 8, 1), (32, 4, 0), (16, 8, 1), (8, 16, 0), (8, 4, 1)]:
+        gpu_ctx.set_launch_config(precision, lanes=lanes, columns_per_block=cols, table_staging=staged)
+        g = run_gpu(gpu_ctx, case0, precision=precision)
+        if base is None:
+            base = g
+        else:
+            for n in ALLF:
+                np.testing.assert_array_equal(g[n], base[n], err_msg=f"{lanes}/{cols}/{staged} {n}")
+    gpu_ctx.set_launch_config(precision, lanes=32, columns_per_block=8, table_staging=1)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batched_and_graph_equal_single(gpu_ctx, precision):
+    import scream_gb300 as p3
+    import torch
+    rng = np.random.default_rng(7)
+    sizes = [(int(n), int(l)) for n, l in zip(np.exp(rng.uniform(0, np.log(3000), 12)).astype(int) + 1,
+                                              rng.choice([72, 128], 12))]
+    dts = [300.0 if i % 2 else 120.0 for i in range(len(sizes))]
+    inputs = [p3.generate_inputs(0, 3000 + i, n, l) for i, (n, l) in enumerate(sizes)]
+    singles = []
+    for inp, dt in zip(inputs, dts):
+        f = p3.P3Fields.from_inputs(inp)
+        gpu_ctx.p3_main(f, dt, precision)
+        singles.append(f.to_host())
+    fields = [p3.P3Fields.from_inputs(inp) for inp in inputs]
+    b = p3.P3Batch(gpu_ctx, fields, dts, precision)
+    b.run()
+    gpu_ctx.check()
+    for s, f in zip(singles, fields):
+        h = f.to_host()
+        for n in ALLF:
+            np.testing.assert_array_equal(h[n], s[n], err_msg=n)
+    # graph capture + replay on fresh copies
+    fields2 = [p3.P3Fields.from_inputs(inp) for inp in inputs]
+    b2 = p3.P3Batch(gpu_ctx, fields2, dts, precision)
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        b2.capture_graph(stream)
+        for f, inp in zip(fields2, inputs):   # capture does not execute: reset not needed
+            pass
+        b2.run(stream)
+    stream.synchronize()
+    gpu_ctx.check()
+    for s, f in zip(singles, fields2):
+        h = f.to_host()
+        for n in ALLF:
+            np.testing.assert_array_equal(h[n], s[n], err_msg="graph " + n)
+    b.close()
+    b2.close()
+
+
+def test_fortran_layout_entry_matches(gpu_ctx, built, case0):
+    """p3x_main_f (the p3_main_c argument list, host arrays, column-fastest
+    layout) gives the same result as p3x_main."""
+    from scream_gb300 import _lib as L
+    lib = built
+    ncol, nlev = case0["qc"].shape
+    g = run_gpu(gpu_ctx, case0)
+    F = {n: np.asfortranarray(np.array(case0[n], copy=True)) for n in case0}
+    out = {n: np.zeros((ncol, nlev), order="F") for n in ["diag_eff_radius_qc", "diag_eff_radius_qi",
+                                                          "diag_eff_radius_qr", "rho_qi", "qv2qi_depos_tend",
+                                                          "liq_ice_exchange", "vap_liq_exchange",
+                                                          "vap_ice_exchange"]}
+    plf = np.zeros((ncol, nlev + 1), order="F")
+    pif = np.zeros((ncol, nlev + 1), order="F")
+    pls = np.zeros(ncol)
+    pis = np.zeros(ncol)
+    el = C.c_double(0)
+
+    def P(a):
+        return a.ctypes.data_as(C.POINTER(C.c_double))
+
+    rc = lib.p3x_main_f(P(F["qc"]), P(F["nc"]), P(F["qr"]), P(F["nr"]), P(F["th"]), P(F["qv"]), 300.0,
+                        P(F["qi"]), P(F["qm"]), P(F["ni"]), P(F["bm"]), P(F["pres"]), P(F["dz"]),
+                        P(F["nc_nuceat_tend"]), P(F["nccn"]), P(F["ni_activated"]), P(F["inv_qc_relvar"]), 1,
+                        P(pls), P(pis), 1, ncol, 1, nlev, P(out["diag_eff_radius_qc"]),
+                        P(out["diag_eff_radius_qi"]), P(out["diag_eff_radius_qr"]), P(out["rho_qi"]), 1, 1,
+                        P(F["dpres"]), P(F["inv_exner"]), P(out["qv2qi_depos_tend"]), P(plf), P(pif),
+                        P(F["cld_frac_r"]), P(F["cld_frac_l"]), P(F["cld_frac_i"]), P(out["liq_ice_exchange"]),
+                        P(out["vap_liq_exchange"]), P(out["vap_ice_exchange"]), P(F["qv_prev"]), P(F["t_prev"]),
+                        C.byref(el))
+    assert rc == L.P3X_OK
+    for n in ["qc", "nc", "qr", "nr", "qi", "qm", "ni", "bm", "qv", "th"]:
+        np.testing.assert_array_equal(F[n], g[n], err_msg=n)
+    for n, a in out.items():
+        np.testing.assert_array_equal(a, g[n], err_msg=n)
+    np.testing.assert_array_equal(plf, g["precip_liq_flux"])
+    np.testing.assert_array_equal(pls, g["precip_liq_surf"])
+    np.testing.assert_array_equal(pis, g["precip_ice_surf"])
+    assert el.value > 0
+
+
+def test_numeric_error_is_reported_and_context_survives(gpu_ctx, case0):
+    """T <= 0 makes the reference abort in check_temperature
+    (share/physics_saturation_impl.hpp:14-36); here the step returns
+    P3X_ENUMERIC and the context keeps working."""
+    import scream_gb300 as p3
+    from scream_gb300 import _lib as L
+    bad = {k: np.array(v, copy=True) for k, v in case0.items()}
+    bad["th"][3, 10] = -5.0
+    f = p3.P3Fields.from_inputs(bad)
+    with pytest.raises(L.P3Error) as ei:
+        gpu_ctx.p3_main(f, 300.0)
+    assert ei.value.code == L.P3X_ENUMERIC
+    f2 = p3.P3Fields.from_inputs(case0)
+    gpu_ctx.p3_main(f2, 300.0)   # no error afterwards
+
+
+def test_budget_kernel_matches_numpy(gpu_ctx, case0):
+    import scream_gb300 as p3
+    f = p3.P3Fields.from_inputs(case0)
+    w, e = gpu_ctx.budgets(f)
+    np.testing.assert_allclose(w.cpu().numpy(), column_water(case0), rtol=1e-13)
+    T = case0["th"] / case0["inv_exner"]
+    e_ref = ((T * 1004.64 + (2501000.0 + 333700.0) * case0["qv"] + 333700.0 * (case0["qc"] + case0["qr"]))
+             * case0["dpres"] / 9.80616).sum(1)
+    np.testing.assert_allclose(e.cpu().numpy(), e_ref, rtol=1e-13)
+
+
+def test_fp32_bulk_precision_form(gpu_ctx, tables, built):
+    """FP32-bulk vs the FP64 oracle: surface precipitation rel-L2 <= 1e-4 after
+    one step on the supersaturation-stress workload; column water conserved to
+    1e-12; every field's error reported."""
+    from scream_gb300.p3 import generate_inputs
+    inp = generate_inputs(1, 1002, 2048, 128)
+    g = run_gpu(gpu_ctx, inp, precision=1)
+    o = run_oracle(tables, inp)
+    w0 = column_water(inp)
+    p = (g["precip_liq_surf"] + g["precip_ice_surf"]) * 1000.0 * 300.0
+    assert np.max(np.abs(column_water(g) + p - w0) / w0) <= 1e-12
+    prec_g = g["precip_liq_surf"] + g["precip_ice_surf"]
+    prec_o = o["precip_liq_surf"] + o["precip_ice_surf"]
+    errs = {n: rel_l2(g[n], o[n]) for n in ALLF}
+    print("FP32-bulk per-field rel-L2 vs FP64 oracle:", {k: f"{v:.2e}" for k, v in errs.items()})
+    assert rel_l2(prec_g, prec_o) <= 1e-4, rel_l2(prec_g, prec_o)

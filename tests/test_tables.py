@@ -1,0 +1,155 @@
+"""CPU checks of the lookup-table pipeline.
+
+- The rain tables (vn, vm, revap) are recomputed here in numpy from the
+  formulas of the Fortran p3_init_b (micro_p3.F90:218-341) and compared with
+  the library's host table builder.
+- The regularised incomplete gamma function Q(a, x) used by the ice-table
+  generator is checked against scipy.special.gammaincc.
+- A few ice-table entries are recomputed from the generator's published
+  formulas with scipy (independent integrals) and compared.
+- The official text format round-trips: write -> read gives the same tables.
+- The generated tables match the committed summary (cross-machine pin).
+"""
+import ctypes as C
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def numpy_rain_tables(mu_r=1.0):
+    pi = 3.14159265358979323
+    piov6 = pi / 6.0
+    jj = np.arange(1, 301, dtype=float)
+    dm = np.where(jj <= 20, (jj * 10.0 - 5.0) * 1e-6, ((jj - 20) * 30.0 + 195.0) * 1e-6)
+    lamr = (mu_r + 1.0) / dm
+    kk = np.arange(1, 10001, dtype=float)
+    dd = 2.0
+    dia = (kk * dd - dd * 0.5) * 1e-6
+    amg = piov6 * 997.0 * dia ** 3 * 1000.0
+    d6 = dia * 1e6
+    vt = np.where(d6 <= 134.43, 4.5795e3 * amg ** (2.0 / 3.0),
+                  np.where(d6 < 1511.64, 4.962e1 * amg ** (1.0 / 3.0),
+                           np.where(d6 < 3477.84, 1.732e1 * amg ** (1.0 / 6.0), 9.17)))
+    e = np.exp(-np.outer(lamr, dia))
+    w0 = 10.0 ** (mu_r * np.log10(dia) + 4 * mu_r) * e * dd * 1e-6
+    w3 = 10.0 ** ((mu_r + 3) * np.log10(dia) + 4 * mu_r) * e * dd * 1e-6
+    w5 = (vt * dia) ** 0.5 * 10.0 ** ((mu_r + 1) * np.log10(dia) + 3 * mu_r) * e * dd * 1e-6
+    vn = (w0 * vt).sum(1) / np.maximum(w0.sum(1), 1e-30)
+    vm = (w3 * vt).sum(1) / np.maximum(w3.sum(1), 1e-30)
+    revap = 10.0 ** (np.log10(np.maximum(w5.sum(1), 1e-30)) + (mu_r + 1) * np.log10(lamr) - 3 * mu_r)
+    return vn, vm, revap
+
+
+def test_rain_tables_match_numpy_restatement(tables):
+    vn, vm, revap = numpy_rain_tables()
+    for name, ref in [("vn", vn), ("vm", vm), ("revap", revap)]:
+        got = tables[name]
+        assert got.shape == (300, 10)
+        for j in range(10):  # constant mu_r: every mu column is the same
+            np.testing.assert_allclose(got[:, j], ref, rtol=1e-12, err_msg=name)
+    assert np.all(tables["mu_r"] == 1.0)
+    assert tables["dnu"][1] == -0.557 and tables["dnu"][15] == -0.966
+
+
+def test_incomplete_gamma_against_scipy(built):
+    sp = pytest.importorskip("scipy.special")
+    lib = built
+    # exposed through the table generator only; check via a tiny ctypes shim of the library
+    f = getattr(lib, "p3x_incomplete_gamma_q", None)
+    if f is None:
+        pytest.skip("no incomplete-gamma export")
+    f.restype = C.c_double
+    f.argtypes = [C.c_double, C.c_double]
+    for a in [1.0, 2.5, 4.0, 4.9, 7.0, 10.0]:
+        for x in [1e-6, 0.1, 1.0, 3.0, 5.0, 9.0, 20.0, 60.0]:
+            ref = sp.gammaincc(a, x)
+            got = f(a, x)
+            assert got == pytest.approx(ref, rel=1e-10, abs=1e-300), (a, x)
+
+
+def test_ice_table_shape_and_physics(tables):
+    ice = tables["ice"]
+    assert ice.shape == (5, 4, 50, 12)
+    assert np.all(np.isfinite(ice))
+    # fall speeds (cols 0, 1) positive; the mass-weighted one grows with mean
+    # mass; both saturate where the lambda limiter fixes the mean size
+    # (the number-weighted one is not monotone: mu_i varies with lambda)
+    for c in (0, 1):
+        assert np.all(ice[..., c] > 0)
+        assert np.all(ice[..., -1, c] == ice[..., -2, c])
+    assert np.all(np.diff(ice[..., 1], axis=2) >= -1e-12)
+    # mass-weighted fall speed >= number-weighted
+    assert np.all(ice[..., 1] >= ice[..., 0] * (1 - 1e-4))
+    # lambda-limiter bounds: nlarge (col 6) >= nsmall (col 7)
+    assert np.all(ice[..., 6] >= ice[..., 7])
+    # effective radius (col 5) between 1 micron and 1 cm; mean density (col 11)
+    # within [0, 917] kg m-3 (solid ice)
+    assert np.all((ice[..., 5] > 1e-6) & (ice[..., 5] < 1e-2))
+    assert np.all((ice[..., 11] > 0) & (ice[..., 11] <= 917.0 * (1 + 1e-4)))
+    coll = tables["collect"]
+    assert coll.shape == (5, 4, 50, 30, 2) and np.all(np.isfinite(coll))
+
+
+def test_ice_table_entries_against_scipy_integrals(tables):
+    """Recomputes the mass-weighted mean size and density moments for the
+    unrimed regime (rime fraction 0) with scipy's incomplete gamma and
+    independent numerical sums, for a few mean-mass classes."""
+    sp = pytest.importorskip("scipy.special")
+    pi, cs, ds = 3.14159, 0.0121, 1.9
+    dcrit = (pi / (6.0 * cs) * 900.0) ** (1.0 / (ds - 3.0))
+    for i_q in [10, 25, 40]:
+        q = 261.7 ** ((i_q + 1 + 10) * 0.1) * 1e-18
+        # lambda search on the generator's grid (first minimum)
+        ii = np.arange(1, 9001)
+        lam = 1.0013 ** ii * 100.0
+        mu = np.clip(0.076 * (lam / 100.0) ** 0.8 - 2.0, 0.0, 6.0)
+        lam = np.minimum(np.maximum(lam, (mu + 1) / 2000e-6), (mu + 1) / 2e-6)
+        n0 = lam ** (mu + 1) / sp.gamma(mu + 1)
+        cs1 = pi / 6 * 900.0
+        d1 = lam ** (-3 - mu - 1) * sp.gamma(mu + 4) * (1 - sp.gammaincc(mu + 4, dcrit * lam))
+        d2 = lam ** (-ds - mu - 1) * sp.gamma(mu + ds + 1) * sp.gammaincc(mu + ds + 1, dcrit * lam)
+        d2 = d2 - lam ** (-ds - mu - 1) * sp.gamma(mu + ds + 1) * sp.gammaincc(mu + ds + 1, 1e6 * lam)
+        qd = n0 * (cs1 * d1 + cs * np.maximum(d2, 0) + cs * lam ** (-ds - mu - 1) * sp.gamma(mu + ds + 1)
+                   * sp.gammaincc(mu + ds + 1, 1e6 * lam))
+        k = int(np.argmin(np.abs(q - qd)))
+        L = lam[k]
+        m = float(np.clip(0.076 * (L / 100.0) ** 0.8 - 2.0, 0.0, 6.0))
+        d = np.arange(1, 10001) * 2e-6 - 1e-6
+        c = np.where(d <= dcrit, cs1, cs)
+        e = np.where(d <= dcrit, 3.0, ds)
+        w = d ** m * np.exp(-L * d)
+        s4 = np.sum(c * d ** e * w)
+        dmm = np.sum(c * d ** (e + 1) * w) / s4
+        rhomm = np.sum((c * d ** e) ** 2 / (pi / 6 * d ** 3) * w) / s4
+        got = tables["ice"][0, 0, i_q]
+        assert got[10] == pytest.approx(dmm, rel=2e-4), i_q
+        assert got[11] == pytest.approx(rhomm, rel=2e-4), i_q
+
+
+def test_table_file_roundtrip(built, tables, tmp_path):
+    from scream_gb300 import _lib as L
+    path = tmp_path / "p3_lookup_table_1.dat-v4.1.1"
+    assert built.p3x_write_ice_table(str(path).encode(), b"4.1.1") == 0
+    first = path.read_text().splitlines()[0]
+    assert first.split() == ["VERSION", "4.1.1"]
+    t2 = L.host_tables(str(path))
+    np.testing.assert_array_equal(t2["ice"], tables["ice"])
+    np.testing.assert_allclose(t2["collect"], tables["collect"], rtol=0, atol=1e-15)
+    # wrong version is rejected with P3X_ETABLE
+    bad = tmp_path / "bad.dat"
+    bad.write_text(path.read_text().replace("VERSION 4.1.1", "VERSION 9.9.9", 1))
+    with pytest.raises(L.P3Error) as ei:
+        L.host_tables(str(bad))
+    assert ei.value.code == L.P3X_ETABLE
+
+
+def test_tables_match_committed_summary(tables):
+    summ = json.loads((GOLDEN / "table_summary.json").read_text())
+    for k, s in summ.items():
+        v = tables[k]
+        assert float(np.sum(np.abs(v))) == pytest.approx(s["abs_sum"], rel=1e-10), k
+        assert float(v.ravel()[v.size // 2]) == pytest.approx(s["mid"], rel=1e-10, abs=1e-300), k
