@@ -118,6 +118,11 @@ dev::RuntimeDev make_runtime(const p3x_runtime& r) {
   dumjj = std::min(dumjj, 9);
   d.t3_rdumjj = rdumjj;
   d.t3_dumjj = dumjj;
+  const double mu_r = r.constant_mu_rain;
+  d.g_mur1 = std::tgamma(mu_r + 1.0);
+  d.g_mur2 = std::tgamma(mu_r + 2.0);
+  d.lg_mur4 = std::log(std::tgamma(mu_r + 4.0));
+  d.lg_mur7 = std::log(std::tgamma(mu_r + 7.0));
   return d;
 }
 

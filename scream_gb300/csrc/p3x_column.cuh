@@ -16,7 +16,7 @@
  *      (p3_upwind_impl.hpp:14-116).  Substep loops are capped.
  *   4. homogeneous freezing + p3_main_part3 (level-parallel).
  *
- * Between phases, per-level quantities live in shared memory (13 FP64
+ * Between phases, per-level quantities live in shared memory (14 FP64
  * arrays per column); prognostic fields are written back to their global
  * arrays after each phase and re-read from L2 by the next.  Lookup tables
  * are read from global memory (L1/L2) or staged into shared memory once per
@@ -77,7 +77,7 @@ constexpr uint64_t kWaitNanosLimit = 2000000000ull; /* 2 s */
 
 /* shared arrays of one column group */
 enum {
-  A_TATM = 0, A_RHO, A_RHOFACR, A_RHOFACI, A_ACN, A_INVDZ, A_QVSL, A_QVSI, A_QVSSI,
+  A_TATM = 0, A_RHO, A_INVRHO, A_RHOFACR, A_RHOFACI, A_ACN, A_INVDZ, A_QVSL, A_QVSI, A_QVSSI,
   A_R0, A_R1, A_R2, A_R3, A_NARR,
   /* sedimentation re-uses the part2-only arrays */
   A_V1 = A_QVSL, A_V2 = A_QVSI, A_PFLUX = A_QVSSI
@@ -291,6 +291,7 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
     in.qv[o] = qv; in.th[o] = th;
     SMA(A_TATM, k) = T;
     SMA(A_RHO, k) = rho;
+    SMA(A_INVRHO, k) = inv_rho;
     SMA(A_RHOFACR, k) = double(rhofacr);
     SMA(A_RHOFACI, k) = double(rhofaci);
     SMA(A_ACN, k) = double(acn);
@@ -340,7 +341,7 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
     v.mu = v.dv = v.sc = v.dqsdt = v.dqsidt = v.ab = v.abi = v.kap = v.eii = TR(0);
     TR tv_fallspd = 0, tv_selfcol = 0, tv_qc2qi = 0, tv_melt = 0, tv_nr = 0, tv_qr2qi = 0,
        tv_lammax = 0, tv_lammin = 0, tv_vent = 0;
-    TR mu_c = 0, lamc = 0, cdist = 0, cdist1 = 0, mu_r = 0, lamr = 0, cdistr = 0, logn0r = 0;
+    TR mu_c = 0, lamc = 0, mu_r = 0, lamr = 0, cdistr = 0, logn0r = 0;
     TR epsi = 0, epsr = 0, epsc = 0, epsi_tot = 0;
     TR rho_qm_cloud = TR(400);
     bool wet = false;
@@ -353,7 +354,7 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
       {
         const TR n_in = TR(inc.nc);
         TR n_out = n_in;
-        get_cloud_dsd2<TR>(TR(inc.qc), n_out, mu_c, rho_r, lamc, cdist, cdist1);
+        get_cloud_dsd2<TR>(TR(inc.qc), n_out, mu_c, rho_r, lamc);
         apply_n_adjust(inc.nc, n_in, n_out);
       }
       s.nc = inc.nc * cld_l;
@@ -363,7 +364,7 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
         get_rain_dsd2<TR>(TR(inc.qr), n_out, mu_r, lamr, rt);
         apply_n_adjust(inc.nr, n_in, n_out);
         if (inc.qr >= C::QSMALL) {
-          cdistr = TR(inc.nr) / m_tgamma(mu_r + TR(1));
+          cdistr = TR(inc.nr) / TR(rt.g_mur1);
           logn0r = m_log10(cdistr) + (mu_r + TR(1)) * m_log10(lamr);
         }
       }
@@ -416,7 +417,7 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
       rho_qm_cloud = calc_rime_density<TR>(T_r, rhofaci_r, tv_fallspd, TR(acn), lamc, mu_c, qc_r,
                                            r.qc2qi_collect_tend);
       if (do_ice) {
-        cldliq_immersion_freezing<TR>(T_r, lamc, mu_c, cdist1, qc_r, r, rt);
+        cldliq_immersion_freezing<TR>(T_r, lamc, mu_c, nc_r, qc_r, r, rt);
         rain_immersion_freezing<TR>(T_r, lamr, mu_r, cdistr, qr_r, r, rt);
       }
       /* calc_liq_relaxation_timescale, p3_calc_liq_relaxation_timescale_impl.hpp:13-43 */
@@ -424,7 +425,7 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
         Table3<TR> t3;
         lookup3<TR>(mu_r, lamr, rt, t3);
         epsr = TR(2) * TR(C::Pi) * cdistr * rho_r * v.dv *
-               (TR(C::f1r) * m_tgamma(mu_r + TR(2)) / lamr +
+               (TR(C::f1r) * TR(rt.g_mur2) / lamr +
                 TR(C::f2r) * m_sqrt(rho_r / v.mu) * m_cbrt(v.sc) * apply_table3<TR>(tb, tb.revap, t3));
       }
       {
@@ -505,6 +506,10 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
   if (!group_any<LANES>(mask, hydro)) return;
 
   /* ---------------- phase 3: sedimentation ---------------- */
+  /* Shared arrays during sedimentation: V1/V2 fall speeds (re-using the
+   * part2-only saturation arrays), R0..R3 the species state, CLD the
+   * species' cloud fraction (cloud and ice re-use A_QVSSI; rain re-uses A_ACN,
+   * free once cloud sedimentation is done), PF the rain flux accumulator. */
   double* const V1 = &SMA(A_V1, 0);
   double* const V2 = &SMA(A_V2, 0);
   double* const PF = &SMA(A_PFLUX, 0);
@@ -512,12 +517,17 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
   double* const R1 = &SMA(A_R1, 0);
   double* const R2 = &SMA(A_R2, 0);
   double* const R3 = &SMA(A_R3, 0);
+  const double* const RHO = &SMA(A_RHO, 0);
+  const double* const INVRHO = &SMA(A_INVRHO, 0);
+  const double* const INVDZ = &SMA(A_INVDZ, 0);
+  constexpr bool kF64 = sizeof(TR) == sizeof(double);
 
 #pragma unroll 1
   for (int sp = 0; sp < 3; ++sp) {
     double* g0 = sp == 0 ? in.qc : (sp == 1 ? in.qr : in.qi);
     double* g1 = sp == 0 ? in.nc : (sp == 1 ? in.nr : in.ni);
     const double* cldp = sp == 0 ? in.cld_frac_l : (sp == 1 ? in.cld_frac_r : in.cld_frac_i);
+    double* const CLD = sp == 1 ? &SMA(A_ACN, 0) : &SMA(A_QVSSI, 0);
     const int nfield = sp == 0 ? (predictNc ? 2 : 1) : (sp == 1 ? 2 : 4);
 
     /* load the species into shared memory; find top / bottom (p3_find_impl.hpp) */
@@ -526,6 +536,7 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
       const double q = g0[co + k];
       R0[k] = q;
       R1[k] = g1[co + k];
+      CLD[k] = cldp[co + k];
       if (sp == 2) {
         R2[k] = in.qm[co + k];
         R3[k] = in.bm[co + k];
@@ -535,14 +546,16 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
         my_bot = max(my_bot, k);
       }
     }
+    const int k_qxtop = group_min_int<LANES>(mask, my_top);
+    int k_qxbot = group_max_int<LANES>(mask, my_bot);
+    if (k_qxbot < 0) continue; /* species absent (group-uniform) */
     if (sp == 1) {
       for (int k = lane; k <= nk; k += LANES) PF[k] = 0;
     }
-    const int k_qxtop = group_min_int<LANES>(mask, my_top);
-    int k_qxbot = group_max_int<LANES>(mask, my_bot);
     __syncwarp(mask);
-    if (k_qxbot < 0) continue; /* species absent */
 
+    /* From here on lane l owns levels k_qxtop + l + j*LANES in both the
+     * fall-speed pass and the flux walk, so only shuffles cross lanes. */
     double dt_left = dt, prt_accum = 0.0;
     bool first = true;
     int nsub = 0;
@@ -553,12 +566,8 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
       }
       /* fall speeds on [k_qxtop, k_qxbot] and the Courant maximum */
       double lmax = 0.0;
-      for (int k = lane; k < nk; k += LANES) {
-        V1[k] = 0;
-        V2[k] = 0;
-        if (k < k_qxtop || k > k_qxbot) continue;
-        const int64_t o = co + k;
-        const double cld = cldp[o];
+      for (int k = k_qxtop + lane; k <= k_qxbot; k += LANES) {
+        const double cld = CLD[k];
         double v1 = 0, v2 = 0;
         if (sp == 0) {
           double qc_incld, nc_incld;
@@ -572,22 +581,31 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
               nc_incld = 0;
             }
             qc_incld = vmin(qc_incld, C::incloud_limit);
-          } else {
+          } else if (kF64) {
             qc_incld = R0[k] / cld;
             nc_incld = R1[k] / cld;
+          } else {
+            qc_incld = double(float(R0[k]) / float(cld));
+            nc_incld = double(float(R1[k]) / float(cld));
           }
           if (qc_incld > C::QSMALL) {
-            TR mu_c, lamc, cdist, cdist1;
+            TR mu_c, lamc;
             const TR n_in = TR(nc_incld);
             TR n_out = n_in;
-            get_cloud_dsd2<TR>(TR(qc_incld), n_out, mu_c, TR(SMA(A_RHO, k)), lamc, cdist, cdist1);
-            apply_n_adjust(nc_incld, n_in, n_out);
-            R1[k] = nc_incld * cld;
-            const TR dum = TR(1) / m_pow(lamc, TR(C::bcn));
+            get_cloud_dsd2<TR>(TR(qc_incld), n_out, mu_c, TR(RHO[k]), lamc);
+            if (kF64) {
+              R1[k] = double(n_out) * cld;
+            } else if (n_out != n_in) {
+              R1[k] = double(n_out) * cld;
+            }
+            /* Stokes fall speeds, p3_cloud_sed_impl.hpp:99-103, with
+             * Gamma(6+mu)/Gamma(4+mu) = (5+mu)(4+mu) and
+             * Gamma(3+mu)/Gamma(1+mu) = (2+mu)(1+mu) (bcn = 2) */
+            const TR dum = TR(1) / (lamc * lamc);
             const TR acn = TR(SMA(A_ACN, k));
-            v1 = double(acn * m_tgamma(TR(4) + TR(C::bcn) + mu_c) * dum / m_tgamma(mu_c + TR(4)));
-            if (predictNc) v2 = double(acn * m_tgamma(TR(1) + TR(C::bcn) + mu_c) * dum / m_tgamma(mu_c + TR(1)));
-            lmax = vmax(lmax, v1 * dt_left * SMA(A_INVDZ, k));
+            v1 = double(acn * ((TR(5) + mu_c) * (TR(4) + mu_c)) * dum);
+            if (predictNc) v2 = double(acn * ((TR(2) + mu_c) * (TR(1) + mu_c)) * dum);
+            lmax = vmax(lmax, v1 * dt_left * INVDZ[k]);
           }
         } else if (sp == 1) {
           double qr_incld, nr_incld;
@@ -601,29 +619,34 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
               nr_incld = 0;
             }
             qr_incld = vmin(qr_incld, C::precip_limit);
-          } else {
+          } else if (kF64) {
             qr_incld = R0[k] / cld;
             nr_incld = R1[k] / cld;
+          } else {
+            qr_incld = double(float(R0[k]) / float(cld));
+            nr_incld = double(float(R1[k]) / float(cld));
           }
           if (qr_incld > C::QSMALL) {
             TR mu_r = 0, lamr;
             const TR n_in = TR(nr_incld);
             TR n_out = n_in;
             get_rain_dsd2<TR>(TR(qr_incld), n_out, mu_r, lamr, rt);
-            apply_n_adjust(nr_incld, n_in, n_out);
             Table3<TR> t3;
             lookup3<TR>(mu_r, lamr, rt, t3);
             const TR rhofacr = TR(SMA(A_RHOFACR, k));
             v1 = double(apply_table3<TR>(tb, tb.vm, t3) * rhofacr);
             v2 = double(apply_table3<TR>(tb, tb.vn, t3) * rhofacr);
-            R1[k] = nr_incld * cld;
-            lmax = vmax(lmax, v1 * dt_left * SMA(A_INVDZ, k));
+            if (kF64) {
+              R1[k] = double(n_out) * cld;
+            } else if (n_out != n_in) {
+              R1[k] = double(n_out) * cld;
+            }
+            lmax = vmax(lmax, v1 * dt_left * INVDZ[k]);
           }
         } else {
           double qi_incld, ni_incld, qm_incld, bm_incld;
           if (first) {
             const double inv_cld = 1 / cld;
-            const double inv_cld_l = 1 / in.cld_frac_l[o];
             if (R0[k] >= C::QSMALL) {
               qi_incld = R0[k] * inv_cld;
               ni_incld = vmax(R1[k] * inv_cld, 0.);
@@ -633,18 +656,24 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
             }
             if (R0[k] >= C::QSMALL && R2[k] >= C::QSMALL) {
               qm_incld = R2[k] * inv_cld;
-              bm_incld = vmax(R3[k] * inv_cld_l, 0.);
+              bm_incld = vmax(R3[k] * (1 / in.cld_frac_l[co + k]), 0.);
             } else {
               qm_incld = 0;
               bm_incld = 0;
             }
             qi_incld = vmin(qi_incld, C::incloud_limit);
             bm_incld = vmin(bm_incld, C::incloud_limit);
-          } else {
+          } else if (kF64) {
             qi_incld = R0[k] / cld;
             ni_incld = R1[k] / cld;
             qm_incld = R2[k] / cld;
             bm_incld = R3[k] / cld;
+          } else {
+            const float icf = 1.0f / float(cld);
+            qi_incld = double(float(R0[k]) * icf);
+            ni_incld = double(float(R1[k]) * icf);
+            qm_incld = double(float(R2[k]) * icf);
+            bm_incld = double(float(R3[k]) * icf);
           }
           if (qi_incld > C::QSMALL) {
             ni_incld = vmax(ni_incld, C::NSMALL);
@@ -663,79 +692,140 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
             const TR rhofaci = TR(SMA(A_RHOFACI, k));
             v1 = double(TR(rt.ice_sedimentation_factor) * tv_q * rhofaci);
             v2 = double(TR(rt.ice_sedimentation_factor) * tv_n * rhofaci);
-            lmax = vmax(lmax, v1 * dt_left * SMA(A_INVDZ, k));
+            lmax = vmax(lmax, v1 * dt_left * INVDZ[k]);
           }
         }
         V1[k] = v1;
         V2[k] = v2;
       }
+      if (k_qxbot < kbot && lane == (k_qxbot + 1 - k_qxtop) % LANES) {
+        V1[k_qxbot + 1] = 0; /* the cell receiving the leading edge has no fall speed */
+        V2[k_qxbot + 1] = 0;
+      }
       const double Co_max = group_max<LANES>(mask, lmax);
-      __syncwarp(mask);
       if (!(Co_max >= 0) || Co_max > 2.0e9) {
         err |= kErrNumeric;
         break;
       }
 
-      /* generalized_sedimentation + calc_first_order_upwind_step (kdir = -1) */
+      /* generalized_sedimentation + calc_first_order_upwind_step (kdir = -1):
+       * fluxes from start-of-substep values, inflow from the level above by a
+       * shuffle (carried across chunks), zero inflow at k_qxtop. */
       const int tmpint1 = static_cast<int>(Co_max + 1);
       const double dt_sub = dt_left / tmpint1;
       const int k_temp = (k_qxbot == kbot) ? k_qxbot : k_qxbot + 1;
-      double carry0 = 0, carry1 = 0, carry2 = 0, carry3 = 0, flux_bot = 0;
-      for (int base = k_qxtop; base <= k_temp; base += LANES) {
-        const int k = base + lane;
-        const bool act = k <= k_temp;
-        double f0 = 0, f1 = 0, f2 = 0, f3 = 0;
-        double rho = 0, invdz = 0, v1 = 0, v2 = 0;
-        if (act) {
-          rho = SMA(A_RHO, k);
-          invdz = SMA(A_INVDZ, k);
-          v1 = V1[k];
-          v2 = V2[k];
-          f0 = v1 * R0[k] * rho;
-          if (nfield > 1) f1 = v2 * R1[k] * rho;
+      if constexpr (kF64) {
+        double carry0 = 0, carry1 = 0, carry2 = 0, carry3 = 0, flux_bot = 0;
+        for (int base = k_qxtop; base <= k_temp; base += LANES) {
+          const int k = base + lane;
+          const bool act = k <= k_temp;
+          double f0 = 0, f1 = 0, f2 = 0, f3 = 0;
+          if (act) {
+            const double rho = RHO[k];
+            const double v1 = V1[k];
+            f0 = v1 * R0[k] * rho;
+            if (nfield > 1) f1 = V2[k] * R1[k] * rho;
+            if (nfield > 2) {
+              f2 = v1 * R2[k] * rho;
+              f3 = v1 * R3[k] * rho;
+            }
+          }
+          double u0 = __shfl_up_sync(mask, f0, 1, LANES);
+          double u1 = __shfl_up_sync(mask, f1, 1, LANES);
+          double u2 = 0, u3 = 0;
           if (nfield > 2) {
-            f2 = v1 * R2[k] * rho;
-            f3 = v1 * R3[k] * rho;
+            u2 = __shfl_up_sync(mask, f2, 1, LANES);
+            u3 = __shfl_up_sync(mask, f3, 1, LANES);
+          }
+          if (lane == 0) {
+            u0 = carry0; u1 = carry1; u2 = carry2; u3 = carry3;
+          }
+          if (act) {
+            const double invdz = INVDZ[k], irho = INVRHO[k];
+            R0[k] += ((u0 - f0) * invdz) * dt_sub * irho;
+            if (nfield > 1) R1[k] += ((u1 - f1) * invdz) * dt_sub * irho;
+            if (nfield > 2) {
+              R2[k] += ((u2 - f2) * invdz) * dt_sub * irho;
+              R3[k] += ((u3 - f3) * invdz) * dt_sub * irho;
+            }
+            if (sp == 1) PF[k + 1] += f0;
+            if (k == kbot) flux_bot = f0;
+          }
+          carry0 = __shfl_sync(mask, f0, LANES - 1, LANES);
+          carry1 = __shfl_sync(mask, f1, LANES - 1, LANES);
+          if (nfield > 2) {
+            carry2 = __shfl_sync(mask, f2, LANES - 1, LANES);
+            carry3 = __shfl_sync(mask, f3, LANES - 1, LANES);
           }
         }
-        double u0 = __shfl_up_sync(mask, f0, 1, LANES);
-        double u1 = __shfl_up_sync(mask, f1, 1, LANES);
-        double u2 = __shfl_up_sync(mask, f2, 1, LANES);
-        double u3 = __shfl_up_sync(mask, f3, 1, LANES);
-        if (lane == 0) {
-          u0 = carry0; u1 = carry1; u2 = carry2; u3 = carry3;
+        if (k_qxbot == kbot) {
+          const int owner = (kbot - k_qxtop) % LANES;
+          prt_accum += __shfl_sync(mask, flux_bot, owner, LANES) * dt_sub;
+        } else {
+          k_qxbot += 1;
         }
-        if (act) {
-          const double irho = 1 / rho;
-          R0[k] += ((u0 - f0) * invdz) * dt_sub * irho;
-          if (nfield > 1) R1[k] += ((u1 - f1) * invdz) * dt_sub * irho;
-          if (nfield > 2) {
-            R2[k] += ((u2 - f2) * invdz) * dt_sub * irho;
-            R3[k] += ((u3 - f3) * invdz) * dt_sub * irho;
-          }
-          if (sp == 1) PF[k + 1] += f0;
-          if (k == kbot) flux_bot = f0;
-        }
-        carry0 = __shfl_sync(mask, f0, LANES - 1, LANES);
-        carry1 = __shfl_sync(mask, f1, LANES - 1, LANES);
-        carry2 = __shfl_sync(mask, f2, LANES - 1, LANES);
-        carry3 = __shfl_sync(mask, f3, LANES - 1, LANES);
-      }
-      if (k_qxbot == kbot) {
-        const int owner = (kbot - k_qxtop) % LANES;
-        const double fb = __shfl_sync(mask, flux_bot, owner, LANES);
-        prt_accum += fb * dt_sub;
       } else {
-        k_qxbot += 1;
+        /* FP32-bulk: fluxes in FP32; every difference and the state update in
+         * FP64 with one FP64 coefficient per level, so the flux leaving a cell
+         * is exactly the flux entering the next (column mass telescopes). */
+        float carry0 = 0, carry1 = 0, carry2 = 0, carry3 = 0, flux_bot = 0;
+        for (int base = k_qxtop; base <= k_temp; base += LANES) {
+          const int k = base + lane;
+          const bool act = k <= k_temp;
+          float f0 = 0, f1 = 0, f2 = 0, f3 = 0;
+          if (act) {
+            const float rho = float(RHO[k]);
+            const float v1 = float(V1[k]);
+            f0 = v1 * float(R0[k]) * rho;
+            if (nfield > 1) f1 = float(V2[k]) * float(R1[k]) * rho;
+            if (nfield > 2) {
+              f2 = v1 * float(R2[k]) * rho;
+              f3 = v1 * float(R3[k]) * rho;
+            }
+          }
+          float u0 = __shfl_up_sync(mask, f0, 1, LANES);
+          float u1 = __shfl_up_sync(mask, f1, 1, LANES);
+          float u2 = 0, u3 = 0;
+          if (nfield > 2) {
+            u2 = __shfl_up_sync(mask, f2, 1, LANES);
+            u3 = __shfl_up_sync(mask, f3, 1, LANES);
+          }
+          if (lane == 0) {
+            u0 = carry0; u1 = carry1; u2 = carry2; u3 = carry3;
+          }
+          if (act) {
+            const double coef = INVDZ[k] * dt_sub * INVRHO[k];
+            R0[k] += (double(u0) - double(f0)) * coef;
+            if (nfield > 1) R1[k] += (double(u1) - double(f1)) * coef;
+            if (nfield > 2) {
+              R2[k] += (double(u2) - double(f2)) * coef;
+              R3[k] += (double(u3) - double(f3)) * coef;
+            }
+            if (sp == 1) PF[k + 1] += double(f0);
+            if (k == kbot) flux_bot = f0;
+          }
+          carry0 = __shfl_sync(mask, f0, LANES - 1, LANES);
+          carry1 = __shfl_sync(mask, f1, LANES - 1, LANES);
+          if (nfield > 2) {
+            carry2 = __shfl_sync(mask, f2, LANES - 1, LANES);
+            carry3 = __shfl_sync(mask, f3, LANES - 1, LANES);
+          }
+        }
+        if (k_qxbot == kbot) {
+          const int owner = (kbot - k_qxtop) % LANES;
+          prt_accum += double(__shfl_sync(mask, flux_bot, owner, LANES)) * dt_sub;
+        } else {
+          k_qxbot += 1;
+        }
       }
       dt_left -= dt_sub;
       first = false;
-      __syncwarp(mask);
     }
     if (sp == 0) precip_liq_surf = prt_accum * C::INV_RHO_H2O * inv_dt;
     else if (sp == 1) precip_liq_surf += prt_accum * C::INV_RHO_H2O * inv_dt;
     else precip_ice_surf += prt_accum * C::INV_RHO_H2O * inv_dt;
 
+    __syncwarp(mask);
     for (int k = lane; k < nk; k += LANES) {
       g0[co + k] = R0[k];
       g1[co + k] = R1[k];
@@ -796,10 +886,10 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
     if (s.qc >= C::QSMALL) {
       const double qc_incld = s.qc / cld_l;
       double nc_incld = s.nc / cld_l;
-      TR mu_c, lamc, cd, cd1;
+      TR mu_c, lamc;
       const TR n_in = TR(nc_incld);
       TR n_out = n_in;
-      get_cloud_dsd2<TR>(TR(qc_incld), n_out, mu_c, TR(rho), lamc, cd, cd1);
+      get_cloud_dsd2<TR>(TR(qc_incld), n_out, mu_c, TR(rho), lamc);
       apply_n_adjust(nc_incld, n_in, n_out);
       s.nc = nc_incld * cld_l;
       eff_qc = double(TR(0.5) * (mu_c + TR(3)) / lamc);
@@ -919,7 +1009,7 @@ __global__ void __launch_bounds__(256) p3_main_kernel(const Inst inst0, const KP
   double* sm = group_base + size_t(g_in_block) * A_NARR * kp.sm_stride;
   /* liquid saturation vapour pressure at 0 C (qsat0 of ice_melting and
    * ice_cldliq_wet_growth), evaluated once */
-  const double esat0 = double(murphy_koop_svp<TR>(TR(C::Tmelt), false, err));
+  const double esat0 = murphy_koop_svp<double>(C::Tmelt, false, err);
 
   const int groups_total = gridDim.x * kp.groups_per_block;
   for (int w = blockIdx.x * kp.groups_per_block + g_in_block; w < kp.nwork; w += groups_total) {

@@ -59,6 +59,11 @@ struct RuntimeDev {
   double cons3;       /* autoconversion CONS3 (p3_autoconversion_impl.hpp:27-32) */
   int t3_dumjj;       /* Table3 mu index for the constant mu_r (p3_table3_impl.hpp:52-62) */
   double t3_rdumjj;
+  /* Gamma function of the constant rain shape parameter mu_r */
+  double g_mur1;      /* Gamma(mu_r + 1)       */
+  double g_mur2;      /* Gamma(mu_r + 2)       */
+  double lg_mur4;     /* log Gamma(mu_r + 4)   */
+  double lg_mur7;     /* log Gamma(mu_r + 7)   */
 };
 
 /* ------------------------------------------------------------------ */
@@ -108,11 +113,13 @@ __device__ __forceinline__ TR murphy_koop_svp(TR t, bool ice, uint32_t& err) {
                 (TR(53.878) - (TR(1331.22) / t) - (TR(9.44523) * logt) + TR(0.014025) * t)));
 }
 
-/* qv_sat_dry (MurphyKoop), physics_saturation_impl.hpp:126-157.  The vapour
- * pressure is evaluated in TR; the mixing ratio is formed in FP64. */
+/* qv_sat_dry (MurphyKoop), physics_saturation_impl.hpp:126-157.  Always FP64,
+ * also in the FP32-bulk form: the saturation mixing ratio enters residuals
+ * (qv - qv_sat) that are small near saturation, where an FP32 vapour pressure
+ * (relative error ~1e-7) would decide evaporation and supersaturation limits. */
 template <class TR>
 __device__ __forceinline__ double qv_sat_dry(double t, double p, bool ice, uint32_t& err) {
-  const double e_pres = double(murphy_koop_svp<TR>(TR(t), ice, err));
+  const double e_pres = murphy_koop_svp<double>(t, ice, err);
   return C::ep_2 * e_pres / vmax(p, 1.e-3);
 }
 
@@ -332,11 +339,13 @@ __device__ __forceinline__ void calc_incloud(double qc, double qr, double qi, do
   }
 }
 
-/* get_cloud_dsd2, p3/impl/p3_dsd2_impl.hpp:14-74 (iparam = 3) */
+/* get_cloud_dsd2, p3/impl/p3_dsd2_impl.hpp:14-74 (iparam = 3).  The
+ * spectral moments cdist (used only by the inactive cloud relaxation time
+ * epsc) and cdist1 = nc/Gamma(mu_c+1) (immersion freezing, evaluated there
+ * with the Gamma recurrence) are not needed by any output. */
 template <class TR>
-__device__ __forceinline__ void get_cloud_dsd2(TR qc, TR& nc, TR& mu_c, TR rho, TR& lamc, TR& cdist,
-                                               TR& cdist1) {
-  lamc = 0; cdist = 0; cdist1 = 0; mu_c = 0;
+__device__ __forceinline__ void get_cloud_dsd2(TR qc, TR& nc, TR& mu_c, TR rho, TR& lamc) {
+  lamc = 0; mu_c = 0;
   if (qc >= TR(C::QSMALL)) {
     nc = vmax(nc, TR(C::NSMALL));
     TR mu = TR(0.0005714) * (nc * TR(1.e-6) * rho) + TR(0.2714);
@@ -354,8 +363,6 @@ __device__ __forceinline__ void get_cloud_dsd2(TR qc, TR& nc, TR& mu_c, TR rho, 
       nc = TR(6) * (lamc * lamc * lamc) * qc /
            (TR(C::Pi) * TR(C::RHO_H2O) * (mu_c + TR(3)) * (mu_c + TR(2)) * (mu_c + TR(1)));
     }
-    cdist = nc * (mu_c + TR(1)) / lamc;
-    cdist1 = nc / m_tgamma(mu_c + TR(1));
   }
 }
 
@@ -558,7 +565,8 @@ __device__ __forceinline__ TR calc_rime_density(TR T_atm, TR rhofaci, TR tv_fall
   if (qc2qi_collect_tend >= TR(C::QSMALL) && T_atm < TR(C::T_zerodegc)) {
     const TR vtrmi1 = tv_fallspd * rhofaci;
     if (qc_incld >= TR(C::QSMALL)) {
-      const TR Vt_qc = acn * m_tgamma(TR(4) + TR(C::bcn) + mu_c) / (m_pow(lamc, TR(C::bcn)) * m_tgamma(TR(4) + mu_c));
+      /* Gamma(4+bcn+mu_c)/Gamma(4+mu_c) = (5+mu_c)(4+mu_c) for bcn = 2 */
+      const TR Vt_qc = acn * ((TR(5) + mu_c) * (TR(4) + mu_c)) / (lamc * lamc);
       const TR D_c = (TR(4) + mu_c) / lamc;
       const TR V_impact = m_fabs(vtrmi1 - Vt_qc);
       const TR inv_Tc = TR(1) / vmin(TR(-0.001), T_atm - TR(C::T_zerodegc));
@@ -573,21 +581,26 @@ __device__ __forceinline__ TR calc_rime_density(TR T_atm, TR rhofaci, TR tv_fall
   return rho_qm_cloud;
 }
 
-/* cldliq_immersion_freezing, p3/impl/p3_cldliq_imm_freezing_impl.hpp:13-50 */
+/* cldliq_immersion_freezing, p3/impl/p3_cldliq_imm_freezing_impl.hpp:13-50.
+ * cdist1 * Gamma(7+mu_c) and cdist1 * Gamma(4+mu_c), with cdist1 =
+ * nc/Gamma(mu_c+1) (p3_dsd2_impl.hpp:72), are evaluated as nc times the
+ * rising products (1+mu)...(6+mu) and (1+mu)(2+mu)(3+mu). */
 template <class TR>
-__device__ __forceinline__ void cldliq_immersion_freezing(TR T_atm, TR lamc, TR mu_c, TR cdist1, TR qc_incld,
+__device__ __forceinline__ void cldliq_immersion_freezing(TR T_atm, TR lamc, TR mu_c, TR nc_incld, TR qc_incld,
                                                           Rates<TR>& r, const RuntimeDev& rt) {
   if (qc_incld >= TR(C::QSMALL) && T_atm <= TR(C::T_rainfrz)) {
     const TR expAimmDt = m_exp(TR(rt.immersion_freezing_exponent) * (TR(C::T_zerodegc) - T_atm));
     const TR inv_lamc = TR(1) / lamc;
     const TR inv_lamc3 = inv_lamc * inv_lamc * inv_lamc;
+    const TR p3 = (TR(1) + mu_c) * (TR(2) + mu_c) * (TR(3) + mu_c);
+    const TR p6 = p3 * ((TR(4) + mu_c) * (TR(5) + mu_c) * (TR(6) + mu_c));
     if constexpr (sizeof(TR) == sizeof(double)) {
-      r.qc2qi_hetero_freeze_tend = TR(C::CONS6) * cdist1 * m_tgamma(TR(7) + mu_c) * expAimmDt * sq(inv_lamc3);
+      r.qc2qi_hetero_freeze_tend = TR(C::CONS6) * (nc_incld * p6) * expAimmDt * sq(inv_lamc3);
     } else {
       /* (1/lamc)^6 underflows single precision: multiply it in twice */
-      r.qc2qi_hetero_freeze_tend = TR(C::CONS6) * cdist1 * m_tgamma(TR(7) + mu_c) * expAimmDt * inv_lamc3 * inv_lamc3;
+      r.qc2qi_hetero_freeze_tend = TR(C::CONS6) * (nc_incld * p6) * expAimmDt * inv_lamc3 * inv_lamc3;
     }
-    r.nc2ni_immers_freeze_tend = TR(C::CONS5) * cdist1 * m_tgamma(TR(4.0) + mu_c) * expAimmDt * inv_lamc3;
+    r.nc2ni_immers_freeze_tend = TR(C::CONS5) * (nc_incld * p3) * expAimmDt * inv_lamc3;
   }
 }
 
@@ -597,10 +610,13 @@ __device__ __forceinline__ void rain_immersion_freezing(TR T_atm, TR lamr, TR mu
                                                         Rates<TR>& r, const RuntimeDev& rt) {
   if (qr_incld >= TR(C::QSMALL) && T_atm <= TR(C::T_rainfrz)) {
     const TR e = m_exp(TR(rt.immersion_freezing_exponent) * (TR(C::T_zerodegc) - T_atm));
+    /* mu_r is the runtime constant here: log(Gamma(7+mu_r)) and
+     * log(Gamma(4+mu_r)) are precomputed on the host */
+    (void)mu_r;
     r.qr2qi_immers_freeze_tend =
-        TR(C::CONS6) * m_exp(m_log(cdistr) + m_log(m_tgamma(TR(7.) + mu_r)) - TR(6.) * m_log(lamr)) * e;
+        TR(C::CONS6) * m_exp(m_log(cdistr) + TR(rt.lg_mur7) - TR(6.) * m_log(lamr)) * e;
     r.nr2ni_immers_freeze_tend =
-        TR(C::CONS5) * m_exp(m_log(cdistr) + m_log(m_tgamma(TR(4.) + mu_r)) - TR(3.) * m_log(lamr)) * e;
+        TR(C::CONS5) * m_exp(m_log(cdistr) + TR(rt.lg_mur4) - TR(3.) * m_log(lamr)) * e;
   }
 }
 

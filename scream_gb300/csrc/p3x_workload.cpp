@@ -215,7 +215,7 @@ void gen_mixed_column(int64_t i, int nk, double* const* f, int64_t off) {
 
 int workload_generate(int kind, uint64_t seed, int col0, int ncol, int nlev, double* const* fields,
                       int64_t ld) {
-  if (ncol < 0 || nlev <= 1 || ld < nlev || !fields) return P3X_EINVAL;
+  if (ncol < 0 || nlev < 1 || ld < nlev || !fields) return P3X_EINVAL;
   for (int fld = 0; fld < P3X_NUM_INPUTS; ++fld)
     if (!fields[fld]) return P3X_EINVAL;
   if (kind == 2 && nlev < 36) return P3X_EINVAL;
