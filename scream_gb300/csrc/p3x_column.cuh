@@ -395,16 +395,17 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
         inc.ni = vmax(inc.ni, double(tv_lammin) * inc.ni);
       }
       const TR qi_r = TR(inc.qi), qc_r = TR(inc.qc), ni_r = TR(inc.ni), nc_r = TR(inc.nc), qr_r = TR(inc.qr);
-      const TR qsat0 = TR(C::ep_2 * esat0 / vmax(pres, 1.e-3));
+      const double dT0 = T - C::Tmelt;
+      const double dqv0 = C::ep_2 * esat0 / vmax(pres, 1.e-3) - s.qv;
       if (do_ice) {
-        ice_cldliq_collection<TR>(rho_r, T_r, rhofaci_r, tv_qc2qi, qi_r, qc_r, ni_r, nc_r, r, rt);
-        ice_rain_collection<TR>(rho_r, T_r, rhofaci_r, logn0r, tv_nr, tv_qr2qi, qi_r, ni_r, qr_r, r, rt);
+        ice_cldliq_collection<TR>(rho_r, T, rhofaci_r, tv_qc2qi, qi_r, qc_r, ni_r, nc_r, r, rt);
+        ice_rain_collection<TR>(rho_r, T, rhofaci_r, logn0r, tv_nr, tv_qr2qi, qi_r, ni_r, qr_r, r, rt);
         ice_self_collection<TR>(rho_r, rhofaci_r, tv_selfcol, v.eii, TR(inc.qm), qi_r, ni_r, r);
       }
-      ice_melting<TR>(rho_r, T_r, qsat0, rhofaci_r, tv_melt, tv_vent, v, TR(s.qv), qi_r, ni_r, r);
+      ice_melting<TR>(rho_r, dT0, dqv0, rhofaci_r, tv_melt, tv_vent, v, qi_r, ni_r, r);
       if (do_ice) {
-        wet = ice_cldliq_wet_growth<TR>(rho_r, T_r, qsat0, rhofaci_r, tv_melt, tv_vent, v, TR(s.qv), qc_r,
-                                        qi_r, ni_r, qr_r, r);
+        wet = ice_cldliq_wet_growth<TR>(rho_r, dT0, dqv0, rhofaci_r, tv_melt, tv_vent, v, qc_r, qi_r, ni_r,
+                                        qr_r, r);
       }
       /* ice_relaxation_timescale, p3_ice_relaxation_timescale_impl.hpp:9-37 */
       if (inc.qi >= C::QSMALL && T < C::Tmelt) {

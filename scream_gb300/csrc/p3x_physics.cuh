@@ -462,10 +462,10 @@ __device__ __forceinline__ void get_time_space_phys_variables(TR T_atm, TR pres,
 
 /* ice_cldliq_collection, p3/impl/p3_ice_collection_impl.hpp:9-52 */
 template <class TR>
-__device__ __forceinline__ void ice_cldliq_collection(TR rho, TR temp, TR rhofaci, TR tv, TR qi_incld,
+__device__ __forceinline__ void ice_cldliq_collection(TR rho, double temp, TR rhofaci, TR tv, TR qi_incld,
                                                       TR qc_incld, TR ni_incld, TR nc_incld,
                                                       Rates<TR>& r, const RuntimeDev& rt) {
-  const bool t_neg = temp <= TR(C::Tmelt);
+  const bool t_neg = temp <= C::Tmelt;
   const bool both = qi_incld >= TR(C::QSMALL) && qc_incld >= TR(C::QSMALL);
   const TR f = TR(rt.cldliq_to_ice_collection_factor);
   if (both && t_neg) r.qc2qi_collect_tend = rhofaci * tv * qc_incld * f * rho * ni_incld;
@@ -479,10 +479,10 @@ __device__ __forceinline__ void ice_cldliq_collection(TR rho, TR temp, TR rhofac
 
 /* ice_rain_collection, p3_ice_collection_impl.hpp:54-101 */
 template <class TR>
-__device__ __forceinline__ void ice_rain_collection(TR rho, TR temp, TR rhofaci, TR logn0r, TR tv_nr,
+__device__ __forceinline__ void ice_rain_collection(TR rho, double temp, TR rhofaci, TR logn0r, TR tv_nr,
                                                     TR tv_qr, TR qi_incld, TR ni_incld, TR qr_incld,
                                                     Rates<TR>& r, const RuntimeDev& rt) {
-  const bool t_neg = temp <= TR(C::Tmelt);
+  const bool t_neg = temp <= C::Tmelt;
   const bool both = qi_incld >= TR(C::QSMALL) && qr_incld >= TR(C::QSMALL);
   const TR f = TR(rt.rain_to_ice_collection_factor);
   if (both && t_neg) {
@@ -510,13 +510,15 @@ __device__ __forceinline__ void ice_self_collection(TR rho, TR rhofaci, TR tv, T
 }
 
 /* ice_melting, p3/impl/p3_ice_melting_impl.hpp:10-53 (max(...,0) inside the branch) */
+/* The departures dT0 = T - T_0C and dqv0 = qsat(T_0C) - qv are formed in FP64
+ * by the caller (small differences of large numbers near the melting point). */
 template <class TR>
-__device__ __forceinline__ void ice_melting(TR rho, TR T_atm, TR qsat0, TR rhofaci, TR tv_melt,
-                                            TR tv_vent, const PhysVars<TR>& v, TR qv, TR qi_incld,
+__device__ __forceinline__ void ice_melting(TR rho, double dT0, double dqv0, TR rhofaci, TR tv_melt,
+                                            TR tv_vent, const PhysVars<TR>& v, TR qi_incld,
                                             TR ni_incld, Rates<TR>& r) {
-  if (qi_incld >= TR(C::QSMALL) && T_atm > TR(C::Tmelt)) {
+  if (qi_incld >= TR(C::QSMALL) && dT0 > 0) {
     TR t = ((tv_melt + tv_vent * m_cbrt(v.sc) * m_sqrt(rhofaci * rho / v.mu)) *
-            ((T_atm - TR(C::Tmelt)) * v.kap - rho * TR(C::LatVap) * v.dv * (qsat0 - qv)) * TR(2) *
+            (TR(dT0) * v.kap - rho * TR(C::LatVap) * v.dv * TR(dqv0)) * TR(2) *
             TR(C::Pi) / TR(C::LatIce)) *
            ni_incld;
     t = vmax(t, TR(0.));
@@ -527,29 +529,34 @@ __device__ __forceinline__ void ice_melting(TR rho, TR T_atm, TR qsat0, TR rhofa
 
 /* ice_cldliq_wet_growth, p3/impl/p3_ice_cldliq_wet_growth_impl.hpp:12-80 */
 template <class TR>
-__device__ __forceinline__ bool ice_cldliq_wet_growth(TR rho, TR temp, TR qsat0, TR rhofaci, TR tv_melt,
-                                                      TR tv_vent, const PhysVars<TR>& v, TR qv,
+__device__ __forceinline__ bool ice_cldliq_wet_growth(TR rho, double dT0, double dqv0, TR rhofaci, TR tv_melt,
+                                                      TR tv_vent, const PhysVars<TR>& v,
                                                       TR qc_incld, TR qi_incld, TR ni_incld, TR qr_incld,
                                                       Rates<TR>& r) {
-  const bool t_neg = temp < TR(C::Tmelt);
+  const bool t_neg = dT0 < 0;
   const bool any_if = qi_incld >= TR(C::QSMALL) && (qc_incld + qr_incld) >= TR(1.0e-6) && t_neg;
   const bool any_if_col = any_if && (r.qc2qi_collect_tend + r.qr2qi_collect_tend) >= TR(1.0e-10);
   bool wet = false;
   if (any_if) {
     TR g = ((tv_melt + tv_vent * m_cbrt(v.sc) * m_sqrt(rhofaci * rho / v.mu)) * TR(C::Pi * 2) *
-            (rho * TR(C::LatVap) * v.dv * (qsat0 - qv) - (temp - TR(C::Tmelt)) * v.kap) /
-            (TR(C::LatIce) + TR(C::CpLiq) * (temp - TR(C::Tmelt)))) *
+            (rho * TR(C::LatVap) * v.dv * TR(dqv0) - TR(dT0) * v.kap) /
+            (TR(C::LatIce) + TR(C::CpLiq) * TR(dT0))) *
            ni_incld;
     g = vmax(g, TR(0.));
-    const TR dum = vmax(TR(0.), (r.qc2qi_collect_tend + r.qr2qi_collect_tend) - g);
-    const bool dum_ge_small = dum >= TR(1.0e-10);
+    /* The shed excess dum = collection - g and the collection that remains,
+     * c - dum * c / (qc2qi + qr2qi), cancel almost completely when the
+     * collection rate exceeds the wet-growth limit by orders of magnitude;
+     * they are evaluated in FP64 (the FP64 form is unchanged by this). */
+    const double qc2qi = double(r.qc2qi_collect_tend), qr2qi = double(r.qr2qi_collect_tend);
+    const double dum = vmax(0., (qc2qi + qr2qi) - double(g));
+    const bool dum_ge_small = dum >= 1.0e-10;
     if (dum_ge_small) {
-      r.nr_ice_shed_tend = r.nr_ice_shed_tend + dum * TR(1.923e+6);
-      const TR dum1 = TR(1.0) / (r.qc2qi_collect_tend + r.qr2qi_collect_tend);
+      r.nr_ice_shed_tend = TR(double(r.nr_ice_shed_tend) + dum * 1.923e+6);
+      const double dum1 = 1.0 / (qc2qi + qr2qi);
       if (any_if_col) {
-        r.qc2qr_ice_shed_tend = r.qc2qr_ice_shed_tend + dum * r.qc2qi_collect_tend * dum1;
-        r.qc2qi_collect_tend = vmax(TR(0.), r.qc2qi_collect_tend - dum * r.qc2qi_collect_tend * dum1);
-        r.qr2qi_collect_tend = vmax(TR(0.), r.qr2qi_collect_tend - dum * r.qr2qi_collect_tend * dum1);
+        r.qc2qr_ice_shed_tend = TR(double(r.qc2qr_ice_shed_tend) + dum * qc2qi * dum1);
+        r.qc2qi_collect_tend = TR(vmax(0., qc2qi - dum * qc2qi * dum1));
+        r.qr2qi_collect_tend = TR(vmax(0., qr2qi - dum * qr2qi * dum1));
       }
     }
     wet = dum_ge_small;
