@@ -29,6 +29,9 @@ struct p3x_context {
   double* d_t3slices = nullptr;
   float* f_t3slices = nullptr;
   uint32_t* d_err = nullptr;
+  /* stream-ordered pool of the per-call K1->K2/K3 scratch (memory is kept
+   * for reuse; released with the context) */
+  cudaMemPool_t pool = nullptr;
   p3x_launch_config cfg[2];
   /* scratch of the Fortran-layout entry (grown on demand) */
   std::vector<double*> fbuf;
@@ -148,8 +151,8 @@ int sm_stride_for(int nlev_max) {
 bool spec_fits(int precision, const LaunchSpec& ls, int stride) {
   if (ls.lanes != 8 && ls.lanes != 16 && ls.lanes != 32) return false;
   if (ls.groups_per_block <= 0 || ls.groups_per_block * ls.lanes > 256) return false;
-  const size_t smem = precision == P3X_FP32_BULK ? p3_smem_bytes<float>(ls, stride) : p3_smem_bytes<double>(ls, stride);
-  return smem <= size_t(227 * 1024);
+  const size_t k1 = precision == P3X_FP32_BULK ? p3_smem_bytes<float>(ls, stride) : p3_smem_bytes<double>(ls, stride);
+  return k1 <= size_t(227 * 1024) && sed_smem_bytes(ls, stride) <= size_t(227 * 1024);
 }
 
 /* Falls back to tables in global memory and then to fewer columns per CTA
@@ -231,11 +234,18 @@ int fill_inst(const p3x_prognostic_state* prog, const p3x_diagnostic_inputs* din
   in.prescribedCCN = prescribedCCN ? 1 : 0;
   in.precision = precision;
   in.pad_ = 0;
+  in.scr = nullptr;
+  in.cflag = nullptr;
   return P3X_OK;
 }
 
-int launch_single(p3x_context* ctx, const p3x_runtime* rt, const dev::Inst& in, cudaStream_t st) {
-  if (in.ncol == 0) return P3X_OK;
+void bind_scratch(dev::Inst& in, unsigned char* base) {
+  in.scr = reinterpret_cast<double*>(base);
+  in.cflag = reinterpret_cast<int32_t*>(base + size_t(dev::kScrFields) * size_t(in.ncol) * size_t(in.ld) *
+                                        sizeof(double));
+}
+
+int launch_kernels(p3x_context* ctx, const p3x_runtime* rt, const dev::Inst& in, cudaStream_t st) {
   const dev::RuntimeDev rtd = make_runtime(*rt);
   const int stride = sm_stride_for(in.nlev);
   const LaunchSpec ls = fit_spec(in.precision, spec_of(ctx->cfg[in.precision]), stride);
@@ -257,6 +267,20 @@ int launch_single(p3x_context* ctx, const p3x_runtime* rt, const dev::Inst& in, 
     e = launch_p3<double>(in, kp, ls, ctx->num_sms, st);
   }
   return cuda_status(e);
+}
+
+/* One step of one instance: the K1->K2/K3 scratch comes from the context's
+ * stream-ordered pool and returns to it behind the three kernels. */
+int launch_single(p3x_context* ctx, const p3x_runtime* rt, const dev::Inst& in_, cudaStream_t st) {
+  if (in_.ncol == 0) return P3X_OK;
+  dev::Inst in = in_;
+  void* scr = nullptr;
+  P3X_CUDA(cudaMallocFromPoolAsync(&scr, dev::scratch_bytes(in.ncol, in.ld), ctx->pool, st));
+  bind_scratch(in, static_cast<unsigned char*>(scr));
+  const int rc = launch_kernels(ctx, rt, in, st);
+  const cudaError_t fe = cudaFreeAsync(scr, st);
+  if (rc) return rc;
+  return cuda_status(fe);
 }
 
 int read_and_clear_err(p3x_context* ctx, cudaStream_t st) {
@@ -354,9 +378,14 @@ int p3x_context_create(const char* table_file, p3x_context** out, int* info) {
   }
   cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device);
   const HostTables& H = ctx->host;
-  if ((st = upload(&ctx->d_ice, H.ice)) || (st = upload(&ctx->d_coll, H.collect)) ||
+  /* device copies of the ice table hold its columns in slot order */
+  std::vector<double> ice_slots(H.ice.size());
+  for (size_t row = 0; row < H.ice.size() / dev::kIceCols; ++row)
+    for (int s = 0; s < dev::kIceCols; ++s)
+      ice_slots[row * dev::kIceCols + s] = H.ice[row * dev::kIceCols + dev::kIceSlotCol[s]];
+  if ((st = upload(&ctx->d_ice, ice_slots)) || (st = upload(&ctx->d_coll, H.collect)) ||
       (st = upload(&ctx->d_vn, H.vn)) || (st = upload(&ctx->d_vm, H.vm)) ||
-      (st = upload(&ctx->d_revap, H.revap)) || (st = upload(&ctx->f_ice, H.ice)) ||
+      (st = upload(&ctx->d_revap, H.revap)) || (st = upload(&ctx->f_ice, ice_slots)) ||
       (st = upload(&ctx->f_coll, H.collect)) || (st = upload(&ctx->f_vn, H.vn)) ||
       (st = upload(&ctx->f_vm, H.vm)) || (st = upload(&ctx->f_revap, H.revap))) {
     if (info) *info = st;
@@ -383,6 +412,19 @@ int p3x_context_create(const char* table_file, p3x_context** out, int* info) {
     p3x_context_destroy(ctx.release());
     return P3X_ENOMEM;
   }
+  {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = ctx->device;
+    uint64_t keep = UINT64_MAX;
+    if (cudaMemPoolCreate(&ctx->pool, &props) != cudaSuccess ||
+        cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) {
+      if (info) *info = P3X_ECUDA;
+      p3x_context_destroy(ctx.release());
+      return P3X_ECUDA;
+    }
+  }
   ctx->cfg[P3X_FP64] = p3x_launch_config{32, 8, 1, 0};
   ctx->cfg[P3X_FP32_BULK] = p3x_launch_config{32, 8, 1, 0};
   *out = ctx.release();
@@ -398,6 +440,10 @@ int p3x_context_destroy(p3x_context* ctx) {
     if (p) cudaFree(p);
   for (double* p : ctx->fbuf)
     if (p) cudaFree(p);
+  if (ctx->pool) {
+    cudaDeviceSynchronize();
+    cudaMemPoolDestroy(ctx->pool);
+  }
   delete ctx;
   return P3X_OK;
 }
@@ -601,6 +647,7 @@ struct p3x_batch {
   p3x_context* ctx = nullptr;
   dev::RuntimeDev rtd{};
   dev::Inst* insts_d = nullptr;
+  void* scratch = nullptr; /* every instance's K1->K2/K3 scratch */
   struct Group {
     int precision = 0;
     dev::WorkItem* work_d = nullptr;
@@ -667,6 +714,16 @@ int p3x_batch_create(p3x_context* ctx, const p3x_runtime* rt, const p3x_instance
   auto b = std::make_unique<p3x_batch>();
   b->ctx = ctx;
   b->rtd = make_runtime(*rt);
+  size_t scr_total = 0;
+  for (int i = 0; i < n; ++i) scr_total += dev::scratch_bytes(insts[i].ncol, insts[i].ld);
+  if (scr_total) P3X_CUDA(cudaMalloc(&b->scratch, scr_total));
+  {
+    size_t off = 0;
+    for (int i = 0; i < n; ++i) {
+      bind_scratch(insts[i], static_cast<unsigned char*>(b->scratch) + off);
+      off += dev::scratch_bytes(insts[i].ncol, insts[i].ld);
+    }
+  }
   P3X_CUDA(cudaMalloc(&b->insts_d, sizeof(dev::Inst) * n));
   P3X_CUDA(cudaMemcpy(b->insts_d, insts.data(), sizeof(dev::Inst) * n, cudaMemcpyHostToDevice));
   for (int p = 0; p < 2; ++p) {
@@ -738,6 +795,7 @@ int p3x_batch_destroy(p3x_batch* b) {
   if (!b) return P3X_EINVAL;
   drop_graph(b);
   if (b->insts_d) cudaFree(b->insts_d);
+  if (b->scratch) cudaFree(b->scratch);
   for (int g = 0; g < b->ngroups; ++g)
     if (b->groups[g].work_d) cudaFree(b->groups[g].work_d);
   delete b;

@@ -1,27 +1,30 @@
 /*
- * The fused P3 column kernel.
+ * The P3 step as three column kernels.
  *
  * One group of LANES threads (8, 16 or 32; a warp or part of one) owns one
  * column at a time; lane l owns levels l, l+LANES, l+2*LANES, ...  Inputs
  * are level-contiguous (EAMxx layout), so a group's loads of one field are
- * coalesced.  Per column the kernel runs, in the reference's stage order
- * (p3/impl/p3_main_impl.hpp:108-325):
+ * coalesced.  The reference's stage order (p3/impl/p3_main_impl.hpp:108-325)
+ * is kept across three launches on one stream:
  *
- *   1. p3_main_init + p3_main_part1 (level-parallel); the column-wide early
- *      exit of p3_main_impl.hpp:237-239 is a group ballot.
- *   2. p3_main_part2 (level-parallel) with the second early exit (:260).
- *   3. cloud, rain and ice sedimentation: CFL substeps with the Courant
- *      maximum as a group shuffle reduction and the upwind flux divergence
- *      walked down the levels chunk by chunk with a shuffle-up and a carry
- *      (p3_upwind_impl.hpp:14-116).  Substep loops are capped.
- *   4. homogeneous freezing + p3_main_part3 (level-parallel).
+ *   K1 p3_part12_kernel: p3_main_init + p3_main_part1 and p3_main_part2
+ *      (level-parallel), with the two column-wide early exits of
+ *      p3_main_impl.hpp:237-239 and :260 as group ballots.  It hands the
+ *      per-level start-of-step temperature, density and fall-speed factors
+ *      to K2/K3 through a scratch array and marks each column that goes on.
+ *   K2 p3_sed_kernel: cloud, rain and ice sedimentation: CFL substeps with
+ *      the Courant maximum as a group shuffle reduction and the upwind flux
+ *      divergence walked down the levels chunk by chunk with a shuffle-up and
+ *      a carry (p3_upwind_impl.hpp:14-116).  Substep loops are capped.
+ *   K3 p3_part3_kernel: homogeneous freezing + p3_main_part3.
  *
- * Between phases, per-level quantities live in shared memory (14 FP64
- * arrays per column); prognostic fields are written back to their global
- * arrays after each phase and re-read from L2 by the next.  Lookup tables
- * are read from global memory (L1/L2) or staged into shared memory once per
- * CTA with cp.async.bulk + mbarrier (tiny Table3 slices for the runtime's
- * constant rain shape parameter, plus the whole ice table).
+ * Splitting lets each kernel keep its own register and shared-memory
+ * footprint: part2's ~45 rates no longer limit the occupancy of the
+ * latency-bound sedimentation walk.  Per-level temporaries of a phase live
+ * in shared memory (10 FP64 arrays per column in K1, 11 in K2).  Lookup
+ * tables are read from global memory (L1/L2) or, in K1, staged into shared
+ * memory once per CTA with cp.async.bulk + mbarrier (Table3 slices for the
+ * runtime's constant rain shape parameter, plus the whole ice table).
  */
 #pragma once
 
@@ -39,6 +42,10 @@ struct Inst {
       *diag_eff_radius_qi, *diag_eff_radius_qr, *rho_qi, *precip_liq_flux, *precip_ice_flux,
       *precip_total_tend, *nevapr;
   double *liq_ice_exchange, *vap_liq_exchange, *vap_ice_exchange;
+  /* hand-over from K1 to K2/K3: [kScrFields][ncol][ld] doubles, and one
+   * continue flag per column (0: the column took an early exit) */
+  double* scr;
+  int32_t* cflag;
   int64_t ld, ld_int;
   int32_t ncol, nlev;
   double dt;
@@ -75,13 +82,24 @@ constexpr int kMaxSubsteps = 100000;
 constexpr long long kWaitSpinLimit = 1ll << 26;
 constexpr uint64_t kWaitNanosLimit = 2000000000ull; /* 2 s */
 
-/* shared arrays of one column group */
-enum {
-  A_TATM = 0, A_RHO, A_INVRHO, A_RHOFACR, A_RHOFACI, A_ACN, A_INVDZ, A_QVSL, A_QVSI, A_QVSSI,
-  A_R0, A_R1, A_R2, A_R3, A_NARR,
-  /* sedimentation re-uses the part2-only arrays */
-  A_V1 = A_QVSL, A_V2 = A_QVSI, A_PFLUX = A_QVSSI
-};
+/* shared arrays of one column group in K1 */
+enum { A_TATM = 0, A_RHO, A_INVRHO, A_RHOFACR, A_RHOFACI, A_ACN, A_INVDZ, A_QVSL, A_QVSI, A_QVSSI, A_NARR };
+/* shared arrays of one column group in K2; FAC is the fall-speed factor of
+ * the species being sedimented (acn, rhofacr or rhofaci), the rain flux
+ * accumulator re-uses R2 (rain has two fields) */
+enum { B_RHO = 0, B_INVRHO, B_INVDZ, B_FAC, B_CLD, B_V1, B_V2, B_R0, B_R1, B_R2, B_R3, B_NARR };
+/* hand-over fields K1 -> K2/K3 */
+enum { S_TATM = 0, S_RHO, S_RHOFACR, S_RHOFACI, S_ACN, kScrFields };
+
+__device__ __forceinline__ double* scr_at(const Inst& in, int f, int col) {
+  return in.scr + (int64_t(f) * in.ncol + col) * in.ld;
+}
+
+/* bytes of the K1->K2/K3 scratch of an instance (doubles, then the flags) */
+__host__ __device__ inline size_t scratch_bytes(int ncol, int64_t ld) {
+  const size_t d = size_t(kScrFields) * size_t(ncol) * size_t(ld) * sizeof(double);
+  return ((d + size_t(ncol) * sizeof(int32_t) + 255) / 256) * 256;
+}
 
 template <class TR>
 __host__ __device__ constexpr size_t table_smem_bytes() {
@@ -189,8 +207,9 @@ __device__ __forceinline__ void apply_n_adjust(double& n_d, TR n_in, TR n_out) {
 /* ------------------------------------------------------------------ */
 /* one column                                                          */
 /* ------------------------------------------------------------------ */
+/* K1: p3_main_init, p3_main_part1, p3_main_part2 of one column. */
 template <class TR, int LANES>
-__device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, const Tabs<TR>& tb,
+__device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, const Tabs<TR>& tb,
                           double* __restrict__ sm, const double esat0, uint32_t& err) {
   const RuntimeDev& rt = kp.rt;
   const unsigned mask = group_mask<LANES>();
@@ -304,12 +323,14 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
     in.precip_liq_flux[ci + k] = 0;
     in.precip_ice_flux[ci + k] = 0;
   }
-  double precip_liq_surf = 0, precip_ice_surf = 0;
   if (lane == 0) {
     in.precip_liq_surf[col] = 0;
     in.precip_ice_surf[col] = 0;
   }
-  if (!group_any<LANES>(mask, nucl || hydro)) return;
+  if (!group_any<LANES>(mask, nucl || hydro)) {
+    if (lane == 0) in.cflag[col] = 0;
+    return;
+  }
 
   /* ---------------- phase 2: p3_main_part2 ---------------- */
   hydro = false;
@@ -380,13 +401,16 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
         lookup_ice<TR>(TR(inc.qi), TR(inc.ni), TR(inc.qm), TR(rhop), ti);
         TableRain<TR> trn;
         lookup_rain<TR>(TR(inc.qr), TR(inc.nr), trn);
-        tv_fallspd = apply_table_ice<TR>(1, tb, ti);
-        tv_selfcol = apply_table_ice<TR>(2, tb, ti);
-        tv_qc2qi = apply_table_ice<TR>(3, tb, ti);
-        tv_melt = apply_table_ice<TR>(4, tb, ti);
-        tv_lammax = apply_table_ice<TR>(6, tb, ti);
-        tv_lammin = apply_table_ice<TR>(7, tb, ti);
-        tv_vent = apply_table_ice<TR>(9, tb, ti);
+        TR ta[4], tc[4];
+        apply_table_ice4<TR>(tb, ti, 0, ta); /* columns 0, 1, 6, 7 */
+        apply_table_ice4<TR>(tb, ti, 4, tc); /* columns 2, 3, 4, 9 */
+        tv_fallspd = ta[1];
+        tv_selfcol = tc[0];
+        tv_qc2qi = tc[1];
+        tv_melt = tc[2];
+        tv_lammax = ta[2];
+        tv_lammin = ta[3];
+        tv_vent = tc[3];
         if (inc.qr >= C::QSMALL) {
           tv_nr = apply_table_coll<TR>(0, tb, ti, trn);
           tv_qr2qi = apply_table_coll<TR>(1, tb, ti, trn);
@@ -504,23 +528,64 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
     in.qi[o] = s.qi; in.qm[o] = s.qm; in.ni[o] = s.ni; in.bm[o] = s.bm;
     in.qv[o] = s.qv; in.th[o] = s.th;
   }
-  if (!group_any<LANES>(mask, hydro)) return;
+  if (!group_any<LANES>(mask, hydro)) {
+    if (lane == 0) in.cflag[col] = 0;
+    return;
+  }
+  for (int k = lane; k < nk; k += LANES) {
+    scr_at(in, S_TATM, col)[k] = SMA(A_TATM, k);
+    scr_at(in, S_RHO, col)[k] = SMA(A_RHO, k);
+    scr_at(in, S_RHOFACR, col)[k] = SMA(A_RHOFACR, k);
+    scr_at(in, S_RHOFACI, col)[k] = SMA(A_RHOFACI, k);
+    scr_at(in, S_ACN, col)[k] = SMA(A_ACN, k);
+  }
+  if (lane == 0) in.cflag[col] = 1;
+#undef SMA
+}
+
+/* K2: cloud, rain and ice sedimentation of one column that went on past
+ * part2. */
+template <class TR, int LANES>
+__device__ void p3_sed(const Inst& in, const int col, const KParams<TR>& kp, const Tabs<TR>& tb,
+                       double* __restrict__ sm, uint32_t& err) {
+  if (in.cflag[col] == 0) return;
+  const RuntimeDev& rt = kp.rt;
+  const unsigned mask = group_mask<LANES>();
+  const int lane = threadIdx.x & (LANES - 1);
+  const int nk = in.nlev;
+  const int S = kp.sm_stride;
+  const int64_t co = int64_t(col) * in.ld;
+  const int64_t ci = int64_t(col) * in.ld_int;
+  const double dt = in.dt;
+  const double inv_dt = 1 / dt;
+  const bool predictNc = in.predictNc != 0;
+  const int kbot = nk - 1;
+#define SMA(a, k) sm[(a)*S + (k)]
+  for (int k = lane; k < nk; k += LANES) {
+    const double rho = scr_at(in, S_RHO, col)[k];
+    SMA(B_RHO, k) = rho;
+    SMA(B_INVRHO, k) = 1 / rho;
+    SMA(B_INVDZ, k) = 1 / in.dz[co + k];
+  }
+  double precip_liq_surf = 0, precip_ice_surf = 0;
 
   /* ---------------- phase 3: sedimentation ---------------- */
   /* Shared arrays during sedimentation: V1/V2 fall speeds (re-using the
    * part2-only saturation arrays), R0..R3 the species state, CLD the
    * species' cloud fraction (cloud and ice re-use A_QVSSI; rain re-uses A_ACN,
    * free once cloud sedimentation is done), PF the rain flux accumulator. */
-  double* const V1 = &SMA(A_V1, 0);
-  double* const V2 = &SMA(A_V2, 0);
-  double* const PF = &SMA(A_PFLUX, 0);
-  double* const R0 = &SMA(A_R0, 0);
-  double* const R1 = &SMA(A_R1, 0);
-  double* const R2 = &SMA(A_R2, 0);
-  double* const R3 = &SMA(A_R3, 0);
-  const double* const RHO = &SMA(A_RHO, 0);
-  const double* const INVRHO = &SMA(A_INVRHO, 0);
-  const double* const INVDZ = &SMA(A_INVDZ, 0);
+  double* const V1 = &SMA(B_V1, 0);
+  double* const V2 = &SMA(B_V2, 0);
+  double* const PF = &SMA(B_R2, 0);
+  double* const R0 = &SMA(B_R0, 0);
+  double* const R1 = &SMA(B_R1, 0);
+  double* const R2 = &SMA(B_R2, 0);
+  double* const R3 = &SMA(B_R3, 0);
+  double* const CLD = &SMA(B_CLD, 0);
+  double* const FAC = &SMA(B_FAC, 0);
+  const double* const RHO = &SMA(B_RHO, 0);
+  const double* const INVRHO = &SMA(B_INVRHO, 0);
+  const double* const INVDZ = &SMA(B_INVDZ, 0);
   constexpr bool kF64 = sizeof(TR) == sizeof(double);
 
 #pragma unroll 1
@@ -528,7 +593,8 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
     double* g0 = sp == 0 ? in.qc : (sp == 1 ? in.qr : in.qi);
     double* g1 = sp == 0 ? in.nc : (sp == 1 ? in.nr : in.ni);
     const double* cldp = sp == 0 ? in.cld_frac_l : (sp == 1 ? in.cld_frac_r : in.cld_frac_i);
-    double* const CLD = sp == 1 ? &SMA(A_ACN, 0) : &SMA(A_QVSSI, 0);
+    const int sfac = sp == 0 ? S_ACN : (sp == 1 ? S_RHOFACR : S_RHOFACI);
+    const double* const facp = scr_at(in, sfac, col);
     const int nfield = sp == 0 ? (predictNc ? 2 : 1) : (sp == 1 ? 2 : 4);
 
     /* load the species into shared memory; find top / bottom (p3_find_impl.hpp) */
@@ -538,6 +604,7 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
       R0[k] = q;
       R1[k] = g1[co + k];
       CLD[k] = cldp[co + k];
+      FAC[k] = facp[k];
       if (sp == 2) {
         R2[k] = in.qm[co + k];
         R3[k] = in.bm[co + k];
@@ -603,7 +670,7 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
              * Gamma(6+mu)/Gamma(4+mu) = (5+mu)(4+mu) and
              * Gamma(3+mu)/Gamma(1+mu) = (2+mu)(1+mu) (bcn = 2) */
             const TR dum = TR(1) / (lamc * lamc);
-            const TR acn = TR(SMA(A_ACN, k));
+            const TR acn = TR(FAC[k]);
             v1 = double(acn * ((TR(5) + mu_c) * (TR(4) + mu_c)) * dum);
             if (predictNc) v2 = double(acn * ((TR(2) + mu_c) * (TR(1) + mu_c)) * dum);
             lmax = vmax(lmax, v1 * dt_left * INVDZ[k]);
@@ -634,7 +701,7 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
             get_rain_dsd2<TR>(TR(qr_incld), n_out, mu_r, lamr, rt);
             Table3<TR> t3;
             lookup3<TR>(mu_r, lamr, rt, t3);
-            const TR rhofacr = TR(SMA(A_RHOFACR, k));
+            const TR rhofacr = TR(FAC[k]);
             v1 = double(apply_table3<TR>(tb, tb.vm, t3) * rhofacr);
             v2 = double(apply_table3<TR>(tb, tb.vn, t3) * rhofacr);
             if (kF64) {
@@ -645,55 +712,80 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
             lmax = vmax(lmax, v1 * dt_left * INVDZ[k]);
           }
         } else {
-          double qi_incld, ni_incld, qm_incld, bm_incld;
-          if (first) {
-            const double inv_cld = 1 / cld;
-            if (R0[k] >= C::QSMALL) {
-              qi_incld = R0[k] * inv_cld;
-              ni_incld = vmax(R1[k] * inv_cld, 0.);
-            } else {
-              qi_incld = 0;
-              ni_incld = 0;
+          bool done = false;
+          if constexpr (!kF64) {
+            if (!first) {
+              /* FP32-bulk, later substeps: in-cloud values, rime density and
+               * the table interpolation in FP32.  The FP64 state is rewritten
+               * only where a limiter changed an in-cloud value, so a substep
+               * adds no rounding to untouched qm, bm, ni. */
+              done = true;
+              const TR icf = TR(1) / TR(cld);
+              const TR qi_f = TR(R0[k]) * icf, ni_f = TR(R1[k]) * icf;
+              const TR qm_f = TR(R2[k]) * icf, bm_f = TR(R3[k]) * icf;
+              if (qi_f > TR(C::QSMALL)) {
+                const TR ni_l = vmax(ni_f, TR(C::NSMALL));
+                TR qm_c = qm_f, bm_c = bm_f;
+                const TR rhop = calc_bulk_rho_rime<TR>(qi_f, qm_c, bm_c, rt);
+                if (qm_c != qm_f) R2[k] = double(qm_c) * cld;
+                if (bm_c != bm_f) R3[k] = double(bm_c) * cld;
+                TableIce<TR> ti;
+                lookup_ice<TR>(qi_f, ni_l, qm_c, rhop, ti);
+                TR tv[4];
+                apply_table_ice4<TR>(tb, ti, 0, tv); /* columns 0, 1, 6, 7 */
+                TR n2 = vmin(ni_l, tv[2] * ni_l);
+                n2 = vmax(n2, tv[3] * n2);
+                if (n2 != ni_f) R1[k] = double(n2) * cld;
+                const TR f = TR(rt.ice_sedimentation_factor) * TR(FAC[k]);
+                v1 = double(f * tv[1]);
+                v2 = double(f * tv[0]);
+                lmax = vmax(lmax, v1 * dt_left * INVDZ[k]);
+              }
             }
-            if (R0[k] >= C::QSMALL && R2[k] >= C::QSMALL) {
-              qm_incld = R2[k] * inv_cld;
-              bm_incld = vmax(R3[k] * (1 / in.cld_frac_l[co + k]), 0.);
-            } else {
-              qm_incld = 0;
-              bm_incld = 0;
-            }
-            qi_incld = vmin(qi_incld, C::incloud_limit);
-            bm_incld = vmin(bm_incld, C::incloud_limit);
-          } else if (kF64) {
-            qi_incld = R0[k] / cld;
-            ni_incld = R1[k] / cld;
-            qm_incld = R2[k] / cld;
-            bm_incld = R3[k] / cld;
-          } else {
-            const float icf = 1.0f / float(cld);
-            qi_incld = double(float(R0[k]) * icf);
-            ni_incld = double(float(R1[k]) * icf);
-            qm_incld = double(float(R2[k]) * icf);
-            bm_incld = double(float(R3[k]) * icf);
           }
-          if (qi_incld > C::QSMALL) {
-            ni_incld = vmax(ni_incld, C::NSMALL);
-            const double rhop = calc_bulk_rho_rime(qi_incld, qm_incld, bm_incld, rt);
-            R2[k] = qm_incld * cld;
-            R3[k] = bm_incld * cld;
-            TableIce<TR> ti;
-            lookup_ice<TR>(TR(qi_incld), TR(ni_incld), TR(qm_incld), TR(rhop), ti);
-            const TR tv_n = apply_table_ice<TR>(0, tb, ti);
-            const TR tv_q = apply_table_ice<TR>(1, tb, ti);
-            const TR tv_lmax = apply_table_ice<TR>(6, tb, ti);
-            const TR tv_lmin = apply_table_ice<TR>(7, tb, ti);
-            ni_incld = vmin(ni_incld, double(tv_lmax) * ni_incld);
-            ni_incld = vmax(ni_incld, double(tv_lmin) * ni_incld);
-            R1[k] = ni_incld * cld;
-            const TR rhofaci = TR(SMA(A_RHOFACI, k));
-            v1 = double(TR(rt.ice_sedimentation_factor) * tv_q * rhofaci);
-            v2 = double(TR(rt.ice_sedimentation_factor) * tv_n * rhofaci);
-            lmax = vmax(lmax, v1 * dt_left * INVDZ[k]);
+          if (!done) {
+            double qi_incld, ni_incld, qm_incld, bm_incld;
+            if (first) {
+              const double inv_cld = 1 / cld;
+              if (R0[k] >= C::QSMALL) {
+                qi_incld = R0[k] * inv_cld;
+                ni_incld = vmax(R1[k] * inv_cld, 0.);
+              } else {
+                qi_incld = 0;
+                ni_incld = 0;
+              }
+              if (R0[k] >= C::QSMALL && R2[k] >= C::QSMALL) {
+                qm_incld = R2[k] * inv_cld;
+                bm_incld = vmax(R3[k] * (1 / in.cld_frac_l[co + k]), 0.);
+              } else {
+                qm_incld = 0;
+                bm_incld = 0;
+              }
+              qi_incld = vmin(qi_incld, C::incloud_limit);
+              bm_incld = vmin(bm_incld, C::incloud_limit);
+            } else {
+              qi_incld = R0[k] / cld;
+              ni_incld = R1[k] / cld;
+              qm_incld = R2[k] / cld;
+              bm_incld = R3[k] / cld;
+            }
+            if (qi_incld > C::QSMALL) {
+              ni_incld = vmax(ni_incld, C::NSMALL);
+              const double rhop = calc_bulk_rho_rime(qi_incld, qm_incld, bm_incld, rt);
+              R2[k] = qm_incld * cld;
+              R3[k] = bm_incld * cld;
+              TableIce<TR> ti;
+              lookup_ice<TR>(TR(qi_incld), TR(ni_incld), TR(qm_incld), TR(rhop), ti);
+              TR tv[4];
+              apply_table_ice4<TR>(tb, ti, 0, tv); /* columns 0, 1, 6, 7 */
+              ni_incld = vmin(ni_incld, double(tv[2]) * ni_incld);
+              ni_incld = vmax(ni_incld, double(tv[3]) * ni_incld);
+              R1[k] = ni_incld * cld;
+              const TR rhofaci = TR(FAC[k]);
+              v1 = double(TR(rt.ice_sedimentation_factor) * tv[1] * rhofaci);
+              v2 = double(TR(rt.ice_sedimentation_factor) * tv[0] * rhofaci);
+              lmax = vmax(lmax, v1 * dt_left * INVDZ[k]);
+            }
           }
         }
         V1[k] = v1;
@@ -845,6 +937,21 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
     in.precip_ice_surf[col] = precip_ice_surf;
   }
 
+#undef SMA
+}
+
+/* K3: homogeneous freezing and p3_main_part3 of one column that went on past
+ * part2. */
+template <class TR, int LANES>
+__device__ void p3_part3(const Inst& in, const int col, const KParams<TR>& kp, const Tabs<TR>& tb) {
+  if (in.cflag[col] == 0) return;
+  const RuntimeDev& rt = kp.rt;
+  const int lane = threadIdx.x & (LANES - 1);
+  const int nk = in.nlev;
+  const int64_t co = int64_t(col) * in.ld;
+  const bool do_ice = rt.do_ice_production != 0;
+  const double* const t_start = scr_at(in, S_TATM, col);
+  const double* const rho_k = scr_at(in, S_RHO, col);
   /* ---------------- phase 4: homogeneous freezing + p3_main_part3 ---------------- */
   for (int k = lane; k < nk; k += LANES) {
     const int64_t o = co + k;
@@ -854,14 +961,14 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
     s.qv = in.qv[o]; s.th = in.th[o];
     const double inv_exner = in.inv_exner[o];
     const double cld_l = in.cld_frac_l[o], cld_r = in.cld_frac_r[o], cld_i = in.cld_frac_i[o];
-    const double rho = SMA(A_RHO, k);
+    const double rho = rho_k[k];
     const double inv_rho = 1 / rho;
     double vap_liq = in.vap_liq_exchange[o];
     double eff_qc = in.diag_eff_radius_qc[o], eff_qr = in.diag_eff_radius_qr[o], eff_qi = in.diag_eff_radius_qi[o];
     double rho_qi = 0;
 
     /* homogeneous_freezing, p3/impl/p3_ice_sed_impl.hpp:207-270 */
-    if (do_ice && SMA(A_TATM, k) < C::T_homogfrz) {
+    if (do_ice && t_start[k] < C::T_homogfrz) {
       const double Qc_nuc = s.qc, Qr_nuc = s.qr;
       const double Nc_nuc = vmax(s.nc, C::NSMALL), Nr_nuc = vmax(s.nr, C::NSMALL);
       const bool qc_ge = s.qc >= C::QSMALL, qr_ge = s.qr >= C::QSMALL;
@@ -937,10 +1044,13 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
       if (qi_gt_small) {
         TableIce<TR> ti;
         lookup_ice<TR>(TR(qi_incld), TR(ni_incld), TR(qm_incld), TR(rhop), ti);
-        const TR tv_eff = apply_table_ice<TR>(5, tb, ti);
-        const TR tv_lmax = apply_table_ice<TR>(6, tb, ti);
-        const TR tv_lmin = apply_table_ice<TR>(7, tb, ti);
-        const TR tv_dens = apply_table_ice<TR>(11, tb, ti);
+        TR ta[4], te[4];
+        apply_table_ice4<TR>(tb, ti, 0, ta); /* columns 0, 1, 6, 7 */
+        apply_table_ice4<TR>(tb, ti, 8, te); /* columns 5, 11, 8, 10 */
+        const TR tv_eff = te[0];
+        const TR tv_lmax = ta[2];
+        const TR tv_lmin = ta[3];
+        const TR tv_dens = te[1];
         ni_incld = vmin(ni_incld, double(tv_lmax) * ni_incld);
         ni_incld = vmax(ni_incld, double(tv_lmin) * ni_incld);
         eff_qi = double(tv_eff);
@@ -968,60 +1078,107 @@ __device__ void p3_column(const Inst& in, const int col, const KParams<TR>& kp, 
     in.diag_eff_radius_qi[o] = eff_qi;
     in.rho_qi[o] = rho_qi;
   }
-#undef SMA
 }
 
 /* ------------------------------------------------------------------ */
-/* kernel                                                              */
+/* kernels                                                             */
 /* ------------------------------------------------------------------ */
-template <class TR, int LANES>
-__global__ void __launch_bounds__(256) p3_main_kernel(const Inst inst0, const KParams<TR> kp) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  uint32_t err = 0;
-  double* group_base;
-  Tabs<TR> tb;
+
+/* Table pointers of a CTA: staged into shared memory (K1, when kp.staged)
+ * or the global copies.  Returns the first byte after the staged tables, or
+ * nullptr when the staging wait gave up. */
+template <class TR>
+__device__ __forceinline__ unsigned char* setup_tables(const KParams<TR>& kp, bool stage, unsigned char* smem_raw,
+                                                       Tabs<TR>& tb, uint32_t& err) {
   tb.collect = kp.collect;
-  if (kp.staged) {
+  if (stage) {
     TR* s_ice = reinterpret_cast<TR*>(smem_raw);
     TR* s_t3 = s_ice + kIceTableElems;
     uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw + table_smem_bytes<TR>() - 16);
-    const bool ok = stage_tables<TR>(kp, s_ice, s_t3, mbar, err);
-    if (!ok) {
-      if (threadIdx.x == 0) atomicOr(kp.err, err);
-      return;
-    }
+    if (!stage_tables<TR>(kp, s_ice, s_t3, mbar, err)) return nullptr;
     tb.ice = s_ice;
     tb.vn = s_t3;
     tb.vm = s_t3 + 600;
     tb.revap = s_t3 + 1200;
     tb.t3_stride = 2;
     tb.t3_j0 = kp.rt.t3_dumjj - 1;
-    group_base = reinterpret_cast<double*>(smem_raw + table_smem_bytes<TR>());
-  } else {
-    tb.ice = kp.ice;
-    tb.vn = kp.vn;
-    tb.vm = kp.vm;
-    tb.revap = kp.revap;
-    tb.t3_stride = kVT1;
-    tb.t3_j0 = 0;
-    group_base = reinterpret_cast<double*>(smem_raw);
+    return smem_raw + table_smem_bytes<TR>();
+  }
+  tb.ice = kp.ice;
+  tb.vn = kp.vn;
+  tb.vm = kp.vm;
+  tb.revap = kp.revap;
+  tb.t3_stride = kVT1;
+  tb.t3_j0 = 0;
+  return smem_raw;
+}
+
+/* Column of work item w (single instance or batched work list). */
+template <class TR>
+__device__ __forceinline__ const Inst& work_inst(const Inst& inst0, const KParams<TR>& kp, int w, int& col) {
+  if (kp.work) {
+    const WorkItem wi = kp.work[w];
+    col = wi.col;
+    return kp.insts[wi.inst];
+  }
+  col = w;
+  return inst0;
+}
+
+template <class TR, int LANES>
+__global__ void __launch_bounds__(256) p3_part12_kernel(const Inst inst0, const KParams<TR> kp) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint32_t err = 0;
+  Tabs<TR> tb;
+  unsigned char* base = setup_tables<TR>(kp, kp.staged != 0, smem_raw, tb, err);
+  if (!base) {
+    if (threadIdx.x == 0) atomicOr(kp.err, err);
+    return;
   }
   const int g_in_block = threadIdx.x / LANES;
-  double* sm = group_base + size_t(g_in_block) * A_NARR * kp.sm_stride;
+  double* sm = reinterpret_cast<double*>(base) + size_t(g_in_block) * A_NARR * kp.sm_stride;
   /* liquid saturation vapour pressure at 0 C (qsat0 of ice_melting and
    * ice_cldliq_wet_growth), evaluated once */
   const double esat0 = murphy_koop_svp<double>(C::Tmelt, false, err);
-
   const int groups_total = gridDim.x * kp.groups_per_block;
   for (int w = blockIdx.x * kp.groups_per_block + g_in_block; w < kp.nwork; w += groups_total) {
-    if (kp.work) {
-      const WorkItem wi = kp.work[w];
-      p3_column<TR, LANES>(kp.insts[wi.inst], wi.col, kp, tb, sm, esat0, err);
-    } else {
-      p3_column<TR, LANES>(inst0, w, kp, tb, sm, esat0, err);
-    }
+    int col;
+    const Inst& in = work_inst(inst0, kp, w, col);
+    p3_part12<TR, LANES>(in, col, kp, tb, sm, esat0, err);
   }
   if (err) atomicOr(kp.err, err);
+}
+
+template <class TR, int LANES>
+__global__ void __launch_bounds__(256) p3_sed_kernel(const Inst inst0, const KParams<TR> kp) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint32_t err = 0;
+  Tabs<TR> tb;
+  setup_tables<TR>(kp, false, smem_raw, tb, err);
+  const int g_in_block = threadIdx.x / LANES;
+  double* sm = reinterpret_cast<double*>(smem_raw) + size_t(g_in_block) * B_NARR * kp.sm_stride;
+  const int groups_total = gridDim.x * kp.groups_per_block;
+  for (int w = blockIdx.x * kp.groups_per_block + g_in_block; w < kp.nwork; w += groups_total) {
+    int col;
+    const Inst& in = work_inst(inst0, kp, w, col);
+    p3_sed<TR, LANES>(in, col, kp, tb, sm, err);
+  }
+  if (err) atomicOr(kp.err, err);
+}
+
+template <class TR, int LANES>
+__global__ void __launch_bounds__(256) p3_part3_kernel(const Inst inst0, const KParams<TR> kp) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint32_t err = 0;
+  Tabs<TR> tb;
+  setup_tables<TR>(kp, false, smem_raw, tb, err);
+  const int g_in_block = threadIdx.x / LANES;
+  const int groups_total = gridDim.x * kp.groups_per_block;
+  for (int w = blockIdx.x * kp.groups_per_block + g_in_block; w < kp.nwork; w += groups_total) {
+    int col;
+    const Inst& in = work_inst(inst0, kp, w, col);
+    p3_part3<TR, LANES>(in, col, kp, tb);
+  }
 }
 
 }  // namespace dev

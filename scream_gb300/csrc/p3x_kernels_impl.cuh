@@ -1,13 +1,31 @@
-/* Launch helpers of the column kernel (included by the per-variant TUs). */
+/* Launch helpers of the column kernels (included by the per-variant TUs). */
 #pragma once
 
 #include "p3x_launch.hpp"
 
 namespace p3x {
 
-/* Persistent launch of p3_main_kernel<TR, LANES>: the grid is the number of
- * CTAs that fit on all SMs at once (capped by blocks_per_sm when given, and by
- * the amount of work); groups walk the work list with a grid stride. */
+/* Persistent launch of one kernel: the grid is the number of CTAs that fit on
+ * all SMs at once (capped by blocks_per_sm when given, and by the amount of
+ * work); groups walk the work list with a grid stride. */
+template <class TR, class Kern>
+cudaError_t launch_persistent(Kern kern, const dev::Inst& inst0, const dev::KParams<TR>& kp, int threads,
+                              size_t smem, int blocks_per_sm, int num_sms, cudaStream_t stream) {
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm <= 0) return cudaErrorInvalidConfiguration;
+  if (blocks_per_sm > 0) per_sm = per_sm < blocks_per_sm ? per_sm : blocks_per_sm;
+  long long grid = (long long)per_sm * num_sms;
+  const long long need = (kp.nwork + kp.groups_per_block - 1) / kp.groups_per_block;
+  if (need < grid) grid = need;
+  if (grid <= 0) return cudaSuccess;
+  kern<<<int(grid), threads, smem, stream>>>(inst0, kp);
+  return cudaGetLastError();
+}
+
 template <class TR, int LANES>
 cudaError_t launch_p3_lanes(const dev::Inst& inst0, const dev::KParams<TR>& kp_in, const LaunchSpec& ls,
                             int num_sms, cudaStream_t stream) {
@@ -16,21 +34,13 @@ cudaError_t launch_p3_lanes(const dev::Inst& inst0, const dev::KParams<TR>& kp_i
   kp.staged = ls.staged;
   const int threads = ls.groups_per_block * LANES;
   if (threads <= 0 || threads > 256) return cudaErrorInvalidValue;
-  const size_t smem = p3_smem_bytes<TR>(ls, kp.sm_stride);
-  auto kern = dev::p3_main_kernel<TR, LANES>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  cudaError_t e = launch_persistent<TR>(dev::p3_part12_kernel<TR, LANES>, inst0, kp, threads,
+                                        p3_smem_bytes<TR>(ls, kp.sm_stride), ls.blocks_per_sm, num_sms, stream);
   if (e != cudaSuccess) return e;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+  e = launch_persistent<TR>(dev::p3_sed_kernel<TR, LANES>, inst0, kp, threads, sed_smem_bytes(ls, kp.sm_stride),
+                            0, num_sms, stream);
   if (e != cudaSuccess) return e;
-  if (per_sm <= 0) return cudaErrorInvalidConfiguration;
-  if (ls.blocks_per_sm > 0) per_sm = per_sm < ls.blocks_per_sm ? per_sm : ls.blocks_per_sm;
-  long long grid = (long long)per_sm * num_sms;
-  const long long need = (kp.nwork + ls.groups_per_block - 1) / ls.groups_per_block;
-  if (need < grid) grid = need;
-  if (grid <= 0) return cudaSuccess;
-  kern<<<int(grid), threads, smem, stream>>>(inst0, kp);
-  return cudaGetLastError();
+  return launch_persistent<TR>(dev::p3_part3_kernel<TR, LANES>, inst0, kp, threads, 0, 0, num_sms, stream);
 }
 
 }  // namespace p3x

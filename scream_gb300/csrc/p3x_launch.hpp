@@ -15,16 +15,22 @@ struct LaunchSpec {
   int blocks_per_sm;    /* 0: as many as fit */
 };
 
-/* Shared-memory bytes of one CTA. */
+/* Shared-memory bytes of one CTA of K1 (part1+part2; staged tables plus the
+ * per-level arrays) and of K2 (sedimentation).  K3 uses none. */
 template <class TR>
 inline size_t p3_smem_bytes(const LaunchSpec& ls, int sm_stride) {
   const size_t tables = ls.staged ? dev::table_smem_bytes<TR>() : 0;
   return tables + size_t(ls.groups_per_block) * dev::A_NARR * size_t(sm_stride) * sizeof(double);
 }
+inline size_t sed_smem_bytes(const LaunchSpec& ls, int sm_stride) {
+  return size_t(ls.groups_per_block) * dev::B_NARR * size_t(sm_stride) * sizeof(double);
+}
 
-/* Persistent launch of the column kernel for one lane count (defined in
- * p3x_kernels_impl.cuh, instantiated in p3x_k_*.cu).  kp.nwork, kp.work,
- * kp.insts and kp.sm_stride are set by the caller. */
+/* Persistent launches of the three column kernels (K1 part1+part2, K2
+ * sedimentation, K3 part3) for one lane count, in order on one stream
+ * (defined in p3x_kernels_impl.cuh, instantiated in p3x_k_*.cu).  kp.nwork,
+ * kp.work, kp.insts and kp.sm_stride are set by the caller, and every
+ * instance's scratch (Inst::scr, Inst::cflag) is bound. */
 template <class TR, int LANES>
 cudaError_t launch_p3_lanes(const dev::Inst& inst0, const dev::KParams<TR>& kp, const LaunchSpec& ls,
                             int num_sms, cudaStream_t stream);

@@ -139,9 +139,25 @@ struct Tabs {
   int t3_stride, t3_j0;
 };
 
+/* Device order of the 12 ice-table columns: slot s holds reference column
+ * kIceSlotCol[s].  Slots 0-3 are the columns ice sedimentation needs (0,1,6,7),
+ * slots 4-7 the rest of part2's (2,3,4,9), slots 8-11 the rest of part3's
+ * (5,11,8,10), so each stage reads a table corner with one or two 16-byte
+ * vector loads instead of one scalar load per column. */
+constexpr int kIceSlotCol[kIceCols] = {0, 1, 6, 7, 2, 3, 4, 9, 5, 11, 8, 10};
+
+__device__ __forceinline__ void ld4(const float* p, float o[4]) {
+  const float4 v = *reinterpret_cast<const float4*>(p);
+  o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+}
+__device__ __forceinline__ void ld4(const double* p, double o[4]) {
+  const double2 a = reinterpret_cast<const double2*>(p)[0];
+  const double2 b = reinterpret_cast<const double2*>(p)[1];
+  o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+}
 template <class TR>
-__device__ __forceinline__ TR ice_at(const Tabs<TR>& t, int jj, int ii, int i, int idx) {
-  return t.ice[((jj * kRimsize + ii) * kIsize + i) * kIceCols + idx];
+__device__ __forceinline__ const TR* ice_row(const Tabs<TR>& t, int jj, int ii, int i) {
+  return t.ice + ((jj * kRimsize + ii) * kIsize + i) * kIceCols;
 }
 template <class TR>
 __device__ __forceinline__ TR coll_at(const Tabs<TR>& t, int jj, int ii, int i, int j, int idx) {
@@ -217,27 +233,33 @@ __device__ __forceinline__ void lookup_rain(TR qr, TR nr, TableRain<TR>& tab) {
   tab.dumj -= 1;
 }
 
-/* apply_table_ice, p3_table_ice_impl.hpp:175-212 */
+/* apply_table_ice, p3_table_ice_impl.hpp:175-212, for the four device slots
+ * s0..s0+3 at once (s0 a multiple of 4); each value is interpolated with the
+ * reference's order of operations. */
 template <class TR>
-__device__ __forceinline__ TR apply_table_ice(int idx, const Tabs<TR>& t, const TableIce<TR>& tab) {
+__device__ __forceinline__ void apply_table_ice4(const Tabs<TR>& t, const TableIce<TR>& tab, int s0, TR out[4]) {
   const TR w1 = tab.dum1 - TR(tab.dumi) - TR(1);
   const TR w4 = tab.dum4 - TR(tab.dumii) - TR(1);
   const TR w5 = tab.dum5 - TR(tab.dumjj) - TR(1);
-  const TR a00 = ice_at(t, tab.dumjj, tab.dumii, tab.dumi, idx);
-  const TR a01 = ice_at(t, tab.dumjj, tab.dumii, tab.dumi + 1, idx);
-  const TR a10 = ice_at(t, tab.dumjj, tab.dumii + 1, tab.dumi, idx);
-  const TR a11 = ice_at(t, tab.dumjj, tab.dumii + 1, tab.dumi + 1, idx);
-  const TR b00 = ice_at(t, tab.dumjj + 1, tab.dumii, tab.dumi, idx);
-  const TR b01 = ice_at(t, tab.dumjj + 1, tab.dumii, tab.dumi + 1, idx);
-  const TR b10 = ice_at(t, tab.dumjj + 1, tab.dumii + 1, tab.dumi, idx);
-  const TR b11 = ice_at(t, tab.dumjj + 1, tab.dumii + 1, tab.dumi + 1, idx);
-  TR iproc1 = a00 + w1 * (a01 - a00);
-  TR gproc1 = a10 + w1 * (a11 - a10);
-  const TR tmp1 = iproc1 + w4 * (gproc1 - iproc1);
-  iproc1 = b00 + w1 * (b01 - b00);
-  gproc1 = b10 + w1 * (b11 - b10);
-  const TR tmp2 = iproc1 + w4 * (gproc1 - iproc1);
-  return tmp1 + w5 * (tmp2 - tmp1);
+  TR a00[4], a01[4], a10[4], a11[4], b00[4], b01[4], b10[4], b11[4];
+  ld4(ice_row(t, tab.dumjj, tab.dumii, tab.dumi) + s0, a00);
+  ld4(ice_row(t, tab.dumjj, tab.dumii, tab.dumi + 1) + s0, a01);
+  ld4(ice_row(t, tab.dumjj, tab.dumii + 1, tab.dumi) + s0, a10);
+  ld4(ice_row(t, tab.dumjj, tab.dumii + 1, tab.dumi + 1) + s0, a11);
+  ld4(ice_row(t, tab.dumjj + 1, tab.dumii, tab.dumi) + s0, b00);
+  ld4(ice_row(t, tab.dumjj + 1, tab.dumii, tab.dumi + 1) + s0, b01);
+  ld4(ice_row(t, tab.dumjj + 1, tab.dumii + 1, tab.dumi) + s0, b10);
+  ld4(ice_row(t, tab.dumjj + 1, tab.dumii + 1, tab.dumi + 1) + s0, b11);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    TR iproc1 = a00[c] + w1 * (a01[c] - a00[c]);
+    TR gproc1 = a10[c] + w1 * (a11[c] - a10[c]);
+    const TR tmp1 = iproc1 + w4 * (gproc1 - iproc1);
+    iproc1 = b00[c] + w1 * (b01[c] - b00[c]);
+    gproc1 = b10[c] + w1 * (b11[c] - b10[c]);
+    const TR tmp2 = iproc1 + w4 * (gproc1 - iproc1);
+    out[c] = tmp1 + w5 * (tmp2 - tmp1);
+  }
 }
 
 /* apply_table_coll, p3_table_ice_impl.hpp:214-297 */
