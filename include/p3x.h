@@ -160,6 +160,14 @@ int p3x_tables_generate(const char* table_file, double* ice, double* collect, do
  * generator (series for x < a+1, Legendre continued fraction otherwise). */
 double p3x_incomplete_gamma_q(double a, double x);
 
+/* Host-only: the FP64 saturation table of the FP32-bulk form.  Murphy-Koop
+ * vapour pressure (share/physics_saturation_impl.hpp:38-81) over liquid
+ * (rows 0..n-1) and ice (rows n..2n-1) as one cubic per interval of width
+ * 1/inv_h K starting at t0: e(T) = c0 + u (c1 + u (c2 + u c3)) with
+ * u = (T - t0) inv_h - i.  coef (may be NULL) receives 2 n 4 doubles.  No
+ * counterpart in the reference, which evaluates the formula. */
+int p3x_saturation_table(double* coef, int32_t* intervals, double* t0, double* inv_h);
+
 /* Writes the generated ice / collection table in the official text format. */
 int p3x_write_ice_table(const char* path, const char* version);
 

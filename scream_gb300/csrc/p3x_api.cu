@@ -28,6 +28,7 @@ struct p3x_context {
    * [9][3][300][2] */
   double* d_t3slices = nullptr;
   float* f_t3slices = nullptr;
+  double* d_svp = nullptr; /* FP32-bulk saturation table */
   uint32_t* d_err = nullptr;
   /* stream-ordered pool of the per-call K1->K2/K3 scratch (memory is kept
    * for reuse; released with the context) */
@@ -177,6 +178,7 @@ dev::KParams<double> make_kparams<double>(p3x_context* ctx, const dev::RuntimeDe
   kp.vm = ctx->d_vm;
   kp.revap = ctx->d_revap;
   kp.t3slice = ctx->d_t3slices + size_t(rtd.t3_dumjj - 1) * dev::kT3SliceElems;
+  kp.rt.svp_tab = ctx->d_svp;
   kp.err = ctx->d_err;
   return kp;
 }
@@ -190,6 +192,7 @@ dev::KParams<float> make_kparams<float>(p3x_context* ctx, const dev::RuntimeDev&
   kp.vm = ctx->f_vm;
   kp.revap = ctx->f_revap;
   kp.t3slice = ctx->f_t3slices + size_t(rtd.t3_dumjj - 1) * dev::kT3SliceElems;
+  kp.rt.svp_tab = ctx->d_svp;
   kp.err = ctx->d_err;
   return kp;
 }
@@ -349,6 +352,22 @@ int p3x_tables_generate(const char* table_file, double* ice, double* collect, do
 
 double p3x_incomplete_gamma_q(double a, double x) { return incomplete_gamma_q(a, x); }
 
+static_assert(p3x::kSvpIntervals == dev::kSvpIntervals && p3x::kSvpT0 == dev::kSvpT0 &&
+                  p3x::kSvpInvH == dev::kSvpInvH,
+              "saturation table layout differs between host and device");
+
+int p3x_saturation_table(double* coef, int32_t* intervals, double* t0, double* inv_h) {
+  if (intervals) *intervals = kSvpIntervals;
+  if (t0) *t0 = kSvpT0;
+  if (inv_h) *inv_h = kSvpInvH;
+  if (coef) {
+    std::vector<double> v;
+    build_svp_table(v);
+    std::copy(v.begin(), v.end(), coef);
+  }
+  return P3X_OK;
+}
+
 int p3x_write_ice_table(const char* path, const char* version) {
   if (!path) return P3X_EINVAL;
   return write_ice_table_file(path, version ? version : "4.1.1") == 0 ? P3X_OK : P3X_ETABLE;
@@ -401,7 +420,9 @@ int p3x_context_create(const char* table_file, p3x_context** out, int* info) {
       for (int i = 0; i < kVT0; ++i)
         for (int c = 0; c < 2; ++c) s[t * 600 + i * 2 + c] = (*tabs[t])[size_t(i) * kVT1 + (j - 1 + c)];
   }
-  if ((st = upload(&ctx->d_t3slices, sl)) || (st = upload(&ctx->f_t3slices, sl))) {
+  std::vector<double> svp;
+  build_svp_table(svp);
+  if ((st = upload(&ctx->d_t3slices, sl)) || (st = upload(&ctx->f_t3slices, sl)) || (st = upload(&ctx->d_svp, svp))) {
     if (info) *info = st;
     p3x_context_destroy(ctx.release());
     return st;
@@ -434,7 +455,7 @@ int p3x_context_create(const char* table_file, p3x_context** out, int* info) {
 int p3x_context_destroy(p3x_context* ctx) {
   if (!ctx) return P3X_EINVAL;
   void* ptrs[] = {ctx->d_ice, ctx->d_coll, ctx->d_vn, ctx->d_vm, ctx->d_revap, ctx->f_ice, ctx->f_coll,
-                  ctx->f_vn, ctx->f_vm, ctx->f_revap, ctx->d_t3slices, ctx->f_t3slices, ctx->d_err,
+                  ctx->f_vn, ctx->f_vm, ctx->f_revap, ctx->d_t3slices, ctx->f_t3slices, ctx->d_svp, ctx->d_err,
                   ctx->fstage};
   for (void* p : ptrs)
     if (p) cudaFree(p);

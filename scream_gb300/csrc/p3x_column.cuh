@@ -259,8 +259,8 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
 
     const double rho = dpres / dz / C::gravit;
     const double inv_rho = 1 / rho;
-    const double qvsl = qv_sat_dry<TR>(T, pres, false, err);
-    const double qvsi = qv_sat_dry<TR>(T, pres, true, err);
+    const double qvsl = qv_sat_dry<TR>(T, pres, false, rt, err);
+    const double qvsi = qv_sat_dry<TR>(T, pres, true, rt, err);
     const double qvssi = qv / qvsi - 1;
     const TR rhofacr = m_pow(TR(C::RHO_1000MB) * TR(inv_rho), TR(.54));
     const TR rhofaci = m_pow(TR(C::RHO_600MB) * TR(inv_rho), TR(.54));
@@ -453,22 +453,31 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
                (TR(C::f1r) * TR(rt.g_mur2) / lamr +
                 TR(C::f2r) * m_sqrt(rho_r / v.mu) * m_cbrt(v.sc) * apply_table3<TR>(tb, tb.revap, t3));
       }
-      {
+      if constexpr (sizeof(TR) == sizeof(double)) {
         double evap, nevap;
         evaporate_rain(inc.qr, inc.qc, inc.nr, inc.qi, cld_l, cld_r, s.qv, in.qv_prev[o], qvsl, qvsi,
                        double(v.ab), double(v.abi), double(epsr), double(epsi_tot), T, in.t_prev[o],
                        double(v.dqsdt), dt, evap, nevap);
         r.qr2qv_evap_tend = TR(evap);
         r.nr_evap_tend = TR(nevap);
-      }
-      if (do_ice) {
-        double vd, sb, nsb, bg;
-        ice_deposition_sublimation(inc.qi, inc.ni, T, qvsl, qvsi, double(epsi), double(v.abi), s.qv, inv_dt,
-                                   vd, sb, nsb, bg);
-        r.qv2qi_vapdep_tend = TR(vd);
-        r.qi2qv_sublim_tend = TR(sb);
-        r.ni_sublim_tend = TR(nsb);
-        r.qc2qi_berg_tend = TR(bg);
+        if (do_ice) {
+          double vd, sb, nsb, bg;
+          ice_deposition_sublimation(inc.qi, inc.ni, T, qvsl, qvsi, double(epsi), double(v.abi), s.qv, inv_dt,
+                                     vd, sb, nsb, bg);
+          r.qv2qi_vapdep_tend = TR(vd);
+          r.qi2qv_sublim_tend = TR(sb);
+          r.ni_sublim_tend = TR(nsb);
+          r.qc2qi_berg_tend = TR(bg);
+        }
+      } else {
+        evaporate_rain_bulk(inc.qr, inc.qc, inc.nr, inc.qi, cld_l, cld_r, s.qv, in.qv_prev[o], qvsl, qvsi, v.ab,
+                            v.abi, epsr, epsi_tot, T, in.t_prev[o], v.dqsdt, dt, r.qr2qv_evap_tend,
+                            r.nr_evap_tend);
+        if (do_ice) {
+          ice_deposition_sublimation_bulk(inc.qi, inc.ni, T, qvsl, qvsi, epsi, v.abi, s.qv, inv_dt,
+                                          r.qv2qi_vapdep_tend, r.qi2qv_sublim_tend, r.ni_sublim_tend,
+                                          r.qc2qi_berg_tend);
+        }
       }
     }
     if (do_ice) {
@@ -485,7 +494,7 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
     water_conservation(s.qc, s.qr, s.qi, dt, rd);
     number_conservation(s.nc, s.nr, s.ni, dt, rd);
     ice_supersat_conservation(rd, cld_i, s.qv, qvsi, s.th / inv_exner, dt);
-    prevent_liq_supersaturation<TR>(pres, T, s.qv, dt, rd, err);
+    prevent_liq_supersaturation<TR>(pres, T, s.qv, dt, rd, rt, err);
     update_prognostics(rd, inv_exner, predictNc, prescribedCCN, wet, dt, double(rho_qm_cloud), inv_rho, s);
 
     in.qv2qi_depos_tend[o] = rd.qv2qi_vapdep_tend - rd.qi2qv_sublim_tend + rd.qv2qi_nucleat_tend;

@@ -27,6 +27,14 @@ int read_ice_table_file(const char* path, const char* expect_version, HostTables
 int write_ice_table_file(const char* path, const char* version);
 double incomplete_gamma_q(double a, double x);
 
+/* Murphy-Koop saturation vapour pressures over liquid (first kSvpIntervals
+ * rows) and ice (next kSvpIntervals rows) as cubic polynomials in the
+ * position u in [0,1) inside each 1/64 K interval from 150 K: row i holds
+ * c0..c3 with e(T) = c0 + u (c1 + u (c2 + u c3)). */
+constexpr double kSvpT0 = 150.0, kSvpInvH = 64.0;
+constexpr int kSvpIntervals = 12800;
+void build_svp_table(std::vector<double>& coef);
+
 /* Synthetic workload, p3x_workload.cpp */
 int workload_generate(int kind, uint64_t seed, int col0, int ncol, int nlev, double* const* fields,
                       int64_t ld);

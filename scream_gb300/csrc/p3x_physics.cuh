@@ -64,6 +64,8 @@ struct RuntimeDev {
   double g_mur2;      /* Gamma(mu_r + 2)       */
   double lg_mur4;     /* log Gamma(mu_r + 4)   */
   double lg_mur7;     /* log Gamma(mu_r + 7)   */
+  /* FP32-bulk saturation table (layout of build_svp_table) */
+  const double* svp_tab;
 };
 
 /* ------------------------------------------------------------------ */
@@ -113,13 +115,34 @@ __device__ __forceinline__ TR murphy_koop_svp(TR t, bool ice, uint32_t& err) {
                 (TR(53.878) - (TR(1331.22) / t) - (TR(9.44523) * logt) + TR(0.014025) * t)));
 }
 
-/* qv_sat_dry (MurphyKoop), physics_saturation_impl.hpp:126-157.  Always FP64,
- * also in the FP32-bulk form: the saturation mixing ratio enters residuals
- * (qv - qv_sat) that are small near saturation, where an FP32 vapour pressure
- * (relative error ~1e-7) would decide evaporation and supersaturation limits. */
+/* Murphy-Koop vapour pressure from the FP64 saturation table of the
+ * FP32-bulk form: one cubic per 1/64 K interval from 150 K (interpolation
+ * error < 1e-12 relative), the formula outside the tabulated range. */
+constexpr double kSvpT0 = 150.0, kSvpInvH = 64.0;
+constexpr int kSvpIntervals = 12800;
+__device__ __forceinline__ double svp_tabulated(const double* tab, double t, bool ice, uint32_t& err) {
+  const double x = (t - kSvpT0) * kSvpInvH;
+  if (!(x >= 0.0 && x < double(kSvpIntervals))) return murphy_koop_svp<double>(t, ice, err);
+  const int i = int(x);
+  const double u = x - double(i);
+  const int row = (ice && t < C::Tmelt) ? kSvpIntervals + i : i;
+  const double2* c = reinterpret_cast<const double2*>(tab) + size_t(row) * 2;
+  const double2 c01 = __ldg(c), c23 = __ldg(c + 1);
+  return c01.x + u * (c01.y + u * (c23.x + u * c23.y));
+}
+
+/* qv_sat_dry (MurphyKoop), physics_saturation_impl.hpp:126-157.  FP64 in
+ * both forms: the saturation mixing ratio enters residuals (qv - qv_sat)
+ * that are small near saturation.  The plain form evaluates the formula; the
+ * FP32-bulk form reads the FP64 saturation table. */
 template <class TR>
-__device__ __forceinline__ double qv_sat_dry(double t, double p, bool ice, uint32_t& err) {
-  const double e_pres = murphy_koop_svp<double>(t, ice, err);
+__device__ __forceinline__ double qv_sat_dry(double t, double p, bool ice, const RuntimeDev& rt, uint32_t& err) {
+  double e_pres;
+  if constexpr (sizeof(TR) == sizeof(double)) {
+    e_pres = murphy_koop_svp<double>(t, ice, err);
+  } else {
+    e_pres = svp_tabulated(rt.svp_tab, t, ice, err);
+  }
   return C::ep_2 * e_pres / vmax(p, 1.e-3);
 }
 
@@ -818,6 +841,82 @@ __device__ __forceinline__ void evaporate_rain(double qr_incld, double qc_incld,
   }
 }
 
+/* evaporate_rain of the FP32-bulk form: the supersaturation residual
+ * ssat_r = qv - qv_sat_l and the A_c source term (differences of the state
+ * against the previous step) are formed in FP64; the relaxation weights,
+ * the equilibrium / instantaneous tendencies and the limits are rate
+ * arithmetic in FP32.  Same formulas and branch order as evaporate_rain. */
+__device__ __forceinline__ void evaporate_rain_bulk(double qr_incld, double qc_incld, double nr_incld,
+                                                    double qi_incld, double cld_frac_l, double cld_frac_r,
+                                                    double qv, double qv_prev, double qv_sat_l, double qv_sat_i,
+                                                    float ab, float abi, float epsr, float epsi_tot,
+                                                    double t_atm, double t_atm_prev, float dqsdt, double dt,
+                                                    float& qr2qv_evap_tend, float& nr_evap_tend) {
+  qr2qv_evap_tend = 0;
+  nr_evap_tend = 0;
+  const double ssat_r_d = qv - qv_sat_l;
+  const double cld_frac = ((qc_incld + qi_incld) < 1.e-6) ? 0.0 : cld_frac_l;
+  if (qr_incld >= C::QSMALL && ssat_r_d < 0 && cld_frac_r > cld_frac) {
+    const double inv_dt_d = 1 / dt;
+    const float inv_dt = float(inv_dt_d), dtf = float(dt);
+    const float ssat_r = float(ssat_r_d);
+    const float tau_r = 1.0f / epsr;
+    const float lat_fac = 1.0f + float((C::LatVap + C::LatIce) / C::Cpair) * dqsdt;
+    float eps_eff;
+    double A_c_d = (qv - qv_prev) * inv_dt_d - double(dqsdt) * (t_atm - t_atm_prev) * inv_dt_d;
+    if (t_atm < C::Tmelt) {
+      eps_eff = epsr + epsi_tot * lat_fac / abi;
+      A_c_d -= (qv_sat_l - qv_sat_i) * double(lat_fac / abi * epsi_tot);
+    } else {
+      eps_eff = epsr;
+    }
+    const float A_c = float(A_c_d);
+    if (eps_eff < 1e-20f) eps_eff = 1e-20f;
+    const float tau_eff = 1.0f / eps_eff;
+    float evap;
+    if (qr_incld < 1e-12 && qv / qv_sat_l < 0.999) {
+      evap = float(qr_incld) * inv_dt;
+    } else {
+      const float dt_over_tau = dtf / tau_eff;
+      const float w = -expm1f(-dt_over_tau) / dt_over_tau;
+      const float equilib = -A_c / ab * tau_eff / tau_r;
+      const float instant = -ssat_r / (ab * tau_r);
+      evap = instant * w + equilib * (1.0f - w);
+    }
+    const float lim = -ssat_r * inv_dt / ab;
+    if (evap > lim) evap = lim;
+    if (evap < 0.0f) evap = 0.0f;
+    const float qlim = float(qr_incld) * inv_dt;
+    if (evap > qlim) evap = qlim;
+    evap = evap * float((cld_frac_r - cld_frac) / cld_frac_r);
+    qr2qv_evap_tend = evap;
+    nr_evap_tend = evap * float(nr_incld / qr_incld);
+  }
+}
+
+/* ice_deposition_sublimation of the FP32-bulk form: the vapour residuals
+ * qv - qv_sat_i and qv_sat_l - qv_sat_i are FP64, the relaxation coefficient
+ * FP32. */
+__device__ __forceinline__ void ice_deposition_sublimation_bulk(double qi_incld, double ni_incld, double T_atm,
+                                                                double qv_sat_l, double qv_sat_i, float epsi,
+                                                                float abi, double qv, double inv_dt,
+                                                                float& vapdep, float& sublim, float& ni_sublim,
+                                                                float& berg) {
+  berg = 0; vapdep = 0; sublim = 0; ni_sublim = 0;
+  if (qi_incld > C::QSMALL) {
+    const float coef = vmin(epsi / abi, float(inv_dt));
+    const float qi_tend = coef * float(qv - qv_sat_i);
+    const bool neg = qi_tend < 0;
+    if (neg) {
+      sublim = -qi_tend;
+      ni_sublim = sublim * float(ni_incld / qi_incld);
+    }
+    const bool T_lt_frz = T_atm < C::T_zerodegc;
+    if (T_lt_frz && !neg) vapdep = qi_tend;
+    if (T_lt_frz) berg = vmax(epsi / abi * float(qv_sat_l - qv_sat_i), 0.0f);
+  }
+}
+
 /* ice_deposition_sublimation, p3/impl/p3_ice_deposition_sublimation_impl.hpp:9-65
  * (the vapour residual qv - qv_sat is FP64). */
 __device__ __forceinline__ void ice_deposition_sublimation(double qi_incld, double ni_incld, double T_atm,
@@ -942,13 +1041,13 @@ __device__ __forceinline__ void ice_supersat_conservation(Rates<double>& r, doub
 /* prevent_liq_supersaturation, p3/impl/p3_prevent_liq_supersaturation_impl.hpp:12-79 */
 template <class TR>
 __device__ __forceinline__ void prevent_liq_supersaturation(double pres, double t_atm, double qv, double dt,
-                                                            Rates<double>& r, uint32_t& err) {
+                                                            Rates<double>& r, const RuntimeDev& rt, uint32_t& err) {
   const double qv_sources = r.qi2qv_sublim_tend + r.qr2qv_evap_tend;
   if (!(qv_sources >= C::QSMALL)) return;
   const double qv_sinks = r.qv2qi_vapdep_tend + r.qv2qi_nucleat_tend;
   const double T_endstep = t_atm + ((qv_sinks - r.qi2qv_sublim_tend) * (C::LatVap + C::LatIce) * C::INV_CP -
                                     r.qr2qv_evap_tend * C::LatVap * C::INV_CP) * dt;
-  const double qsl = qv_sat_dry<TR>(T_endstep, pres, false, err);
+  const double qsl = qv_sat_dry<TR>(T_endstep, pres, false, rt, err);
   const double A = C::LatVap * qsl * dt * C::INV_CP / (C::RV * T_endstep * T_endstep) *
                    ((C::LatVap + C::LatIce) * r.qi2qv_sublim_tend + C::LatVap * r.qr2qv_evap_tend);
   double frac = (qsl - qv + qv_sinks * dt + A) / (qv_sources * dt + A);

@@ -707,4 +707,44 @@ int read_ice_table_file(const char* path, const char* expect_version, HostTables
   return 0;
 }
 
+/* Saturation table of the FP32-bulk form.  Cubic Hermite interpolants of the
+ * Murphy-Koop vapour pressures (share/physics_saturation_impl.hpp:38-81) and
+ * their analytic temperature derivatives, evaluated in long double, on a
+ * 1/64 K grid: the interpolation error is below 1e-12 relative at 150 K and
+ * below 1e-13 above 200 K. */
+namespace {
+void mk_log_svp(long double T, bool ice, long double& lnf, long double& dlnf) {
+  if (ice) {
+    lnf = 9.550426L - 5723.265L / T + 3.53068L * std::log(T) - 0.00728332L * T;
+    dlnf = 5723.265L / (T * T) + 3.53068L / T - 0.00728332L;
+    return;
+  }
+  const long double th = std::tanh(0.0415L * (T - 218.8L));
+  const long double B = 53.878L - 1331.22L / T - 9.44523L * std::log(T) + 0.014025L * T;
+  const long double dB = 1331.22L / (T * T) - 9.44523L / T + 0.014025L;
+  lnf = 54.842763L - 6763.22L / T - 4.210L * std::log(T) + 0.000367L * T + th * B;
+  dlnf = 6763.22L / (T * T) - 4.210L / T + 0.000367L + 0.0415L * (1 - th * th) * B + th * dB;
+}
+}  // namespace
+
+void build_svp_table(std::vector<double>& coef) {
+  coef.assign(size_t(2) * kSvpIntervals * 4, 0.0);
+  const long double h = 1.0L / kSvpInvH;
+  for (int phase = 0; phase < 2; ++phase) {
+    for (int i = 0; i < kSvpIntervals; ++i) {
+      const long double Ta = kSvpT0 + i * h, Tb = Ta + h;
+      long double la, da, lb, db;
+      mk_log_svp(Ta, phase == 1, la, da);
+      mk_log_svp(Tb, phase == 1, lb, db);
+      const long double fa = std::exp(la), fb = std::exp(lb);
+      const long double ga = h * fa * da, gb = h * fb * db; /* d e / d u */
+      double* r = &coef[(size_t(phase) * kSvpIntervals + i) * 4];
+      r[0] = double(fa);
+      r[1] = double(ga);
+      r[2] = double(3 * (fb - fa) - 2 * ga - gb);
+      r[3] = double(2 * (fa - fb) + ga + gb);
+    }
+  }
+}
+
 }  // namespace p3x
