@@ -303,17 +303,26 @@ int p3x_server_create(p3x_context* ctx, const p3x_runtime* rt, int64_t budget_by
                       int32_t max_inflight, p3x_server** out);
 int p3x_server_destroy(p3x_server* s);
 
-/* Submits a request: instance `instance_id` (created on first use with a
- * synthetic workload of ncol x nlev from `seed`, kept resident until its
- * last step) advances by one step.  arrival_s is the request's arrival time
- * on the server clock.  Non-blocking. */
+/* Submits a request: instance `instance_id` (created on first use, nlev 72
+ * or 128, ncol <= 65536) advances by one step.  Its initial state is columns
+ * [c0, c0 + ncol) of the server's synthetic workload (config-0 distributions,
+ * workload seed 5000) with c0 = seed mod (65536 - ncol + 1).  The instance
+ * stays resident, readable with p3x_server_read_field, until the server is
+ * destroyed.  arrival_s is the request's arrival time on the server clock
+ * (seconds since p3x_server_create).  Non-blocking: requests run in
+ * p3x_server_drain.  Returns P3X_ENOMEM (and counts a rejection) when the
+ * instance alone exceeds the budget. */
 int p3x_server_submit(p3x_server* s, int64_t instance_id, int32_t ncol, int32_t nlev,
                       int32_t precision, int32_t total_steps, uint64_t seed, double dt,
                       double arrival_s);
 
-/* Runs an open-loop Poisson load: n requests drawn from a seeded generator
- * (ncol log-uniform in [1, max_ncol], nlev from {72,128}, FP64 / FP32-bulk
- * 50/50, 1..20 steps per instance), arriving at rate_hz. */
+/* Runs a Poisson load of n sessions drawn from a seeded generator (ncol
+ * log-uniform in [1, max_ncol], nlev from {72,128}, FP64 / FP32-bulk 50/50,
+ * 1..20 steps each).  Sessions arrive at rate_hz; a session's first step
+ * request arrives with it, each further step request arrives when the
+ * previous step completes, and its memory is released after its last step.
+ * Blocks until every session has finished; stats cover this run only
+ * (latency = completion - arrival of each step request). */
 int p3x_server_run_poisson(p3x_server* s, double rate_hz, int32_t n_requests,
                            int32_t max_ncol, uint64_t seed, p3x_serve_stats* stats);
 

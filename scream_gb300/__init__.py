@@ -6,8 +6,8 @@ this package holds the Python-side mirror of the reference interface.
 from . import _lib
 from ._lib import (P3X_FP64, P3X_FP32_BULK, P3Error, Runtime, default_runtime, load, INPUT_FIELDS,
                    OUTPUT_FIELDS, PROG_FIELDS, ALL_FIELDS)
-from .p3 import P3Batch, P3Context, P3Fields, P3Microphysics, generate_inputs
+from .p3 import P3Batch, P3Context, P3Fields, P3Microphysics, P3Server, generate_inputs
 
 __all__ = ["P3X_FP64", "P3X_FP32_BULK", "P3Error", "Runtime", "default_runtime", "load", "P3Batch",
-           "P3Context", "P3Fields", "P3Microphysics", "generate_inputs", "INPUT_FIELDS",
+           "P3Context", "P3Fields", "P3Microphysics", "P3Server", "generate_inputs", "INPUT_FIELDS",
            "OUTPUT_FIELDS", "PROG_FIELDS", "ALL_FIELDS"]

@@ -683,30 +683,30 @@ struct p3x_batch {
 
 namespace p3x {
 namespace {
-int batch_launch(p3x_batch* b, cudaStream_t st) {
+template <class TR>
+int launch_work_t(p3x_context* ctx, const dev::RuntimeDev& rtd, const LaunchSpec& ls0, const dev::Inst* insts_d,
+                  const dev::WorkItem* work_d, int nwork, int nlev_max, cudaStream_t st) {
+  if (nwork == 0) return P3X_OK;
+  const int stride = sm_stride_for(nlev_max);
+  const int prec = sizeof(TR) == sizeof(double) ? P3X_FP64 : P3X_FP32_BULK;
+  const LaunchSpec ls = fit_spec(prec, ls0, stride);
+  if (!spec_fits(prec, ls, stride)) return P3X_EINVAL;
+  dev::KParams<TR> kp = make_kparams<TR>(ctx, rtd);
+  kp.sm_stride = stride;
+  kp.nwork = nwork;
+  kp.work = work_d;
+  kp.insts = insts_d;
   dev::Inst dummy{};
+  return cuda_status(launch_p3<TR>(dummy, kp, ls, ctx->num_sms, st));
+}
+
+int batch_launch(p3x_batch* b, cudaStream_t st) {
   for (int g = 0; g < b->ngroups; ++g) {
     auto& G = b->groups[g];
-    if (G.nwork == 0) continue;
-    const int stride = sm_stride_for(G.nlev_max);
-    const LaunchSpec ls = fit_spec(G.precision, G.ls, stride);
-    cudaError_t e;
-    if (G.precision == P3X_FP32_BULK) {
-      dev::KParams<float> kp = make_kparams<float>(b->ctx, b->rtd);
-      kp.sm_stride = stride;
-      kp.nwork = G.nwork;
-      kp.work = G.work_d;
-      kp.insts = b->insts_d;
-      e = launch_p3<float>(dummy, kp, ls, b->ctx->num_sms, st);
-    } else {
-      dev::KParams<double> kp = make_kparams<double>(b->ctx, b->rtd);
-      kp.sm_stride = stride;
-      kp.nwork = G.nwork;
-      kp.work = G.work_d;
-      kp.insts = b->insts_d;
-      e = launch_p3<double>(dummy, kp, ls, b->ctx->num_sms, st);
-    }
-    if (e != cudaSuccess) return cuda_status(e);
+    const int rc = G.precision == P3X_FP32_BULK
+                       ? launch_work_t<float>(b->ctx, b->rtd, G.ls, b->insts_d, G.work_d, G.nwork, G.nlev_max, st)
+                       : launch_work_t<double>(b->ctx, b->rtd, G.ls, b->insts_d, G.work_d, G.nwork, G.nlev_max, st);
+    if (rc) return rc;
   }
   return P3X_OK;
 }
@@ -717,6 +717,16 @@ void drop_graph(p3x_batch* b) {
   b->graph = nullptr;
 }
 }  // namespace
+
+int launch_work(p3x_context* ctx, const p3x_runtime& rt, int precision, const dev::Inst* insts_d,
+                const dev::WorkItem* work_d, int nwork, int nlev_max, cudaStream_t st) {
+  if (!ctx || (precision != P3X_FP64 && precision != P3X_FP32_BULK)) return P3X_EINVAL;
+  const dev::RuntimeDev rtd = make_runtime(rt);
+  const LaunchSpec ls = spec_of(ctx->cfg[precision]);
+  return precision == P3X_FP32_BULK ? launch_work_t<float>(ctx, rtd, ls, insts_d, work_d, nwork, nlev_max, st)
+                                    : launch_work_t<double>(ctx, rtd, ls, insts_d, work_d, nwork, nlev_max, st);
+}
+
 }  // namespace p3x
 
 extern "C" {

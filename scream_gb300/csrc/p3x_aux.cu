@@ -72,6 +72,32 @@ __global__ void column_budgets(const double* __restrict__ qv, const double* __re
 
 }  // namespace
 
+__global__ void postamble_kernel(const dev::Inst* __restrict__ insts, const dev::WorkItem* __restrict__ work,
+                                 int nwork) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nwork; w += warps) {
+    const dev::WorkItem wi = work[w];
+    const dev::Inst& in = insts[wi.inst];
+    const int64_t co = int64_t(wi.col) * in.ld;
+    double* qv_prev = const_cast<double*>(in.qv_prev);
+    double* t_prev = const_cast<double*>(in.t_prev);
+    for (int k = lane; k < in.nlev; k += 32) {
+      qv_prev[co + k] = in.qv[co + k];
+      t_prev[co + k] = in.th[co + k] / in.inv_exner[co + k];
+    }
+  }
+}
+
+cudaError_t launch_postamble(const dev::Inst* insts_d, const dev::WorkItem* work_d, int nwork, cudaStream_t st) {
+  if (nwork <= 0) return cudaSuccess;
+  const int threads = 256, per_block = threads / 32;
+  int blocks = (nwork + per_block - 1) / per_block;
+  if (blocks > 4096) blocks = 4096;
+  postamble_kernel<<<blocks, threads, 0, st>>>(insts_d, work_d, nwork);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_transpose_to_levels(const double* src, double* dst, int ncol, int nlev, int64_t ld,
                                        cudaStream_t st) {
   if (ncol <= 0 || nlev <= 0) return cudaSuccess;

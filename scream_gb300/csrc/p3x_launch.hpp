@@ -4,7 +4,10 @@
 
 #include <cuda_runtime.h>
 
+#include "p3x.h"
 #include "p3x_column.cuh"
+
+struct p3x_context;
 
 namespace p3x {
 
@@ -51,6 +54,18 @@ cudaError_t launch_transpose_to_levels(const double* src, double* dst, int ncol,
                                        cudaStream_t st);
 cudaError_t launch_transpose_to_columns(const double* src, double* dst, int ncol, int nlev, int64_t ld,
                                         cudaStream_t st);
+
+/* One step of a work list of (instance, column) items whose instances all
+ * have the given precision: K1, K2, K3 with the context's launch
+ * configuration for that precision (p3x_api.cu).  Every instance's scratch
+ * must be bound. */
+int launch_work(p3x_context* ctx, const p3x_runtime& rt, int precision, const dev::Inst* insts_d,
+                const dev::WorkItem* work_d, int nwork, int nlev_max, cudaStream_t st);
+
+/* The state hand-over of the P3 process interface between steps
+ * (eamxx_p3_process_interface.hpp:218,237 with dry = wet mixing ratios):
+ * qv_prev <- qv and t_prev <- th / inv_exner, for every work item. */
+cudaError_t launch_postamble(const dev::Inst* insts_d, const dev::WorkItem* work_d, int nwork, cudaStream_t st);
 
 cudaError_t launch_budgets(const double* qv, const double* qc, const double* qr, const double* qi,
                            const double* th, const double* dpres, const double* inv_exner, int ncol,

@@ -1,20 +1,625 @@
-/* Serving loop of libp3x (continuous batching of P3 steps). */
+/*
+ * Serving loop of libp3x: continuous batching of P3 steps under a
+ * device-memory budget.
+ *
+ * A request advances one resident instance (its own ncol x nlev state, FP64
+ * or FP32-bulk) by one P3 step.  A single host thread runs the loop:
+ *
+ *   arrivals   -> per-instance FIFO of step requests (steps of one instance
+ *                 run in order, one at a time);
+ *   admission  -> an instance's memory (fields + hand-over scratch) is taken
+ *                 from a stream-ordered pool only while the resident total
+ *                 stays within the budget; admission is first come, first
+ *                 served, so a large instance is not starved by small ones;
+ *   dispatch   -> whenever one of `max_inflight` slots (a CUDA stream each)
+ *                 is free, every ready request of one precision (up to a
+ *                 column cap) is packed into one work list and stepped by
+ *                 the batched kernels (part1+2, sedimentation, part3) plus
+ *                 the state hand-over; slots overlap on the device;
+ *   completion -> an event per slot, polled; latency = completion - arrival
+ *                 on the host clock; a Poisson session's memory returns to
+ *                 the pool after its last step; an instance created by
+ *                 p3x_server_submit stays resident (readable) after its last
+ *                 step until admission needs the memory (oldest first).
+ *
+ * If nothing is running, nothing is due and the instance at the head of the
+ * admission queue still does not fit (memory held by idle instances that
+ * wait for further requests), that instance is rejected instead of waiting
+ * for memory that cannot come free.
+ *
+ * Instance workloads are column slices of synthetic templates (65536
+ * columns of the config-0 distributions per level count), generated once per
+ * server and kept on the device: instance `seed` starts at template column
+ * seed mod (65536 - ncol + 1), so a request's data does not cross PCIe on the
+ * latency path and the same instance has the same data alone and in a mix.
+ * Columns are independent, so an instance's result does not depend on what
+ * it was batched with.
+ */
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <random>
+#include <thread>
+#include <vector>
+
 #include "p3x.h"
+#include "p3x_internal.hpp"
+#include "p3x_launch.hpp"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+using p3x::dev::Inst;
+using p3x::dev::WorkItem;
+
+constexpr int kTemplateCols = 65536;
+constexpr uint64_t kTemplateSeed = 5000;   /* config-4 instance seeds start at 1000 * (4 + 1) */
+constexpr int kMidOutputs = 10;             /* 7 per-level diagnostics + 3 history fields */
+constexpr int kBatchColumnCap = 1 << 18;    /* columns per dispatched work list */
+
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+struct Instance {
+  int64_t id = 0;
+  int32_t ncol = 0, nlev = 0, precision = 0, total_steps = 1, done = 0;
+  double dt = 300.0;
+  uint64_t seed = 0;
+  size_t bytes = 0;
+  void* mem = nullptr;
+  bool admitted = false, busy = false, closed_loop = false;
+  double retired_at = -1; /* explicit instance after its last step: evictable */
+  std::deque<double> arrivals; /* arrival times of queued steps */
+  Inst in{};
+};
+
+struct Slot {
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev = nullptr;
+  bool busy = false;
+  std::vector<int64_t> ids;     /* instances stepped by this dispatch */
+  std::vector<double> arrivals; /* their requests' arrival times */
+  Inst* h_insts = nullptr;
+  WorkItem* h_work = nullptr;
+  Inst* d_insts = nullptr;
+  WorkItem* d_work = nullptr;
+  int cap_insts = 0, cap_work = 0;
+};
+
+}  // namespace
+
+struct p3x_server {
+  p3x_context* ctx = nullptr;
+  p3x_runtime rt{};
+  int64_t budget = 0;
+  int64_t resident = 0, peak_resident = 0;
+  int32_t peak_inflight = 0;
+  cudaMemPool_t pool = nullptr;
+  double* tmpl[2] = {nullptr, nullptr}; /* nlev 72, 128: [P3X_NUM_INPUTS][65536][nlev] */
+  std::vector<Slot> slots;
+  std::map<int64_t, Instance> inst;
+  std::deque<int64_t> admit_fifo;                 /* instances waiting for memory */
+  std::multimap<double, int64_t> future;          /* arrivals not yet due: time -> instance */
+  Clock::time_point t0;
+  std::vector<double> lat_ms;
+  int64_t completed = 0, rejected = 0;
+  double cl_done = 0;
+  double first_arrival = -1, last_done = 0;
+};
+
+namespace {
+
+int cuda_rc(cudaError_t e) {
+  if (e == cudaSuccess) return P3X_OK;
+  return e == cudaErrorMemoryAllocation ? P3X_ENOMEM : P3X_ECUDA;
+}
+#define SRV_CUDA(x)                                 \
+  do {                                              \
+    const cudaError_t e_ = (x);                     \
+    if (e_ != cudaSuccess) return cuda_rc(e_);      \
+  } while (0)
+
+double now_s(const p3x_server* s) { return std::chrono::duration<double>(Clock::now() - s->t0).count(); }
+
+size_t instance_bytes(int ncol, int nlev) {
+  const size_t mid = align256(size_t(ncol) * nlev * sizeof(double));
+  const size_t itf = align256(size_t(ncol) * (nlev + 1) * sizeof(double));
+  const size_t srf = align256(size_t(ncol) * sizeof(double));
+  return size_t(P3X_NUM_INPUTS + kMidOutputs) * mid + 2 * itf + 2 * srf + p3x::dev::scratch_bytes(ncol, nlev);
+}
+
+/* Binds the device pointers of an instance laid out in one allocation. */
+void bind_instance(Instance& I) {
+  const int ncol = I.ncol, nlev = I.nlev;
+  const size_t mid = align256(size_t(ncol) * nlev * sizeof(double));
+  const size_t itf = align256(size_t(ncol) * (nlev + 1) * sizeof(double));
+  const size_t srf = align256(size_t(ncol) * sizeof(double));
+  unsigned char* p = static_cast<unsigned char*>(I.mem);
+  double* f[P3X_NUM_INPUTS + kMidOutputs];
+  for (int k = 0; k < P3X_NUM_INPUTS + kMidOutputs; ++k, p += mid) f[k] = reinterpret_cast<double*>(p);
+  double* liq_flux = reinterpret_cast<double*>(p); p += itf;
+  double* ice_flux = reinterpret_cast<double*>(p); p += itf;
+  double* liq_surf = reinterpret_cast<double*>(p); p += srf;
+  double* ice_surf = reinterpret_cast<double*>(p); p += srf;
+  Inst& in = I.in;
+  in = Inst{};
+  in.qc = f[P3X_F_QC]; in.nc = f[P3X_F_NC]; in.qr = f[P3X_F_QR]; in.nr = f[P3X_F_NR];
+  in.qi = f[P3X_F_QI]; in.qm = f[P3X_F_QM]; in.ni = f[P3X_F_NI]; in.bm = f[P3X_F_BM];
+  in.qv = f[P3X_F_QV]; in.th = f[P3X_F_TH];
+  in.nc_nuceat_tend = f[P3X_F_NC_NUCEAT_TEND]; in.nccn = f[P3X_F_NCCN]; in.ni_activated = f[P3X_F_NI_ACTIVATED];
+  in.inv_qc_relvar = f[P3X_F_INV_QC_RELVAR]; in.cld_frac_i = f[P3X_F_CLD_FRAC_I];
+  in.cld_frac_l = f[P3X_F_CLD_FRAC_L]; in.cld_frac_r = f[P3X_F_CLD_FRAC_R]; in.pres = f[P3X_F_PRES];
+  in.dz = f[P3X_F_DZ]; in.dpres = f[P3X_F_DPRES]; in.inv_exner = f[P3X_F_INV_EXNER];
+  in.qv_prev = f[P3X_F_QV_PREV]; in.t_prev = f[P3X_F_T_PREV];
+  double** o = f + P3X_NUM_INPUTS;
+  in.qv2qi_depos_tend = o[0]; in.precip_total_tend = o[1]; in.nevapr = o[2];
+  in.diag_eff_radius_qc = o[3]; in.diag_eff_radius_qi = o[4]; in.diag_eff_radius_qr = o[5]; in.rho_qi = o[6];
+  in.liq_ice_exchange = o[7]; in.vap_liq_exchange = o[8]; in.vap_ice_exchange = o[9];
+  in.precip_liq_flux = liq_flux; in.precip_ice_flux = ice_flux;
+  in.precip_liq_surf = liq_surf; in.precip_ice_surf = ice_surf;
+  in.scr = reinterpret_cast<double*>(p);
+  in.cflag = reinterpret_cast<int32_t*>(p + size_t(p3x::dev::kScrFields) * ncol * nlev * sizeof(double));
+  in.ld = nlev;
+  in.ld_int = nlev + 1;
+  in.ncol = ncol;
+  in.nlev = nlev;
+  in.dt = I.dt;
+  in.predictNc = 1;
+  in.prescribedCCN = 1;
+  in.precision = I.precision;
+}
+
+int template_index(int nlev) { return nlev == 72 ? 0 : (nlev == 128 ? 1 : -1); }
+
+int build_template(p3x_server* s, int which, int nlev) {
+  const size_t n = size_t(kTemplateCols) * nlev;
+  std::vector<double> host(size_t(P3X_NUM_INPUTS) * n);
+  std::vector<double*> fields(P3X_NUM_INPUTS);
+  for (int f = 0; f < P3X_NUM_INPUTS; ++f) fields[f] = host.data() + size_t(f) * n;
+  const int rc = p3x::workload_generate(0, kTemplateSeed, 0, kTemplateCols, nlev, fields.data(), nlev);
+  if (rc) return rc;
+  SRV_CUDA(cudaMalloc(&s->tmpl[which], host.size() * sizeof(double)));
+  SRV_CUDA(cudaMemcpy(s->tmpl[which], host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice));
+  return P3X_OK;
+}
+
+/* Takes memory for the instance and copies its initial state (template
+ * slice) on stream st.  Host-side budget accounting happened already. */
+int materialise(p3x_server* s, Instance& I, cudaStream_t st) {
+  SRV_CUDA(cudaMallocFromPoolAsync(&I.mem, I.bytes, s->pool, st));
+  bind_instance(I);
+  const int w = template_index(I.nlev);
+  const int64_t c0 = int64_t(I.seed % uint64_t(kTemplateCols - I.ncol + 1));
+  const size_t n = size_t(kTemplateCols) * I.nlev;
+  double* dst[P3X_NUM_INPUTS] = {I.in.qc, I.in.nc, I.in.qr, I.in.nr, I.in.qi, I.in.qm, I.in.ni, I.in.bm,
+                                 I.in.qv, I.in.th,
+                                 const_cast<double*>(I.in.nc_nuceat_tend), const_cast<double*>(I.in.nccn),
+                                 const_cast<double*>(I.in.ni_activated), const_cast<double*>(I.in.inv_qc_relvar),
+                                 const_cast<double*>(I.in.cld_frac_i), const_cast<double*>(I.in.cld_frac_l),
+                                 const_cast<double*>(I.in.cld_frac_r), const_cast<double*>(I.in.pres),
+                                 const_cast<double*>(I.in.dz), const_cast<double*>(I.in.dpres),
+                                 const_cast<double*>(I.in.inv_exner), const_cast<double*>(I.in.qv_prev),
+                                 const_cast<double*>(I.in.t_prev)};
+  for (int f = 0; f < P3X_NUM_INPUTS; ++f) {
+    const double* src = s->tmpl[w] + size_t(f) * n + size_t(c0) * I.nlev;
+    SRV_CUDA(cudaMemcpyAsync(dst[f], src, size_t(I.ncol) * I.nlev * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  }
+  return P3X_OK;
+}
+
+int ensure_capacity(Slot& sl, int ninst, int nwork) {
+  if (ninst > sl.cap_insts) {
+    if (sl.h_insts) cudaFreeHost(sl.h_insts);
+    if (sl.d_insts) cudaFree(sl.d_insts);
+    const int cap = std::max(ninst, 2 * sl.cap_insts);
+    SRV_CUDA(cudaMallocHost(&sl.h_insts, sizeof(Inst) * cap));
+    SRV_CUDA(cudaMalloc(&sl.d_insts, sizeof(Inst) * cap));
+    sl.cap_insts = cap;
+  }
+  if (nwork > sl.cap_work) {
+    if (sl.h_work) cudaFreeHost(sl.h_work);
+    if (sl.d_work) cudaFree(sl.d_work);
+    const int cap = std::max(nwork, 2 * sl.cap_work);
+    SRV_CUDA(cudaMallocHost(&sl.h_work, sizeof(WorkItem) * cap));
+    SRV_CUDA(cudaMalloc(&sl.d_work, sizeof(WorkItem) * cap));
+    sl.cap_work = cap;
+  }
+  return P3X_OK;
+}
+
+/* Moves due arrivals into their instances' queues. */
+void take_arrivals(p3x_server* s, double t) {
+  while (!s->future.empty() && s->future.begin()->first <= t) {
+    const double at = s->future.begin()->first;
+    const int64_t id = s->future.begin()->second;
+    s->future.erase(s->future.begin());
+    Instance& I = s->inst.at(id);
+    I.arrivals.push_back(at);
+    if (s->first_arrival < 0 || at < s->first_arrival) s->first_arrival = at;
+  }
+}
+
+/* Frees retired explicit instances, oldest first, until `need` more bytes
+ * fit in the budget.  Returns whether they fit. */
+bool evict_for(p3x_server* s, int64_t need) {
+  while (s->resident + need > s->budget) {
+    int64_t victim = -1;
+    double oldest = 1e300;
+    for (auto& kv : s->inst) {
+      const Instance& I = kv.second;
+      if (I.retired_at >= 0 && !I.busy && I.arrivals.empty() && I.mem && I.retired_at < oldest) {
+        oldest = I.retired_at;
+        victim = kv.first;
+      }
+    }
+    if (victim < 0) return false;
+    Instance& V = s->inst.at(victim);
+    cudaFreeAsync(V.mem, s->slots[0].st);
+    s->resident -= int64_t(V.bytes);
+    s->inst.erase(victim);
+  }
+  return true;
+}
+
+/* First come, first served admission against the budget. */
+void admit(p3x_server* s) {
+  while (!s->admit_fifo.empty()) {
+    Instance& I = s->inst.at(s->admit_fifo.front());
+    if (I.arrivals.empty()) break; /* not arrived yet */
+    if (!evict_for(s, int64_t(I.bytes))) break;
+    s->resident += int64_t(I.bytes);
+    s->peak_resident = std::max(s->peak_resident, s->resident);
+    I.admitted = true;
+    s->admit_fifo.pop_front();
+  }
+}
+
+/* Packs every ready request of the oldest ready precision into one work
+ * list and launches it on slot sl. */
+int dispatch(p3x_server* s, Slot& sl) {
+  int prec = -1;
+  double oldest = 1e300;
+  for (auto& kv : s->inst) {
+    const Instance& I = kv.second;
+    if (I.admitted && !I.busy && !I.arrivals.empty() && I.arrivals.front() < oldest) {
+      oldest = I.arrivals.front();
+      prec = I.precision;
+    }
+  }
+  if (prec < 0) return 1; /* nothing ready */
+  std::vector<Instance*> take;
+  int cols = 0, nlev_max = 1;
+  /* oldest first */
+  std::vector<std::pair<double, Instance*>> ready;
+  for (auto& kv : s->inst) {
+    Instance& I = kv.second;
+    if (I.admitted && !I.busy && !I.arrivals.empty() && I.precision == prec) ready.push_back({I.arrivals.front(), &I});
+  }
+  std::sort(ready.begin(), ready.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+  for (auto& r : ready) {
+    if (!take.empty() && cols + r.second->ncol > kBatchColumnCap) break;
+    take.push_back(r.second);
+    cols += r.second->ncol;
+    nlev_max = std::max(nlev_max, r.second->nlev);
+  }
+  int rc = ensure_capacity(sl, int(take.size()), cols);
+  if (rc) return rc;
+  sl.ids.clear();
+  sl.arrivals.clear();
+  int w = 0;
+  for (size_t i = 0; i < take.size(); ++i) {
+    Instance& I = *take[i];
+    if (!I.mem) {
+      rc = materialise(s, I, sl.st);
+      if (rc) return rc;
+    }
+    sl.h_insts[i] = I.in;
+    for (int c = 0; c < I.ncol; ++c) sl.h_work[w++] = WorkItem{int32_t(i), c};
+    sl.ids.push_back(I.id);
+    sl.arrivals.push_back(I.arrivals.front());
+    I.arrivals.pop_front();
+    I.busy = true;
+  }
+  SRV_CUDA(cudaMemcpyAsync(sl.d_insts, sl.h_insts, sizeof(Inst) * take.size(), cudaMemcpyHostToDevice, sl.st));
+  SRV_CUDA(cudaMemcpyAsync(sl.d_work, sl.h_work, sizeof(WorkItem) * w, cudaMemcpyHostToDevice, sl.st));
+  rc = p3x::launch_work(s->ctx, s->rt, prec, sl.d_insts, sl.d_work, w, nlev_max, sl.st);
+  if (rc) return rc;
+  SRV_CUDA(p3x::launch_postamble(sl.d_insts, sl.d_work, w, sl.st));
+  SRV_CUDA(cudaEventRecord(sl.ev, sl.st));
+  sl.busy = true;
+  return P3X_OK;
+}
+
+/* Retires a finished dispatch. */
+int complete(p3x_server* s, Slot& sl, double t) {
+  for (size_t i = 0; i < sl.ids.size(); ++i) {
+    Instance& I = s->inst.at(sl.ids[i]);
+    s->lat_ms.push_back((t - sl.arrivals[i]) * 1e3);
+    s->completed += 1;
+    s->cl_done += double(I.ncol) * I.nlev;
+    I.busy = false;
+    I.done += 1;
+    if (I.closed_loop && I.done >= I.total_steps) {
+      SRV_CUDA(cudaFreeAsync(I.mem, sl.st));
+      I.mem = nullptr;
+      s->resident -= int64_t(I.bytes);
+      s->inst.erase(sl.ids[i]);
+    } else if (I.closed_loop) {
+      s->future.insert({t, I.id}); /* the next step of a session arrives on completion */
+    } else if (I.done >= I.total_steps && I.arrivals.empty()) {
+      I.retired_at = t;
+    }
+  }
+  s->last_done = t;
+  sl.busy = false;
+  return P3X_OK;
+}
+
+bool idle(const p3x_server* s) {
+  if (!s->future.empty()) return false;
+  for (const auto& sl : s->slots)
+    if (sl.busy) return false;
+  for (const auto& kv : s->inst)
+    if (!kv.second.arrivals.empty()) return false;
+  return true;
+}
+
+/* Runs the loop until every submitted (and every closed-loop follow-up)
+ * request has completed. */
+int run_loop(p3x_server* s) {
+  double last_progress = now_s(s);
+  while (!idle(s)) {
+    const double t = now_s(s);
+    /* watchdog: a loop that makes no progress for a minute (nothing
+     * completes, dispatches or arrives) ends with P3X_ETIMEOUT */
+    if (t - last_progress > 60.0 && (s->future.empty() || s->future.begin()->first < t)) return P3X_ETIMEOUT;
+    take_arrivals(s, t);
+    bool progressed = false;
+    int inflight = 0;
+    for (auto& sl : s->slots) {
+      if (!sl.busy) continue;
+      const cudaError_t q = cudaEventQuery(sl.ev);
+      if (q == cudaSuccess) {
+        const int rc = complete(s, sl, now_s(s));
+        if (rc) return rc;
+        progressed = true;
+      } else if (q != cudaErrorNotReady) {
+        return cuda_rc(q);
+      } else {
+        ++inflight;
+      }
+    }
+    admit(s);
+    for (auto& sl : s->slots) {
+      if (sl.busy) continue;
+      const int rc = dispatch(s, sl);
+      if (rc == 1) break;
+      if (rc) return rc;
+      ++inflight;
+      progressed = true;
+    }
+    s->peak_inflight = std::max(s->peak_inflight, inflight);
+    if (progressed) last_progress = now_s(s);
+    if (!progressed && inflight == 0 && s->future.empty() && !s->admit_fifo.empty()) {
+      /* nothing can free memory for the head of the admission queue */
+      bool dispatchable = false;
+      for (const auto& kv : s->inst) {
+        const Instance& I = kv.second;
+        if (I.admitted && !I.busy && !I.arrivals.empty()) dispatchable = true;
+      }
+      if (!dispatchable) {
+        const int64_t id = s->admit_fifo.front();
+        s->admit_fifo.pop_front();
+        Instance& I = s->inst.at(id);
+        s->rejected += int64_t(I.arrivals.size());
+        s->inst.erase(id);
+        continue;
+      }
+    }
+    if (!progressed) {
+      /* wait for the next arrival or completion without burning a core */
+      double wait = 50e-6;
+      if (!s->future.empty()) wait = std::min(wait, std::max(0.0, s->future.begin()->first - now_s(s)));
+      if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(wait));
+    }
+  }
+  return P3X_OK;
+}
+
+double percentile(std::vector<double> v, double q) {
+  if (v.empty()) return 0;
+  std::sort(v.begin(), v.end());
+  const double pos = q * (v.size() - 1);
+  const size_t i = size_t(pos);
+  const double f = pos - double(i);
+  return i + 1 < v.size() ? v[i] * (1 - f) + v[i + 1] * f : v[i];
+}
+
+void fill_stats(p3x_server* s, p3x_serve_stats* st, double offered) {
+  if (!st) return;
+  std::memset(st, 0, sizeof(*st));
+  st->completed = s->completed;
+  st->rejected = s->rejected;
+  st->p50_ms = percentile(s->lat_ms, 0.50);
+  st->p90_ms = percentile(s->lat_ms, 0.90);
+  st->p99_ms = percentile(s->lat_ms, 0.99);
+  st->max_ms = s->lat_ms.empty() ? 0 : *std::max_element(s->lat_ms.begin(), s->lat_ms.end());
+  double sum = 0;
+  for (double v : s->lat_ms) sum += v;
+  st->mean_ms = s->lat_ms.empty() ? 0 : sum / s->lat_ms.size();
+  st->wall_s = s->first_arrival >= 0 ? s->last_done - s->first_arrival : 0;
+  st->column_levels_per_s = st->wall_s > 0 ? s->cl_done / st->wall_s : 0;
+  st->offered_rate_hz = offered;
+  st->peak_bytes = s->peak_resident;
+  st->peak_inflight = s->peak_inflight;
+}
+
+void reset_stats(p3x_server* s) {
+  s->lat_ms.clear();
+  s->completed = s->rejected = 0;
+  s->cl_done = 0;
+  s->first_arrival = -1;
+  s->last_done = 0;
+  s->peak_resident = s->resident;
+  s->peak_inflight = 0;
+}
+
+/* Registers a step request; creates the instance record on first use. */
+int enqueue(p3x_server* s, int64_t id, int32_t ncol, int32_t nlev, int32_t precision, int32_t total_steps,
+            uint64_t seed, double dt, double arrival, bool closed_loop) {
+  if (ncol <= 0 || ncol > kTemplateCols || template_index(nlev) < 0 || total_steps <= 0 || !(dt > 0) ||
+      (precision != P3X_FP64 && precision != P3X_FP32_BULK))
+    return P3X_EINVAL;
+  auto it = s->inst.find(id);
+  if (it == s->inst.end()) {
+    const size_t bytes = instance_bytes(ncol, nlev);
+    if (int64_t(bytes) > s->budget) {
+      s->rejected += 1;
+      return P3X_ENOMEM;
+    }
+    Instance I;
+    I.id = id;
+    I.ncol = ncol;
+    I.nlev = nlev;
+    I.precision = precision;
+    I.total_steps = total_steps;
+    I.seed = seed;
+    I.dt = dt;
+    I.bytes = bytes;
+    I.closed_loop = closed_loop;
+    s->inst.emplace(id, std::move(I));
+    s->admit_fifo.push_back(id);
+  } else {
+    const Instance& I = it->second;
+    if (I.ncol != ncol || I.nlev != nlev || I.precision != precision) return P3X_EINVAL;
+  }
+  s->future.insert({arrival, id});
+  return P3X_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
-int p3x_server_create(p3x_context*, const p3x_runtime*, int64_t, int32_t, p3x_server** out) {
-  if (out) *out = nullptr;
-  return P3X_EINVAL;
+int p3x_server_create(p3x_context* ctx, const p3x_runtime* rt, int64_t budget_bytes, int32_t max_inflight,
+                      p3x_server** out) {
+  if (!out) return P3X_EINVAL;
+  *out = nullptr;
+  if (!ctx || !rt || budget_bytes <= 0 || max_inflight <= 0 || max_inflight > 64) return P3X_EINVAL;
+  auto s = std::make_unique<p3x_server>();
+  s->ctx = ctx;
+  s->rt = *rt;
+  s->budget = budget_bytes;
+  int dev = 0;
+  SRV_CUDA(cudaGetDevice(&dev));
+  cudaMemPoolProps props{};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = dev;
+  SRV_CUDA(cudaMemPoolCreate(&s->pool, &props));
+  uint64_t keep = UINT64_MAX;
+  SRV_CUDA(cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  int rc;
+  if ((rc = build_template(s.get(), 0, 72)) || (rc = build_template(s.get(), 1, 128))) {
+    p3x_server_destroy(s.release());
+    return rc;
+  }
+  s->slots.resize(max_inflight);
+  for (auto& sl : s->slots) {
+    SRV_CUDA(cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking));
+    SRV_CUDA(cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming));
+  }
+  s->t0 = Clock::now();
+  *out = s.release();
+  return P3X_OK;
 }
-int p3x_server_destroy(p3x_server*) { return P3X_EINVAL; }
-int p3x_server_submit(p3x_server*, int64_t, int32_t, int32_t, int32_t, int32_t, uint64_t, double, double) {
-  return P3X_EINVAL;
+
+int p3x_server_destroy(p3x_server* s) {
+  if (!s) return P3X_EINVAL;
+  cudaDeviceSynchronize();
+  for (auto& kv : s->inst)
+    if (kv.second.mem) cudaFreeAsync(kv.second.mem, nullptr);
+  cudaDeviceSynchronize();
+  for (auto& sl : s->slots) {
+    if (sl.ev) cudaEventDestroy(sl.ev);
+    if (sl.st) cudaStreamDestroy(sl.st);
+    if (sl.h_insts) cudaFreeHost(sl.h_insts);
+    if (sl.h_work) cudaFreeHost(sl.h_work);
+    if (sl.d_insts) cudaFree(sl.d_insts);
+    if (sl.d_work) cudaFree(sl.d_work);
+  }
+  for (double* t : s->tmpl)
+    if (t) cudaFree(t);
+  if (s->pool) cudaMemPoolDestroy(s->pool);
+  delete s;
+  return P3X_OK;
 }
-int p3x_server_run_poisson(p3x_server*, double, int32_t, int32_t, uint64_t, p3x_serve_stats*) {
-  return P3X_EINVAL;
+
+int p3x_server_submit(p3x_server* s, int64_t instance_id, int32_t ncol, int32_t nlev, int32_t precision,
+                      int32_t total_steps, uint64_t seed, double dt, double arrival_s) {
+  if (!s) return P3X_EINVAL;
+  return enqueue(s, instance_id, ncol, nlev, precision, total_steps, seed, dt, arrival_s, false);
 }
-int p3x_server_read_field(p3x_server*, int64_t, int32_t, double*, int64_t) { return P3X_EINVAL; }
-int p3x_server_drain(p3x_server*, p3x_serve_stats*) { return P3X_EINVAL; }
+
+int p3x_server_drain(p3x_server* s, p3x_serve_stats* stats) {
+  if (!s) return P3X_EINVAL;
+  const int rc = run_loop(s);
+  fill_stats(s, stats, 0.0);
+  return rc;
+}
+
+int p3x_server_run_poisson(p3x_server* s, double rate_hz, int32_t n_requests, int32_t max_ncol, uint64_t seed,
+                           p3x_serve_stats* stats) {
+  if (!s || !(rate_hz > 0) || n_requests <= 0 || max_ncol <= 0 || max_ncol > kTemplateCols) return P3X_EINVAL;
+  int rc = run_loop(s); /* finish earlier work first */
+  if (rc) return rc;
+  reset_stats(s);
+  std::mt19937_64 gen(seed);
+  std::exponential_distribution<double> gap(rate_hz);
+  std::uniform_real_distribution<double> u01(0.0, 1.0);
+  std::uniform_int_distribution<int> steps(1, 20);
+  const double start = now_s(s);
+  double t = start;
+  int64_t id = int64_t(1) << 40;
+  for (int i = 0; i < n_requests; ++i) {
+    t += gap(gen);
+    const int ncol = std::max(1, std::min(max_ncol, int(std::floor(std::exp(u01(gen) * std::log(double(max_ncol) + 1.0))))));
+    const int nlev = u01(gen) < 0.5 ? 72 : 128;
+    const int prec = u01(gen) < 0.5 ? P3X_FP64 : P3X_FP32_BULK;
+    const int nsteps = steps(gen);
+    const uint64_t iseed = kTemplateSeed + uint64_t(i);
+    rc = enqueue(s, id + i, ncol, nlev, prec, nsteps, iseed, 300.0, t, true);
+    if (rc && rc != P3X_ENOMEM) return rc;
+  }
+  rc = run_loop(s);
+  fill_stats(s, stats, rate_hz);
+  return rc;
+}
+
+int p3x_server_read_field(p3x_server* s, int64_t instance_id, int32_t field, double* host_out, int64_t n) {
+  if (!s || !host_out) return P3X_EINVAL;
+  auto it = s->inst.find(instance_id);
+  if (it == s->inst.end() || !it->second.mem) return P3X_EINVAL;
+  const Instance& I = it->second;
+  const double* src;
+  int64_t count;
+  if (field == -1 || field == -2) {
+    src = field == -1 ? I.in.precip_liq_surf : I.in.precip_ice_surf;
+    count = I.ncol;
+  } else if (field >= P3X_F_QC && field <= P3X_F_TH) {
+    const double* f[] = {I.in.qc, I.in.nc, I.in.qr, I.in.nr, I.in.qi, I.in.qm, I.in.ni, I.in.bm, I.in.qv, I.in.th};
+    src = f[field];
+    count = int64_t(I.ncol) * I.nlev;
+  } else {
+    return P3X_EINVAL;
+  }
+  if (n < count) return P3X_EINVAL;
+  SRV_CUDA(cudaDeviceSynchronize());
+  SRV_CUDA(cudaMemcpy(host_out, src, sizeof(double) * count, cudaMemcpyDeviceToHost));
+  return P3X_OK;
+}
 
 }  // extern "C"

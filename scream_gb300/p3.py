@@ -223,6 +223,54 @@ class P3Batch:
             pass
 
 
+class P3Server:
+    """Continuous-batching request loop over resident P3 instances
+    (p3x_server_* in include/p3x.h): admission under a device-memory budget,
+    up to ``max_inflight`` overlapping dispatches, p50/p99 latency."""
+
+    def __init__(self, ctx: P3Context, budget_bytes: int = 120 * 10**9, max_inflight: int = 4,
+                 runtime: L.Runtime = None):
+        self.ctx = ctx
+        rt = runtime if runtime is not None else L.default_runtime()
+        self.h = C.c_void_p()
+        L.check("p3x_server_create", ctx.lib.p3x_server_create(ctx.h, C.byref(rt), int(budget_bytes),
+                                                               int(max_inflight), C.byref(self.h)))
+
+    def submit(self, instance_id: int, ncol: int, nlev: int, precision: int, total_steps: int = 1,
+               seed: int = 0, dt: float = 300.0, arrival_s: float = 0.0):
+        L.check("p3x_server_submit", self.ctx.lib.p3x_server_submit(
+            self.h, int(instance_id), int(ncol), int(nlev), int(precision), int(total_steps), int(seed),
+            float(dt), float(arrival_s)))
+
+    def drain(self) -> dict:
+        st = L.ServeStats()
+        L.check("p3x_server_drain", self.ctx.lib.p3x_server_drain(self.h, C.byref(st)))
+        return st.as_dict()
+
+    def run_poisson(self, rate_hz: float, n_sessions: int, max_ncol: int = 65536, seed: int = 4) -> dict:
+        st = L.ServeStats()
+        L.check("p3x_server_run_poisson", self.ctx.lib.p3x_server_run_poisson(
+            self.h, float(rate_hz), int(n_sessions), int(max_ncol), int(seed), C.byref(st)))
+        return st.as_dict()
+
+    def read_field(self, instance_id: int, field: int, n: int) -> np.ndarray:
+        out = np.empty(n, dtype=np.float64)
+        L.check("p3x_server_read_field", self.ctx.lib.p3x_server_read_field(
+            self.h, int(instance_id), int(field), out.ctypes.data_as(C.POINTER(C.c_double)), int(n)))
+        return out
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.p3x_server_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class P3Microphysics:
     """Mirror of the ``P3Microphysics`` atmosphere process for resident device
     state: ``set_grids`` fixes (ncol, nlev), ``initialize`` creates the tables

@@ -1,0 +1,113 @@
+"""Serving loop (p3x_server_*): continuous batching under a memory budget.
+
+Each instance's result must be the same alone and in a mix: columns are
+independent and the kernels' arithmetic does not depend on batching, so the
+tolerance is exact equality.  A one-step instance must also equal a direct
+p3_main of the same inputs (the server's instance data is a column slice of
+its synthetic workload, seed 5000).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TEMPLATE_SEED = 5000
+TEMPLATE_COLS = 65536
+PROG = ["qc", "nc", "qr", "nr", "qi", "qm", "ni", "bm", "qv", "th"]
+
+
+def read_state(srv, iid, ncol, nlev):
+    out = {n: srv.read_field(iid, f, ncol * nlev).reshape(ncol, nlev) for f, n in enumerate(PROG)}
+    out["precip_liq_surf"] = srv.read_field(iid, -1, ncol)
+    out["precip_ice_surf"] = srv.read_field(iid, -2, ncol)
+    return out
+
+
+@pytest.fixture(scope="module")
+def server_cls(built):
+    import scream_gb300 as p3
+    return p3.P3Server
+
+
+def test_one_step_equals_direct_p3_main(gpu_ctx, server_cls):
+    import scream_gb300 as p3
+    srv = server_cls(gpu_ctx, budget_bytes=4 * 10**9, max_inflight=2)
+    try:
+        cases = [(1, 257, 128, p3.P3X_FP64, 11), (2, 1000, 72, p3.P3X_FP32_BULK, 77777)]
+        for iid, ncol, nlev, prec, seed in cases:
+            srv.submit(iid, ncol, nlev, prec, total_steps=1, seed=seed)
+        srv.drain()
+        for iid, ncol, nlev, prec, seed in cases:
+            c0 = seed % (TEMPLATE_COLS - ncol + 1)
+            inp = p3.generate_inputs(0, TEMPLATE_SEED, ncol, nlev, col0=c0)
+            f = p3.P3Fields.from_inputs(inp)
+            gpu_ctx.p3_main(f, 300.0, prec)
+            ref = f.to_host()
+            got = read_state(srv, iid, ncol, nlev)
+            for n in PROG + ["precip_liq_surf", "precip_ice_surf"]:
+                assert np.array_equal(got[n], ref[n]), n
+    finally:
+        srv.close()
+
+
+def test_result_alone_equals_result_in_mix(gpu_ctx, server_cls):
+    import scream_gb300 as p3
+    probes = [(7, 300, 72, p3.P3X_FP64, 3, 123), (8, 2000, 128, p3.P3X_FP32_BULK, 4, 456)]
+
+    def run(mix):
+        srv = server_cls(gpu_ctx, budget_bytes=6 * 10**9, max_inflight=4)
+        try:
+            rng = np.random.default_rng(3)
+            if mix:
+                for j in range(40):
+                    ncol = int(np.exp(rng.uniform(0, np.log(8192))))
+                    nlev = 72 if rng.random() < 0.5 else 128
+                    prec = p3.P3X_FP64 if rng.random() < 0.5 else p3.P3X_FP32_BULK
+                    steps = int(rng.integers(1, 4))
+                    for s in range(steps):
+                        srv.submit(1000 + j, ncol, nlev, prec, steps, seed=int(rng.integers(1 << 30)),
+                                   arrival_s=float(rng.uniform(0, 0.05)))
+            for iid, ncol, nlev, prec, steps, seed in probes:
+                for s in range(steps):
+                    srv.submit(iid, ncol, nlev, prec, steps, seed=seed, arrival_s=0.01 * s if mix else 0.0)
+            st = srv.drain()
+            return {iid: read_state(srv, iid, ncol, nlev) for iid, ncol, nlev, _, _, _ in probes}, st
+        finally:
+            srv.close()
+
+    alone, st_alone = run(False)
+    mixed, st_mix = run(True)
+    assert st_mix["completed"] > st_alone["completed"]
+    for iid in alone:
+        for n in alone[iid]:
+            assert np.array_equal(alone[iid][n], mixed[iid][n]), (iid, n)
+
+
+def test_budget_admission_and_rejection(gpu_ctx, server_cls):
+    import scream_gb300 as p3
+    from scream_gb300 import _lib as L
+    # one 8192 x 128 instance needs ~400 MB: a 600 MB budget holds one at a time
+    srv = server_cls(gpu_ctx, budget_bytes=600 * 10**6, max_inflight=4)
+    try:
+        for iid in range(3):
+            srv.submit(iid, 8192, 128, p3.P3X_FP32_BULK, total_steps=1, seed=iid)
+        st = srv.drain()
+        assert st["completed"] == 3
+        assert 0 < st["peak_bytes"] <= 600 * 10**6
+        with pytest.raises(L.P3Error):
+            srv.submit(99, 65536, 128, p3.P3X_FP64, total_steps=1, seed=1)
+    finally:
+        srv.close()
+
+
+def test_poisson_load_reports_latency(gpu_ctx, server_cls):
+    srv = server_cls(gpu_ctx, budget_bytes=20 * 10**9, max_inflight=4)
+    try:
+        st = srv.run_poisson(rate_hz=100.0, n_sessions=30, max_ncol=4096, seed=9)
+        assert st["completed"] >= 30
+        assert st["rejected"] == 0
+        assert 0 < st["p50_ms"] <= st["p90_ms"] <= st["p99_ms"] <= st["max_ms"]
+        assert st["column_levels_per_s"] > 0
+        assert st["peak_bytes"] <= 20 * 10**9
+    finally:
+        srv.close()
