@@ -11,8 +11,17 @@ needed between steps.
   e2e         the same step through the public API with pinned HOST buffers:
               every step copies the 23 input fields host->device and the
               20 per-level outputs + 2 interface fluxes + 2 surface fields back
-  roofline    HBM roofline of the column kernel at 360 algorithmic bytes per
-              column-level (23 FP64 inputs read, 22 FP64 outputs written)
+  roofline    HBM roofline of the P3 step (three kernels: part1+part2,
+              sedimentation, part3) at 360 algorithmic bytes per column-level
+              (23 FP64 inputs read, 22 FP64 outputs written), with each
+              kernel's share of the step measured live with CUDA events
+  batched     the batched form: 256 instances (ncol log-uniform [1,16384],
+              nlev 72/128, dt 300/120 s) in one persistent launch sequence
+              replayed from a captured CUDA graph, launch configuration picked
+              by the autotuner, FP64 and FP32-bulk
+  serving     the request loop: Poisson sessions (ncol log-uniform
+              [1,65536], nlev 72/128, FP64/FP32-bulk 50/50, 1-20 steps) at
+              80% of the capacity measured in the same run, 120 GB budget
   cpu_baseline  the CPU oracle (a C++/OpenMP restatement of the reference
               p3_main) on a bounded sample, all host cores
 
@@ -123,7 +132,9 @@ class ClockSampler:
 
 
 def cpu_baseline(seconds_target=15.0, nlev=NLEV):
-    """CPU oracle on a bounded sample of the same workload (all host cores)."""
+    """CPU oracle on a bounded sample of the same workload (all host cores):
+    runs of 10 steps with state carried, each run restarting from the initial
+    state (as the GPU runs do), until the time budget is spent."""
     import numpy as np
     from scream_gb300 import _lib as L
     from scream_gb300.p3 import generate_inputs
@@ -132,19 +143,27 @@ def cpu_baseline(seconds_target=15.0, nlev=NLEV):
     cores = os.cpu_count() or 1
     ncol = max(256, 64 * cores)
     inp = generate_inputs(1, SEED, ncol, nlev)
-    st = {k: np.array(v, copy=True) for k, v in inp.items()}
-    st.update(O.empty_outputs(ncol, nlev))
-    O.p3_main(st, tab, DT, nthreads=cores)  # warm-up step
-    total_us, steps = 0.0, 0
+
+    def fresh():
+        st = {k: np.array(v, copy=True) for k, v in inp.items()}
+        st.update(O.empty_outputs(ncol, nlev))
+        return st
+
+    O.p3_main(fresh(), tab, DT, nthreads=cores)  # warm-up step
+    total_us, steps, runs = 0.0, 0, 0
     t_end = time.time() + seconds_target
-    while time.time() < t_end or steps < 2:
-        err, us = O.p3_main(st, tab, DT, it=steps + 2, nthreads=cores)
-        total_us += us
-        steps += 1
+    while time.time() < t_end or runs < 1:
+        st = fresh()
+        for s in range(10):
+            err, us = O.p3_main(st, tab, DT, it=s + 1, nthreads=cores)
+            total_us += us
+            steps += 1
+        runs += 1
     value = ncol * nlev * steps / (total_us * 1e-6)
     return {"value": value, "unit": "column-levels/s", "cores": cores, "kind": "port",
             "sample": f"{ncol} columns x {nlev} levels (RH-stress workload, config-2 distributions), "
-                      f"{steps} steps, oracle p3_main with OpenMP over columns"}
+                      f"{runs} runs of 10 steps from the initial state, oracle p3_main (C++ restatement of "
+                      f"the reference) with OpenMP over columns on {cores} threads"}
 
 
 def run_reference(args):
@@ -162,6 +181,71 @@ def run_reference(args):
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def run_batched(ctx, args):
+    """Batched form: 256 instances in one persistent launch sequence under a
+    captured CUDA graph, launch configuration from the autotuner; FP64 and
+    FP32-bulk."""
+    import numpy as np
+    import torch
+    import scream_gb300 as p3
+
+    rng = np.random.default_rng(4000)
+    n = args.batch_instances
+    ncols = np.floor(np.exp(rng.uniform(0, np.log(16385), n))).astype(int).clip(1, 16384)
+    nlevs = np.where(rng.random(n) < 0.5, 72, 128)
+    dts = np.where(rng.random(n) < 0.5, 300.0, 120.0)
+    inputs = [p3.generate_inputs(0, 4000 + j, int(ncols[j]), int(nlevs[j])) for j in range(n)]
+    cl = float(np.sum(ncols * nlevs))
+    out = {"instances": n, "columns": int(ncols.sum()), "column_levels_per_step": cl}
+    stream = torch.cuda.Stream()
+    for prec, tag in ((p3.P3X_FP64, "fp64"), (p3.P3X_FP32_BULK, "fp32_bulk")):
+        fields = [p3.P3Fields.from_inputs(x) for x in inputs]
+        batch = p3.P3Batch(ctx, fields, dts, prec)
+        with torch.cuda.stream(stream):
+            best, ms_best = batch.autotune(reps=1, stream=stream)  # keeps the fastest configuration
+            batch.capture_graph(stream)
+            for _ in range(args.warmup):
+                batch.run(stream)
+            stream.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            steps = max(3, args.steps // 2)
+            e0.record(stream)
+            for _ in range(steps):
+                batch.run(stream)
+            e1.record(stream)
+            e1.synchronize()
+        ctx.check()
+        ms = e0.elapsed_time(e1) / steps
+        out[tag] = {"value": cl / (ms * 1e-3), "unit": "column-levels/s", "ms_per_step": ms,
+                    "graph": True, "autotuned": best, "autotune_best_ms": ms_best}
+        batch.close()
+        del fields
+        torch.cuda.empty_cache()
+    out["fp32_bulk_speedup"] = out["fp32_bulk"]["value"] / out["fp64"]["value"]
+    return out
+
+
+def run_serving(ctx, args):
+    """Request loop at 80% of the capacity measured here: capacity = sessions
+    per second completed when every session arrives at once."""
+    import scream_gb300 as p3
+
+    srv = p3.P3Server(ctx, budget_bytes=120 * 10**9, max_inflight=4)
+    try:
+        sat = srv.run_poisson(rate_hz=1e6, n_sessions=args.serve_sessions, max_ncol=65536, seed=41)
+        cap_hz = args.serve_sessions / sat["wall_s"]
+        rate = args.serve_load * cap_hz
+        st = srv.run_poisson(rate_hz=rate, n_sessions=args.serve_sessions, max_ncol=65536, seed=42)
+    finally:
+        srv.close()
+    return {"load": args.serve_load, "capacity_sessions_per_s": cap_hz, "rate_sessions_per_s": rate,
+            "capacity_column_levels_per_s": sat["column_levels_per_s"], "budget_bytes": 120 * 10**9,
+            "max_inflight": 4, **{k: st[k] for k in ("completed", "rejected", "p50_ms", "p90_ms", "p99_ms",
+                                                      "max_ms", "mean_ms", "wall_s", "column_levels_per_s",
+                                                      "peak_bytes", "peak_inflight")},
+            "p99_over_p50": st["p99_ms"] / st["p50_ms"] if st["p50_ms"] > 0 else None}
 
 
 def run_gpu(args):
@@ -187,6 +271,8 @@ def run_gpu(args):
         torch.cuda.synchronize()
 
     def timed_device(precision, steps, warmup):
+        """K timed steps (events on the launching stream), then two untimed
+        steps with per-kernel events for the kernel shares."""
         f = p3.P3Fields.from_inputs(inputs)
         for s in range(warmup):
             ctx.p3_main(f, DT, precision, it=s + 1, sync=False)
@@ -202,15 +288,22 @@ def run_gpu(args):
         wall = time.perf_counter() - t0
         ctx.check()
         kms = [a.elapsed_time(b) for a, b in ev]
+        ctx.set_kernel_timing(True)
+        parts = []
+        for s in range(2):
+            ctx.p3_main(f, DT, precision, it=warmup + steps + s + 1, sync=False)
+            parts.append(ctx.kernel_times())
+        ctx.set_kernel_timing(False)
+        ctx.check()
         del f
         torch.cuda.empty_cache()
-        return wall, kms
+        return wall, kms, [sum(p[i] for p in parts) / len(parts) for i in range(3)]
 
     # FP64 plain form (reported beside the headline)
-    wall64, k64 = timed_device(L.P3X_FP64, args.steps, args.warmup)
+    wall64, k64, parts64 = timed_device(L.P3X_FP64, args.steps, args.warmup)
     # FP32-bulk headline, with clocks sampled during the timed region
     with ClockSampler(local) as clk:
-        wall32, k32 = timed_device(L.P3X_FP32_BULK, args.steps, args.warmup)
+        wall32, k32, parts32 = timed_device(L.P3X_FP32_BULK, args.steps, args.warmup)
     clocks = clk.summary()
 
     def maxr(x):
@@ -257,17 +350,28 @@ def run_gpu(args):
     del f, host_in, host_out
     torch.cuda.empty_cache()
 
+    batched = run_batched(ctx, args) if not args.no_batched else None
+    serving = run_serving(ctx, args) if not args.no_serving else None
+
     if rank != 0:
         return 0
     hbm_peak, peak_kind = _peaks()
     kmean32 = sum(k32) / len(k32) * 1e-3
     achieved = ALG_BYTES_PER_CL * cl_step / kmean32 / 1e9
     tpc = _traffic_per_cl("fp32")
+    names = ["p3_part12_kernel", "p3_sed_kernel", "p3_part3_kernel"]
+
+    def shares(parts):
+        tot = sum(parts)
+        return {n: {"ms": p, "share": p / tot} for n, p in zip(names, parts)}
+
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
             "frac": achieved / hbm_peak, "peak_source": peak_kind,
             "traffic": (tpc * cl_step if tpc is not None else None),
-            "kernel": "p3_main_kernel<float> (fused part1/part2/sedimentation/part3)",
-            "alg_bytes_per_cl": ALG_BYTES_PER_CL}
+            "kernel": "P3 step <float>: p3_part12_kernel + p3_sed_kernel + p3_part3_kernel, one launch "
+                      "sequence per step; achieved = 360 B/cl x cl / mean event-timed step",
+            "alg_bytes_per_cl": ALG_BYTES_PER_CL,
+            "kernels": shares(parts32)}
     kmean64 = sum(k64) / len(k64) * 1e-3
     cb = cpu_baseline(seconds_target=args.cpu_seconds) if not args.no_cpu else None
     line = {
@@ -281,12 +385,14 @@ def run_gpu(args):
         "fp64": {"value": value64, "unit": "column-levels/s", "ms_per_step": wall64 / args.steps * 1e3,
                  "kernel_ms": kmean64 * 1e3,
                  "hbm_gbs_alg": ALG_BYTES_PER_CL * cl_step / kmean64 / 1e9,
-                 "fp32_bulk_speedup": value / value64},
+                 "fp32_bulk_speedup": value / value64, "kernels": shares(parts64)},
         "roofline": roof,
         "e2e": {"value": e2e_value, "unit": "column-levels/s", "h2d_bytes_per_step": h2d_bytes,
                 "d2h_bytes_per_step": d2h_bytes, "steps": e2e_steps,
                 "path": "pinned host tensors -> P3Context.p3_main (libp3x C ABI) -> pinned host"},
-        "gpu_launches": args.steps,
+        "gpu_launches": 3 * args.steps,
+        "batched": batched,
+        "serving": serving,
         "clocks": clocks,
         "cpu_baseline": cb,
     }
@@ -306,6 +412,11 @@ def main():
     ap.add_argument("--ncol", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--batch-instances", type=int, default=256)
+    ap.add_argument("--serve-sessions", type=int, default=120)
+    ap.add_argument("--serve-load", type=float, default=0.8)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

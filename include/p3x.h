@@ -180,13 +180,24 @@ int p3x_main(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_state
              const p3x_infrastructure* infra, const p3x_history_only* hist, int32_t nj, int32_t nk,
              const p3x_layout* layout, int32_t precision, void* stream, double* elapsed_us);
 
-/* Same, stream-ordered and asynchronous: no host synchronisation, no
- * allocation.  Device-side error bits accumulate in the context; read them
- * with p3x_context_check. */
+/* Same, stream-ordered and asynchronous: no host synchronisation.  The
+ * per-step hand-over scratch between the three kernels (40 B per
+ * column-level + 4 B per column) is taken from and returned to the
+ * context's stream-ordered memory pool on `stream`, so concurrent calls on
+ * different streams do not share scratch.  Device-side error bits accumulate
+ * in the context; read them with p3x_context_check. */
 int p3x_main_async(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_state* prog,
                    const p3x_diagnostic_inputs* din, const p3x_diagnostic_outputs* dout,
                    const p3x_infrastructure* infra, const p3x_history_only* hist, int32_t nj,
                    int32_t nk, const p3x_layout* layout, int32_t precision, void* stream);
+
+/* Per-kernel timing of single-instance steps (no counterpart in the
+ * reference, which times p3_main as a whole): while on, every p3x_main /
+ * p3x_main_async records CUDA events around its three kernels (part1+part2,
+ * sedimentation, part3); p3x_kernel_times waits for the latest such step and
+ * returns the three durations in ms. */
+int p3x_set_kernel_timing(p3x_context* ctx, int32_t on);
+int p3x_kernel_times(p3x_context* ctx, float* ms3);
 
 /* Synchronises `stream`, returns and clears the accumulated device status. */
 int p3x_context_check(p3x_context* ctx, void* stream);

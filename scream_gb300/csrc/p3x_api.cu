@@ -33,6 +33,9 @@ struct p3x_context {
   /* stream-ordered pool of the per-call K1->K2/K3 scratch (memory is kept
    * for reuse; released with the context) */
   cudaMemPool_t pool = nullptr;
+  /* optional per-kernel timing of single-instance steps */
+  int ktime = 0;
+  cudaEvent_t kev[4] = {nullptr, nullptr, nullptr, nullptr};
   p3x_launch_config cfg[2];
   /* scratch of the Fortran-layout entry (grown on demand) */
   std::vector<double*> fbuf;
@@ -251,7 +254,8 @@ void bind_scratch(dev::Inst& in, unsigned char* base) {
 int launch_kernels(p3x_context* ctx, const p3x_runtime* rt, const dev::Inst& in, cudaStream_t st) {
   const dev::RuntimeDev rtd = make_runtime(*rt);
   const int stride = sm_stride_for(in.nlev);
-  const LaunchSpec ls = fit_spec(in.precision, spec_of(ctx->cfg[in.precision]), stride);
+  LaunchSpec ls = fit_spec(in.precision, spec_of(ctx->cfg[in.precision]), stride);
+  if (ctx->ktime) ls.marks = ctx->kev;
   if (!spec_fits(in.precision, ls, stride)) return P3X_EINVAL;
   cudaError_t e;
   if (in.precision == P3X_FP32_BULK) {
@@ -465,6 +469,8 @@ int p3x_context_destroy(p3x_context* ctx) {
     cudaDeviceSynchronize();
     cudaMemPoolDestroy(ctx->pool);
   }
+  for (cudaEvent_t e : ctx->kev)
+    if (e) cudaEventDestroy(e);
   delete ctx;
   return P3X_OK;
 }
@@ -507,6 +513,21 @@ int p3x_main_async(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic
                            infra->prescribedCCN, precision, in);
   if (st) return st;
   return launch_single(ctx, rt, in, static_cast<cudaStream_t>(stream));
+}
+
+int p3x_set_kernel_timing(p3x_context* ctx, int32_t on) {
+  if (!ctx) return P3X_EINVAL;
+  if (on && !ctx->kev[0])
+    for (cudaEvent_t& e : ctx->kev) P3X_CUDA(cudaEventCreate(&e));
+  ctx->ktime = on ? 1 : 0;
+  return P3X_OK;
+}
+
+int p3x_kernel_times(p3x_context* ctx, float* ms3) {
+  if (!ctx || !ms3 || !ctx->kev[0]) return P3X_EINVAL;
+  P3X_CUDA(cudaEventSynchronize(ctx->kev[3]));
+  for (int i = 0; i < 3; ++i) P3X_CUDA(cudaEventElapsedTime(&ms3[i], ctx->kev[i], ctx->kev[i + 1]));
+  return P3X_OK;
 }
 
 int p3x_context_check(p3x_context* ctx, void* stream) {
@@ -833,8 +854,11 @@ int p3x_batch_destroy(p3x_batch* b) {
   return P3X_OK;
 }
 
-/* Times every candidate configuration on the batch (each run advances the
- * batch's instances by one step) and keeps the fastest. */
+/* Times every candidate configuration on the batch and keeps the fastest.
+ * The sweep covers threads per column (8, 16, 32 lanes, i.e. nlev/8 .. nlev/32
+ * levels per thread), columns per CTA and staging of the ice / Table3 tables
+ * into shared memory.  Each timed run advances the batch's instances by one
+ * step. */
 int p3x_autotune_batch(p3x_batch* b, void* stream, int32_t reps, p3x_launch_config* best, double* ms_best) {
   if (!b || reps <= 0) return P3X_EINVAL;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -842,7 +866,7 @@ int p3x_autotune_batch(p3x_batch* b, void* stream, int32_t reps, p3x_launch_conf
   const int lanes_c[] = {8, 16, 32};
   const int groups_c[] = {2, 4, 8};
   const int staged_c[] = {0, 1};
-  const int bps_c[] = {0, 1};
+  const int bps_c[] = {0};
   p3x_launch_config best_cfg{32, 8, 1, 0};
   double best_ms = 1e300;
   cudaEvent_t e0, e1;

@@ -34,13 +34,19 @@ cudaError_t launch_p3_lanes(const dev::Inst& inst0, const dev::KParams<TR>& kp_i
   kp.staged = ls.staged;
   const int threads = ls.groups_per_block * LANES;
   if (threads <= 0 || threads > 256) return cudaErrorInvalidValue;
+  if (ls.marks) cudaEventRecord(ls.marks[0], stream);
   cudaError_t e = launch_persistent<TR>(dev::p3_part12_kernel<TR, LANES>, inst0, kp, threads,
                                         p3_smem_bytes<TR>(ls, kp.sm_stride), ls.blocks_per_sm, num_sms, stream);
   if (e != cudaSuccess) return e;
+  if (ls.marks) cudaEventRecord(ls.marks[1], stream);
   e = launch_persistent<TR>(dev::p3_sed_kernel<TR, LANES>, inst0, kp, threads, sed_smem_bytes(ls, kp.sm_stride),
                             0, num_sms, stream);
   if (e != cudaSuccess) return e;
-  return launch_persistent<TR>(dev::p3_part3_kernel<TR, LANES>, inst0, kp, threads, 0, 0, num_sms, stream);
+  if (ls.marks) cudaEventRecord(ls.marks[2], stream);
+  e = launch_persistent<TR>(dev::p3_part3_kernel<TR, LANES>, inst0, kp, threads, 0, 0, num_sms, stream);
+  if (e != cudaSuccess) return e;
+  if (ls.marks) cudaEventRecord(ls.marks[3], stream);
+  return cudaSuccess;
 }
 
 }  // namespace p3x

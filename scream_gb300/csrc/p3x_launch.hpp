@@ -16,6 +16,7 @@ struct LaunchSpec {
   int groups_per_block; /* columns per CTA */
   int staged;           /* tables in shared memory */
   int blocks_per_sm;    /* 0: as many as fit */
+  cudaEvent_t* marks = nullptr; /* optional: 4 events recorded around K1, K2, K3 */
 };
 
 /* Shared-memory bytes of one CTA of K1 (part1+part2; staged tables plus the

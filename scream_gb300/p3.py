@@ -166,6 +166,16 @@ class P3Context:
         L.check("p3x_main_async", rc)
         return 0.0
 
+    def set_kernel_timing(self, on: bool = True):
+        L.check("p3x_set_kernel_timing", self.lib.p3x_set_kernel_timing(self.h, int(bool(on))))
+
+    def kernel_times(self):
+        """(part1+part2, sedimentation, part3) durations in ms of the latest
+        timed step."""
+        ms = (C.c_float * 3)()
+        L.check("p3x_kernel_times", self.lib.p3x_kernel_times(self.h, ms))
+        return [float(x) for x in ms]
+
     def check(self, stream=None):
         L.check("p3x_context_check", self.lib.p3x_context_check(self.h, _stream_handle(stream)))
 
