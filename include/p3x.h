@@ -191,6 +191,27 @@ int p3x_main_async(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic
                    const p3x_infrastructure* infra, const p3x_history_only* hist, int32_t nj,
                    int32_t nk, const p3x_layout* layout, int32_t precision, void* stream);
 
+/* Same step as p3x_main_async, but the hand-over scratch between its three
+ * kernels comes from one 64 MiB array of static device storage instead of
+ * the context's memory pool, so the call allocates no device memory: for
+ * hosts that reserve the device's memory for themselves at start-up and
+ * cannot let a library allocate during their time loop.  No counterpart in
+ * the reference.
+ *   - Limit: 40 * ncol * ld + 4 * ncol bytes (rounded up to 256) must fit in
+ *     64 MiB, e.g. 13,000 columns of 128 levels; larger calls return
+ *     P3X_ENOMEM and launch nothing.
+ *   - The array is one per device and shared by every context: calls that
+ *     overlap on the device (different streams or host threads) race on it
+ *     and must be serialised by the caller.
+ *   - The first call on each device looks the array's address up
+ *     (cudaGetSymbolAddress, once per device with that device current); make
+ *     that first call before any stream capture begins.
+ *   - Nothing in the array has to be zeroed. */
+int p3x_main_fixed_scratch(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_state* prog,
+                           const p3x_diagnostic_inputs* din, const p3x_diagnostic_outputs* dout,
+                           const p3x_infrastructure* infra, const p3x_history_only* hist, int32_t nj,
+                           int32_t nk, const p3x_layout* layout, int32_t precision, void* stream);
+
 /* Per-kernel timing of single-instance steps (no counterpart in the
  * reference, which times p3_main as a whole): while on, every p3x_main /
  * p3x_main_async records CUDA events around its three kernels (part1+part2,

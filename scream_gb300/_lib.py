@@ -130,6 +130,10 @@ PROTOTYPES = {
                                  C.POINTER(DiagnosticInputs), C.POINTER(DiagnosticOutputs),
                                  C.POINTER(Infrastructure), C.POINTER(HistoryOnly), _I, _I,
                                  C.POINTER(Layout), _I, _V]),
+    "p3x_main_fixed_scratch": (C.c_int, [_V, C.POINTER(Runtime), C.POINTER(PrognosticState),
+                                 C.POINTER(DiagnosticInputs), C.POINTER(DiagnosticOutputs),
+                                 C.POINTER(Infrastructure), C.POINTER(HistoryOnly), _I, _I,
+                                 C.POINTER(Layout), _I, _V]),
     "p3x_context_check": (C.c_int, [_V, _V]),
     "p3x_set_launch_config": (C.c_int, [_V, _I, C.POINTER(LaunchConfig)]),
     "p3x_get_launch_config": (C.c_int, [_V, _I, C.POINTER(LaunchConfig)]),

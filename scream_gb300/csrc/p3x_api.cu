@@ -910,3 +910,60 @@ int p3x_autotune_batch(p3x_batch* b, void* stream, int32_t reps, p3x_launch_conf
 }
 
 }  // extern "C"
+
+/* ------------------------------------------------------------------ */
+/* P3 step with a fixed, pre-reserved hand-over scratch               */
+/* ------------------------------------------------------------------ */
+/* Some hosts cannot let a library take device memory while their time loop
+ * runs: a model that reserves nearly all of HBM for its own pool at
+ * start-up, or one that must keep a fixed, audited device footprint for a
+ * whole simulation, has no memory to give and no way to account for a pool
+ * that grows behind its back.  For them the three kernels' hand-over scratch
+ * (40 bytes per column-level plus 4 bytes per column) lives in one array of
+ * static device storage, reserved when the library's module is loaded.
+ * Nothing in the array needs to start at zero: part1+part2 writes every
+ * column's continue flag, and the hand-over values of every column that
+ * goes on, before sedimentation and part3 read them. */
+static __device__ __align__(256) unsigned char g_step_scratch[p3x::kFixedScratchBytes];
+
+namespace p3x {
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_step_scratch_mu;
+void* g_step_scratch_ptr[kMaxDevices] = {};
+
+/* Address of the array on the current device, looked up once per device. */
+int step_scratch_address(void** out) {
+  int dev = 0;
+  P3X_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return P3X_EINVAL;
+  std::lock_guard<std::mutex> lk(g_step_scratch_mu);
+  if (!g_step_scratch_ptr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_step_scratch);
+    if (e != cudaSuccess) return cuda_status(e);
+    g_step_scratch_ptr[dev] = p;
+  }
+  *out = g_step_scratch_ptr[dev];
+  return P3X_OK;
+}
+}  // namespace
+}  // namespace p3x
+
+extern "C" int p3x_main_fixed_scratch(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_state* prog,
+                                      const p3x_diagnostic_inputs* din, const p3x_diagnostic_outputs* dout,
+                                      const p3x_infrastructure* infra, const p3x_history_only* hist, int32_t nj,
+                                      int32_t nk, const p3x_layout* layout, int32_t precision, void* stream) {
+  if (!ctx || !rt || !infra || !valid_runtime(*rt)) return P3X_EINVAL;
+  dev::Inst in;
+  const int st = fill_inst(prog, din, dout, hist, layout, nj, nk, infra->dt, infra->predictNc,
+                           infra->prescribedCCN, precision, in);
+  if (st) return st;
+  if (in.ncol == 0) return P3X_OK;
+  if (dev::scratch_bytes(in.ncol, in.ld) > kFixedScratchBytes) return P3X_ENOMEM;
+  void* scr = nullptr;
+  const int rc = step_scratch_address(&scr);
+  if (rc) return rc;
+  bind_scratch(in, static_cast<unsigned char*>(scr));
+  return launch_kernels(ctx, rt, in, static_cast<cudaStream_t>(stream));
+}

@@ -35,6 +35,9 @@ constexpr double kSvpT0 = 150.0, kSvpInvH = 64.0;
 constexpr int kSvpIntervals = 12800;
 void build_svp_table(std::vector<double>& coef);
 
+/* Size of the static hand-over scratch of p3x_main_fixed_scratch. */
+constexpr size_t kFixedScratchBytes = size_t(64) << 20;
+
 /* Synthetic workload, p3x_workload.cpp */
 int workload_generate(int kind, uint64_t seed, int col0, int ncol, int nlev, double* const* fields,
                       int64_t ld);
