@@ -55,6 +55,29 @@ def _dist():
     return ws, rank, local
 
 
+def rank_seed(rank):
+    """Workload seed of a rank: each rank steps its own columns (weak scaling)."""
+    return SEED + 7919 * rank
+
+
+def reduce_max(x):
+    """Maximum of a host float over all ranks (the slowest rank sets the
+    job's time); identity without a process group."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def weak_value(world_size, cl_per_rank_step, steps, wall_max):
+    """Whole-job column-levels/s: every rank's work over the slowest rank's time."""
+    return world_size * cl_per_rank_step * steps / wall_max
+
+
 def _peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -261,7 +284,7 @@ def run_gpu(args):
         dist.init_process_group("nccl")
     ncol = args.ncol or NCOL
     ctx = p3.P3Context()
-    inputs = p3.generate_inputs(1, SEED + 7919 * rank, ncol, NLEV)
+    inputs = p3.generate_inputs(1, rank_seed(rank), ncol, NLEV)
     stream = torch.cuda.current_stream()
 
     def barrier():
@@ -306,19 +329,12 @@ def run_gpu(args):
         wall32, k32, parts32 = timed_device(L.P3X_FP32_BULK, args.steps, args.warmup)
     clocks = clk.summary()
 
-    def maxr(x):
-        if ws > 1:
-            import torch.distributed as dist
-            t = torch.tensor([x], dtype=torch.float64, device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            return float(t.item())
-        return x
-
+    maxr = reduce_max
     wall32 = maxr(wall32)
     wall64 = maxr(wall64)
     cl_step = ncol * NLEV
-    value = ws * cl_step * args.steps / wall32
-    value64 = ws * cl_step * args.steps / wall64
+    value = weak_value(ws, cl_step, args.steps, wall32)
+    value64 = weak_value(ws, cl_step, args.steps, wall64)
 
     # e2e: pinned host buffers through the public API
     h2d_fields = L.INPUT_FIELDS
@@ -346,7 +362,7 @@ def run_gpu(args):
     barrier()
     e2e_wall = maxr(time.perf_counter() - t0)
     ctx.check()
-    e2e_value = ws * cl_step * e2e_steps / e2e_wall
+    e2e_value = weak_value(ws, cl_step, e2e_steps, e2e_wall)
     del f, host_in, host_out
     torch.cuda.empty_cache()
 
