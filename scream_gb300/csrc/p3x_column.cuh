@@ -21,7 +21,7 @@
  * Splitting lets each kernel keep its own register and shared-memory
  * footprint: part2's ~45 rates no longer limit the occupancy of the
  * latency-bound sedimentation walk.  Per-level temporaries of a phase live
- * in shared memory (10 FP64 arrays per column in K1, 11 in K2).  Lookup
+ * in shared memory (8 FP64 arrays per column in K1, 11 in K2).  Lookup
  * tables are read from global memory (L1/L2) or, in K1, staged into shared
  * memory once per CTA with cp.async.bulk + mbarrier (Table3 slices for the
  * runtime's constant rain shape parameter, plus the whole ice table).
@@ -83,7 +83,7 @@ constexpr long long kWaitSpinLimit = 1ll << 26;
 constexpr uint64_t kWaitNanosLimit = 2000000000ull; /* 2 s */
 
 /* shared arrays of one column group in K1 */
-enum { A_TATM = 0, A_RHO, A_INVRHO, A_RHOFACR, A_RHOFACI, A_ACN, A_INVDZ, A_QVSL, A_QVSI, A_QVSSI, A_NARR };
+enum { A_TATM = 0, A_RHO, A_RHOFACR, A_RHOFACI, A_ACN, A_QVSL, A_QVSI, A_QVSSI, A_NARR };
 /* shared arrays of one column group in K2; FAC is the fall-speed factor of
  * the species being sedimented (acn, rhofacr or rhofaci), the rain flux
  * accumulator re-uses R2 (rain has two fields) */
@@ -211,6 +211,7 @@ __device__ __forceinline__ void apply_n_adjust(double& n_d, TR n_in, TR n_out) {
 template <class TR, int LANES>
 __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, const Tabs<TR>& tb,
                           double* __restrict__ sm, const double esat0, uint32_t& err) {
+  constexpr bool kF64 = sizeof(TR) == sizeof(double);
   const RuntimeDev& rt = kp.rt;
   const unsigned mask = group_mask<LANES>();
   const int lane = threadIdx.x & (LANES - 1);
@@ -251,17 +252,30 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
     in.vap_liq_exchange[o] = 0;
     in.vap_ice_exchange[o] = 0;
 
-    const double inv_cld_l = 1 / cld_l;
+    double rho, inv_rho, qvsl, qvsi, qvssi, ccn_nc;
     const double exner = 1 / inv_exner;
     double T = th * exner;
     qv = vmax(qv, 0.);
-    const double inv_dz = 1 / dz;
-
-    const double rho = dpres / dz / C::gravit;
-    const double inv_rho = 1 / rho;
-    const double qvsl = qv_sat_dry<TR>(T, pres, false, rt, err);
-    const double qvsi = qv_sat_dry<TR>(T, pres, true, rt, err);
-    const double qvssi = qv / qvsi - 1;
+    if constexpr (kF64) {
+      const double inv_cld_l = 1 / cld_l;
+      rho = dpres / dz / C::gravit;
+      inv_rho = 1 / rho;
+      qvsl = qv_sat_dry<TR>(T, pres, false, rt, err);
+      qvsi = qv_sat_dry<TR>(T, pres, true, rt, err);
+      qvssi = qv / qvsi - 1;
+      ccn_nc = rt.spa_ccn_to_nc_factor * in.nccn[o] / inv_cld_l;
+    } else {
+      /* FP32-bulk: the same quantities with one FP64 division each for rho
+       * and for the pressure shared by both saturation ratios; 1/rho and the
+       * supersaturation ratio (threshold and rate inputs) in FP32 */
+      rho = dpres / (dz * C::gravit);
+      inv_rho = double(1.0f / float(rho));
+      const double inv_p = 1 / vmax(pres, 1.e-3);
+      qvsl = C::ep_2 * svp_tabulated(rt.svp_tab, T, false, err) * inv_p;
+      qvsi = C::ep_2 * svp_tabulated(rt.svp_tab, T, true, err) * inv_p;
+      qvssi = double(float(qv) / float(qvsi) - 1.0f);
+      ccn_nc = rt.spa_ccn_to_nc_factor * in.nccn[o] * cld_l;
+    }
     const TR rhofacr = m_pow(TR(C::RHO_1000MB) * TR(inv_rho), TR(.54));
     const TR rhofaci = m_pow(TR(C::RHO_600MB) * TR(inv_rho), TR(.54));
     const TR dum = TR(1.496e-6) * m_pow(TR(T), TR(1.5)) / (TR(T) + TR(120));
@@ -276,7 +290,7 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
     } else {
       hydro = true;
       if (prescribedCCN) {
-        nc = vmax(nc, rt.spa_ccn_to_nc_factor * in.nccn[o] / inv_cld_l);
+        nc = vmax(nc, ccn_nc);
       } else if (predictNc) {
         nc = vmax(nc + in.nc_nuceat_tend[o] * dt, 0.0);
       } else {
@@ -310,11 +324,9 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
     in.qv[o] = qv; in.th[o] = th;
     SMA(A_TATM, k) = T;
     SMA(A_RHO, k) = rho;
-    SMA(A_INVRHO, k) = inv_rho;
     SMA(A_RHOFACR, k) = double(rhofacr);
     SMA(A_RHOFACI, k) = double(rhofaci);
     SMA(A_ACN, k) = double(acn);
-    SMA(A_INVDZ, k) = inv_dz;
     SMA(A_QVSL, k) = qvsl;
     SMA(A_QVSI, k) = qvsi;
     SMA(A_QVSSI, k) = qvssi;
@@ -349,12 +361,20 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
     const double cld_i = in.cld_frac_i[o], cld_l = in.cld_frac_l[o], cld_r = in.cld_frac_r[o];
     const double inv_exner = in.inv_exner[o];
     const double rho = SMA(A_RHO, k);
-    const double inv_rho = 1 / rho;
+    const double inv_rho = kF64 ? 1 / rho : double(1.0f / float(rho));
     const double qvsl = SMA(A_QVSL, k), qvsi = SMA(A_QVSI, k);
     const double rhofaci = SMA(A_RHOFACI, k);
     const double acn = SMA(A_ACN, k);
+    /* In-cloud values.  FP32-bulk: reciprocal cloud fractions in FP32 (the
+     * in-cloud values only feed rates) and the FP64 state is rewritten below
+     * only where a DSD or rime limiter changed an in-cloud value. */
     Incld inc;
-    calc_incloud(s.qc, s.qr, s.qi, s.qm, s.nc, s.nr, s.ni, s.bm, 1 / cld_l, 1 / cld_i, 1 / cld_r, inc);
+    if constexpr (kF64) {
+      calc_incloud(s.qc, s.qr, s.qi, s.qm, s.nc, s.nr, s.ni, s.bm, 1 / cld_l, 1 / cld_i, 1 / cld_r, inc);
+    } else {
+      calc_incloud(s.qc, s.qr, s.qi, s.qm, s.nc, s.nr, s.ni, s.bm, double(1.0f / float(cld_l)),
+                   double(1.0f / float(cld_i)), double(1.0f / float(cld_r)), inc);
+    }
 
     Rates<TR> r;
     r.zero();
@@ -377,8 +397,8 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
         TR n_out = n_in;
         get_cloud_dsd2<TR>(TR(inc.qc), n_out, mu_c, rho_r, lamc);
         apply_n_adjust(inc.nc, n_in, n_out);
+        if (kF64 || n_out != n_in) s.nc = inc.nc * cld_l;
       }
-      s.nc = inc.nc * cld_l;
       {
         const TR n_in = TR(inc.nr);
         TR n_out = n_in;
@@ -388,15 +408,36 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
           cdistr = TR(inc.nr) / TR(rt.g_mur1);
           logn0r = m_log10(cdistr) + (mu_r + TR(1)) * m_log10(lamr);
         }
+        if (kF64 || n_out != n_in) s.nr = inc.nr * cld_r;
       }
-      s.nr = inc.nr * cld_r;
-      impose_max_total_ni(inc.ni, rt.max_total_ni, inv_rho);
+      if constexpr (kF64) {
+        impose_max_total_ni(inc.ni, rt.max_total_ni, inv_rho);
+      } else {
+        float ni_f = float(inc.ni);
+        impose_max_total_ni(ni_f, rt.max_total_ni, float(inv_rho));
+        inc.ni = ni_f;
+      }
       if (inc.qi >= C::QSMALL) {
         inc.ni = vmax(inc.ni, C::NSMALL);
         inc.nr = vmax(inc.nr, C::NSMALL);
-        const double rhop = calc_bulk_rho_rime(inc.qi, inc.qm, inc.bm, rt);
-        s.qm = inc.qm * cld_i;
-        s.bm = inc.bm * cld_i;
+        double rhop;
+        if constexpr (kF64) {
+          rhop = calc_bulk_rho_rime(inc.qi, inc.qm, inc.bm, rt);
+          s.qm = inc.qm * cld_i;
+          s.bm = inc.bm * cld_i;
+        } else {
+          const float qm0 = float(inc.qm), bm0 = float(inc.bm);
+          float qm_f = qm0, bm_f = bm0;
+          rhop = calc_bulk_rho_rime<float>(float(inc.qi), qm_f, bm_f, rt);
+          if (qm_f != qm0) {
+            inc.qm = qm_f;
+            s.qm = inc.qm * cld_i;
+          }
+          if (bm_f != bm0) {
+            inc.bm = bm_f;
+            s.bm = inc.bm * cld_i;
+          }
+        }
         TableIce<TR> ti;
         lookup_ice<TR>(TR(inc.qi), TR(inc.ni), TR(inc.qm), TR(rhop), ti);
         TableRain<TR> trn;
@@ -490,20 +531,33 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
     rain_self_collection<TR>(TR(rho), TR(inc.qr), TR(inc.nr), r, rt);
     back_to_cell_average<TR>(TR(cld_l), TR(cld_r), TR(cld_i), r);
 
-    Rates<double> rd = to_double(r);
-    water_conservation(s.qc, s.qr, s.qi, dt, rd);
-    number_conservation(s.nc, s.nr, s.ni, dt, rd);
-    ice_supersat_conservation(rd, cld_i, s.qv, qvsi, s.th / inv_exner, dt);
-    prevent_liq_supersaturation<TR>(pres, T, s.qv, dt, rd, rt, err);
-    update_prognostics(rd, inv_exner, predictNc, prescribedCCN, wet, dt, double(rho_qm_cloud), inv_rho, s);
+    if constexpr (sizeof(TR) == sizeof(double)) {
+      Rates<double>& rd = r;
+      water_conservation<double>(s.qc, s.qr, s.qi, dt, rd);
+      number_conservation<double>(s.nc, s.nr, s.ni, dt, rd);
+      ice_supersat_conservation(rd, cld_i, s.qv, qvsi, s.th / inv_exner, dt);
+      prevent_liq_supersaturation<TR>(pres, T, s.qv, dt, rd, rt, err);
+      update_prognostics(rd, inv_exner, predictNc, prescribedCCN, wet, dt, double(rho_qm_cloud), inv_rho, s);
+    } else {
+      /* FP32-bulk: limiters on the FP32 rates (FP64 vapour residuals), one
+       * FP64 application of each prognostic's FP32 tendency */
+      const float dtf = float(dt);
+      const int wlim = water_conservation<float>(float(s.qc), float(s.qr), float(s.qi), dtf, r);
+      const int nlim = number_conservation<float>(float(s.nc), float(s.nr), float(s.ni), dtf, r);
+      const Rates<float> r_lim = r;
+      ice_supersat_conservation_bulk(r, cld_i, s.qv, qvsi, T, dt);
+      prevent_liq_supersaturation_bulk(pres, T, s.qv, dt, r, rt, err);
+      update_prognostics_bulk(r, inv_exner, predictNc, prescribedCCN, wet, dt, rho_qm_cloud, inv_rho, wlim, nlim,
+                              r_lim, s);
+    }
 
-    in.qv2qi_depos_tend[o] = rd.qv2qi_vapdep_tend - rd.qi2qv_sublim_tend + rd.qv2qi_nucleat_tend;
-    in.precip_total_tend[o] = rd.qc2qr_accret_tend + rd.qc2qr_autoconv_tend + rd.qc2qr_ice_shed_tend + rd.qc2qi_collect_tend;
-    in.nevapr[o] = rd.qi2qv_sublim_tend + rd.qr2qv_evap_tend;
-    in.vap_ice_exchange[o] = rd.qv2qi_vapdep_tend - rd.qi2qv_sublim_tend + rd.qv2qi_nucleat_tend;
-    in.vap_liq_exchange[o] = -rd.qr2qv_evap_tend;
-    in.liq_ice_exchange[o] = rd.qc2qi_hetero_freeze_tend + rd.qr2qi_immers_freeze_tend - rd.qi2qr_melt_tend +
-                             rd.qc2qi_berg_tend + rd.qc2qi_collect_tend + rd.qr2qi_collect_tend;
+    in.qv2qi_depos_tend[o] = double(r.qv2qi_vapdep_tend - r.qi2qv_sublim_tend + r.qv2qi_nucleat_tend);
+    in.precip_total_tend[o] = double(r.qc2qr_accret_tend + r.qc2qr_autoconv_tend + r.qc2qr_ice_shed_tend + r.qc2qi_collect_tend);
+    in.nevapr[o] = double(r.qi2qv_sublim_tend + r.qr2qv_evap_tend);
+    in.vap_ice_exchange[o] = double(r.qv2qi_vapdep_tend - r.qi2qv_sublim_tend + r.qv2qi_nucleat_tend);
+    in.vap_liq_exchange[o] = double(-r.qr2qv_evap_tend);
+    in.liq_ice_exchange[o] = double(r.qc2qi_hetero_freeze_tend + r.qr2qi_immers_freeze_tend - r.qi2qr_melt_tend +
+                                    r.qc2qi_berg_tend + r.qc2qi_collect_tend + r.qr2qi_collect_tend);
 
     if (s.qc < C::QSMALL) {
       s.qv = s.qv + s.qc;
@@ -528,10 +582,14 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
     } else {
       hydro = true;
     }
-    {
+    if constexpr (kF64) {
       double ni_incld = s.ni / cld_i;
       impose_max_total_ni(ni_incld, rt.max_total_ni, inv_rho);
       s.ni = ni_incld * cld_i;
+    } else if (s.ni >= 1e-20) {
+      /* impose_max_total_ni as a factor applied only when it limits */
+      const float f = vmin(float(rt.max_total_ni) * float(inv_rho) * float(cld_i) / float(s.ni), 1.0f);
+      if (f < 1.0f) s.ni = s.ni * double(f);
     }
     in.qc[o] = s.qc; in.nc[o] = s.nc; in.qr[o] = s.qr; in.nr[o] = s.nr;
     in.qi[o] = s.qi; in.qm[o] = s.qm; in.ni[o] = s.ni; in.bm[o] = s.bm;
@@ -971,7 +1029,7 @@ __device__ void p3_part3(const Inst& in, const int col, const KParams<TR>& kp, c
     const double inv_exner = in.inv_exner[o];
     const double cld_l = in.cld_frac_l[o], cld_r = in.cld_frac_r[o], cld_i = in.cld_frac_i[o];
     const double rho = rho_k[k];
-    const double inv_rho = 1 / rho;
+    const double inv_rho = sizeof(TR) == sizeof(double) ? 1 / rho : double(1.0f / float(rho));
     double vap_liq = in.vap_liq_exchange[o];
     double eff_qc = in.diag_eff_radius_qc[o], eff_qr = in.diag_eff_radius_qr[o], eff_qi = in.diag_eff_radius_qi[o];
     double rho_qi = 0;
@@ -999,81 +1057,150 @@ __device__ void p3_part3(const Inst& in, const int col, const KParams<TR>& kp, c
       if (qr_ge) { s.qr = 0; s.nr = 0; }
     }
 
-    /* part3: cloud */
-    if (s.qc >= C::QSMALL) {
-      const double qc_incld = s.qc / cld_l;
-      double nc_incld = s.nc / cld_l;
-      TR mu_c, lamc;
-      const TR n_in = TR(nc_incld);
-      TR n_out = n_in;
-      get_cloud_dsd2<TR>(TR(qc_incld), n_out, mu_c, TR(rho), lamc);
-      apply_n_adjust(nc_incld, n_in, n_out);
-      s.nc = nc_incld * cld_l;
-      eff_qc = double(TR(0.5) * (mu_c + TR(3)) / lamc);
+    if constexpr (sizeof(TR) == sizeof(double)) {
+      /* part3: cloud */
+      if (s.qc >= C::QSMALL) {
+        const double qc_incld = s.qc / cld_l;
+        double nc_incld = s.nc / cld_l;
+        TR mu_c, lamc;
+        const TR n_in = TR(nc_incld);
+        TR n_out = n_in;
+        get_cloud_dsd2<TR>(TR(qc_incld), n_out, mu_c, TR(rho), lamc);
+        apply_n_adjust(nc_incld, n_in, n_out);
+        s.nc = nc_incld * cld_l;
+        eff_qc = double(TR(0.5) * (mu_c + TR(3)) / lamc);
+      } else {
+        s.qv = s.qv + s.qc;
+        s.th = s.th - inv_exner * s.qc * C::LatVap * C::INV_CP;
+        vap_liq = vap_liq - s.qc;
+        s.qc = 0;
+        s.nc = 0;
+      }
+      /* part3: rain */
+      if (s.qr >= C::QSMALL) {
+        const double qr_incld = s.qr / cld_r;
+        double nr_incld = s.nr / cld_r;
+        TR mu_r = 0, lamr;
+        const TR n_in = TR(nr_incld);
+        TR n_out = n_in;
+        get_rain_dsd2<TR>(TR(qr_incld), n_out, mu_r, lamr, rt);
+        apply_n_adjust(nr_incld, n_in, n_out);
+        s.nr = nr_incld * cld_r;
+        eff_qr = double(TR(1.5) / lamr);
+      } else {
+        s.qv = s.qv + s.qr;
+        s.th = s.th - inv_exner * s.qr * C::LatVap * C::INV_CP;
+        vap_liq = vap_liq - s.qr;
+        s.qr = 0;
+        s.nr = 0;
+      }
+      /* part3: ice */
+      {
+        const bool qi_gt_small = s.qi >= C::QSMALL;
+        s.ni = vmax(s.ni, C::NSMALL);
+        const double qi_incld = s.qi / cld_i;
+        double ni_incld = s.ni / cld_i;
+        double qm_incld = s.qm / cld_i;
+        double bm_incld = s.bm / cld_i;
+        double rhop = 0;
+        if (qi_gt_small) {
+          rhop = calc_bulk_rho_rime(qi_incld, qm_incld, bm_incld, rt);
+          s.qm = qm_incld * cld_i;
+          s.bm = bm_incld * cld_i;
+        }
+        impose_max_total_ni(ni_incld, rt.max_total_ni, inv_rho);
+        if (qi_gt_small) {
+          TableIce<TR> ti;
+          lookup_ice<TR>(TR(qi_incld), TR(ni_incld), TR(qm_incld), TR(rhop), ti);
+          TR ta[4], te[4];
+          apply_table_ice4<TR>(tb, ti, 0, ta); /* columns 0, 1, 6, 7 */
+          apply_table_ice4<TR>(tb, ti, 8, te); /* columns 5, 11, 8, 10 */
+          const TR tv_eff = te[0];
+          const TR tv_lmax = ta[2];
+          const TR tv_lmin = ta[3];
+          const TR tv_dens = te[1];
+          ni_incld = vmin(ni_incld, double(tv_lmax) * ni_incld);
+          ni_incld = vmax(ni_incld, double(tv_lmin) * ni_incld);
+          eff_qi = double(tv_eff);
+          rho_qi = double(tv_dens);
+        }
+        s.ni = ni_incld * cld_i;
+        if (s.qm < C::QSMALL && qi_gt_small) {
+          s.qm = 0;
+          s.bm = 0;
+        }
+        if (!qi_gt_small) {
+          s.qv = s.qv + s.qi;
+          s.th = s.th - inv_exner * s.qi * (C::LatVap + C::LatIce) * C::INV_CP;
+          s.qi = 0; s.ni = 0; s.qm = 0; s.bm = 0;
+        }
+      }
     } else {
-      s.qv = s.qv + s.qc;
-      s.th = s.th - inv_exner * s.qc * C::LatVap * C::INV_CP;
-      vap_liq = vap_liq - s.qc;
-      s.qc = 0;
-      s.nc = 0;
-    }
-    /* part3: rain */
-    if (s.qr >= C::QSMALL) {
-      const double qr_incld = s.qr / cld_r;
-      double nr_incld = s.nr / cld_r;
-      TR mu_r = 0, lamr;
-      const TR n_in = TR(nr_incld);
-      TR n_out = n_in;
-      get_rain_dsd2<TR>(TR(qr_incld), n_out, mu_r, lamr, rt);
-      apply_n_adjust(nr_incld, n_in, n_out);
-      s.nr = nr_incld * cld_r;
-      eff_qr = double(TR(1.5) / lamr);
-    } else {
-      s.qv = s.qv + s.qr;
-      s.th = s.th - inv_exner * s.qr * C::LatVap * C::INV_CP;
-      vap_liq = vap_liq - s.qr;
-      s.qr = 0;
-      s.nr = 0;
-    }
-    /* part3: ice */
-    {
-      const bool qi_gt_small = s.qi >= C::QSMALL;
-      s.ni = vmax(s.ni, C::NSMALL);
-      const double qi_incld = s.qi / cld_i;
-      double ni_incld = s.ni / cld_i;
-      double qm_incld = s.qm / cld_i;
-      double bm_incld = s.bm / cld_i;
-      double rhop = 0;
-      if (qi_gt_small) {
-        rhop = calc_bulk_rho_rime(qi_incld, qm_incld, bm_incld, rt);
-        s.qm = qm_incld * cld_i;
-        s.bm = bm_incld * cld_i;
+      /* FP32-bulk part3: in-cloud values, DSDs and the diagnostics in FP32; the
+       * FP64 state is rewritten only where a limiter changed an in-cloud value */
+      if (s.qc >= C::QSMALL) {
+        const float icl = 1.0f / float(cld_l);
+        const float qc_f = float(s.qc) * icl;
+        const float n_in = float(s.nc) * icl;
+        float n_out = n_in, mu_c, lamc;
+        get_cloud_dsd2<float>(qc_f, n_out, mu_c, float(rho), lamc);
+        if (n_out != n_in) s.nc = double(n_out) * cld_l;
+        eff_qc = double(0.5f * (mu_c + 3.0f) / lamc);
+      } else {
+        s.qv = s.qv + s.qc;
+        s.th = s.th - inv_exner * s.qc * C::LatVap * C::INV_CP;
+        vap_liq = vap_liq - s.qc;
+        s.qc = 0;
+        s.nc = 0;
       }
-      impose_max_total_ni(ni_incld, rt.max_total_ni, inv_rho);
-      if (qi_gt_small) {
-        TableIce<TR> ti;
-        lookup_ice<TR>(TR(qi_incld), TR(ni_incld), TR(qm_incld), TR(rhop), ti);
-        TR ta[4], te[4];
-        apply_table_ice4<TR>(tb, ti, 0, ta); /* columns 0, 1, 6, 7 */
-        apply_table_ice4<TR>(tb, ti, 8, te); /* columns 5, 11, 8, 10 */
-        const TR tv_eff = te[0];
-        const TR tv_lmax = ta[2];
-        const TR tv_lmin = ta[3];
-        const TR tv_dens = te[1];
-        ni_incld = vmin(ni_incld, double(tv_lmax) * ni_incld);
-        ni_incld = vmax(ni_incld, double(tv_lmin) * ni_incld);
-        eff_qi = double(tv_eff);
-        rho_qi = double(tv_dens);
+      if (s.qr >= C::QSMALL) {
+        const float icr = 1.0f / float(cld_r);
+        const float qr_f = float(s.qr) * icr;
+        const float n_in = float(s.nr) * icr;
+        float n_out = n_in, mu_r = 0, lamr;
+        get_rain_dsd2<float>(qr_f, n_out, mu_r, lamr, rt);
+        if (n_out != n_in) s.nr = double(n_out) * cld_r;
+        eff_qr = double(1.5f / lamr);
+      } else {
+        s.qv = s.qv + s.qr;
+        s.th = s.th - inv_exner * s.qr * C::LatVap * C::INV_CP;
+        vap_liq = vap_liq - s.qr;
+        s.qr = 0;
+        s.nr = 0;
       }
-      s.ni = ni_incld * cld_i;
-      if (s.qm < C::QSMALL && qi_gt_small) {
-        s.qm = 0;
-        s.bm = 0;
-      }
-      if (!qi_gt_small) {
-        s.qv = s.qv + s.qi;
-        s.th = s.th - inv_exner * s.qi * (C::LatVap + C::LatIce) * C::INV_CP;
-        s.qi = 0; s.ni = 0; s.qm = 0; s.bm = 0;
+      {
+        const bool qi_gt_small = s.qi >= C::QSMALL;
+        s.ni = vmax(s.ni, C::NSMALL);
+        if (qi_gt_small) {
+          const float ici = 1.0f / float(cld_i);
+          const float qi_f = float(s.qi) * ici;
+          const float ni0 = float(s.ni) * ici;
+          const float qm0 = float(s.qm) * ici, bm0 = float(s.bm) * ici;
+          float qm_f = qm0, bm_f = bm0;
+          const float rhop = calc_bulk_rho_rime<float>(qi_f, qm_f, bm_f, rt);
+          if (qm_f != qm0) s.qm = double(qm_f) * cld_i;
+          if (bm_f != bm0) s.bm = double(bm_f) * cld_i;
+          float ni_f = ni0;
+          impose_max_total_ni(ni_f, rt.max_total_ni, float(inv_rho));
+          TableIce<float> ti;
+          lookup_ice<float>(qi_f, ni_f, qm_f, rhop, ti);
+          float ta[4], te[4];
+          apply_table_ice4<float>(tb, ti, 0, ta); /* columns 0, 1, 6, 7 */
+          apply_table_ice4<float>(tb, ti, 8, te); /* columns 5, 11, 8, 10 */
+          ni_f = vmin(ni_f, ta[2] * ni_f);
+          ni_f = vmax(ni_f, ta[3] * ni_f);
+          eff_qi = double(te[0]);
+          rho_qi = double(te[1]);
+          if (ni_f != ni0) s.ni = double(ni_f) * cld_i;
+          if (s.qm < C::QSMALL) {
+            s.qm = 0;
+            s.bm = 0;
+          }
+        } else {
+          s.qv = s.qv + s.qi;
+          s.th = s.th - inv_exner * s.qi * (C::LatVap + C::LatIce) * C::INV_CP;
+          s.qi = 0; s.ni = 0; s.qm = 0; s.bm = 0;
+        }
       }
     }
     if (s.qr < C::QSMALL) s.nr = 0;

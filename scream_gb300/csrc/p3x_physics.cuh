@@ -938,14 +938,19 @@ __device__ __forceinline__ void ice_deposition_sublimation(double qi_incld, doub
   }
 }
 
-/* cloud/rain/ice water conservation, p3/impl/p3_conservation_impl.hpp:9-98 */
-__device__ __forceinline__ void water_conservation(double qc, double qr, double qi, double dt, Rates<double>& r) {
+/* cloud/rain/ice water conservation, p3/impl/p3_conservation_impl.hpp:9-98
+ * (T = double in the plain form; float in the FP32-bulk form, where the
+ * limiters only scale rates and the state update stays water-conserving). */
+template <class T>
+__device__ __forceinline__ int water_conservation(T qc, T qr, T qi, T dt, Rates<T>& r) {
+  int limited = 0;
   {
-    const double sinks = (r.qc2qr_autoconv_tend + r.qc2qr_accret_tend + r.qc2qi_collect_tend +
+    const T sinks = (r.qc2qr_autoconv_tend + r.qc2qr_accret_tend + r.qc2qi_collect_tend +
                           r.qc2qi_hetero_freeze_tend + r.qc2qr_ice_shed_tend + r.qc2qi_berg_tend) * dt;
-    const double sources = qc;
-    double ratio;
-    if (sinks > sources && sinks >= C::QTENDSMALL) {
+    const T sources = qc;
+    T ratio;
+    if (sinks > sources && sinks >= T(C::QTENDSMALL)) {
+      limited |= 1;
       ratio = sources / sinks;
       r.qc2qr_autoconv_tend *= ratio;
       r.qc2qr_accret_tend *= ratio;
@@ -954,44 +959,50 @@ __device__ __forceinline__ void water_conservation(double qc, double qr, double 
       r.qc2qr_ice_shed_tend *= ratio;
       r.qc2qi_berg_tend *= ratio;
     } else {
-      ratio = 1;
+      ratio = T(1);
     }
-    if (sources > C::QTENDSMALL) {
-      r.qv2qi_vapdep_tend *= (1 - ratio);
-      r.qi2qv_sublim_tend *= (1 - ratio);
+    if (sources > T(C::QTENDSMALL)) {
+      r.qv2qi_vapdep_tend *= (T(1) - ratio);
+      r.qi2qv_sublim_tend *= (T(1) - ratio);
     }
   }
   {
-    const double sinks = (r.qr2qv_evap_tend + r.qr2qi_collect_tend + r.qr2qi_immers_freeze_tend) * dt;
-    const double sources = qr + (r.qc2qr_autoconv_tend + r.qc2qr_accret_tend + r.qi2qr_melt_tend +
+    const T sinks = (r.qr2qv_evap_tend + r.qr2qi_collect_tend + r.qr2qi_immers_freeze_tend) * dt;
+    const T sources = qr + (r.qc2qr_autoconv_tend + r.qc2qr_accret_tend + r.qi2qr_melt_tend +
                                  r.qc2qr_ice_shed_tend) * dt;
-    if (sinks > sources && sinks >= C::QTENDSMALL) {
-      const double ratio = sources / sinks;
+    if (sinks > sources && sinks >= T(C::QTENDSMALL)) {
+      limited |= 2;
+      const T ratio = sources / sinks;
       r.qr2qv_evap_tend *= ratio;
       r.qr2qi_collect_tend *= ratio;
       r.qr2qi_immers_freeze_tend *= ratio;
     }
   }
   {
-    const double sinks = (r.qi2qv_sublim_tend + r.qi2qr_melt_tend) * dt;
-    const double sources = qi + (r.qv2qi_vapdep_tend + r.qv2qi_nucleat_tend + r.qr2qi_collect_tend +
+    const T sinks = (r.qi2qv_sublim_tend + r.qi2qr_melt_tend) * dt;
+    const T sources = qi + (r.qv2qi_vapdep_tend + r.qv2qi_nucleat_tend + r.qr2qi_collect_tend +
                                  r.qc2qi_collect_tend + r.qr2qi_immers_freeze_tend +
                                  r.qc2qi_hetero_freeze_tend + r.qc2qi_berg_tend) * dt;
-    if (sinks > sources && sinks >= C::QTENDSMALL) {
-      const double ratio = sources / sinks;
+    if (sinks > sources && sinks >= T(C::QTENDSMALL)) {
+      limited |= 4;
+      const T ratio = sources / sinks;
       r.qi2qv_sublim_tend *= ratio;
       r.qi2qr_melt_tend *= ratio;
     }
   }
+  return limited;
 }
 
 /* nc/nr/ni conservation, p3/impl/p3_{nc,nr,ni}_conservation_impl.hpp */
-__device__ __forceinline__ void number_conservation(double nc, double nr, double ni, double dt, Rates<double>& r) {
+template <class T>
+__device__ __forceinline__ int number_conservation(T nc, T nr, T ni, T dt, Rates<T>& r) {
+  int limited = 0;
   {
-    const double sink = (r.nc_collect_tend + r.nc2ni_immers_freeze_tend + r.nc_accret_tend + r.nc2nr_autoconv_tend) * dt;
-    const double source = nc + r.nc_selfcollect_tend * dt;
+    const T sink = (r.nc_collect_tend + r.nc2ni_immers_freeze_tend + r.nc_accret_tend + r.nc2nr_autoconv_tend) * dt;
+    const T source = nc + r.nc_selfcollect_tend * dt;
     if (sink > source) {
-      const double ratio = source / sink;
+      limited |= 1;
+      const T ratio = source / sink;
       r.nc_collect_tend *= ratio;
       r.nc2ni_immers_freeze_tend *= ratio;
       r.nc_accret_tend *= ratio;
@@ -999,10 +1010,11 @@ __device__ __forceinline__ void number_conservation(double nc, double nr, double
     }
   }
   {
-    const double sink = (r.nr_collect_tend + r.nr2ni_immers_freeze_tend + r.nr_selfcollect_tend + r.nr_evap_tend) * dt;
-    const double source = nr + (r.ni2nr_melt_tend * C::nmltratio + r.nr_ice_shed_tend + r.ncshdc + r.nc2nr_autoconv_tend) * dt;
+    const T sink = (r.nr_collect_tend + r.nr2ni_immers_freeze_tend + r.nr_selfcollect_tend + r.nr_evap_tend) * dt;
+    const T source = nr + (r.ni2nr_melt_tend * T(C::nmltratio) + r.nr_ice_shed_tend + r.ncshdc + r.nc2nr_autoconv_tend) * dt;
     if (sink > source) {
-      const double ratio = source / sink;
+      limited |= 2;
+      const T ratio = source / sink;
       r.nr_collect_tend *= ratio;
       r.nr2ni_immers_freeze_tend *= ratio;
       r.nr_selfcollect_tend *= ratio;
@@ -1010,15 +1022,17 @@ __device__ __forceinline__ void number_conservation(double nc, double nr, double
     }
   }
   {
-    const double sink = (r.ni2nr_melt_tend + r.ni_sublim_tend + r.ni_selfcollect_tend) * dt;
-    const double source = ni + (r.ni_nucleat_tend + r.nr2ni_immers_freeze_tend + r.nc2ni_immers_freeze_tend) * dt;
+    const T sink = (r.ni2nr_melt_tend + r.ni_sublim_tend + r.ni_selfcollect_tend) * dt;
+    const T source = ni + (r.ni_nucleat_tend + r.nr2ni_immers_freeze_tend + r.nc2ni_immers_freeze_tend) * dt;
     if (sink > source) {
-      const double ratio = source / sink;
+      limited |= 4;
+      const T ratio = source / sink;
       r.ni2nr_melt_tend *= ratio;
       r.ni_sublim_tend *= ratio;
       r.ni_selfcollect_tend *= ratio;
     }
   }
+  return limited;
 }
 
 /* ice_supersat_conservation, p3/impl/p3_ice_supersat_conservation_impl.hpp:12-40 */
@@ -1055,6 +1069,49 @@ __device__ __forceinline__ void prevent_liq_supersaturation(double pres, double 
   frac = vmin(1., frac);
   r.qi2qv_sublim_tend = frac * r.qi2qv_sublim_tend;
   r.qr2qv_evap_tend = frac * r.qr2qv_evap_tend;
+}
+
+/* ice_supersat_conservation and prevent_liq_supersaturation of the FP32-bulk
+ * form: the vapour residuals (qv + sources dt - qv_sat) are FP64, the
+ * limiting fractions FP32. */
+__device__ __forceinline__ void ice_supersat_conservation_bulk(Rates<float>& r, double cld_frac_i, double qv,
+                                                               double qv_sat_i, double t_atm, double dt) {
+  const float qv_sink = r.qv2qi_vapdep_tend + r.qv2qi_nucleat_tend;
+  if (qv_sink > float(C::QSMALL) && cld_frac_i > 1e-20) {
+    const float dtf = float(dt);
+    const double resid = qv + double((r.qi2qv_sublim_tend + r.qr2qv_evap_tend) * dtf) - qv_sat_i;
+    const float tf = float(t_atm);
+    constexpr float latsublim2 = float((C::LatVap + C::LatIce) * (C::LatVap + C::LatIce) / (C::CP * C::RH2O));
+    float qv_avail = float(resid) / (1.0f + latsublim2 * float(qv_sat_i) / (tf * tf)) / dtf;
+    qv_avail = vmax(qv_avail, 0.0f);
+    if (qv_sink > qv_avail) {
+      const float fract = qv_avail / qv_sink;
+      r.qv2qi_nucleat_tend *= fract;
+      r.qv2qi_vapdep_tend *= fract;
+    }
+  }
+}
+
+__device__ __forceinline__ bool prevent_liq_supersaturation_bulk(double pres, double t_atm, double qv, double dt,
+                                                                 Rates<float>& r, const RuntimeDev& rt,
+                                                                 uint32_t& err) {
+  const float qv_sources = r.qi2qv_sublim_tend + r.qr2qv_evap_tend;
+  if (!(qv_sources >= float(C::QSMALL))) return false;
+  const float dtf = float(dt);
+  const float qv_sinks = r.qv2qi_vapdep_tend + r.qv2qi_nucleat_tend;
+  constexpr float lvs = float((C::LatVap + C::LatIce) * C::INV_CP), lv = float(C::LatVap * C::INV_CP);
+  const double T_endstep = t_atm + double(((qv_sinks - r.qi2qv_sublim_tend) * lvs - r.qr2qv_evap_tend * lv) * dtf);
+  const double qsl = qv_sat_dry<float>(T_endstep, pres, false, rt, err);
+  const float te = float(T_endstep);
+  const float A = float(C::LatVap * C::INV_CP / C::RV) * float(qsl) * dtf / (te * te) *
+                  (float(C::LatVap + C::LatIce) * r.qi2qv_sublim_tend + float(C::LatVap) * r.qr2qv_evap_tend);
+  const double resid = qsl - qv + double(qv_sinks * dtf);
+  float frac = (float(resid) + A) / (qv_sources * dtf + A);
+  frac = vmax(0.0f, frac);
+  frac = vmin(1.0f, frac);
+  r.qi2qv_sublim_tend = frac * r.qi2qv_sublim_tend;
+  r.qr2qv_evap_tend = frac * r.qr2qv_evap_tend;
+  return frac < 1.0f; /* sublimation / evaporation were rescaled */
 }
 
 /* update_prognostic_ice / update_prognostic_liquid,
@@ -1102,6 +1159,80 @@ __device__ __forceinline__ void update_prognostics(const Rates<double>& r, doubl
   s.nr = s.nr + (r.ncautr - r.nr_selfcollect_tend - r.nr_evap_tend) * dt;
   s.qv = s.qv + r.qr2qv_evap_tend * dt;
   s.th = s.th + inv_exner * (-r.qr2qv_evap_tend * C::LatVap * C::INV_CP) * dt;
+}
+
+/* update_prognostic_ice / update_prognostic_liquid of the FP32-bulk form:
+ * each prognostic's tendency is summed in FP32 from the FP32 rates (same
+ * terms as update_prognostics) and applied to the FP64 state once; the
+ * vapour change is minus the condensate changes, formed in FP64, so the
+ * water of every cell is conserved to FP64 round-off. */
+__device__ __forceinline__ void update_prognostics_bulk(const Rates<float>& r, double inv_exner, bool predictNc,
+                                                        bool prescribedCCN, bool log_wetgrowth, double dt,
+                                                        float rho_qm_cloud, double inv_rho, int wlim, int nlim,
+                                                        const Rates<float>& r_lim, State& s) {
+  const float dtf = float(dt);
+  const float sink_i = r.qi2qv_sublim_tend + r.qi2qr_melt_tend;
+  float dqi = 0, dqm = 0, dbm = 0;
+  if (s.qi >= C::QSMALL) {
+    const float frac = sink_i * dtf / float(s.qi);
+    dbm = -frac * float(s.bm);
+    dqm = -frac * float(s.qm);
+    dqi = -sink_i * dtf;
+  }
+  const float dum = (r.qr2qi_collect_tend + r.qc2qi_collect_tend + r.qr2qi_immers_freeze_tend +
+                     r.qc2qi_hetero_freeze_tend) * dtf;
+  dqi += (r.qv2qi_vapdep_tend + r.qv2qi_nucleat_tend + r.qc2qi_berg_tend) * dtf + dum;
+  dqm += dum;
+  dbm += (r.qr2qi_collect_tend * float(C::INV_RHO_RIMEMAX) + r.qc2qi_collect_tend / rho_qm_cloud +
+          (r.qr2qi_immers_freeze_tend + r.qc2qi_hetero_freeze_tend) * float(C::INV_RHO_RIMEMAX)) * dtf;
+  const float dni = (r.ni_nucleat_tend - r.ni2nr_melt_tend - r.ni_sublim_tend - r.ni_selfcollect_tend +
+                     r.nr2ni_immers_freeze_tend + r.nc2ni_immers_freeze_tend) * dtf;
+  const float dqc = (-r.qc2qi_hetero_freeze_tend - r.qc2qi_collect_tend - r.qc2qr_ice_shed_tend -
+                     r.qc2qi_berg_tend - r.qc2qr_accret_tend - r.qc2qr_autoconv_tend) * dtf;
+  const float dqr = (-r.qr2qi_collect_tend + r.qi2qr_melt_tend - r.qr2qi_immers_freeze_tend +
+                     r.qc2qr_ice_shed_tend + r.qc2qr_accret_tend + r.qc2qr_autoconv_tend - r.qr2qv_evap_tend) * dtf;
+  const float dnr = (-r.nr_collect_tend - r.nr2ni_immers_freeze_tend + float(C::nmltratio) * r.ni2nr_melt_tend +
+                     r.nr_ice_shed_tend + r.ncshdc + r.ncautr - r.nr_selfcollect_tend - r.nr_evap_tend) * dtf;
+  constexpr float lvs = float((C::LatVap + C::LatIce) * C::INV_CP), lf = float(C::LatIce * C::INV_CP),
+                  lv = float(C::LatVap * C::INV_CP);
+  const float dth = ((r.qv2qi_vapdep_tend - r.qi2qv_sublim_tend + r.qv2qi_nucleat_tend) * lvs +
+                     (r.qr2qi_collect_tend + r.qc2qi_collect_tend + r.qc2qi_hetero_freeze_tend +
+                      r.qr2qi_immers_freeze_tend - r.qi2qr_melt_tend + r.qc2qi_berg_tend) * lf -
+                     r.qr2qv_evap_tend * lv) * dtf;
+  /* A reservoir whose conservation limiter engaged has limited sinks equal to
+   * its sources, so its new value is exactly the change that later limiters
+   * made to its rates (r_lim: the rates right after the conservation
+   * limiters): rain evaporation and ice sublimation, deposition and
+   * nucleation.  The FP64 update reaches this up to a round-off residue
+   * (< qsmall, clipped to zero); an FP32 sum of the cancelling terms would
+   * leave ~1e-7 of the sources instead.  The same holds for ni and, when
+   * predicted, nc, whose limiters count exactly the update's terms (the nr
+   * limiter counts nc2nr_autoconv where the update adds ncautr). */
+  const double Dqc = (wlim & 1) ? -s.qc : double(dqc);
+  const double Dqr = (wlim & 2) ? -s.qr + double((r_lim.qr2qv_evap_tend - r.qr2qv_evap_tend) * dtf) : double(dqr);
+  const double Dqi = ((wlim & 4) && s.qi >= C::QSMALL)
+                         ? -s.qi + double(((r.qv2qi_vapdep_tend - r_lim.qv2qi_vapdep_tend) +
+                                           (r.qv2qi_nucleat_tend - r_lim.qv2qi_nucleat_tend) -
+                                           (r.qi2qv_sublim_tend - r_lim.qi2qv_sublim_tend)) * dtf)
+                         : double(dqi);
+  s.qi = s.qi + Dqi;
+  s.qm = s.qm + double(dqm);
+  s.bm = s.bm + double(dbm);
+  s.ni = (nlim & 4) ? 0.0 : s.ni + double(dni);
+  if (s.qm < 0) { s.qm = 0; s.bm = 0; }
+  if (log_wetgrowth) { s.qm = s.qi; s.bm = s.qm * C::INV_RHO_RIMEMAX; }
+  s.qc = s.qc + Dqc;
+  s.qr = s.qr + Dqr;
+  s.qv = s.qv - (Dqc + Dqr + Dqi);
+  s.th = s.th + inv_exner * double(dth);
+  if (predictNc || prescribedCCN) {
+    float dnc = (-r.nc_accret_tend - r.nc2nr_autoconv_tend + r.nc_selfcollect_tend) * dtf;
+    if (predictNc) dnc += (-r.nc_collect_tend - r.nc2ni_immers_freeze_tend) * dtf;
+    s.nc = ((nlim & 1) && predictNc) ? 0.0 : s.nc + double(dnc);
+  } else {
+    s.nc = C::NCCNST * inv_rho;
+  }
+  s.nr = s.nr + double(dnr);
 }
 
 }  // namespace dev
