@@ -154,7 +154,7 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(seconds_target=15.0, nlev=NLEV):
+def cpu_baseline(seconds_target=15.0, nlev=NLEV, keep=None):
     """CPU oracle on a bounded sample of the same workload (all host cores):
     runs of 10 steps with state carried, each run restarting from the initial
     state (as the GPU runs do), until the time budget is spent."""
@@ -175,6 +175,7 @@ def cpu_baseline(seconds_target=15.0, nlev=NLEV):
     O.p3_main(fresh(), tab, DT, nthreads=cores)  # warm-up step
     total_us, steps, runs = 0.0, 0, 0
     t_end = time.time() + seconds_target
+    final = None
     while time.time() < t_end or runs < 1:
         st = fresh()
         for s in range(10):
@@ -182,7 +183,16 @@ def cpu_baseline(seconds_target=15.0, nlev=NLEV):
             total_us += us
             steps += 1
         runs += 1
+        final = st
     value = ncol * nlev * steps / (total_us * 1e-6)
+    if keep is not None:
+        # the oracle's own round-off envelope: the same 10 steps with th
+        # moved by one ulp
+        pert = fresh()
+        pert["th"] = np.nextafter(pert["th"], np.inf)
+        for s in range(10):
+            O.p3_main(pert, tab, DT, it=s + 1, nthreads=cores)
+        keep.update(inputs=inp, oracle=final, oracle_1ulp=pert)
     return {"value": value, "unit": "column-levels/s", "cores": cores, "kind": "port",
             "sample": f"{ncol} columns x {nlev} levels (RH-stress workload, config-2 distributions), "
                       f"{runs} runs of 10 steps from the initial state, oracle p3_main (C++ restatement of "
@@ -204,6 +214,42 @@ def run_reference(args):
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def precision_report(ctx, sample):
+    """Per-field rel-L2 and max-abs error of the GPU forms against the FP64
+    oracle after 10 steps on the CPU baseline's column sample (the oracle run
+    the baseline just timed).  The FP64 row is the round-off envelope: P3's
+    ice fields respond at ~1e-2 to 1-ulp input changes."""
+    import numpy as np
+    import scream_gb300 as p3
+    inp, ref = sample["inputs"], sample["oracle"]
+    names = ["qc", "nc", "qr", "nr", "qi", "qm", "ni", "bm", "qv", "th", "precip_liq_surf", "precip_ice_surf",
+             "precip_liq_flux", "diag_eff_radius_qc", "diag_eff_radius_qr", "diag_eff_radius_qi", "rho_qi",
+             "qv2qi_depos_tend", "precip_total_tend", "nevapr", "liq_ice_exchange", "vap_liq_exchange",
+             "vap_ice_exchange"]
+    out = {"sample": f"{inp['qc'].shape[0]} columns x {inp['qc'].shape[1]} levels, 10 steps, RH-stress workload",
+           "note": "oracle_1ulp: the oracle itself after th moved by one ulp (round-off envelope)"}
+    for prec, tag in ((p3.P3X_FP32_BULK, "fp32_bulk"), (p3.P3X_FP64, "fp64"), (None, "oracle_1ulp")):
+        if prec is None:
+            g = sample["oracle_1ulp"]
+        else:
+            f = p3.P3Fields.from_inputs(inp)
+            for s in range(10):
+                ctx.p3_main(f, DT, prec, it=s + 1)
+            g = f.to_host()
+        rows = {}
+        for n in names:
+            den = np.linalg.norm(ref[n])
+            diff = g[n] - ref[n]
+            rows[n] = {"rel_l2": float(np.linalg.norm(diff) / den) if den > 0 else float(np.linalg.norm(diff)),
+                       "max_abs": float(np.max(np.abs(diff)))}
+        tot_g = g["precip_liq_surf"] + g["precip_ice_surf"]
+        tot_r = ref["precip_liq_surf"] + ref["precip_ice_surf"]
+        rows["surface_precip_total"] = {"rel_l2": float(np.linalg.norm(tot_g - tot_r) / np.linalg.norm(tot_r)),
+                                        "max_abs": float(np.max(np.abs(tot_g - tot_r)))}
+        out[tag] = rows
+    return out
 
 
 def run_batched(ctx, args):
@@ -389,7 +435,9 @@ def run_gpu(args):
             "alg_bytes_per_cl": ALG_BYTES_PER_CL,
             "kernels": shares(parts32)}
     kmean64 = sum(k64) / len(k64) * 1e-3
-    cb = cpu_baseline(seconds_target=args.cpu_seconds) if not args.no_cpu else None
+    sample = {}
+    cb = cpu_baseline(seconds_target=args.cpu_seconds, keep=sample) if not args.no_cpu else None
+    precision = precision_report(ctx, sample) if sample else None
     line = {
         "metric": "P3 column-levels/sec at nlev=128 (FP32-bulk; FP64 beside it)",
         "value": value, "unit": "column-levels/s", "n_gpus": ws, "steps": args.steps,
@@ -411,6 +459,7 @@ def run_gpu(args):
         "serving": serving,
         "clocks": clocks,
         "cpu_baseline": cb,
+        "precision": precision,
     }
     print(json.dumps(line), flush=True)
     if ws > 1:
