@@ -1007,6 +1007,360 @@ __device__ void p3_sed(const Inst& in, const int col, const KParams<TR>& kp, con
 #undef SMA
 }
 
+/* K2 of the FP32-bulk form.  Same algorithm and order as p3_sed; fall
+ * speeds, density, fall-speed factors and a float shadow of each species
+ * field live in FP32 shared arrays, so a level costs no FP64 conversions
+ * except those of the FP64 flux accumulation itself
+ * (R += (double(F_in) - double(F_out)) * dt_sub / (dz rho)), which keeps
+ * the column's mass telescoping exactly.  The shared slots of p3_sed are
+ * reused: two float arrays share one double slot. */
+template <int LANES>
+__device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>& kp, const Tabs<float>& tb,
+                            double* __restrict__ sm, uint32_t& err) {
+  if (in.cflag[col] == 0) return;
+  const RuntimeDev& rt = kp.rt;
+  const unsigned mask = group_mask<LANES>();
+  const int lane = threadIdx.x & (LANES - 1);
+  const int nk = in.nlev;
+  const int S = kp.sm_stride;
+  const int64_t co = int64_t(col) * in.ld;
+  const int64_t ci = int64_t(col) * in.ld_int;
+  const double dt = in.dt;
+  const double inv_dt = 1 / dt;
+  const bool predictNc = in.predictNc != 0;
+  const int kbot = nk - 1;
+#define SMA(a, k) sm[(a)*S + (k)]
+  float* const RHOf = reinterpret_cast<float*>(&SMA(B_RHO, 0));
+  float* const FACf = RHOf + S;
+  double* const COEF = &SMA(B_INVRHO, 0); /* 1 / (dz rho) */
+  double* const INVDZ = &SMA(B_INVDZ, 0);
+  float* const R2f = reinterpret_cast<float*>(&SMA(B_FAC, 0));
+  float* const R3f = R2f + S;
+  double* const CLD = &SMA(B_CLD, 0);
+  float* const V1f = reinterpret_cast<float*>(&SMA(B_V1, 0));
+  float* const V2f = V1f + S;
+  float* const R0f = reinterpret_cast<float*>(&SMA(B_V2, 0));
+  float* const R1f = R0f + S;
+  double* const R0 = &SMA(B_R0, 0);
+  double* const R1 = &SMA(B_R1, 0);
+  double* const R2 = &SMA(B_R2, 0);
+  double* const R3 = &SMA(B_R3, 0);
+  double* const PF = R2; /* rain flux accumulator (rain has two fields) */
+  for (int k = lane; k < nk; k += LANES) {
+    const double rho = scr_at(in, S_RHO, col)[k];
+    const double inv_dz = 1 / in.dz[co + k];
+    RHOf[k] = float(rho);
+    INVDZ[k] = inv_dz;
+    COEF[k] = inv_dz / rho;
+  }
+  double precip_liq_surf = 0, precip_ice_surf = 0;
+
+#pragma unroll 1
+  for (int sp = 0; sp < 3; ++sp) {
+    double* g0 = sp == 0 ? in.qc : (sp == 1 ? in.qr : in.qi);
+    double* g1 = sp == 0 ? in.nc : (sp == 1 ? in.nr : in.ni);
+    const double* cldp = sp == 0 ? in.cld_frac_l : (sp == 1 ? in.cld_frac_r : in.cld_frac_i);
+    const int sfac = sp == 0 ? S_ACN : (sp == 1 ? S_RHOFACR : S_RHOFACI);
+    const double* const facp = scr_at(in, sfac, col);
+    const int nfield = sp == 0 ? (predictNc ? 2 : 1) : (sp == 1 ? 2 : 4);
+
+    int my_top = 1 << 30, my_bot = -1;
+    for (int k = lane; k < nk; k += LANES) {
+      const double q = g0[co + k];
+      const double n = g1[co + k];
+      R0[k] = q;
+      R1[k] = n;
+      R0f[k] = float(q);
+      R1f[k] = float(n);
+      CLD[k] = cldp[co + k];
+      FACf[k] = float(facp[k]);
+      if (sp == 2) {
+        const double m = in.qm[co + k], b = in.bm[co + k];
+        R2[k] = m;
+        R3[k] = b;
+        R2f[k] = float(m);
+        R3f[k] = float(b);
+      }
+      if (q >= C::QSMALL) {
+        my_top = min(my_top, k);
+        my_bot = max(my_bot, k);
+      }
+    }
+    const int k_qxtop = group_min_int<LANES>(mask, my_top);
+    int k_qxbot = group_max_int<LANES>(mask, my_bot);
+    if (k_qxbot < 0) continue; /* species absent (group-uniform) */
+    if (sp == 1) {
+      for (int k = lane; k <= nk; k += LANES) PF[k] = 0;
+    }
+    __syncwarp(mask);
+
+    double dt_left = dt, prt_accum = 0.0;
+    bool first = true;
+    int nsub = 0;
+    while (dt_left > C::dt_left_tol) {
+      if (++nsub > kMaxSubsteps) {
+        err |= kErrSubstep;
+        break;
+      }
+      double lmax = 0.0;
+      for (int k = k_qxtop + lane; k <= k_qxbot; k += LANES) {
+        float v1 = 0, v2 = 0;
+        bool fall = false;
+        if (first) {
+          /* first substep: the in-cloud values with the reference's
+           * thresholds and limits, in FP64 (as p3_sed) */
+          const double cld = CLD[k];
+          const double inv_cld = 1 / cld;
+          if (sp == 0) {
+            double qc_incld = 0, nc_incld = 0;
+            if (R0[k] >= C::QSMALL) {
+              qc_incld = R0[k] * inv_cld;
+              nc_incld = vmax(R1[k] * inv_cld, 0.);
+            }
+            qc_incld = vmin(qc_incld, C::incloud_limit);
+            if (qc_incld > C::QSMALL) {
+              float mu_c, lamc;
+              const float n_in = float(nc_incld);
+              float n_out = n_in;
+              get_cloud_dsd2<float>(float(qc_incld), n_out, mu_c, RHOf[k], lamc);
+              if (n_out != n_in) {
+                R1[k] = double(n_out) * cld;
+                R1f[k] = float(R1[k]);
+              }
+              const float dum = 1.0f / (lamc * lamc);
+              v1 = FACf[k] * ((5.0f + mu_c) * (4.0f + mu_c)) * dum;
+              if (predictNc) v2 = FACf[k] * ((2.0f + mu_c) * (1.0f + mu_c)) * dum;
+              fall = true;
+            }
+          } else if (sp == 1) {
+            double qr_incld = 0, nr_incld = 0;
+            if (R0[k] >= C::QSMALL) {
+              qr_incld = R0[k] * inv_cld;
+              nr_incld = vmax(R1[k] * inv_cld, 0.);
+            }
+            qr_incld = vmin(qr_incld, C::precip_limit);
+            if (qr_incld > C::QSMALL) {
+              float mu_r = 0, lamr;
+              const float n_in = float(nr_incld);
+              float n_out = n_in;
+              get_rain_dsd2<float>(float(qr_incld), n_out, mu_r, lamr, rt);
+              Table3<float> t3;
+              lookup3<float>(mu_r, lamr, rt, t3);
+              v1 = apply_table3<float>(tb, tb.vm, t3) * FACf[k];
+              v2 = apply_table3<float>(tb, tb.vn, t3) * FACf[k];
+              if (n_out != n_in) {
+                R1[k] = double(n_out) * cld;
+                R1f[k] = float(R1[k]);
+              }
+              fall = true;
+            }
+          } else {
+            double qi_incld = 0, ni_incld = 0, qm_incld = 0, bm_incld = 0;
+            if (R0[k] >= C::QSMALL) {
+              qi_incld = R0[k] * inv_cld;
+              ni_incld = vmax(R1[k] * inv_cld, 0.);
+            }
+            if (R0[k] >= C::QSMALL && R2[k] >= C::QSMALL) {
+              qm_incld = R2[k] * inv_cld;
+              bm_incld = vmax(R3[k] * (1 / in.cld_frac_l[co + k]), 0.);
+            }
+            qi_incld = vmin(qi_incld, C::incloud_limit);
+            bm_incld = vmin(bm_incld, C::incloud_limit);
+            if (qi_incld > C::QSMALL) {
+              ni_incld = vmax(ni_incld, C::NSMALL);
+              const double rhop = calc_bulk_rho_rime(qi_incld, qm_incld, bm_incld, rt);
+              R2[k] = qm_incld * cld;
+              R3[k] = bm_incld * cld;
+              R2f[k] = float(R2[k]);
+              R3f[k] = float(R3[k]);
+              TableIce<float> ti;
+              lookup_ice<float>(float(qi_incld), float(ni_incld), float(qm_incld), float(rhop), ti);
+              float tv[4];
+              apply_table_ice4<float>(tb, ti, 0, tv); /* columns 0, 1, 6, 7 */
+              ni_incld = vmin(ni_incld, double(tv[2]) * ni_incld);
+              ni_incld = vmax(ni_incld, double(tv[3]) * ni_incld);
+              R1[k] = ni_incld * cld;
+              R1f[k] = float(R1[k]);
+              const float f = float(rt.ice_sedimentation_factor) * FACf[k];
+              v1 = f * tv[1];
+              v2 = f * tv[0];
+              fall = true;
+            }
+          }
+        } else {
+          /* later substeps: in-cloud values and fall speeds in FP32; the FP64
+           * state is rewritten only where a limiter changed a value */
+          const float icf = 1.0f / float(CLD[k]);
+          if (sp == 0) {
+            const float qc_f = R0f[k] * icf;
+            if (qc_f > float(C::QSMALL)) {
+              float mu_c, lamc;
+              const float n_in = R1f[k] * icf;
+              float n_out = n_in;
+              get_cloud_dsd2<float>(qc_f, n_out, mu_c, RHOf[k], lamc);
+              if (n_out != n_in) {
+                R1[k] = double(n_out) * CLD[k];
+                R1f[k] = float(R1[k]);
+              }
+              const float dum = 1.0f / (lamc * lamc);
+              v1 = FACf[k] * ((5.0f + mu_c) * (4.0f + mu_c)) * dum;
+              if (predictNc) v2 = FACf[k] * ((2.0f + mu_c) * (1.0f + mu_c)) * dum;
+              fall = true;
+            }
+          } else if (sp == 1) {
+            const float qr_f = R0f[k] * icf;
+            if (qr_f > float(C::QSMALL)) {
+              float mu_r = 0, lamr;
+              const float n_in = R1f[k] * icf;
+              float n_out = n_in;
+              get_rain_dsd2<float>(qr_f, n_out, mu_r, lamr, rt);
+              Table3<float> t3;
+              lookup3<float>(mu_r, lamr, rt, t3);
+              v1 = apply_table3<float>(tb, tb.vm, t3) * FACf[k];
+              v2 = apply_table3<float>(tb, tb.vn, t3) * FACf[k];
+              if (n_out != n_in) {
+                R1[k] = double(n_out) * CLD[k];
+                R1f[k] = float(R1[k]);
+              }
+              fall = true;
+            }
+          } else {
+            const float qi_f = R0f[k] * icf;
+            if (qi_f > float(C::QSMALL)) {
+              const float ni_f = R1f[k] * icf;
+              const float qm_f = R2f[k] * icf, bm_f = R3f[k] * icf;
+              const float ni_l = vmax(ni_f, float(C::NSMALL));
+              float qm_c = qm_f, bm_c = bm_f;
+              const float rhop = calc_bulk_rho_rime<float>(qi_f, qm_c, bm_c, rt);
+              if (qm_c != qm_f) {
+                R2[k] = double(qm_c) * CLD[k];
+                R2f[k] = float(R2[k]);
+              }
+              if (bm_c != bm_f) {
+                R3[k] = double(bm_c) * CLD[k];
+                R3f[k] = float(R3[k]);
+              }
+              TableIce<float> ti;
+              lookup_ice<float>(qi_f, ni_l, qm_c, rhop, ti);
+              float tv[4];
+              apply_table_ice4<float>(tb, ti, 0, tv); /* columns 0, 1, 6, 7 */
+              float n2 = vmin(ni_l, tv[2] * ni_l);
+              n2 = vmax(n2, tv[3] * n2);
+              if (n2 != ni_f) {
+                R1[k] = double(n2) * CLD[k];
+                R1f[k] = float(R1[k]);
+              }
+              const float f = float(rt.ice_sedimentation_factor) * FACf[k];
+              v1 = f * tv[1];
+              v2 = f * tv[0];
+              fall = true;
+            }
+          }
+        }
+        V1f[k] = v1;
+        V2f[k] = v2;
+        if (fall) lmax = vmax(lmax, double(v1) * dt_left * INVDZ[k]);
+      }
+      if (k_qxbot < kbot && lane == (k_qxbot + 1 - k_qxtop) % LANES) {
+        V1f[k_qxbot + 1] = 0; /* the cell receiving the leading edge has no fall speed */
+        V2f[k_qxbot + 1] = 0;
+      }
+      const double Co_max = group_max<LANES>(mask, lmax);
+      if (!(Co_max >= 0) || Co_max > 2.0e9) {
+        err |= kErrNumeric;
+        break;
+      }
+      const int tmpint1 = static_cast<int>(Co_max + 1);
+      const double dt_sub = dt_left / tmpint1;
+      const int k_temp = (k_qxbot == kbot) ? k_qxbot : k_qxbot + 1;
+      /* fluxes in FP32, every flux difference and state update in FP64 */
+      float carry0 = 0, carry1 = 0, carry2 = 0, carry3 = 0, flux_bot = 0;
+      for (int base = k_qxtop; base <= k_temp; base += LANES) {
+        const int k = base + lane;
+        const bool act = k <= k_temp;
+        float f0 = 0, f1 = 0, f2 = 0, f3 = 0;
+        if (act) {
+          const float rho = RHOf[k];
+          const float v1 = V1f[k];
+          f0 = v1 * R0f[k] * rho;
+          if (nfield > 1) f1 = V2f[k] * R1f[k] * rho;
+          if (nfield > 2) {
+            f2 = v1 * R2f[k] * rho;
+            f3 = v1 * R3f[k] * rho;
+          }
+        }
+        float u0 = __shfl_up_sync(mask, f0, 1, LANES);
+        float u1 = __shfl_up_sync(mask, f1, 1, LANES);
+        float u2 = 0, u3 = 0;
+        if (nfield > 2) {
+          u2 = __shfl_up_sync(mask, f2, 1, LANES);
+          u3 = __shfl_up_sync(mask, f3, 1, LANES);
+        }
+        if (lane == 0) {
+          u0 = carry0; u1 = carry1; u2 = carry2; u3 = carry3;
+        }
+        if (act) {
+          const double coef = COEF[k] * dt_sub;
+          const double r0 = R0[k] + (double(u0) - double(f0)) * coef;
+          R0[k] = r0;
+          R0f[k] = float(r0);
+          if (nfield > 1) {
+            const double r1 = R1[k] + (double(u1) - double(f1)) * coef;
+            R1[k] = r1;
+            R1f[k] = float(r1);
+          }
+          if (nfield > 2) {
+            const double r2 = R2[k] + (double(u2) - double(f2)) * coef;
+            const double r3 = R3[k] + (double(u3) - double(f3)) * coef;
+            R2[k] = r2;
+            R3[k] = r3;
+            R2f[k] = float(r2);
+            R3f[k] = float(r3);
+          }
+          if (sp == 1) PF[k + 1] += double(f0);
+          if (k == kbot) flux_bot = f0;
+        }
+        carry0 = __shfl_sync(mask, f0, LANES - 1, LANES);
+        carry1 = __shfl_sync(mask, f1, LANES - 1, LANES);
+        if (nfield > 2) {
+          carry2 = __shfl_sync(mask, f2, LANES - 1, LANES);
+          carry3 = __shfl_sync(mask, f3, LANES - 1, LANES);
+        }
+      }
+      if (k_qxbot == kbot) {
+        const int owner = (kbot - k_qxtop) % LANES;
+        prt_accum += double(__shfl_sync(mask, flux_bot, owner, LANES)) * dt_sub;
+      } else {
+        k_qxbot += 1;
+      }
+      dt_left -= dt_sub;
+      first = false;
+    }
+    if (sp == 0) precip_liq_surf = prt_accum * C::INV_RHO_H2O * inv_dt;
+    else if (sp == 1) precip_liq_surf += prt_accum * C::INV_RHO_H2O * inv_dt;
+    else precip_ice_surf += prt_accum * C::INV_RHO_H2O * inv_dt;
+
+    __syncwarp(mask);
+    for (int k = lane; k < nk; k += LANES) {
+      g0[co + k] = R0[k];
+      g1[co + k] = R1[k];
+      if (sp == 2) {
+        in.qm[co + k] = R2[k];
+        in.bm[co + k] = R3[k];
+      }
+    }
+    if (sp == 1) {
+      for (int k = lane; k <= nk; k += LANES) in.precip_liq_flux[ci + k] = PF[k];
+    }
+    __syncwarp(mask);
+  }
+  if (lane == 0) {
+    in.precip_liq_surf[col] = precip_liq_surf;
+    in.precip_ice_surf[col] = precip_ice_surf;
+  }
+#undef SMA
+}
+
 /* K3: homogeneous freezing and p3_main_part3 of one column that went on past
  * part2. */
 template <class TR, int LANES>
@@ -1297,7 +1651,11 @@ __global__ void __launch_bounds__(256) p3_sed_kernel(const Inst inst0, const KPa
   for (int w = blockIdx.x * kp.groups_per_block + g_in_block; w < kp.nwork; w += groups_total) {
     int col;
     const Inst& in = work_inst(inst0, kp, w, col);
-    p3_sed<TR, LANES>(in, col, kp, tb, sm, err);
+    if constexpr (sizeof(TR) == sizeof(float)) {
+      p3_sed_bulk<LANES>(in, col, kp, tb, sm, err);
+    } else {
+      p3_sed<TR, LANES>(in, col, kp, tb, sm, err);
+    }
   }
   if (err) atomicOr(kp.err, err);
 }
