@@ -610,11 +610,12 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
 #undef SMA
 }
 
-/* K2: cloud, rain and ice sedimentation of one column that went on past
- * part2. */
+/* K2 (FP64 form): cloud, rain and ice sedimentation of one column that went
+ * on past part2. */
 template <class TR, int LANES>
 __device__ void p3_sed(const Inst& in, const int col, const KParams<TR>& kp, const Tabs<TR>& tb,
                        double* __restrict__ sm, uint32_t& err) {
+  static_assert(sizeof(TR) == sizeof(double), "the FP32-bulk sedimentation is p3_sed_bulk");
   if (in.cflag[col] == 0) return;
   const RuntimeDev& rt = kp.rt;
   const unsigned mask = group_mask<LANES>();
@@ -653,7 +654,6 @@ __device__ void p3_sed(const Inst& in, const int col, const KParams<TR>& kp, con
   const double* const RHO = &SMA(B_RHO, 0);
   const double* const INVRHO = &SMA(B_INVRHO, 0);
   const double* const INVDZ = &SMA(B_INVDZ, 0);
-  constexpr bool kF64 = sizeof(TR) == sizeof(double);
 
 #pragma unroll 1
   for (int sp = 0; sp < 3; ++sp) {
@@ -716,23 +716,16 @@ __device__ void p3_sed(const Inst& in, const int col, const KParams<TR>& kp, con
               nc_incld = 0;
             }
             qc_incld = vmin(qc_incld, C::incloud_limit);
-          } else if (kF64) {
+          } else {
             qc_incld = R0[k] / cld;
             nc_incld = R1[k] / cld;
-          } else {
-            qc_incld = double(float(R0[k]) / float(cld));
-            nc_incld = double(float(R1[k]) / float(cld));
           }
           if (qc_incld > C::QSMALL) {
             TR mu_c, lamc;
             const TR n_in = TR(nc_incld);
             TR n_out = n_in;
             get_cloud_dsd2<TR>(TR(qc_incld), n_out, mu_c, TR(RHO[k]), lamc);
-            if (kF64) {
-              R1[k] = double(n_out) * cld;
-            } else if (n_out != n_in) {
-              R1[k] = double(n_out) * cld;
-            }
+            R1[k] = double(n_out) * cld;
             /* Stokes fall speeds, p3_cloud_sed_impl.hpp:99-103, with
              * Gamma(6+mu)/Gamma(4+mu) = (5+mu)(4+mu) and
              * Gamma(3+mu)/Gamma(1+mu) = (2+mu)(1+mu) (bcn = 2) */
@@ -754,12 +747,9 @@ __device__ void p3_sed(const Inst& in, const int col, const KParams<TR>& kp, con
               nr_incld = 0;
             }
             qr_incld = vmin(qr_incld, C::precip_limit);
-          } else if (kF64) {
+          } else {
             qr_incld = R0[k] / cld;
             nr_incld = R1[k] / cld;
-          } else {
-            qr_incld = double(float(R0[k]) / float(cld));
-            nr_incld = double(float(R1[k]) / float(cld));
           }
           if (qr_incld > C::QSMALL) {
             TR mu_r = 0, lamr;
@@ -771,46 +761,11 @@ __device__ void p3_sed(const Inst& in, const int col, const KParams<TR>& kp, con
             const TR rhofacr = TR(FAC[k]);
             v1 = double(apply_table3<TR>(tb, tb.vm, t3) * rhofacr);
             v2 = double(apply_table3<TR>(tb, tb.vn, t3) * rhofacr);
-            if (kF64) {
-              R1[k] = double(n_out) * cld;
-            } else if (n_out != n_in) {
-              R1[k] = double(n_out) * cld;
-            }
+            R1[k] = double(n_out) * cld;
             lmax = vmax(lmax, v1 * dt_left * INVDZ[k]);
           }
         } else {
-          bool done = false;
-          if constexpr (!kF64) {
-            if (!first) {
-              /* FP32-bulk, later substeps: in-cloud values, rime density and
-               * the table interpolation in FP32.  The FP64 state is rewritten
-               * only where a limiter changed an in-cloud value, so a substep
-               * adds no rounding to untouched qm, bm, ni. */
-              done = true;
-              const TR icf = TR(1) / TR(cld);
-              const TR qi_f = TR(R0[k]) * icf, ni_f = TR(R1[k]) * icf;
-              const TR qm_f = TR(R2[k]) * icf, bm_f = TR(R3[k]) * icf;
-              if (qi_f > TR(C::QSMALL)) {
-                const TR ni_l = vmax(ni_f, TR(C::NSMALL));
-                TR qm_c = qm_f, bm_c = bm_f;
-                const TR rhop = calc_bulk_rho_rime<TR>(qi_f, qm_c, bm_c, rt);
-                if (qm_c != qm_f) R2[k] = double(qm_c) * cld;
-                if (bm_c != bm_f) R3[k] = double(bm_c) * cld;
-                TableIce<TR> ti;
-                lookup_ice<TR>(qi_f, ni_l, qm_c, rhop, ti);
-                TR tv[4];
-                apply_table_ice4<TR>(tb, ti, 0, tv); /* columns 0, 1, 6, 7 */
-                TR n2 = vmin(ni_l, tv[2] * ni_l);
-                n2 = vmax(n2, tv[3] * n2);
-                if (n2 != ni_f) R1[k] = double(n2) * cld;
-                const TR f = TR(rt.ice_sedimentation_factor) * TR(FAC[k]);
-                v1 = double(f * tv[1]);
-                v2 = double(f * tv[0]);
-                lmax = vmax(lmax, v1 * dt_left * INVDZ[k]);
-              }
-            }
-          }
-          if (!done) {
+          {
             double qi_incld, ni_incld, qm_incld, bm_incld;
             if (first) {
               const double inv_cld = 1 / cld;
@@ -874,109 +829,54 @@ __device__ void p3_sed(const Inst& in, const int col, const KParams<TR>& kp, con
       const int tmpint1 = static_cast<int>(Co_max + 1);
       const double dt_sub = dt_left / tmpint1;
       const int k_temp = (k_qxbot == kbot) ? k_qxbot : k_qxbot + 1;
-      if constexpr (kF64) {
-        double carry0 = 0, carry1 = 0, carry2 = 0, carry3 = 0, flux_bot = 0;
-        for (int base = k_qxtop; base <= k_temp; base += LANES) {
-          const int k = base + lane;
-          const bool act = k <= k_temp;
-          double f0 = 0, f1 = 0, f2 = 0, f3 = 0;
-          if (act) {
-            const double rho = RHO[k];
-            const double v1 = V1[k];
-            f0 = v1 * R0[k] * rho;
-            if (nfield > 1) f1 = V2[k] * R1[k] * rho;
-            if (nfield > 2) {
-              f2 = v1 * R2[k] * rho;
-              f3 = v1 * R3[k] * rho;
-            }
-          }
-          double u0 = __shfl_up_sync(mask, f0, 1, LANES);
-          double u1 = __shfl_up_sync(mask, f1, 1, LANES);
-          double u2 = 0, u3 = 0;
+      double carry0 = 0, carry1 = 0, carry2 = 0, carry3 = 0, flux_bot = 0;
+      for (int base = k_qxtop; base <= k_temp; base += LANES) {
+        const int k = base + lane;
+        const bool act = k <= k_temp;
+        double f0 = 0, f1 = 0, f2 = 0, f3 = 0;
+        if (act) {
+          const double rho = RHO[k];
+          const double v1 = V1[k];
+          f0 = v1 * R0[k] * rho;
+          if (nfield > 1) f1 = V2[k] * R1[k] * rho;
           if (nfield > 2) {
-            u2 = __shfl_up_sync(mask, f2, 1, LANES);
-            u3 = __shfl_up_sync(mask, f3, 1, LANES);
-          }
-          if (lane == 0) {
-            u0 = carry0; u1 = carry1; u2 = carry2; u3 = carry3;
-          }
-          if (act) {
-            const double invdz = INVDZ[k], irho = INVRHO[k];
-            R0[k] += ((u0 - f0) * invdz) * dt_sub * irho;
-            if (nfield > 1) R1[k] += ((u1 - f1) * invdz) * dt_sub * irho;
-            if (nfield > 2) {
-              R2[k] += ((u2 - f2) * invdz) * dt_sub * irho;
-              R3[k] += ((u3 - f3) * invdz) * dt_sub * irho;
-            }
-            if (sp == 1) PF[k + 1] += f0;
-            if (k == kbot) flux_bot = f0;
-          }
-          carry0 = __shfl_sync(mask, f0, LANES - 1, LANES);
-          carry1 = __shfl_sync(mask, f1, LANES - 1, LANES);
-          if (nfield > 2) {
-            carry2 = __shfl_sync(mask, f2, LANES - 1, LANES);
-            carry3 = __shfl_sync(mask, f3, LANES - 1, LANES);
+            f2 = v1 * R2[k] * rho;
+            f3 = v1 * R3[k] * rho;
           }
         }
-        if (k_qxbot == kbot) {
-          const int owner = (kbot - k_qxtop) % LANES;
-          prt_accum += __shfl_sync(mask, flux_bot, owner, LANES) * dt_sub;
-        } else {
-          k_qxbot += 1;
+        double u0 = __shfl_up_sync(mask, f0, 1, LANES);
+        double u1 = __shfl_up_sync(mask, f1, 1, LANES);
+        double u2 = 0, u3 = 0;
+        if (nfield > 2) {
+          u2 = __shfl_up_sync(mask, f2, 1, LANES);
+          u3 = __shfl_up_sync(mask, f3, 1, LANES);
         }
+        if (lane == 0) {
+          u0 = carry0; u1 = carry1; u2 = carry2; u3 = carry3;
+        }
+        if (act) {
+          const double invdz = INVDZ[k], irho = INVRHO[k];
+          R0[k] += ((u0 - f0) * invdz) * dt_sub * irho;
+          if (nfield > 1) R1[k] += ((u1 - f1) * invdz) * dt_sub * irho;
+          if (nfield > 2) {
+            R2[k] += ((u2 - f2) * invdz) * dt_sub * irho;
+            R3[k] += ((u3 - f3) * invdz) * dt_sub * irho;
+          }
+          if (sp == 1) PF[k + 1] += f0;
+          if (k == kbot) flux_bot = f0;
+        }
+        carry0 = __shfl_sync(mask, f0, LANES - 1, LANES);
+        carry1 = __shfl_sync(mask, f1, LANES - 1, LANES);
+        if (nfield > 2) {
+          carry2 = __shfl_sync(mask, f2, LANES - 1, LANES);
+          carry3 = __shfl_sync(mask, f3, LANES - 1, LANES);
+        }
+      }
+      if (k_qxbot == kbot) {
+        const int owner = (kbot - k_qxtop) % LANES;
+        prt_accum += __shfl_sync(mask, flux_bot, owner, LANES) * dt_sub;
       } else {
-        /* FP32-bulk: fluxes in FP32; every difference and the state update in
-         * FP64 with one FP64 coefficient per level, so the flux leaving a cell
-         * is exactly the flux entering the next (column mass telescopes). */
-        float carry0 = 0, carry1 = 0, carry2 = 0, carry3 = 0, flux_bot = 0;
-        for (int base = k_qxtop; base <= k_temp; base += LANES) {
-          const int k = base + lane;
-          const bool act = k <= k_temp;
-          float f0 = 0, f1 = 0, f2 = 0, f3 = 0;
-          if (act) {
-            const float rho = float(RHO[k]);
-            const float v1 = float(V1[k]);
-            f0 = v1 * float(R0[k]) * rho;
-            if (nfield > 1) f1 = float(V2[k]) * float(R1[k]) * rho;
-            if (nfield > 2) {
-              f2 = v1 * float(R2[k]) * rho;
-              f3 = v1 * float(R3[k]) * rho;
-            }
-          }
-          float u0 = __shfl_up_sync(mask, f0, 1, LANES);
-          float u1 = __shfl_up_sync(mask, f1, 1, LANES);
-          float u2 = 0, u3 = 0;
-          if (nfield > 2) {
-            u2 = __shfl_up_sync(mask, f2, 1, LANES);
-            u3 = __shfl_up_sync(mask, f3, 1, LANES);
-          }
-          if (lane == 0) {
-            u0 = carry0; u1 = carry1; u2 = carry2; u3 = carry3;
-          }
-          if (act) {
-            const double coef = INVDZ[k] * dt_sub * INVRHO[k];
-            R0[k] += (double(u0) - double(f0)) * coef;
-            if (nfield > 1) R1[k] += (double(u1) - double(f1)) * coef;
-            if (nfield > 2) {
-              R2[k] += (double(u2) - double(f2)) * coef;
-              R3[k] += (double(u3) - double(f3)) * coef;
-            }
-            if (sp == 1) PF[k + 1] += double(f0);
-            if (k == kbot) flux_bot = f0;
-          }
-          carry0 = __shfl_sync(mask, f0, LANES - 1, LANES);
-          carry1 = __shfl_sync(mask, f1, LANES - 1, LANES);
-          if (nfield > 2) {
-            carry2 = __shfl_sync(mask, f2, LANES - 1, LANES);
-            carry3 = __shfl_sync(mask, f3, LANES - 1, LANES);
-          }
-        }
-        if (k_qxbot == kbot) {
-          const int owner = (kbot - k_qxtop) % LANES;
-          prt_accum += double(__shfl_sync(mask, flux_bot, owner, LANES)) * dt_sub;
-        } else {
-          k_qxbot += 1;
-        }
+        k_qxbot += 1;
       }
       dt_left -= dt_sub;
       first = false;
