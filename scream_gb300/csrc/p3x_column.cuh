@@ -908,12 +908,12 @@ __device__ void p3_sed(const Inst& in, const int col, const KParams<TR>& kp, con
 }
 
 /* K2 of the FP32-bulk form.  Same algorithm and order as p3_sed; fall
- * speeds, density, fall-speed factors and a float shadow of each species
- * field live in FP32 shared arrays, so a level costs no FP64 conversions
- * except those of the FP64 flux accumulation itself
- * (R += (double(F_in) - double(F_out)) * dt_sub / (dz rho)), which keeps
- * the column's mass telescoping exactly.  The shared slots of p3_sed are
- * reused: two float arrays share one double slot. */
+ * speeds, density, fall-speed factors, 1/dz and an FP32 shadow of each
+ * species field live in FP32 shared arrays, and the Courant maximum is taken
+ * in FP32, so a level's only FP64 work is the flux accumulation itself
+ * (R += (F_in - F_out) * dt_sub / (dz rho) with both fluxes as FP64), which
+ * keeps the column's mass telescoping exactly.  The shared slots of p3_sed
+ * are reused: two float arrays share one double slot. */
 template <int LANES>
 __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>& kp, const Tabs<float>& tb,
                             double* __restrict__ sm, uint32_t& err) {
@@ -933,7 +933,8 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
   float* const RHOf = reinterpret_cast<float*>(&SMA(B_RHO, 0));
   float* const FACf = RHOf + S;
   double* const COEF = &SMA(B_INVRHO, 0); /* 1 / (dz rho) */
-  double* const INVDZ = &SMA(B_INVDZ, 0);
+  float* const INVDZf = reinterpret_cast<float*>(&SMA(B_INVDZ, 0));
+  float* const COEFf = INVDZf + S;
   float* const R2f = reinterpret_cast<float*>(&SMA(B_FAC, 0));
   float* const R3f = R2f + S;
   double* const CLD = &SMA(B_CLD, 0);
@@ -949,9 +950,11 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
   for (int k = lane; k < nk; k += LANES) {
     const double rho = scr_at(in, S_RHO, col)[k];
     const double inv_dz = 1 / in.dz[co + k];
+    const double coef = inv_dz / rho;
     RHOf[k] = float(rho);
-    INVDZ[k] = inv_dz;
-    COEF[k] = inv_dz / rho;
+    INVDZf[k] = float(inv_dz);
+    COEF[k] = coef;
+    COEFf[k] = float(coef);
   }
   double precip_liq_surf = 0, precip_ice_surf = 0;
 
@@ -1002,7 +1005,7 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
         err |= kErrSubstep;
         break;
       }
-      double lmax = 0.0;
+      float lmax = 0.0f; /* max of V / dz; the Courant number is that times dt_left */
       for (int k = k_qxtop + lane; k <= k_qxbot; k += LANES) {
         float v1 = 0, v2 = 0;
         bool fall = false;
@@ -1159,13 +1162,13 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
         }
         V1f[k] = v1;
         V2f[k] = v2;
-        if (fall) lmax = vmax(lmax, double(v1) * dt_left * INVDZ[k]);
+        if (fall) lmax = vmax(lmax, v1 * INVDZf[k]);
       }
       if (k_qxbot < kbot && lane == (k_qxbot + 1 - k_qxtop) % LANES) {
         V1f[k_qxbot + 1] = 0; /* the cell receiving the leading edge has no fall speed */
         V2f[k_qxbot + 1] = 0;
       }
-      const double Co_max = group_max<LANES>(mask, lmax);
+      const double Co_max = double(group_max<LANES>(mask, lmax)) * dt_left;
       if (!(Co_max >= 0) || Co_max > 2.0e9) {
         err |= kErrNumeric;
         break;
@@ -1173,8 +1176,13 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
       const int tmpint1 = static_cast<int>(Co_max + 1);
       const double dt_sub = dt_left / tmpint1;
       const int k_temp = (k_qxbot == kbot) ? k_qxbot : k_qxbot + 1;
-      /* fluxes in FP32, every flux difference and state update in FP64 */
-      float carry0 = 0, carry1 = 0, carry2 = 0, carry3 = 0, flux_bot = 0;
+      /* Fluxes in FP32; each flux is converted to FP64 once and handed to the
+       * level below as a double, so every flux difference and state update is
+       * FP64 (the column's mass telescopes exactly).  The FP32 shadows follow
+       * with FP32 arithmetic. */
+      const float dt_sub_f = float(dt_sub);
+      double cd0 = 0, cd1 = 0, cd2 = 0, cd3 = 0;
+      float cf0 = 0, cf1 = 0, cf2 = 0, cf3 = 0, flux_bot = 0;
       for (int base = k_qxtop; base <= k_temp; base += LANES) {
         const int k = base + lane;
         const bool act = k <= k_temp;
@@ -1189,42 +1197,55 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
             f3 = v1 * R3f[k] * rho;
           }
         }
-        float u0 = __shfl_up_sync(mask, f0, 1, LANES);
-        float u1 = __shfl_up_sync(mask, f1, 1, LANES);
-        float u2 = 0, u3 = 0;
+        const double d0 = f0, d1 = nfield > 1 ? double(f1) : 0.0;
+        const double d2 = nfield > 2 ? double(f2) : 0.0, d3 = nfield > 2 ? double(f3) : 0.0;
+        double ud0 = __shfl_up_sync(mask, d0, 1, LANES);
+        float uf0 = __shfl_up_sync(mask, f0, 1, LANES);
+        double ud1 = 0, ud2 = 0, ud3 = 0;
+        float uf1 = 0, uf2 = 0, uf3 = 0;
+        if (nfield > 1) {
+          ud1 = __shfl_up_sync(mask, d1, 1, LANES);
+          uf1 = __shfl_up_sync(mask, f1, 1, LANES);
+        }
         if (nfield > 2) {
-          u2 = __shfl_up_sync(mask, f2, 1, LANES);
-          u3 = __shfl_up_sync(mask, f3, 1, LANES);
+          ud2 = __shfl_up_sync(mask, d2, 1, LANES);
+          ud3 = __shfl_up_sync(mask, d3, 1, LANES);
+          uf2 = __shfl_up_sync(mask, f2, 1, LANES);
+          uf3 = __shfl_up_sync(mask, f3, 1, LANES);
         }
         if (lane == 0) {
-          u0 = carry0; u1 = carry1; u2 = carry2; u3 = carry3;
+          ud0 = cd0; ud1 = cd1; ud2 = cd2; ud3 = cd3;
+          uf0 = cf0; uf1 = cf1; uf2 = cf2; uf3 = cf3;
         }
         if (act) {
           const double coef = COEF[k] * dt_sub;
-          const double r0 = R0[k] + (double(u0) - double(f0)) * coef;
-          R0[k] = r0;
-          R0f[k] = float(r0);
+          const float coef_f = COEFf[k] * dt_sub_f;
+          R0[k] += (ud0 - d0) * coef;
+          R0f[k] += (uf0 - f0) * coef_f;
           if (nfield > 1) {
-            const double r1 = R1[k] + (double(u1) - double(f1)) * coef;
-            R1[k] = r1;
-            R1f[k] = float(r1);
+            R1[k] += (ud1 - d1) * coef;
+            R1f[k] += (uf1 - f1) * coef_f;
           }
           if (nfield > 2) {
-            const double r2 = R2[k] + (double(u2) - double(f2)) * coef;
-            const double r3 = R3[k] + (double(u3) - double(f3)) * coef;
-            R2[k] = r2;
-            R3[k] = r3;
-            R2f[k] = float(r2);
-            R3f[k] = float(r3);
+            R2[k] += (ud2 - d2) * coef;
+            R3[k] += (ud3 - d3) * coef;
+            R2f[k] += (uf2 - f2) * coef_f;
+            R3f[k] += (uf3 - f3) * coef_f;
           }
-          if (sp == 1) PF[k + 1] += double(f0);
+          if (sp == 1) PF[k + 1] += d0;
           if (k == kbot) flux_bot = f0;
         }
-        carry0 = __shfl_sync(mask, f0, LANES - 1, LANES);
-        carry1 = __shfl_sync(mask, f1, LANES - 1, LANES);
+        cd0 = __shfl_sync(mask, d0, LANES - 1, LANES);
+        cf0 = __shfl_sync(mask, f0, LANES - 1, LANES);
+        if (nfield > 1) {
+          cd1 = __shfl_sync(mask, d1, LANES - 1, LANES);
+          cf1 = __shfl_sync(mask, f1, LANES - 1, LANES);
+        }
         if (nfield > 2) {
-          carry2 = __shfl_sync(mask, f2, LANES - 1, LANES);
-          carry3 = __shfl_sync(mask, f3, LANES - 1, LANES);
+          cd2 = __shfl_sync(mask, d2, LANES - 1, LANES);
+          cd3 = __shfl_sync(mask, d3, LANES - 1, LANES);
+          cf2 = __shfl_sync(mask, f2, LANES - 1, LANES);
+          cf3 = __shfl_sync(mask, f3, LANES - 1, LANES);
         }
       }
       if (k_qxbot == kbot) {
