@@ -212,6 +212,39 @@ int p3x_main_fixed_scratch(p3x_context* ctx, const p3x_runtime* rt, const p3x_pr
                            const p3x_infrastructure* infra, const p3x_history_only* hist, int32_t nj,
                            int32_t nk, const p3x_layout* layout, int32_t precision, void* stream);
 
+/* ------------------------------------------------------------------ */
+/* Process interface around the step (P3Microphysics pre/postamble)    */
+/* ------------------------------------------------------------------ */
+/* Host-model fields of the P3 atmosphere process
+ * (physics/p3/eamxx_p3_process_interface.hpp:63-353).  Device pointers;
+ * per-level fields are (ncol, nlev) with the layout's ld, per-column fields
+ * have ncol entries.  Per-column pointers may be NULL (skipped). */
+typedef struct p3x_interface_fields {
+  const double *pmid, *pseudo_density, *pseudo_density_dry, *cld_frac_t;
+  double* T_atm;                /* preamble: in; postamble: in/out          */
+  double* T_prev;               /* postamble: out                           */
+  double *precip_liq_surf_mass, /* per column, accumulated by the postamble */
+      *precip_ice_surf_mass;
+  double *vapor_flux, *water_flux, *ice_flux, *heat_flux; /* per column, out */
+} p3x_interface_fields;
+
+/* p3_preamble (eamxx_p3_process_interface.hpp:63-132): dz from the wet
+ * state, wet -> dry mixing ratios of the 9 prognostic species and qv_prev,
+ * inv_exner and th from T_atm and pmid, cloud fractions floored at 1e-4 and
+ * the rain fraction's maximum overlap with the level above.  Writes prog and
+ * din's dz, inv_exner, cld_frac_l/i/r and qv_prev (which must be writable). */
+int p3x_preamble(const p3x_interface_fields* f, const p3x_prognostic_state* prog,
+                 const p3x_diagnostic_inputs* din, int32_t nj, int32_t nk, const p3x_layout* layout,
+                 void* stream);
+
+/* p3_postamble (eamxx_p3_process_interface.hpp:200-269): T_atm from th with
+ * the dry/wet rescaled increment, T_prev, dry -> wet mixing ratios and
+ * qv_prev, effective radii in microns, surface precipitation mass
+ * accumulated over dt, and the mass/energy boundary fluxes. */
+int p3x_postamble(const p3x_interface_fields* f, const p3x_prognostic_state* prog,
+                  const p3x_diagnostic_inputs* din, const p3x_diagnostic_outputs* dout, int32_t nj,
+                  int32_t nk, const p3x_layout* layout, double dt, void* stream);
+
 /* Per-kernel timing of single-instance steps (no counterpart in the
  * reference, which times p3_main as a whole): while on, every p3x_main /
  * p3x_main_async records CUDA events around its three kernels (part1+part2,

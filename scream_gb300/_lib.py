@@ -82,6 +82,15 @@ class Layout(C.Structure):
     _fields_ = [("ld", C.c_int64), ("ld_int", C.c_int64)]
 
 
+HOST_MODEL_FIELDS = ["pmid", "pseudo_density", "pseudo_density_dry", "cld_frac_t", "T_atm", "T_prev",
+                    "precip_liq_surf_mass", "precip_ice_surf_mass", "vapor_flux", "water_flux", "ice_flux",
+                    "heat_flux"]
+
+
+class InterfaceFields(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in HOST_MODEL_FIELDS]
+
+
 class LaunchConfig(C.Structure):
     _fields_ = [("lanes_per_column", C.c_int32), ("columns_per_block", C.c_int32),
                 ("table_staging", C.c_int32), ("blocks_per_sm", C.c_int32)]
@@ -149,6 +158,11 @@ PROTOTYPES = {
     "p3x_autotune_batch": (C.c_int, [_V, _V, _I, C.POINTER(LaunchConfig), C.POINTER(C.c_double)]),
     "p3x_workload_generate": (C.c_int, [_I, C.c_uint64, _I, _I, _I, C.POINTER(_V), C.c_int64]),
     "p3x_column_budgets": (C.c_int, [C.POINTER(PrognosticState), _V, _V, _I, _I, C.c_int64, _V, _V, _V]),
+    "p3x_preamble": (C.c_int, [C.POINTER(InterfaceFields), C.POINTER(PrognosticState),
+                               C.POINTER(DiagnosticInputs), _I, _I, C.POINTER(Layout), _V]),
+    "p3x_postamble": (C.c_int, [C.POINTER(InterfaceFields), C.POINTER(PrognosticState),
+                                C.POINTER(DiagnosticInputs), C.POINTER(DiagnosticOutputs), _I, _I,
+                                C.POINTER(Layout), C.c_double, _V]),
     "p3x_server_create": (C.c_int, [_V, C.POINTER(Runtime), C.c_int64, _I, C.POINTER(_V)]),
     "p3x_server_destroy": (C.c_int, [_V]),
     "p3x_server_submit": (C.c_int, [_V, C.c_int64, _I, _I, _I, _I, C.c_uint64, C.c_double, C.c_double]),

@@ -664,6 +664,68 @@ int p3x_main_f(double* qc, double* nc, double* qr, double* nr, double* th_atm, d
 }
 
 /* ------------------------------------------------------------------ */
+/* process interface pre/postamble                                    */
+/* ------------------------------------------------------------------ */
+static int interface_ptrs(const p3x_interface_fields* f, const p3x_prognostic_state* prog,
+                          const p3x_diagnostic_inputs* din, const p3x_diagnostic_outputs* dout, bool post,
+                          p3x::InterfacePtrs& p) {
+  if (!f || !prog || !din) return P3X_EINVAL;
+  if (!f->pmid || !f->pseudo_density || !f->pseudo_density_dry || !f->T_atm) return P3X_EINVAL;
+  p = p3x::InterfacePtrs{};
+  p.pmid = f->pmid; p.pd = f->pseudo_density; p.pdd = f->pseudo_density_dry; p.cld_t = f->cld_frac_t;
+  p.T = f->T_atm; p.T_prev = f->T_prev;
+  double* q[9] = {prog->qc, prog->nc, prog->qr, prog->nr, prog->qi, prog->ni, prog->qm, prog->bm, prog->qv};
+  for (int s = 0; s < 9; ++s) {
+    if (!q[s]) return P3X_EINVAL;
+    p.q[s] = q[s];
+  }
+  p.th = prog->th;
+  p.qv_prev = const_cast<double*>(din->qv_prev);
+  if (!p.th || !p.qv_prev) return P3X_EINVAL;
+  if (!post) {
+    if (!f->cld_frac_t || !din->inv_exner || !din->dz || !din->cld_frac_l || !din->cld_frac_i || !din->cld_frac_r)
+      return P3X_EINVAL;
+    p.inv_exner = const_cast<double*>(din->inv_exner);
+    p.dz = const_cast<double*>(din->dz);
+    p.cld_l = const_cast<double*>(din->cld_frac_l);
+    p.cld_i = const_cast<double*>(din->cld_frac_i);
+    p.cld_r = const_cast<double*>(din->cld_frac_r);
+  } else {
+    if (!dout || !f->T_prev || !dout->diag_eff_radius_qc || !dout->diag_eff_radius_qi || !dout->diag_eff_radius_qr ||
+        !dout->precip_liq_surf || !dout->precip_ice_surf)
+      return P3X_EINVAL;
+    p.eff_qc = dout->diag_eff_radius_qc; p.eff_qi = dout->diag_eff_radius_qi; p.eff_qr = dout->diag_eff_radius_qr;
+    p.liq_surf = dout->precip_liq_surf; p.ice_surf = dout->precip_ice_surf;
+    p.liq_mass = f->precip_liq_surf_mass; p.ice_mass = f->precip_ice_surf_mass;
+    p.vapor_flux = f->vapor_flux; p.water_flux = f->water_flux; p.ice_flux = f->ice_flux; p.heat_flux = f->heat_flux;
+  }
+  return P3X_OK;
+}
+
+int p3x_preamble(const p3x_interface_fields* f, const p3x_prognostic_state* prog, const p3x_diagnostic_inputs* din,
+                 int32_t nj, int32_t nk, const p3x_layout* layout, void* stream) {
+  if (nj < 0 || nk <= 0) return P3X_EINVAL;
+  p3x::InterfacePtrs p;
+  const int st = interface_ptrs(f, prog, din, nullptr, false, p);
+  if (st) return st;
+  const int64_t ld = (layout && layout->ld > 0) ? layout->ld : nk;
+  if (ld < nk) return P3X_EINVAL;
+  return cuda_status(p3x::launch_interface(p, nj, nk, ld, false, 0.0, static_cast<cudaStream_t>(stream)));
+}
+
+int p3x_postamble(const p3x_interface_fields* f, const p3x_prognostic_state* prog, const p3x_diagnostic_inputs* din,
+                  const p3x_diagnostic_outputs* dout, int32_t nj, int32_t nk, const p3x_layout* layout, double dt,
+                  void* stream) {
+  if (nj < 0 || nk <= 0 || !(dt > 0)) return P3X_EINVAL;
+  p3x::InterfacePtrs p;
+  const int st = interface_ptrs(f, prog, din, dout, true, p);
+  if (st) return st;
+  const int64_t ld = (layout && layout->ld > 0) ? layout->ld : nk;
+  if (ld < nk) return P3X_EINVAL;
+  return cuda_status(p3x::launch_interface(p, nj, nk, ld, true, dt, static_cast<cudaStream_t>(stream)));
+}
+
+/* ------------------------------------------------------------------ */
 /* workload / budgets                                                  */
 /* ------------------------------------------------------------------ */
 int p3x_workload_generate(int32_t kind, uint64_t seed, int32_t col0, int32_t ncol, int32_t nlev,

@@ -68,6 +68,19 @@ int launch_work(p3x_context* ctx, const p3x_runtime& rt, int precision, const de
  * qv_prev <- qv and t_prev <- th / inv_exner, for every work item. */
 cudaError_t launch_postamble(const dev::Inst* insts_d, const dev::WorkItem* work_d, int nwork, cudaStream_t st);
 
+/* Device pointers of the process-interface pre/postamble kernels. */
+struct InterfacePtrs {
+  const double *pmid, *pd, *pdd, *cld_t;
+  double *T, *T_prev;
+  double* q[9]; /* qc nc qr nr qi qm ni bm qv */
+  double *th, *qv_prev, *inv_exner, *dz, *cld_l, *cld_i, *cld_r;
+  double *eff_qc, *eff_qi, *eff_qr;
+  const double *liq_surf, *ice_surf;
+  double *liq_mass, *ice_mass, *vapor_flux, *water_flux, *ice_flux, *heat_flux;
+};
+cudaError_t launch_interface(const InterfacePtrs& p, int ncol, int nlev, int64_t ld, bool post, double dt,
+                             cudaStream_t st);
+
 cudaError_t launch_budgets(const double* qv, const double* qc, const double* qr, const double* qi,
                            const double* th, const double* dpres, const double* inv_exner, int ncol,
                            int nlev, int64_t ld, double* water, double* energy, cudaStream_t st);

@@ -166,6 +166,30 @@ class P3Context:
         L.check("p3x_main_async", rc)
         return 0.0
 
+    def _interface(self, host_fields: Dict[str, "torch.Tensor"]):
+        return L.InterfaceFields(*[(_ptr(host_fields[n]) if host_fields.get(n) is not None else None)
+                                   for n in L.HOST_MODEL_FIELDS])
+
+    def preamble(self, host_fields: Dict[str, "torch.Tensor"], f: P3Fields, stream=None):
+        """P3Microphysics preamble on the device: host-model fields (pmid,
+        pseudo_density(_dry), cld_frac_t, T_atm) and wet mixing ratios in ``f``
+        -> P3 inputs in ``f`` (dry mixing ratios, th, inv_exner, dz, cloud
+        fractions, dry qv_prev)."""
+        itf = self._interface(host_fields)
+        L.check("p3x_preamble", self.lib.p3x_preamble(C.byref(itf), C.byref(f.prog()), C.byref(f.din()), f.ncol,
+                                                      f.nlev, C.byref(L.Layout(f.nlev, f.nlev + 1)),
+                                                      _stream_handle(stream)))
+
+    def postamble(self, host_fields: Dict[str, "torch.Tensor"], f: P3Fields, dt: float, stream=None):
+        """P3Microphysics postamble on the device (T_atm, T_prev, wet mixing
+        ratios, qv_prev, effective radii in microns, precipitation mass,
+        boundary fluxes)."""
+        itf = self._interface(host_fields)
+        L.check("p3x_postamble", self.lib.p3x_postamble(C.byref(itf), C.byref(f.prog()), C.byref(f.din()),
+                                                        C.byref(f.dout()), f.ncol, f.nlev,
+                                                        C.byref(L.Layout(f.nlev, f.nlev + 1)), float(dt),
+                                                        _stream_handle(stream)))
+
     def set_kernel_timing(self, on: bool = True):
         L.check("p3x_set_kernel_timing", self.lib.p3x_set_kernel_timing(self.h, int(bool(on))))
 
@@ -325,6 +349,17 @@ class P3Microphysics:
         self.it += 1
         return self.ctx.p3_main(self.fields, dt, self.precision, self.runtime, self.predictNc,
                                 self.prescribedCCN, self.it, stream)
+
+    def run_process(self, host_fields, dt: float, stream=None) -> float:
+        """One atmosphere-process step as run_impl does it
+        (eamxx_p3_run.cpp:5-45): preamble (wet -> dry, th, dz, cloud
+        fractions), p3_main, postamble (T_atm, T_prev, dry -> wet, qv_prev,
+        radii, precipitation mass, boundary fluxes).  ``host_fields`` holds the
+        host model's device tensors named as in p3x_interface_fields."""
+        self.ctx.preamble(host_fields, self.fields, stream)
+        us = self.run(dt, stream)
+        self.ctx.postamble(host_fields, self.fields, dt, stream)
+        return us
 
     def finalize(self):
         if self.ctx is not None:

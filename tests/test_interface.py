@@ -1,0 +1,122 @@
+"""P3Microphysics pre/postamble (p3x_preamble / p3x_postamble) against a
+NumPy restatement of the reference's formulas
+(physics/p3/eamxx_p3_process_interface.hpp:63-269 and
+share/util/scream_common_physics_functions_impl.hpp:88-426)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+RD, G, EP2, P0, CP = 287.042, 9.80616, 18.016 / 28.966, 100000.0, 1004.64
+SPECIES = ["qc", "nc", "qr", "nr", "qi", "ni", "qm", "bm", "qv"]
+
+
+def np_preamble(h, s):
+    out = {k: v.copy() for k, v in s.items()}
+    c1 = -1.0 + 1.0 / EP2
+    out["dz"] = (RD / G) * h["pseudo_density"] * (h["T_atm"] * (1.0 + c1 * s["qv"])) / h["pmid"]
+    for n in SPECIES + ["qv_prev"]:
+        out[n] = s[n] * h["pseudo_density"] / h["pseudo_density_dry"]
+    exner = (h["pmid"] / P0) ** (RD * (1.0 / CP))
+    out["inv_exner"] = 1.0 / exner
+    out["th"] = h["T_atm"] / exner
+    cl = np.maximum(h["cld_frac_t"], 1e-4)
+    out["cld_frac_l"] = cl
+    out["cld_frac_i"] = cl.copy()
+    cr = cl.copy()
+    cr[:, 1:] = np.where(h["cld_frac_t"][:, :-1] > cr[:, 1:], h["cld_frac_t"][:, :-1], cr[:, 1:])
+    out["cld_frac_r"] = cr
+    return out
+
+
+def np_postamble(h, s, dt):
+    hh = {k: v.copy() for k, v in h.items()}
+    out = {k: v.copy() for k, v in s.items()}
+    exner = (h["pmid"] / P0) ** (RD * (1.0 / CP))
+    T = (s["th"] * exner - h["T_atm"]) * h["pseudo_density_dry"] / h["pseudo_density"]
+    T = T + h["T_atm"]
+    hh["T_atm"], hh["T_prev"] = T, T.copy()
+    for n in SPECIES:
+        out[n] = s[n] * h["pseudo_density_dry"] / h["pseudo_density"]
+    out["qv_prev"] = out["qv"].copy()
+    for n in ["diag_eff_radius_qc", "diag_eff_radius_qi", "diag_eff_radius_qr"]:
+        out[n] = s[n] * 1e6
+    liq, ice = s["precip_liq_surf"], s["precip_ice_surf"]
+    hh["precip_liq_surf_mass"] = h["precip_liq_surf_mass"] + liq * 1000.0 * dt
+    hh["precip_ice_surf_mass"] = h["precip_ice_surf_mass"] + ice * 1000.0 * dt
+    hh["vapor_flux"] = np.zeros_like(liq)
+    hh["water_flux"] = liq + ice
+    hh["ice_flux"] = ice.copy()
+    hh["heat_flux"] = np.zeros_like(liq)
+    return hh, out
+
+
+def test_interface_rejects_bad_arguments(built):
+    from scream_gb300 import _lib as L
+    lib = L.load()
+    f = L.InterfaceFields()
+    prog, din, dout = L.PrognosticState(), L.DiagnosticInputs(), L.DiagnosticOutputs()
+    assert lib.p3x_preamble(None, C.byref(prog), C.byref(din), 4, 8, None, None) == L.P3X_EINVAL
+    assert lib.p3x_preamble(C.byref(f), C.byref(prog), C.byref(din), 4, 8, None, None) == L.P3X_EINVAL
+    assert lib.p3x_postamble(C.byref(f), C.byref(prog), C.byref(din), C.byref(dout), 4, 8, None, 0.0,
+                             None) == L.P3X_EINVAL
+
+
+def _host_state(ncol, nlev, seed):
+    import scream_gb300 as p3
+    inp = p3.generate_inputs(0, seed, ncol, nlev)
+    rng = np.random.default_rng(seed)
+    pdd = inp["dpres"]
+    h = {"pmid": inp["pres"], "pseudo_density_dry": pdd, "pseudo_density": pdd * (1.0 + inp["qv"]),
+         "cld_frac_t": rng.uniform(0.0, 1.0, (ncol, nlev)) * (rng.random((ncol, nlev)) < 0.6),
+         "T_atm": inp["th"] / inp["inv_exner"], "T_prev": np.zeros((ncol, nlev)),
+         "precip_liq_surf_mass": rng.uniform(0, 1, ncol), "precip_ice_surf_mass": rng.uniform(0, 1, ncol),
+         "vapor_flux": np.full(ncol, 7.0), "water_flux": np.zeros(ncol), "ice_flux": np.zeros(ncol),
+         "heat_flux": np.full(ncol, 7.0)}
+    return inp, h
+
+
+@pytest.mark.gpu
+def test_preamble_and_postamble_match_numpy(gpu_ctx):
+    import torch
+    import scream_gb300 as p3
+    ncol, nlev, dt = 300, 72, 300.0
+    inp, h = _host_state(ncol, nlev, 2024)
+    f = p3.P3Fields.from_inputs(inp)
+    hd = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in h.items()}
+    gpu_ctx.preamble(hd, f)
+    torch.cuda.synchronize()
+    got = f.to_host()
+    exp = np_preamble(h, {k: v.copy() for k, v in inp.items()})
+    for n in SPECIES + ["qv_prev", "dz", "inv_exner", "th", "cld_frac_l", "cld_frac_i", "cld_frac_r"]:
+        np.testing.assert_allclose(got[n], exp[n], rtol=1e-15, atol=0, err_msg=n)
+
+    # postamble on a state with outputs (one P3 step in between)
+    gpu_ctx.p3_main(f, dt, p3.P3X_FP64)
+    s = f.to_host()
+    hh_exp, out_exp = np_postamble(h, s, dt)
+    gpu_ctx.postamble(hd, f, dt)
+    torch.cuda.synchronize()
+    got = f.to_host()
+    for n in SPECIES + ["qv_prev", "diag_eff_radius_qc", "diag_eff_radius_qi", "diag_eff_radius_qr"]:
+        np.testing.assert_allclose(got[n], out_exp[n], rtol=1e-15, atol=0, err_msg=n)
+    for n in ["T_atm", "T_prev", "precip_liq_surf_mass", "precip_ice_surf_mass", "vapor_flux", "water_flux",
+              "ice_flux", "heat_flux"]:
+        np.testing.assert_allclose(hd[n].cpu().numpy(), hh_exp[n], rtol=1e-15, atol=0, err_msg=n)
+
+
+@pytest.mark.gpu
+def test_preamble_then_postamble_restores_the_wet_state(gpu_ctx):
+    import torch
+    import scream_gb300 as p3
+    ncol, nlev = 128, 128
+    inp, h = _host_state(ncol, nlev, 77)
+    f = p3.P3Fields.from_inputs(inp)
+    hd = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in h.items()}
+    gpu_ctx.preamble(hd, f)
+    gpu_ctx.postamble(hd, f, 300.0)
+    torch.cuda.synchronize()
+    got = f.to_host()
+    for n in SPECIES:
+        np.testing.assert_allclose(got[n], inp[n], rtol=1e-15, atol=0, err_msg=n)
+    np.testing.assert_allclose(hd["T_atm"].cpu().numpy(), h["T_atm"], rtol=1e-15, err_msg="T_atm")
