@@ -21,7 +21,7 @@
  * Splitting lets each kernel keep its own register and shared-memory
  * footprint: part2's ~45 rates no longer limit the occupancy of the
  * latency-bound sedimentation walk.  Per-level temporaries of a phase live
- * in shared memory (8 FP64 arrays per column in K1, 11 in K2).  Lookup
+ * in shared memory (9 FP64 arrays per column in K1, 11 in K2).  Lookup
  * tables are read from global memory (L1/L2) or, in K1, staged into shared
  * memory once per CTA with cp.async.bulk + mbarrier (Table3 slices for the
  * runtime's constant rain shape parameter, plus the whole ice table).
@@ -83,7 +83,7 @@ constexpr long long kWaitSpinLimit = 1ll << 26;
 constexpr uint64_t kWaitNanosLimit = 2000000000ull; /* 2 s */
 
 /* shared arrays of one column group in K1 */
-enum { A_TATM = 0, A_RHO, A_RHOFACR, A_RHOFACI, A_ACN, A_QVSL, A_QVSI, A_QVSSI, A_NARR };
+enum { A_TATM = 0, A_RHO, A_RHOFACR, A_RHOFACI, A_ACN, A_QVSL, A_QVSI, A_QVSSI, A_INVP, A_NARR };
 /* shared arrays of one column group in K2; FAC is the fall-speed factor of
  * the species being sedimented (acn, rhofacr or rhofaci), the rain flux
  * accumulator re-uses R2 (rain has two fields) */
@@ -271,6 +271,7 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
       rho = dpres / (dz * C::gravit);
       inv_rho = double(1.0f / float(rho));
       const double inv_p = 1 / vmax(pres, 1.e-3);
+      SMA(A_INVP, k) = inv_p;
       qvsl = C::ep_2 * svp_tabulated(rt.svp_tab, T, false, err) * inv_p;
       qvsi = C::ep_2 * svp_tabulated(rt.svp_tab, T, true, err) * inv_p;
       qvssi = double(float(qv) / float(qvsi) - 1.0f);
@@ -461,7 +462,7 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
       }
       const TR qi_r = TR(inc.qi), qc_r = TR(inc.qc), ni_r = TR(inc.ni), nc_r = TR(inc.nc), qr_r = TR(inc.qr);
       const double dT0 = T - C::Tmelt;
-      const double dqv0 = C::ep_2 * esat0 / vmax(pres, 1.e-3) - s.qv;
+      const double dqv0 = kF64 ? C::ep_2 * esat0 / vmax(pres, 1.e-3) - s.qv : C::ep_2 * esat0 * SMA(A_INVP, k) - s.qv;
       if (do_ice) {
         ice_cldliq_collection<TR>(rho_r, T, rhofaci_r, tv_qc2qi, qi_r, qc_r, ni_r, nc_r, r, rt);
         ice_rain_collection<TR>(rho_r, T, rhofaci_r, logn0r, tv_nr, tv_qr2qi, qi_r, ni_r, qr_r, r, rt);
@@ -512,7 +513,7 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
         }
       } else {
         evaporate_rain_bulk(inc.qr, inc.qc, inc.nr, inc.qi, cld_l, cld_r, s.qv, in.qv_prev[o], qvsl, qvsi, v.ab,
-                            v.abi, epsr, epsi_tot, T, in.t_prev[o], v.dqsdt, dt, r.qr2qv_evap_tend,
+                            v.abi, epsr, epsi_tot, T, in.t_prev[o], v.dqsdt, dt, inv_dt, r.qr2qv_evap_tend,
                             r.nr_evap_tend);
         if (do_ice) {
           ice_deposition_sublimation_bulk(inc.qi, inc.ni, T, qvsl, qvsi, epsi, v.abi, s.qv, inv_dt,
@@ -546,7 +547,7 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
       const int nlim = number_conservation<float>(float(s.nc), float(s.nr), float(s.ni), dtf, r);
       const Rates<float> r_lim = r;
       ice_supersat_conservation_bulk(r, cld_i, s.qv, qvsi, T, dt);
-      prevent_liq_supersaturation_bulk(pres, T, s.qv, dt, r, rt, err);
+      prevent_liq_supersaturation_bulk(SMA(A_INVP, k), T, s.qv, dt, r, rt, err);
       update_prognostics_bulk(r, inv_exner, predictNc, prescribedCCN, wet, dt, rho_qm_cloud, inv_rho, wlim, nlim,
                               r_lim, s);
     }

@@ -851,13 +851,12 @@ __device__ __forceinline__ void evaporate_rain_bulk(double qr_incld, double qc_i
                                                     double qv, double qv_prev, double qv_sat_l, double qv_sat_i,
                                                     float ab, float abi, float epsr, float epsi_tot,
                                                     double t_atm, double t_atm_prev, float dqsdt, double dt,
-                                                    float& qr2qv_evap_tend, float& nr_evap_tend) {
+                                                    double inv_dt_d, float& qr2qv_evap_tend, float& nr_evap_tend) {
   qr2qv_evap_tend = 0;
   nr_evap_tend = 0;
   const double ssat_r_d = qv - qv_sat_l;
   const double cld_frac = ((qc_incld + qi_incld) < 1.e-6) ? 0.0 : cld_frac_l;
   if (qr_incld >= C::QSMALL && ssat_r_d < 0 && cld_frac_r > cld_frac) {
-    const double inv_dt_d = 1 / dt;
     const float inv_dt = float(inv_dt_d), dtf = float(dt);
     const float ssat_r = float(ssat_r_d);
     const float tau_r = 1.0f / epsr;
@@ -874,7 +873,7 @@ __device__ __forceinline__ void evaporate_rain_bulk(double qr_incld, double qc_i
     if (eps_eff < 1e-20f) eps_eff = 1e-20f;
     const float tau_eff = 1.0f / eps_eff;
     float evap;
-    if (qr_incld < 1e-12 && qv / qv_sat_l < 0.999) {
+    if (qr_incld < 1e-12 && qv < 0.999 * qv_sat_l) {
       evap = float(qr_incld) * inv_dt;
     } else {
       const float dt_over_tau = dtf / tau_eff;
@@ -888,9 +887,9 @@ __device__ __forceinline__ void evaporate_rain_bulk(double qr_incld, double qc_i
     if (evap < 0.0f) evap = 0.0f;
     const float qlim = float(qr_incld) * inv_dt;
     if (evap > qlim) evap = qlim;
-    evap = evap * float((cld_frac_r - cld_frac) / cld_frac_r);
+    evap = evap * (float(cld_frac_r - cld_frac) / float(cld_frac_r));
     qr2qv_evap_tend = evap;
-    nr_evap_tend = evap * float(nr_incld / qr_incld);
+    nr_evap_tend = evap * (float(nr_incld) / float(qr_incld));
   }
 }
 
@@ -909,7 +908,7 @@ __device__ __forceinline__ void ice_deposition_sublimation_bulk(double qi_incld,
     const bool neg = qi_tend < 0;
     if (neg) {
       sublim = -qi_tend;
-      ni_sublim = sublim * float(ni_incld / qi_incld);
+      ni_sublim = sublim * (float(ni_incld) / float(qi_incld));
     }
     const bool T_lt_frz = T_atm < C::T_zerodegc;
     if (T_lt_frz && !neg) vapdep = qi_tend;
@@ -1092,7 +1091,7 @@ __device__ __forceinline__ void ice_supersat_conservation_bulk(Rates<float>& r, 
   }
 }
 
-__device__ __forceinline__ bool prevent_liq_supersaturation_bulk(double pres, double t_atm, double qv, double dt,
+__device__ __forceinline__ bool prevent_liq_supersaturation_bulk(double inv_p, double t_atm, double qv, double dt,
                                                                  Rates<float>& r, const RuntimeDev& rt,
                                                                  uint32_t& err) {
   const float qv_sources = r.qi2qv_sublim_tend + r.qr2qv_evap_tend;
@@ -1101,7 +1100,7 @@ __device__ __forceinline__ bool prevent_liq_supersaturation_bulk(double pres, do
   const float qv_sinks = r.qv2qi_vapdep_tend + r.qv2qi_nucleat_tend;
   constexpr float lvs = float((C::LatVap + C::LatIce) * C::INV_CP), lv = float(C::LatVap * C::INV_CP);
   const double T_endstep = t_atm + double(((qv_sinks - r.qi2qv_sublim_tend) * lvs - r.qr2qv_evap_tend * lv) * dtf);
-  const double qsl = qv_sat_dry<float>(T_endstep, pres, false, rt, err);
+  const double qsl = C::ep_2 * svp_tabulated(rt.svp_tab, T_endstep, false, err) * inv_p; /* inv_p = 1 / max(p, 1e-3) */
   const float te = float(T_endstep);
   const float A = float(C::LatVap * C::INV_CP / C::RV) * float(qsl) * dtf / (te * te) *
                   (float(C::LatVap + C::LatIce) * r.qi2qv_sublim_tend + float(C::LatVap) * r.qr2qv_evap_tend);
