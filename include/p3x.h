@@ -245,6 +245,12 @@ int p3x_postamble(const p3x_interface_fields* f, const p3x_prognostic_state* pro
                   const p3x_diagnostic_inputs* din, const p3x_diagnostic_outputs* dout, int32_t nj,
                   int32_t nk, const p3x_layout* layout, double dt, void* stream);
 
+/* Device self-test of numeric building blocks (no counterpart in the
+ * reference): compares the FP32-bulk form's integer-pipe float -> double
+ * conversion with the hardware conversion for all 2^32 float bit patterns;
+ * *mismatches receives the number that differ (0 expected). */
+int p3x_selftest(uint64_t* mismatches);
+
 /* Per-kernel timing of single-instance steps (no counterpart in the
  * reference, which times p3_main as a whole): while on, every p3x_main /
  * p3x_main_async records CUDA events around its three kernels (part1+part2,

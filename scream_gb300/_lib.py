@@ -130,6 +130,7 @@ PROTOTYPES = {
     "p3x_tables_generate": (C.c_int, [C.c_char_p, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "p3x_saturation_table": (C.c_int, [_dp, C.POINTER(C.c_int32), _dp, _dp]),
     "p3x_set_kernel_timing": (C.c_int, [_V, _I]),
+    "p3x_selftest": (C.c_int, [C.POINTER(C.c_uint64)]),
     "p3x_kernel_times": (C.c_int, [_V, C.POINTER(C.c_float)]),
     "p3x_main": (C.c_int, [_V, C.POINTER(Runtime), C.POINTER(PrognosticState),
                            C.POINTER(DiagnosticInputs), C.POINTER(DiagnosticOutputs),

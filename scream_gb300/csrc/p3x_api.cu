@@ -515,6 +515,20 @@ int p3x_main_async(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic
   return launch_single(ctx, rt, in, static_cast<cudaStream_t>(stream));
 }
 
+int p3x_selftest(uint64_t* mismatches) {
+  if (!mismatches) return P3X_EINVAL;
+  unsigned long long* d = nullptr;
+  P3X_CUDA(cudaMalloc(&d, sizeof(*d)));
+  cudaError_t e = cudaMemset(d, 0, sizeof(*d));
+  if (e == cudaSuccess) e = launch_selftest(d, nullptr);
+  unsigned long long h = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_status(e);
+  *mismatches = uint64_t(h);
+  return P3X_OK;
+}
+
 int p3x_set_kernel_timing(p3x_context* ctx, int32_t on) {
   if (!ctx) return P3X_EINVAL;
   if (on && !ctx->kev[0])

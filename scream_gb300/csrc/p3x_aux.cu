@@ -174,6 +174,24 @@ cudaError_t launch_postamble(const dev::Inst* insts_d, const dev::WorkItem* work
   return cudaGetLastError();
 }
 
+/* Exhaustive check of the integer-pipe float -> double conversion against
+ * the hardware conversion: every one of the 2^32 float bit patterns. */
+__global__ void f2d_selftest_kernel(unsigned long long* mismatches) {
+  unsigned long long bad = 0;
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < (uint64_t(1) << 32); i += stride) {
+    const float x = __uint_as_float(uint32_t(i));
+    const double a = dev::f2d(x), b = double(x);
+    if (__double_as_longlong(a) != __double_as_longlong(b)) ++bad;
+  }
+  if (bad) atomicAdd(mismatches, bad);
+}
+
+cudaError_t launch_selftest(unsigned long long* mismatches_d, cudaStream_t st) {
+  f2d_selftest_kernel<<<4096, 256, 0, st>>>(mismatches_d);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_transpose_to_levels(const double* src, double* dst, int ncol, int nlev, int64_t ld,
                                        cudaStream_t st) {
   if (ncol <= 0 || nlev <= 0) return cudaSuccess;

@@ -265,11 +265,13 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
       qvssi = qv / qvsi - 1;
       ccn_nc = rt.spa_ccn_to_nc_factor * in.nccn[o] / inv_cld_l;
     } else {
-      /* FP32-bulk: the same quantities with one FP64 division each for rho
-       * and for the pressure shared by both saturation ratios; 1/rho and the
-       * supersaturation ratio (threshold and rate inputs) in FP32 */
-      rho = dpres / (dz * C::gravit);
-      inv_rho = double(1.0f / float(rho));
+      /* FP32-bulk: rho and 1/rho only feed rates, fall speeds and fluxes
+       * (the sedimentation's FP64 coefficient is g / dpres), so they are
+       * FP32; one FP64 division for the pressure shared by both saturation
+       * ratios; the supersaturation ratio (threshold and rate input) in FP32 */
+      const float rho_f = float(dpres) / (float(dz) * float(C::gravit));
+      rho = rho_f;
+      inv_rho = double(1.0f / rho_f);
       const double inv_p = 1 / vmax(pres, 1.e-3);
       SMA(A_INVP, k) = inv_p;
       qvsl = C::ep_2 * svp_tabulated(rt.svp_tab, T, false, err) * inv_p;
@@ -948,12 +950,12 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
   double* const R2 = &SMA(B_R2, 0);
   double* const R3 = &SMA(B_R3, 0);
   double* const PF = R2; /* rain flux accumulator (rain has two fields) */
+  /* 1 / (dz rho) = g / dpres: one FP64 division per level, and the mass
+   * update is then exactly (F_in - F_out) dt g / dpres */
   for (int k = lane; k < nk; k += LANES) {
-    const double rho = scr_at(in, S_RHO, col)[k];
-    const double inv_dz = 1 / in.dz[co + k];
-    const double coef = inv_dz / rho;
-    RHOf[k] = float(rho);
-    INVDZf[k] = float(inv_dz);
+    const double coef = C::gravit / in.dpres[co + k];
+    RHOf[k] = float(scr_at(in, S_RHO, col)[k]);
+    INVDZf[k] = 1.0f / float(in.dz[co + k]);
     COEF[k] = coef;
     COEFf[k] = float(coef);
   }
@@ -1010,155 +1012,107 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
       for (int k = k_qxtop + lane; k <= k_qxbot; k += LANES) {
         float v1 = 0, v2 = 0;
         bool fall = false;
-        if (first) {
-          /* first substep: the in-cloud values with the reference's
-           * thresholds and limits, in FP64 (as p3_sed) */
-          const double cld = CLD[k];
-          const double inv_cld = 1 / cld;
-          if (sp == 0) {
-            double qc_incld = 0, nc_incld = 0;
+        /* In-cloud values in FP32.  The first substep applies the reference's
+         * thresholds and limits (and the bm quirk: bm_incld uses 1/cld_frac_l);
+         * the FP64 state is rewritten wherever a limiter made an in-cloud value
+         * differ from the plain one. */
+        const double cld = CLD[k];
+        const float icf = 1.0f / float(cld);
+        if (sp == 0) {
+          const float n_plain = R1f[k] * icf;
+          float qc_f = R0f[k] * icf, n_in = n_plain;
+          if (first) {
             if (R0[k] >= C::QSMALL) {
-              qc_incld = R0[k] * inv_cld;
-              nc_incld = vmax(R1[k] * inv_cld, 0.);
+              n_in = vmax(n_in, 0.0f);
+            } else {
+              qc_f = 0;
+              n_in = 0;
             }
-            qc_incld = vmin(qc_incld, C::incloud_limit);
-            if (qc_incld > C::QSMALL) {
-              float mu_c, lamc;
-              const float n_in = float(nc_incld);
-              float n_out = n_in;
-              get_cloud_dsd2<float>(float(qc_incld), n_out, mu_c, RHOf[k], lamc);
-              if (n_out != n_in) {
-                R1[k] = double(n_out) * cld;
-                R1f[k] = float(R1[k]);
-              }
-              const float dum = 1.0f / (lamc * lamc);
-              v1 = FACf[k] * ((5.0f + mu_c) * (4.0f + mu_c)) * dum;
-              if (predictNc) v2 = FACf[k] * ((2.0f + mu_c) * (1.0f + mu_c)) * dum;
-              fall = true;
-            }
-          } else if (sp == 1) {
-            double qr_incld = 0, nr_incld = 0;
-            if (R0[k] >= C::QSMALL) {
-              qr_incld = R0[k] * inv_cld;
-              nr_incld = vmax(R1[k] * inv_cld, 0.);
-            }
-            qr_incld = vmin(qr_incld, C::precip_limit);
-            if (qr_incld > C::QSMALL) {
-              float mu_r = 0, lamr;
-              const float n_in = float(nr_incld);
-              float n_out = n_in;
-              get_rain_dsd2<float>(float(qr_incld), n_out, mu_r, lamr, rt);
-              Table3<float> t3;
-              lookup3<float>(mu_r, lamr, rt, t3);
-              v1 = apply_table3<float>(tb, tb.vm, t3) * FACf[k];
-              v2 = apply_table3<float>(tb, tb.vn, t3) * FACf[k];
-              if (n_out != n_in) {
-                R1[k] = double(n_out) * cld;
-                R1f[k] = float(R1[k]);
-              }
-              fall = true;
-            }
-          } else {
-            double qi_incld = 0, ni_incld = 0, qm_incld = 0, bm_incld = 0;
-            if (R0[k] >= C::QSMALL) {
-              qi_incld = R0[k] * inv_cld;
-              ni_incld = vmax(R1[k] * inv_cld, 0.);
-            }
-            if (R0[k] >= C::QSMALL && R2[k] >= C::QSMALL) {
-              qm_incld = R2[k] * inv_cld;
-              bm_incld = vmax(R3[k] * (1 / in.cld_frac_l[co + k]), 0.);
-            }
-            qi_incld = vmin(qi_incld, C::incloud_limit);
-            bm_incld = vmin(bm_incld, C::incloud_limit);
-            if (qi_incld > C::QSMALL) {
-              ni_incld = vmax(ni_incld, C::NSMALL);
-              const double rhop = calc_bulk_rho_rime(qi_incld, qm_incld, bm_incld, rt);
-              R2[k] = qm_incld * cld;
-              R3[k] = bm_incld * cld;
-              R2f[k] = float(R2[k]);
-              R3f[k] = float(R3[k]);
-              TableIce<float> ti;
-              lookup_ice<float>(float(qi_incld), float(ni_incld), float(qm_incld), float(rhop), ti);
-              float tv[4];
-              apply_table_ice4<float>(tb, ti, 0, tv); /* columns 0, 1, 6, 7 */
-              ni_incld = vmin(ni_incld, double(tv[2]) * ni_incld);
-              ni_incld = vmax(ni_incld, double(tv[3]) * ni_incld);
-              R1[k] = ni_incld * cld;
+            qc_f = vmin(qc_f, float(C::incloud_limit));
+          }
+          if (qc_f > float(C::QSMALL)) {
+            float mu_c, lamc;
+            float n_out = n_in;
+            get_cloud_dsd2<float>(qc_f, n_out, mu_c, RHOf[k], lamc);
+            if (n_out != n_plain) {
+              R1[k] = double(n_out) * cld;
               R1f[k] = float(R1[k]);
-              const float f = float(rt.ice_sedimentation_factor) * FACf[k];
-              v1 = f * tv[1];
-              v2 = f * tv[0];
-              fall = true;
             }
+            const float dum = 1.0f / (lamc * lamc);
+            v1 = FACf[k] * ((5.0f + mu_c) * (4.0f + mu_c)) * dum;
+            if (predictNc) v2 = FACf[k] * ((2.0f + mu_c) * (1.0f + mu_c)) * dum;
+            fall = true;
+          }
+        } else if (sp == 1) {
+          const float n_plain = R1f[k] * icf;
+          float qr_f = R0f[k] * icf, n_in = n_plain;
+          if (first) {
+            if (R0[k] >= C::QSMALL) {
+              n_in = vmax(n_in, 0.0f);
+            } else {
+              qr_f = 0;
+              n_in = 0;
+            }
+            qr_f = vmin(qr_f, float(C::precip_limit));
+          }
+          if (qr_f > float(C::QSMALL)) {
+            float mu_r = 0, lamr;
+            float n_out = n_in;
+            get_rain_dsd2<float>(qr_f, n_out, mu_r, lamr, rt);
+            Table3<float> t3;
+            lookup3<float>(mu_r, lamr, rt, t3);
+            v1 = apply_table3<float>(tb, tb.vm, t3) * FACf[k];
+            v2 = apply_table3<float>(tb, tb.vn, t3) * FACf[k];
+            if (n_out != n_plain) {
+              R1[k] = double(n_out) * cld;
+              R1f[k] = float(R1[k]);
+            }
+            fall = true;
           }
         } else {
-          /* later substeps: in-cloud values and fall speeds in FP32; the FP64
-           * state is rewritten only where a limiter changed a value */
-          const float icf = 1.0f / float(CLD[k]);
-          if (sp == 0) {
-            const float qc_f = R0f[k] * icf;
-            if (qc_f > float(C::QSMALL)) {
-              float mu_c, lamc;
-              const float n_in = R1f[k] * icf;
-              float n_out = n_in;
-              get_cloud_dsd2<float>(qc_f, n_out, mu_c, RHOf[k], lamc);
-              if (n_out != n_in) {
-                R1[k] = double(n_out) * CLD[k];
-                R1f[k] = float(R1[k]);
-              }
-              const float dum = 1.0f / (lamc * lamc);
-              v1 = FACf[k] * ((5.0f + mu_c) * (4.0f + mu_c)) * dum;
-              if (predictNc) v2 = FACf[k] * ((2.0f + mu_c) * (1.0f + mu_c)) * dum;
-              fall = true;
+          const float ni_plain = R1f[k] * icf, qm_plain = R2f[k] * icf, bm_plain = R3f[k] * icf;
+          float qi_f = R0f[k] * icf, ni_f = ni_plain, qm_f = qm_plain, bm_f = bm_plain;
+          if (first) {
+            if (R0[k] >= C::QSMALL) {
+              ni_f = vmax(ni_f, 0.0f);
+            } else {
+              qi_f = 0;
+              ni_f = 0;
             }
-          } else if (sp == 1) {
-            const float qr_f = R0f[k] * icf;
-            if (qr_f > float(C::QSMALL)) {
-              float mu_r = 0, lamr;
-              const float n_in = R1f[k] * icf;
-              float n_out = n_in;
-              get_rain_dsd2<float>(qr_f, n_out, mu_r, lamr, rt);
-              Table3<float> t3;
-              lookup3<float>(mu_r, lamr, rt, t3);
-              v1 = apply_table3<float>(tb, tb.vm, t3) * FACf[k];
-              v2 = apply_table3<float>(tb, tb.vn, t3) * FACf[k];
-              if (n_out != n_in) {
-                R1[k] = double(n_out) * CLD[k];
-                R1f[k] = float(R1[k]);
-              }
-              fall = true;
+            if (R0[k] >= C::QSMALL && R2[k] >= C::QSMALL) {
+              bm_f = vmax(R3f[k] * (1.0f / float(in.cld_frac_l[co + k])), 0.0f);
+            } else {
+              qm_f = 0;
+              bm_f = 0;
             }
-          } else {
-            const float qi_f = R0f[k] * icf;
-            if (qi_f > float(C::QSMALL)) {
-              const float ni_f = R1f[k] * icf;
-              const float qm_f = R2f[k] * icf, bm_f = R3f[k] * icf;
-              const float ni_l = vmax(ni_f, float(C::NSMALL));
-              float qm_c = qm_f, bm_c = bm_f;
-              const float rhop = calc_bulk_rho_rime<float>(qi_f, qm_c, bm_c, rt);
-              if (qm_c != qm_f) {
-                R2[k] = double(qm_c) * CLD[k];
-                R2f[k] = float(R2[k]);
-              }
-              if (bm_c != bm_f) {
-                R3[k] = double(bm_c) * CLD[k];
-                R3f[k] = float(R3[k]);
-              }
-              TableIce<float> ti;
-              lookup_ice<float>(qi_f, ni_l, qm_c, rhop, ti);
-              float tv[4];
-              apply_table_ice4<float>(tb, ti, 0, tv); /* columns 0, 1, 6, 7 */
-              float n2 = vmin(ni_l, tv[2] * ni_l);
-              n2 = vmax(n2, tv[3] * n2);
-              if (n2 != ni_f) {
-                R1[k] = double(n2) * CLD[k];
-                R1f[k] = float(R1[k]);
-              }
-              const float f = float(rt.ice_sedimentation_factor) * FACf[k];
-              v1 = f * tv[1];
-              v2 = f * tv[0];
-              fall = true;
+            qi_f = vmin(qi_f, float(C::incloud_limit));
+            bm_f = vmin(bm_f, float(C::incloud_limit));
+          }
+          if (qi_f > float(C::QSMALL)) {
+            const float ni_l = vmax(ni_f, float(C::NSMALL));
+            const float rhop = calc_bulk_rho_rime<float>(qi_f, qm_f, bm_f, rt);
+            if (qm_f != qm_plain) {
+              R2[k] = double(qm_f) * cld;
+              R2f[k] = float(R2[k]);
             }
+            if (bm_f != bm_plain) {
+              R3[k] = double(bm_f) * cld;
+              R3f[k] = float(R3[k]);
+            }
+            TableIce<float> ti;
+            lookup_ice<float>(qi_f, ni_l, qm_f, rhop, ti);
+            float tv[4];
+            apply_table_ice4<float>(tb, ti, 0, tv); /* columns 0, 1, 6, 7 */
+            float n2 = vmin(ni_l, tv[2] * ni_l);
+            n2 = vmax(n2, tv[3] * n2);
+            if (n2 != ni_plain) {
+              R1[k] = double(n2) * cld;
+              R1f[k] = float(R1[k]);
+            }
+            const float f = float(rt.ice_sedimentation_factor) * FACf[k];
+            v1 = f * tv[1];
+            v2 = f * tv[0];
+            fall = true;
           }
         }
         V1f[k] = v1;
@@ -1198,8 +1152,8 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
             f3 = v1 * R3f[k] * rho;
           }
         }
-        const double d0 = f0, d1 = nfield > 1 ? double(f1) : 0.0;
-        const double d2 = nfield > 2 ? double(f2) : 0.0, d3 = nfield > 2 ? double(f3) : 0.0;
+        const double d0 = f2d(f0), d1 = nfield > 1 ? f2d(f1) : 0.0;
+        const double d2 = nfield > 2 ? f2d(f2) : 0.0, d3 = nfield > 2 ? f2d(f3) : 0.0;
         double ud0 = __shfl_up_sync(mask, d0, 1, LANES);
         float uf0 = __shfl_up_sync(mask, f0, 1, LANES);
         double ud1 = 0, ud2 = 0, ud3 = 0;

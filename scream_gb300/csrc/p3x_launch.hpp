@@ -81,6 +81,8 @@ struct InterfacePtrs {
 cudaError_t launch_interface(const InterfacePtrs& p, int ncol, int nlev, int64_t ld, bool post, double dt,
                              cudaStream_t st);
 
+cudaError_t launch_selftest(unsigned long long* mismatches_d, cudaStream_t st);
+
 cudaError_t launch_budgets(const double* qv, const double* qc, const double* qr, const double* qi,
                            const double* th, const double* dpres, const double* inv_exner, int ncol,
                            int nlev, int64_t ld, double* water, double* energy, cudaStream_t st);

@@ -92,6 +92,23 @@ __device__ __forceinline__ float m_tanh(float x) { return tanhf(x); }
 __device__ __forceinline__ double m_fabs(double x) { return fabs(x); }
 __device__ __forceinline__ float m_fabs(float x) { return fabsf(x); }
 
+/* Exact float -> double conversion on the integer pipes: a normal float's
+ * exponent is re-biased (+896) and its 23-bit significand shifted into the
+ * double's 52-bit field; signed zeros map to signed zeros.  Subnormals,
+ * infinities and NaNs take the hardware conversion.  On this part the FP64
+ * pipe, which also executes conversions, is the bottleneck of every kernel,
+ * while the integer pipes are nearly idle. */
+__device__ __forceinline__ double f2d(float x) {
+  const uint32_t u = __float_as_uint(x);
+  const uint32_t e = (u >> 23) & 0xffu;
+  const uint32_t mag = u & 0x7fffffffu;
+  if ((e - 1u) >= 254u && mag != 0u) return double(x);
+  const uint32_t m = u & 0x7fffffu;
+  const uint32_t hi = (u & 0x80000000u) | (mag ? (((e + 896u) << 20) | (m >> 3)) : 0u);
+  const uint32_t lo = (m & 7u) << 29;
+  return __hiloint2double(int(hi), int(lo));
+}
+
 /* std::max / std::min semantics ((a < b) ? b : a), as the CPU reference. */
 template <class T> __device__ __forceinline__ T vmax(T a, T b) { return (a < b) ? b : a; }
 template <class T> __device__ __forceinline__ T vmin(T a, T b) { return (b < a) ? b : a; }

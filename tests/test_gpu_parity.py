@@ -317,3 +317,12 @@ def test_fp32_bulk_precision_form(gpu_ctx, tables, built):
             for n in ICE:
                 assert errs[n] <= 1e-4 + 10 * env[n], (n, errs[n], env[n])
             assert rel_l2(prec_g, prec_o) <= 1e-4 + 10 * env["prec"], (rel_l2(prec_g, prec_o), env["prec"])
+
+
+def test_integer_float_to_double_conversion_is_exact(gpu_ctx):
+    """The FP32-bulk form's float -> double conversion on the integer pipes
+    agrees bitwise with the hardware conversion for every float bit pattern."""
+    from scream_gb300 import _lib as L
+    n = C.c_uint64(123)
+    assert gpu_ctx.lib.p3x_selftest(C.byref(n)) == 0
+    assert n.value == 0
