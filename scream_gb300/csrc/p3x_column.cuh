@@ -910,13 +910,19 @@ __device__ void p3_sed(const Inst& in, const int col, const KParams<TR>& kp, con
 #undef SMA
 }
 
-/* K2 of the FP32-bulk form.  Same algorithm and order as p3_sed; fall
+/* K2 of the FP32-bulk form.  Same algorithm and order as p3_sed.  Fall
  * speeds, density, fall-speed factors, 1/dz and an FP32 shadow of each
- * species field live in FP32 shared arrays, and the Courant maximum is taken
- * in FP32, so a level's only FP64 work is the flux accumulation itself
- * (R += (F_in - F_out) * dt_sub / (dz rho) with both fluxes as FP64), which
- * keeps the column's mass telescoping exactly.  The shared slots of p3_sed
- * are reused: two float arrays share one double slot. */
+ * species field live in FP32 shared arrays and drive the fluxes; the Courant
+ * maximum is taken in FP32.
+ *
+ * The FP64 accumulation of the flux divergence is carried by time-integrated
+ * face fluxes: G_k = sum over substeps of F_k dt_sub (FP64), the flux leaving
+ * level k downward.  A level's FP64 state after any number of substeps is
+ * R_k = B_k + (g / dpres_k) (G_{k-1} - G_k), with B_k its value at the start
+ * (kept in the species' global array).  So a substep costs one FP64 FMA per
+ * field and level, and the column's mass telescopes exactly.  Where a limiter
+ * rewrites a level's state to x during the walk, B_k is reset so that R_k = x
+ * at that moment. */
 template <int LANES>
 __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>& kp, const Tabs<float>& tb,
                             double* __restrict__ sm, uint32_t& err) {
@@ -933,25 +939,21 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
   const bool predictNc = in.predictNc != 0;
   const int kbot = nk - 1;
 #define SMA(a, k) sm[(a)*S + (k)]
-  float* const RHOf = reinterpret_cast<float*>(&SMA(B_RHO, 0));
+  /* 11 slots of S doubles; two float arrays share a slot */
+  float* const RHOf = reinterpret_cast<float*>(&SMA(0, 0));
   float* const FACf = RHOf + S;
-  double* const COEF = &SMA(B_INVRHO, 0); /* 1 / (dz rho) */
-  float* const INVDZf = reinterpret_cast<float*>(&SMA(B_INVDZ, 0));
+  double* const COEF = &SMA(1, 0); /* g / dpres */
+  float* const INVDZf = reinterpret_cast<float*>(&SMA(2, 0));
   float* const COEFf = INVDZf + S;
-  float* const R2f = reinterpret_cast<float*>(&SMA(B_FAC, 0));
+  float* const R2f = reinterpret_cast<float*>(&SMA(3, 0));
   float* const R3f = R2f + S;
-  double* const CLD = &SMA(B_CLD, 0);
-  float* const V1f = reinterpret_cast<float*>(&SMA(B_V1, 0));
+  float* const CLDf = reinterpret_cast<float*>(&SMA(4, 0));
+  float* const V1f = reinterpret_cast<float*>(&SMA(5, 0));
   float* const V2f = V1f + S;
-  float* const R0f = reinterpret_cast<float*>(&SMA(B_V2, 0));
+  float* const R0f = reinterpret_cast<float*>(&SMA(6, 0));
   float* const R1f = R0f + S;
-  double* const R0 = &SMA(B_R0, 0);
-  double* const R1 = &SMA(B_R1, 0);
-  double* const R2 = &SMA(B_R2, 0);
-  double* const R3 = &SMA(B_R3, 0);
-  double* const PF = R2; /* rain flux accumulator (rain has two fields) */
-  /* 1 / (dz rho) = g / dpres: one FP64 division per level, and the mass
-   * update is then exactly (F_in - F_out) dt g / dpres */
+  double* const G[4] = {&SMA(7, 0), &SMA(8, 0), &SMA(9, 0), &SMA(10, 0)};
+  double* const PF = G[2]; /* rain flux accumulator (rain has two fields) */
   for (int k = lane; k < nk; k += LANES) {
     const double coef = C::gravit / in.dpres[co + k];
     RHOf[k] = float(scr_at(in, S_RHO, col)[k]);
@@ -963,29 +965,39 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
 
 #pragma unroll 1
   for (int sp = 0; sp < 3; ++sp) {
-    double* g0 = sp == 0 ? in.qc : (sp == 1 ? in.qr : in.qi);
-    double* g1 = sp == 0 ? in.nc : (sp == 1 ? in.nr : in.ni);
+    double* const B0 = sp == 0 ? in.qc : (sp == 1 ? in.qr : in.qi);
+    double* const B1 = sp == 0 ? in.nc : (sp == 1 ? in.nr : in.ni);
+    double* const B2 = in.qm;
+    double* const B3 = in.bm;
+    double* const Bf[4] = {B0, B1, B2, B3};
     const double* cldp = sp == 0 ? in.cld_frac_l : (sp == 1 ? in.cld_frac_r : in.cld_frac_i);
     const int sfac = sp == 0 ? S_ACN : (sp == 1 ? S_RHOFACR : S_RHOFACI);
     const double* const facp = scr_at(in, sfac, col);
     const int nfield = sp == 0 ? (predictNc ? 2 : 1) : (sp == 1 ? 2 : 4);
+    const int nstate = sp == 2 ? 4 : 2; /* fields that limiters may rewrite */
+    float* const Rf[4] = {R0f, R1f, R2f, R3f};
+    /* R_k := x now (k owned by this lane; G_{k-1} belongs to the lane above
+     * and is final for this substep after the warp barrier) */
+    auto set_state = [&](int f, int k, double x) {
+      const double gin = k > 0 ? G[f][k - 1] : 0.0;
+      Bf[f][co + k] = x - COEF[k] * (gin - G[f][k]);
+      Rf[f][k] = float(x);
+    };
 
     int my_top = 1 << 30, my_bot = -1;
     for (int k = lane; k < nk; k += LANES) {
-      const double q = g0[co + k];
-      const double n = g1[co + k];
-      R0[k] = q;
-      R1[k] = n;
+      const double q = B0[co + k];
       R0f[k] = float(q);
-      R1f[k] = float(n);
-      CLD[k] = cldp[co + k];
+      R1f[k] = float(B1[co + k]);
+      CLDf[k] = float(cldp[co + k]);
       FACf[k] = float(facp[k]);
+      G[0][k] = 0;
+      G[1][k] = 0;
       if (sp == 2) {
-        const double m = in.qm[co + k], b = in.bm[co + k];
-        R2[k] = m;
-        R3[k] = b;
-        R2f[k] = float(m);
-        R3f[k] = float(b);
+        R2f[k] = float(B2[co + k]);
+        R3f[k] = float(B3[co + k]);
+        G[2][k] = 0;
+        G[3][k] = 0;
       }
       if (q >= C::QSMALL) {
         my_top = min(my_top, k);
@@ -1016,13 +1028,13 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
          * thresholds and limits (and the bm quirk: bm_incld uses 1/cld_frac_l);
          * the FP64 state is rewritten wherever a limiter made an in-cloud value
          * differ from the plain one. */
-        const double cld = CLD[k];
-        const float icf = 1.0f / float(cld);
+        const double cld = CLDf[k];
+        const float icf = 1.0f / CLDf[k];
         if (sp == 0) {
           const float n_plain = R1f[k] * icf;
           float qc_f = R0f[k] * icf, n_in = n_plain;
           if (first) {
-            if (R0[k] >= C::QSMALL) {
+            if (B0[co + k] >= C::QSMALL) {
               n_in = vmax(n_in, 0.0f);
             } else {
               qc_f = 0;
@@ -1035,8 +1047,7 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
             float n_out = n_in;
             get_cloud_dsd2<float>(qc_f, n_out, mu_c, RHOf[k], lamc);
             if (n_out != n_plain) {
-              R1[k] = double(n_out) * cld;
-              R1f[k] = float(R1[k]);
+              set_state(1, k, double(n_out) * cld);
             }
             const float dum = 1.0f / (lamc * lamc);
             v1 = FACf[k] * ((5.0f + mu_c) * (4.0f + mu_c)) * dum;
@@ -1047,7 +1058,7 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
           const float n_plain = R1f[k] * icf;
           float qr_f = R0f[k] * icf, n_in = n_plain;
           if (first) {
-            if (R0[k] >= C::QSMALL) {
+            if (B0[co + k] >= C::QSMALL) {
               n_in = vmax(n_in, 0.0f);
             } else {
               qr_f = 0;
@@ -1064,8 +1075,7 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
             v1 = apply_table3<float>(tb, tb.vm, t3) * FACf[k];
             v2 = apply_table3<float>(tb, tb.vn, t3) * FACf[k];
             if (n_out != n_plain) {
-              R1[k] = double(n_out) * cld;
-              R1f[k] = float(R1[k]);
+              set_state(1, k, double(n_out) * cld);
             }
             fall = true;
           }
@@ -1073,13 +1083,13 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
           const float ni_plain = R1f[k] * icf, qm_plain = R2f[k] * icf, bm_plain = R3f[k] * icf;
           float qi_f = R0f[k] * icf, ni_f = ni_plain, qm_f = qm_plain, bm_f = bm_plain;
           if (first) {
-            if (R0[k] >= C::QSMALL) {
+            if (B0[co + k] >= C::QSMALL) {
               ni_f = vmax(ni_f, 0.0f);
             } else {
               qi_f = 0;
               ni_f = 0;
             }
-            if (R0[k] >= C::QSMALL && R2[k] >= C::QSMALL) {
+            if (B0[co + k] >= C::QSMALL && B2[co + k] >= C::QSMALL) {
               bm_f = vmax(R3f[k] * (1.0f / float(in.cld_frac_l[co + k])), 0.0f);
             } else {
               qm_f = 0;
@@ -1092,12 +1102,10 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
             const float ni_l = vmax(ni_f, float(C::NSMALL));
             const float rhop = calc_bulk_rho_rime<float>(qi_f, qm_f, bm_f, rt);
             if (qm_f != qm_plain) {
-              R2[k] = double(qm_f) * cld;
-              R2f[k] = float(R2[k]);
+              set_state(2, k, double(qm_f) * cld);
             }
             if (bm_f != bm_plain) {
-              R3[k] = double(bm_f) * cld;
-              R3f[k] = float(R3[k]);
+              set_state(3, k, double(bm_f) * cld);
             }
             TableIce<float> ti;
             lookup_ice<float>(qi_f, ni_l, qm_f, rhop, ti);
@@ -1106,8 +1114,7 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
             float n2 = vmin(ni_l, tv[2] * ni_l);
             n2 = vmax(n2, tv[3] * n2);
             if (n2 != ni_plain) {
-              R1[k] = double(n2) * cld;
-              R1f[k] = float(R1[k]);
+              set_state(1, k, double(n2) * cld);
             }
             const float f = float(rt.ice_sedimentation_factor) * FACf[k];
             v1 = f * tv[1];
@@ -1130,13 +1137,10 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
       }
       const int tmpint1 = static_cast<int>(Co_max + 1);
       const double dt_sub = dt_left / tmpint1;
-      const int k_temp = (k_qxbot == kbot) ? k_qxbot : k_qxbot + 1;
-      /* Fluxes in FP32; each flux is converted to FP64 once and handed to the
-       * level below as a double, so every flux difference and state update is
-       * FP64 (the column's mass telescopes exactly).  The FP32 shadows follow
-       * with FP32 arithmetic. */
       const float dt_sub_f = float(dt_sub);
-      double cd0 = 0, cd1 = 0, cd2 = 0, cd3 = 0;
+      const int k_temp = (k_qxbot == kbot) ? k_qxbot : k_qxbot + 1;
+      /* FP32 fluxes from the shadows; FP64 time-integrated face fluxes; the
+       * shadows follow with the FP32 flux divergence */
       float cf0 = 0, cf1 = 0, cf2 = 0, cf3 = 0, flux_bot = 0;
       for (int base = k_qxtop; base <= k_temp; base += LANES) {
         const int k = base + lane;
@@ -1152,53 +1156,37 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
             f3 = v1 * R3f[k] * rho;
           }
         }
-        const double d0 = f2d(f0), d1 = nfield > 1 ? f2d(f1) : 0.0;
-        const double d2 = nfield > 2 ? f2d(f2) : 0.0, d3 = nfield > 2 ? f2d(f3) : 0.0;
-        double ud0 = __shfl_up_sync(mask, d0, 1, LANES);
         float uf0 = __shfl_up_sync(mask, f0, 1, LANES);
-        double ud1 = 0, ud2 = 0, ud3 = 0;
         float uf1 = 0, uf2 = 0, uf3 = 0;
-        if (nfield > 1) {
-          ud1 = __shfl_up_sync(mask, d1, 1, LANES);
-          uf1 = __shfl_up_sync(mask, f1, 1, LANES);
-        }
+        if (nfield > 1) uf1 = __shfl_up_sync(mask, f1, 1, LANES);
         if (nfield > 2) {
-          ud2 = __shfl_up_sync(mask, d2, 1, LANES);
-          ud3 = __shfl_up_sync(mask, d3, 1, LANES);
           uf2 = __shfl_up_sync(mask, f2, 1, LANES);
           uf3 = __shfl_up_sync(mask, f3, 1, LANES);
         }
         if (lane == 0) {
-          ud0 = cd0; ud1 = cd1; ud2 = cd2; ud3 = cd3;
           uf0 = cf0; uf1 = cf1; uf2 = cf2; uf3 = cf3;
         }
         if (act) {
-          const double coef = COEF[k] * dt_sub;
           const float coef_f = COEFf[k] * dt_sub_f;
-          R0[k] += (ud0 - d0) * coef;
+          const double d0 = f2d(f0);
+          G[0][k] += d0 * dt_sub;
           R0f[k] += (uf0 - f0) * coef_f;
           if (nfield > 1) {
-            R1[k] += (ud1 - d1) * coef;
+            G[1][k] += f2d(f1) * dt_sub;
             R1f[k] += (uf1 - f1) * coef_f;
           }
           if (nfield > 2) {
-            R2[k] += (ud2 - d2) * coef;
-            R3[k] += (ud3 - d3) * coef;
+            G[2][k] += f2d(f2) * dt_sub;
+            G[3][k] += f2d(f3) * dt_sub;
             R2f[k] += (uf2 - f2) * coef_f;
             R3f[k] += (uf3 - f3) * coef_f;
           }
           if (sp == 1) PF[k + 1] += d0;
           if (k == kbot) flux_bot = f0;
         }
-        cd0 = __shfl_sync(mask, d0, LANES - 1, LANES);
         cf0 = __shfl_sync(mask, f0, LANES - 1, LANES);
-        if (nfield > 1) {
-          cd1 = __shfl_sync(mask, d1, LANES - 1, LANES);
-          cf1 = __shfl_sync(mask, f1, LANES - 1, LANES);
-        }
+        if (nfield > 1) cf1 = __shfl_sync(mask, f1, LANES - 1, LANES);
         if (nfield > 2) {
-          cd2 = __shfl_sync(mask, d2, LANES - 1, LANES);
-          cd3 = __shfl_sync(mask, d3, LANES - 1, LANES);
           cf2 = __shfl_sync(mask, f2, LANES - 1, LANES);
           cf3 = __shfl_sync(mask, f3, LANES - 1, LANES);
         }
@@ -1211,18 +1199,18 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
       }
       dt_left -= dt_sub;
       first = false;
+      __syncwarp(mask); /* G of the level above is read by set_state */
     }
     if (sp == 0) precip_liq_surf = prt_accum * C::INV_RHO_H2O * inv_dt;
     else if (sp == 1) precip_liq_surf += prt_accum * C::INV_RHO_H2O * inv_dt;
     else precip_ice_surf += prt_accum * C::INV_RHO_H2O * inv_dt;
 
     __syncwarp(mask);
+    /* FP64 state: R_k = B_k + (g / dpres_k) (G_{k-1} - G_k) */
     for (int k = lane; k < nk; k += LANES) {
-      g0[co + k] = R0[k];
-      g1[co + k] = R1[k];
-      if (sp == 2) {
-        in.qm[co + k] = R2[k];
-        in.bm[co + k] = R3[k];
+      for (int f = 0; f < nstate; ++f) {
+        const double gin = k > 0 ? G[f][k - 1] : 0.0;
+        Bf[f][co + k] = Bf[f][co + k] + COEF[k] * (gin - G[f][k]);
       }
     }
     if (sp == 1) {
