@@ -260,8 +260,8 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
       const double inv_cld_l = 1 / cld_l;
       rho = dpres / dz / C::gravit;
       inv_rho = 1 / rho;
-      qvsl = qv_sat_dry<TR>(T, pres, false, rt, err);
-      qvsi = qv_sat_dry<TR>(T, pres, true, rt, err);
+      qvsl = qv_sat_dry(T, pres, false, err);
+      qvsi = qv_sat_dry(T, pres, true, err);
       qvssi = qv / qvsi - 1;
       ccn_nc = rt.spa_ccn_to_nc_factor * in.nccn[o] / inv_cld_l;
     } else {
@@ -539,7 +539,7 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
       water_conservation<double>(s.qc, s.qr, s.qi, dt, rd);
       number_conservation<double>(s.nc, s.nr, s.ni, dt, rd);
       ice_supersat_conservation(rd, cld_i, s.qv, qvsi, s.th / inv_exner, dt);
-      prevent_liq_supersaturation<TR>(pres, T, s.qv, dt, rd, rt, err);
+      prevent_liq_supersaturation(pres, T, s.qv, dt, rd, err);
       update_prognostics(rd, inv_exner, predictNc, prescribedCCN, wet, dt, double(rho_qm_cloud), inv_rho, s);
     } else {
       /* FP32-bulk: limiters on the FP32 rates (FP64 vapour residuals), one

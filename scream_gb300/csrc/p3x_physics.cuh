@@ -148,18 +148,10 @@ __device__ __forceinline__ double svp_tabulated(const double* tab, double t, boo
   return c01.x + u * (c01.y + u * (c23.x + u * c23.y));
 }
 
-/* qv_sat_dry (MurphyKoop), physics_saturation_impl.hpp:126-157.  FP64 in
- * both forms: the saturation mixing ratio enters residuals (qv - qv_sat)
- * that are small near saturation.  The plain form evaluates the formula; the
- * FP32-bulk form reads the FP64 saturation table. */
-template <class TR>
-__device__ __forceinline__ double qv_sat_dry(double t, double p, bool ice, const RuntimeDev& rt, uint32_t& err) {
-  double e_pres;
-  if constexpr (sizeof(TR) == sizeof(double)) {
-    e_pres = murphy_koop_svp<double>(t, ice, err);
-  } else {
-    e_pres = svp_tabulated(rt.svp_tab, t, ice, err);
-  }
+/* qv_sat_dry (MurphyKoop), physics_saturation_impl.hpp:126-157, as the
+ * plain form evaluates it (the FP32-bulk form reads svp_tabulated). */
+__device__ __forceinline__ double qv_sat_dry(double t, double p, bool ice, uint32_t& err) {
+  const double e_pres = murphy_koop_svp<double>(t, ice, err);
   return C::ep_2 * e_pres / vmax(p, 1.e-3);
 }
 
@@ -788,26 +780,6 @@ __device__ __forceinline__ void back_to_cell_average(TR cld_l, TR cld_r, TR cld_
   r.qc2qi_berg_tend *= il;
 }
 
-/* Converts a rate set to FP64 (identity for the plain form). */
-template <class TR>
-__device__ __forceinline__ Rates<double> to_double(const Rates<TR>& a) {
-  Rates<double> b;
-  b.qc2qr_accret_tend = a.qc2qr_accret_tend; b.qr2qv_evap_tend = a.qr2qv_evap_tend;
-  b.qc2qr_autoconv_tend = a.qc2qr_autoconv_tend; b.nc_accret_tend = a.nc_accret_tend;
-  b.nc_selfcollect_tend = a.nc_selfcollect_tend; b.nc2nr_autoconv_tend = a.nc2nr_autoconv_tend;
-  b.nr_selfcollect_tend = a.nr_selfcollect_tend; b.nr_evap_tend = a.nr_evap_tend; b.ncautr = a.ncautr;
-  b.qi2qv_sublim_tend = a.qi2qv_sublim_tend; b.nr_ice_shed_tend = a.nr_ice_shed_tend;
-  b.qc2qi_hetero_freeze_tend = a.qc2qi_hetero_freeze_tend; b.qr2qi_collect_tend = a.qr2qi_collect_tend;
-  b.qc2qr_ice_shed_tend = a.qc2qr_ice_shed_tend; b.qi2qr_melt_tend = a.qi2qr_melt_tend;
-  b.qc2qi_collect_tend = a.qc2qi_collect_tend; b.qr2qi_immers_freeze_tend = a.qr2qi_immers_freeze_tend;
-  b.qv2qi_nucleat_tend = a.qv2qi_nucleat_tend; b.ni2nr_melt_tend = a.ni2nr_melt_tend;
-  b.nc_collect_tend = a.nc_collect_tend; b.ncshdc = a.ncshdc; b.nc2ni_immers_freeze_tend = a.nc2ni_immers_freeze_tend;
-  b.nr_collect_tend = a.nr_collect_tend; b.ni_selfcollect_tend = a.ni_selfcollect_tend;
-  b.ni_nucleat_tend = a.ni_nucleat_tend; b.qv2qi_vapdep_tend = a.qv2qi_vapdep_tend;
-  b.qc2qi_berg_tend = a.qc2qi_berg_tend; b.nr2ni_immers_freeze_tend = a.nr2ni_immers_freeze_tend;
-  b.ni_sublim_tend = a.ni_sublim_tend;
-  return b;
-}
 
 /* ------------------------------------------------------------------ */
 /* FP64 residual routines                                               */
@@ -1069,15 +1041,14 @@ __device__ __forceinline__ void ice_supersat_conservation(Rates<double>& r, doub
 }
 
 /* prevent_liq_supersaturation, p3/impl/p3_prevent_liq_supersaturation_impl.hpp:12-79 */
-template <class TR>
 __device__ __forceinline__ void prevent_liq_supersaturation(double pres, double t_atm, double qv, double dt,
-                                                            Rates<double>& r, const RuntimeDev& rt, uint32_t& err) {
+                                                            Rates<double>& r, uint32_t& err) {
   const double qv_sources = r.qi2qv_sublim_tend + r.qr2qv_evap_tend;
   if (!(qv_sources >= C::QSMALL)) return;
   const double qv_sinks = r.qv2qi_vapdep_tend + r.qv2qi_nucleat_tend;
   const double T_endstep = t_atm + ((qv_sinks - r.qi2qv_sublim_tend) * (C::LatVap + C::LatIce) * C::INV_CP -
                                     r.qr2qv_evap_tend * C::LatVap * C::INV_CP) * dt;
-  const double qsl = qv_sat_dry<TR>(T_endstep, pres, false, rt, err);
+  const double qsl = qv_sat_dry(T_endstep, pres, false, err);
   const double A = C::LatVap * qsl * dt * C::INV_CP / (C::RV * T_endstep * T_endstep) *
                    ((C::LatVap + C::LatIce) * r.qi2qv_sublim_tend + C::LatVap * r.qr2qv_evap_tend);
   double frac = (qsl - qv + qv_sinks * dt + A) / (qv_sources * dt + A);
