@@ -255,7 +255,7 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
     double rho, inv_rho, qvsl, qvsi, qvssi, ccn_nc;
     const double exner = 1 / inv_exner;
     double T = th * exner;
-    qv = vmax(qv, 0.);
+    qv = dmax0(qv);
     if constexpr (kF64) {
       const double inv_cld_l = 1 / cld_l;
       rho = dpres / dz / C::gravit;
@@ -270,22 +270,22 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
        * FP32; one FP64 division for the pressure shared by both saturation
        * ratios; the supersaturation ratio (threshold and rate input) in FP32 */
       const float rho_f = float(dpres) / (float(dz) * float(C::gravit));
-      rho = rho_f;
-      inv_rho = double(1.0f / rho_f);
-      const double inv_p = 1 / vmax(pres, 1.e-3);
+      rho = f2d(rho_f);
+      inv_rho = f2d(1.0f / rho_f);
+      const double inv_p = 1 / dmax_c(pres, 1.e-3);
       SMA(A_INVP, k) = inv_p;
       qvsl = C::ep_2 * svp_tabulated(rt.svp_tab, T, false, err) * inv_p;
       qvsi = C::ep_2 * svp_tabulated(rt.svp_tab, T, true, err) * inv_p;
-      qvssi = double(float(qv) / float(qvsi) - 1.0f);
+      qvssi = f2d(float(qv) / float(qvsi) - 1.0f);
       ccn_nc = rt.spa_ccn_to_nc_factor * in.nccn[o] * cld_l;
     }
     const TR rhofacr = m_pow(TR(C::RHO_1000MB) * TR(inv_rho), TR(.54));
     const TR rhofaci = m_pow(TR(C::RHO_600MB) * TR(inv_rho), TR(.54));
     const TR dum = TR(1.496e-6) * m_pow(TR(T), TR(1.5)) / (TR(T) + TR(120));
     const TR acn = TR(C::gravit) * TR(C::RHO_H2O) / (TR(18) * dum);
-    if (T < C::T_zerodegc && qvssi >= -0.05) nucl = true;
+    if (dlt(T, C::T_zerodegc) && dge_neg(qvssi, -0.05)) nucl = true;
 
-    if (qc < C::QSMALL) {
+    if (dlt(qc, C::QSMALL)) {
       qv = qv + qc;
       th = th - inv_exner * qc * C::LatVap * C::INV_CP;
       qc = 0;
@@ -295,12 +295,12 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
       if (prescribedCCN) {
         nc = vmax(nc, ccn_nc);
       } else if (predictNc) {
-        nc = vmax(nc + in.nc_nuceat_tend[o] * dt, 0.0);
+        nc = dmax0(nc + in.nc_nuceat_tend[o] * dt);
       } else {
         nc = C::NCCNST * inv_rho;
       }
     }
-    if (qr < C::QSMALL) {
+    if (dlt(qr, C::QSMALL)) {
       qv = qv + qr;
       th = th - inv_exner * qr * C::LatVap * C::INV_CP;
       qr = 0;
@@ -308,14 +308,14 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
     } else {
       hydro = true;
     }
-    if (qi < C::QSMALL || (qi < 1.e-8 && qvssi < -0.1)) {
+    if (dlt(qi, C::QSMALL) || (dlt(qi, 1.e-8) && dlt_neg(qvssi, -0.1))) {
       qv = qv + qi;
       th = th - inv_exner * qi * (C::LatVap + C::LatIce) * C::INV_CP;
       qi = 0; ni = 0; qm = 0; bm = 0;
     } else {
       hydro = true;
     }
-    if (qi >= C::QSMALL && qi < 1.e-8 && T >= C::T_zerodegc) {
+    if (dge(qi, C::QSMALL) && dlt(qi, 1.e-8) && dge(T, C::T_zerodegc)) {
       qr = qr + qi;
       th = th - inv_exner * qi * C::LatIce * C::INV_CP;
       qi = 0; ni = 0; qm = 0; bm = 0;
@@ -327,9 +327,9 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
     in.qv[o] = qv; in.th[o] = th;
     SMA(A_TATM, k) = T;
     SMA(A_RHO, k) = rho;
-    SMA(A_RHOFACR, k) = double(rhofacr);
-    SMA(A_RHOFACI, k) = double(rhofaci);
-    SMA(A_ACN, k) = double(acn);
+    SMA(A_RHOFACR, k) = widen(rhofacr);
+    SMA(A_RHOFACI, k) = widen(rhofaci);
+    SMA(A_ACN, k) = widen(acn);
     SMA(A_QVSL, k) = qvsl;
     SMA(A_QVSI, k) = qvsi;
     SMA(A_QVSSI, k) = qvssi;
@@ -357,14 +357,15 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
     s.qv = in.qv[o]; s.th = in.th[o];
     const double T = SMA(A_TATM, k);
     const double qvssi = SMA(A_QVSSI, k);
-    if (s.qc < C::QSMALL && s.qr < C::QSMALL && s.qi < C::QSMALL && T < C::T_zerodegc && qvssi < -0.05)
+    if (dlt(s.qc, C::QSMALL) && dlt(s.qr, C::QSMALL) && dlt(s.qi, C::QSMALL) && dlt(T, C::T_zerodegc) &&
+        dlt_neg(qvssi, -0.05))
       continue;
 
     const double pres = in.pres[o];
     const double cld_i = in.cld_frac_i[o], cld_l = in.cld_frac_l[o], cld_r = in.cld_frac_r[o];
     const double inv_exner = in.inv_exner[o];
     const double rho = SMA(A_RHO, k);
-    const double inv_rho = kF64 ? 1 / rho : double(1.0f / float(rho));
+    const double inv_rho = kF64 ? 1 / rho : f2d(1.0f / float(rho));
     const double qvsl = SMA(A_QVSL, k), qvsi = SMA(A_QVSI, k);
     const double rhofaci = SMA(A_RHOFACI, k);
     const double acn = SMA(A_ACN, k);
@@ -375,8 +376,8 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
     if constexpr (kF64) {
       calc_incloud(s.qc, s.qr, s.qi, s.qm, s.nc, s.nr, s.ni, s.bm, 1 / cld_l, 1 / cld_i, 1 / cld_r, inc);
     } else {
-      calc_incloud(s.qc, s.qr, s.qi, s.qm, s.nc, s.nr, s.ni, s.bm, double(1.0f / float(cld_l)),
-                   double(1.0f / float(cld_i)), double(1.0f / float(cld_r)), inc);
+      calc_incloud(s.qc, s.qr, s.qi, s.qm, s.nc, s.nr, s.ni, s.bm, f2d(1.0f / float(cld_l)),
+                   f2d(1.0f / float(cld_i)), f2d(1.0f / float(cld_r)), inc);
     }
 
     Rates<TR> r;
@@ -407,7 +408,7 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
         TR n_out = n_in;
         get_rain_dsd2<TR>(TR(inc.qr), n_out, mu_r, lamr, rt);
         apply_n_adjust(inc.nr, n_in, n_out);
-        if (inc.qr >= C::QSMALL) {
+        if (dge(inc.qr, C::QSMALL)) {
           cdistr = TR(inc.nr) / TR(rt.g_mur1);
           logn0r = m_log10(cdistr) + (mu_r + TR(1)) * m_log10(lamr);
         }
@@ -418,12 +419,12 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
       } else {
         float ni_f = float(inc.ni);
         impose_max_total_ni(ni_f, rt.max_total_ni, float(inv_rho));
-        inc.ni = ni_f;
+        inc.ni = f2d(ni_f);
       }
-      if (inc.qi >= C::QSMALL) {
-        inc.ni = vmax(inc.ni, C::NSMALL);
-        inc.nr = vmax(inc.nr, C::NSMALL);
-        double rhop;
+      if (dge(inc.qi, C::QSMALL)) {
+        inc.ni = dmax_c(inc.ni, C::NSMALL);
+        inc.nr = dmax_c(inc.nr, C::NSMALL);
+        TR rhop;
         if constexpr (kF64) {
           rhop = calc_bulk_rho_rime(inc.qi, inc.qm, inc.bm, rt);
           s.qm = inc.qm * cld_i;
@@ -433,16 +434,16 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
           float qm_f = qm0, bm_f = bm0;
           rhop = calc_bulk_rho_rime<float>(float(inc.qi), qm_f, bm_f, rt);
           if (qm_f != qm0) {
-            inc.qm = qm_f;
+            inc.qm = f2d(qm_f);
             s.qm = inc.qm * cld_i;
           }
           if (bm_f != bm0) {
-            inc.bm = bm_f;
+            inc.bm = f2d(bm_f);
             s.bm = inc.bm * cld_i;
           }
         }
         TableIce<TR> ti;
-        lookup_ice<TR>(TR(inc.qi), TR(inc.ni), TR(inc.qm), TR(rhop), ti);
+        lookup_ice<TR>(TR(inc.qi), TR(inc.ni), TR(inc.qm), rhop, ti);
         TableRain<TR> trn;
         lookup_rain<TR>(TR(inc.qr), TR(inc.nr), trn);
         TR ta[4], tc[4];
@@ -455,12 +456,12 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
         tv_lammax = ta[2];
         tv_lammin = ta[3];
         tv_vent = tc[3];
-        if (inc.qr >= C::QSMALL) {
+        if (dge(inc.qr, C::QSMALL)) {
           tv_nr = apply_table_coll<TR>(0, tb, ti, trn);
           tv_qr2qi = apply_table_coll<TR>(1, tb, ti, trn);
         }
-        inc.ni = vmin(inc.ni, double(tv_lammax) * inc.ni);
-        inc.ni = vmax(inc.ni, double(tv_lammin) * inc.ni);
+        inc.ni = vmin(inc.ni, widen(tv_lammax) * inc.ni);
+        inc.ni = vmax(inc.ni, widen(tv_lammin) * inc.ni);
       }
       const TR qi_r = TR(inc.qi), qc_r = TR(inc.qc), ni_r = TR(inc.ni), nc_r = TR(inc.nc), qr_r = TR(inc.qr);
       const double dT0 = T - C::Tmelt;
@@ -476,7 +477,7 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
                                         qr_r, r);
       }
       /* ice_relaxation_timescale, p3_ice_relaxation_timescale_impl.hpp:9-37 */
-      if (inc.qi >= C::QSMALL && T < C::Tmelt) {
+      if (dge(inc.qi, C::QSMALL) && dlt(T, C::Tmelt)) {
         epsi = ((tv_melt + tv_vent * m_cbrt(v.sc) * m_sqrt(rhofaci_r * rho_r / v.mu)) * TR(2.0) * TR(C::Pi) *
                 rho_r * v.dv) * ni_r;
         epsi_tot = epsi_tot + epsi;
@@ -490,7 +491,7 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
         rain_immersion_freezing<TR>(T_r, lamr, mu_r, cdistr, qr_r, r, rt);
       }
       /* calc_liq_relaxation_timescale, p3_calc_liq_relaxation_timescale_impl.hpp:13-43 */
-      if (inc.qr >= C::QSMALL) {
+      if (dge(inc.qr, C::QSMALL)) {
         Table3<TR> t3;
         lookup3<TR>(mu_r, lamr, rt, t3);
         epsr = TR(2) * TR(C::Pi) * cdistr * rho_r * v.dv *
@@ -529,7 +530,7 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
                          prescribedCCN, r, rt);
     }
     cloud_water_autoconversion<TR>(TR(rho), TR(inc.qc), TR(inc.nc), r, rt);
-    if (inc.qc >= C::QSMALL) r.nc_selfcollect_tend = TR(0);
+    if (dge(inc.qc, C::QSMALL)) r.nc_selfcollect_tend = TR(0);
     cloud_rain_accretion<TR>(TR(inc.qc), TR(inc.nc), TR(inc.qr), r, rt);
     rain_self_collection<TR>(TR(rho), TR(inc.qr), TR(inc.nr), r, rt);
     back_to_cell_average<TR>(TR(cld_l), TR(cld_r), TR(cld_i), r);
@@ -554,15 +555,15 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
                               r_lim, s);
     }
 
-    in.qv2qi_depos_tend[o] = double(r.qv2qi_vapdep_tend - r.qi2qv_sublim_tend + r.qv2qi_nucleat_tend);
-    in.precip_total_tend[o] = double(r.qc2qr_accret_tend + r.qc2qr_autoconv_tend + r.qc2qr_ice_shed_tend + r.qc2qi_collect_tend);
-    in.nevapr[o] = double(r.qi2qv_sublim_tend + r.qr2qv_evap_tend);
-    in.vap_ice_exchange[o] = double(r.qv2qi_vapdep_tend - r.qi2qv_sublim_tend + r.qv2qi_nucleat_tend);
-    in.vap_liq_exchange[o] = double(-r.qr2qv_evap_tend);
-    in.liq_ice_exchange[o] = double(r.qc2qi_hetero_freeze_tend + r.qr2qi_immers_freeze_tend - r.qi2qr_melt_tend +
+    in.qv2qi_depos_tend[o] = widen(r.qv2qi_vapdep_tend - r.qi2qv_sublim_tend + r.qv2qi_nucleat_tend);
+    in.precip_total_tend[o] = widen(r.qc2qr_accret_tend + r.qc2qr_autoconv_tend + r.qc2qr_ice_shed_tend + r.qc2qi_collect_tend);
+    in.nevapr[o] = widen(r.qi2qv_sublim_tend + r.qr2qv_evap_tend);
+    in.vap_ice_exchange[o] = widen(r.qv2qi_vapdep_tend - r.qi2qv_sublim_tend + r.qv2qi_nucleat_tend);
+    in.vap_liq_exchange[o] = widen(-r.qr2qv_evap_tend);
+    in.liq_ice_exchange[o] = widen(r.qc2qi_hetero_freeze_tend + r.qr2qi_immers_freeze_tend - r.qi2qr_melt_tend +
                                     r.qc2qi_berg_tend + r.qc2qi_collect_tend + r.qr2qi_collect_tend);
 
-    if (s.qc < C::QSMALL) {
+    if (dlt(s.qc, C::QSMALL)) {
       s.qv = s.qv + s.qc;
       s.th = s.th - inv_exner * s.qc * C::LatVap * C::INV_CP;
       s.qc = 0;
@@ -570,7 +571,7 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
     } else {
       hydro = true;
     }
-    if (s.qr < C::QSMALL) {
+    if (dlt(s.qr, C::QSMALL)) {
       s.qv = s.qv + s.qr;
       s.th = s.th - inv_exner * s.qr * C::LatVap * C::INV_CP;
       s.qr = 0;
@@ -578,7 +579,7 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
     } else {
       hydro = true;
     }
-    if (s.qi < C::QSMALL) {
+    if (dlt(s.qi, C::QSMALL)) {
       s.qv = s.qv + s.qi;
       s.th = s.th - inv_exner * s.qi * (C::LatVap + C::LatIce) * C::INV_CP;
       s.qi = 0; s.ni = 0; s.qm = 0; s.bm = 0;
@@ -589,10 +590,10 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
       double ni_incld = s.ni / cld_i;
       impose_max_total_ni(ni_incld, rt.max_total_ni, inv_rho);
       s.ni = ni_incld * cld_i;
-    } else if (s.ni >= 1e-20) {
+    } else if (dge(s.ni, 1e-20)) {
       /* impose_max_total_ni as a factor applied only when it limits */
       const float f = vmin(float(rt.max_total_ni) * float(inv_rho) * float(cld_i) / float(s.ni), 1.0f);
-      if (f < 1.0f) s.ni = s.ni * double(f);
+      if (f < 1.0f) s.ni = s.ni * f2d(f);
     }
     in.qc[o] = s.qc; in.nc[o] = s.nc; in.qr[o] = s.qr; in.nr[o] = s.nr;
     in.qi[o] = s.qi; in.qm[o] = s.qm; in.ni[o] = s.ni; in.bm[o] = s.bm;
@@ -915,14 +916,16 @@ __device__ void p3_sed(const Inst& in, const int col, const KParams<TR>& kp, con
  * species field live in FP32 shared arrays and drive the fluxes; the Courant
  * maximum is taken in FP32.
  *
- * The FP64 accumulation of the flux divergence is carried by time-integrated
- * face fluxes: G_k = sum over substeps of F_k dt_sub (FP64), the flux leaving
- * level k downward.  A level's FP64 state after any number of substeps is
- * R_k = B_k + (g / dpres_k) (G_{k-1} - G_k), with B_k its value at the start
- * (kept in the species' global array).  So a substep costs one FP64 FMA per
- * field and level, and the column's mass telescopes exactly.  Where a limiter
- * rewrites a level's state to x during the walk, B_k is reset so that R_k = x
- * at that moment. */
+ * The accumulation of the flux divergence is carried by time-integrated face
+ * fluxes: G_k = sum over substeps of F_k dt_sub, the flux leaving level k
+ * downward, kept as a double-float (~48 significant bits).  A level's FP64
+ * state after any number of substeps is R_k = B_k + (g / dpres_k) (G_{k-1} -
+ * G_k), with B_k its value at the start (kept in the species' global array).
+ * So a substep costs one double-float multiply-add (FP32 instructions only)
+ * per field and level; both neighbours of a face read the same G, so the
+ * column's mass telescopes exactly, and the surface precipitation is the
+ * bottom face's G.  Where a limiter rewrites a level's state to x during the
+ * walk, B_k is reset so that R_k = x at that moment. */
 template <int LANES>
 __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>& kp, const Tabs<float>& tb,
                             double* __restrict__ sm, uint32_t& err) {
@@ -952,8 +955,10 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
   float* const V2f = V1f + S;
   float* const R0f = reinterpret_cast<float*>(&SMA(6, 0));
   float* const R1f = R0f + S;
-  double* const G[4] = {&SMA(7, 0), &SMA(8, 0), &SMA(9, 0), &SMA(10, 0)};
-  double* const PF = G[2]; /* rain flux accumulator (rain has two fields) */
+  /* time-integrated face fluxes and the rain flux sum, as double-floats */
+  float2* const G[4] = {reinterpret_cast<float2*>(&SMA(7, 0)), reinterpret_cast<float2*>(&SMA(8, 0)),
+                        reinterpret_cast<float2*>(&SMA(9, 0)), reinterpret_cast<float2*>(&SMA(10, 0))};
+  float2* const PF = G[2]; /* rain flux accumulator (rain has two fields) */
   for (int k = lane; k < nk; k += LANES) {
     const double coef = C::gravit / in.dpres[co + k];
     RHOf[k] = float(scr_at(in, S_RHO, col)[k]);
@@ -979,8 +984,8 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
     /* R_k := x now (k owned by this lane; G_{k-1} belongs to the lane above
      * and is final for this substep after the warp barrier) */
     auto set_state = [&](int f, int k, double x) {
-      const double gin = k > 0 ? G[f][k - 1] : 0.0;
-      Bf[f][co + k] = x - COEF[k] * (gin - G[f][k]);
+      const double gin = k > 0 ? dfloat_value(G[f][k - 1]) : 0.0;
+      Bf[f][co + k] = x - COEF[k] * (gin - dfloat_value(G[f][k]));
       Rf[f][k] = float(x);
     };
 
@@ -991,13 +996,13 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
       R1f[k] = float(B1[co + k]);
       CLDf[k] = float(cldp[co + k]);
       FACf[k] = float(facp[k]);
-      G[0][k] = 0;
-      G[1][k] = 0;
+      G[0][k] = make_float2(0.f, 0.f);
+      G[1][k] = make_float2(0.f, 0.f);
       if (sp == 2) {
         R2f[k] = float(B2[co + k]);
         R3f[k] = float(B3[co + k]);
-        G[2][k] = 0;
-        G[3][k] = 0;
+        G[2][k] = make_float2(0.f, 0.f);
+        G[3][k] = make_float2(0.f, 0.f);
       }
       if (q >= C::QSMALL) {
         my_top = min(my_top, k);
@@ -1008,11 +1013,11 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
     int k_qxbot = group_max_int<LANES>(mask, my_bot);
     if (k_qxbot < 0) continue; /* species absent (group-uniform) */
     if (sp == 1) {
-      for (int k = lane; k <= nk; k += LANES) PF[k] = 0;
+      for (int k = lane; k <= nk; k += LANES) PF[k] = make_float2(0.f, 0.f);
     }
     __syncwarp(mask);
 
-    double dt_left = dt, prt_accum = 0.0;
+    double dt_left = dt;
     bool first = true;
     int nsub = 0;
     while (dt_left > C::dt_left_tol) {
@@ -1028,8 +1033,8 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
          * thresholds and limits (and the bm quirk: bm_incld uses 1/cld_frac_l);
          * the FP64 state is rewritten wherever a limiter made an in-cloud value
          * differ from the plain one. */
-        const double cld = CLDf[k];
-        const float icf = 1.0f / CLDf[k];
+        const float cldf = CLDf[k];
+        const float icf = 1.0f / cldf;
         if (sp == 0) {
           const float n_plain = R1f[k] * icf;
           float qc_f = R0f[k] * icf, n_in = n_plain;
@@ -1047,7 +1052,7 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
             float n_out = n_in;
             get_cloud_dsd2<float>(qc_f, n_out, mu_c, RHOf[k], lamc);
             if (n_out != n_plain) {
-              set_state(1, k, double(n_out) * cld);
+              set_state(1, k, f2d(n_out) * f2d(cldf));
             }
             const float dum = 1.0f / (lamc * lamc);
             v1 = FACf[k] * ((5.0f + mu_c) * (4.0f + mu_c)) * dum;
@@ -1075,7 +1080,7 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
             v1 = apply_table3<float>(tb, tb.vm, t3) * FACf[k];
             v2 = apply_table3<float>(tb, tb.vn, t3) * FACf[k];
             if (n_out != n_plain) {
-              set_state(1, k, double(n_out) * cld);
+              set_state(1, k, f2d(n_out) * f2d(cldf));
             }
             fall = true;
           }
@@ -1102,10 +1107,10 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
             const float ni_l = vmax(ni_f, float(C::NSMALL));
             const float rhop = calc_bulk_rho_rime<float>(qi_f, qm_f, bm_f, rt);
             if (qm_f != qm_plain) {
-              set_state(2, k, double(qm_f) * cld);
+              set_state(2, k, f2d(qm_f) * f2d(cldf));
             }
             if (bm_f != bm_plain) {
-              set_state(3, k, double(bm_f) * cld);
+              set_state(3, k, f2d(bm_f) * f2d(cldf));
             }
             TableIce<float> ti;
             lookup_ice<float>(qi_f, ni_l, qm_f, rhop, ti);
@@ -1114,7 +1119,7 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
             float n2 = vmin(ni_l, tv[2] * ni_l);
             n2 = vmax(n2, tv[3] * n2);
             if (n2 != ni_plain) {
-              set_state(1, k, double(n2) * cld);
+              set_state(1, k, f2d(n2) * f2d(cldf));
             }
             const float f = float(rt.ice_sedimentation_factor) * FACf[k];
             v1 = f * tv[1];
@@ -1137,11 +1142,12 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
       }
       const int tmpint1 = static_cast<int>(Co_max + 1);
       const double dt_sub = dt_left / tmpint1;
-      const float dt_sub_f = float(dt_sub);
+      const dfloat dt_sub_d = dfloat_of(dt_sub);
+      const float dt_sub_f = dt_sub_d.hi;
       const int k_temp = (k_qxbot == kbot) ? k_qxbot : k_qxbot + 1;
-      /* FP32 fluxes from the shadows; FP64 time-integrated face fluxes; the
-       * shadows follow with the FP32 flux divergence */
-      float cf0 = 0, cf1 = 0, cf2 = 0, cf3 = 0, flux_bot = 0;
+      /* FP32 fluxes from the shadows; double-float time-integrated face
+       * fluxes; the shadows follow with the FP32 flux divergence */
+      float cf0 = 0, cf1 = 0, cf2 = 0, cf3 = 0;
       for (int base = k_qxtop; base <= k_temp; base += LANES) {
         const int k = base + lane;
         const bool act = k <= k_temp;
@@ -1168,21 +1174,19 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
         }
         if (act) {
           const float coef_f = COEFf[k] * dt_sub_f;
-          const double d0 = f2d(f0);
-          G[0][k] += d0 * dt_sub;
+          dfloat_add_prod(G[0][k], f0, dt_sub_d);
           R0f[k] += (uf0 - f0) * coef_f;
           if (nfield > 1) {
-            G[1][k] += f2d(f1) * dt_sub;
+            dfloat_add_prod(G[1][k], f1, dt_sub_d);
             R1f[k] += (uf1 - f1) * coef_f;
           }
           if (nfield > 2) {
-            G[2][k] += f2d(f2) * dt_sub;
-            G[3][k] += f2d(f3) * dt_sub;
+            dfloat_add_prod(G[2][k], f2, dt_sub_d);
+            dfloat_add_prod(G[3][k], f3, dt_sub_d);
             R2f[k] += (uf2 - f2) * coef_f;
             R3f[k] += (uf3 - f3) * coef_f;
           }
-          if (sp == 1) PF[k + 1] += d0;
-          if (k == kbot) flux_bot = f0;
+          if (sp == 1) dfloat_add(PF[k + 1], f0);
         }
         cf0 = __shfl_sync(mask, f0, LANES - 1, LANES);
         if (nfield > 1) cf1 = __shfl_sync(mask, f1, LANES - 1, LANES);
@@ -1191,30 +1195,29 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
           cf3 = __shfl_sync(mask, f3, LANES - 1, LANES);
         }
       }
-      if (k_qxbot == kbot) {
-        const int owner = (kbot - k_qxtop) % LANES;
-        prt_accum += double(__shfl_sync(mask, flux_bot, owner, LANES)) * dt_sub;
-      } else {
-        k_qxbot += 1;
-      }
+      if (k_qxbot < kbot) k_qxbot += 1;
       dt_left -= dt_sub;
       first = false;
       __syncwarp(mask); /* G of the level above is read by set_state */
     }
+    __syncwarp(mask);
+    /* the bottom face's integral is what left the column: V is zero at the
+     * leading edge, so G_kbot gains only in substeps where the species
+     * reaches the surface */
+    const double prt_accum = dfloat_value(G[0][kbot]);
     if (sp == 0) precip_liq_surf = prt_accum * C::INV_RHO_H2O * inv_dt;
     else if (sp == 1) precip_liq_surf += prt_accum * C::INV_RHO_H2O * inv_dt;
     else precip_ice_surf += prt_accum * C::INV_RHO_H2O * inv_dt;
 
-    __syncwarp(mask);
     /* FP64 state: R_k = B_k + (g / dpres_k) (G_{k-1} - G_k) */
     for (int k = lane; k < nk; k += LANES) {
       for (int f = 0; f < nstate; ++f) {
-        const double gin = k > 0 ? G[f][k - 1] : 0.0;
-        Bf[f][co + k] = Bf[f][co + k] + COEF[k] * (gin - G[f][k]);
+        const double gin = k > 0 ? dfloat_value(G[f][k - 1]) : 0.0;
+        Bf[f][co + k] = Bf[f][co + k] + COEF[k] * (gin - dfloat_value(G[f][k]));
       }
     }
     if (sp == 1) {
-      for (int k = lane; k <= nk; k += LANES) in.precip_liq_flux[ci + k] = PF[k];
+      for (int k = lane; k <= nk; k += LANES) in.precip_liq_flux[ci + k] = dfloat_value(PF[k]);
     }
     __syncwarp(mask);
   }

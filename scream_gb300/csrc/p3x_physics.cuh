@@ -109,6 +109,83 @@ __device__ __forceinline__ double f2d(float x) {
   return __hiloint2double(int(hi), int(lo));
 }
 
+/* widen(x): exact conversion to double (identity for doubles) */
+__device__ __forceinline__ double widen(double x) { return x; }
+__device__ __forceinline__ double widen(float x) { return f2d(x); }
+
+/* Threshold tests of a double against a constant, on the integer pipes.
+ * For c > 0 the IEEE order of x against c is the signed order of the two
+ * bit patterns for every x that is not NaN: a negative x (or -0) has the sign
+ * bit set and compares below any positive pattern.  For c < 0 and x < 0 the
+ * signed order of the patterns is the reverse of the order of the values.
+ * A NaN compares by its bit pattern; only an already invalid state holds
+ * one, and the saturation step reports that separately. */
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+/* x < c, x >= c, x > c, x <= c for a constant c > 0 */
+__device__ __forceinline__ bool dlt(double x, double c) { return dbits(x) < dbits(c); }
+__device__ __forceinline__ bool dge(double x, double c) { return dbits(x) >= dbits(c); }
+__device__ __forceinline__ bool dgt(double x, double c) { return dbits(x) > dbits(c); }
+__device__ __forceinline__ bool dle(double x, double c) { return dbits(x) <= dbits(c); }
+/* x >= c and x < c for a constant c < 0 */
+__device__ __forceinline__ bool dge_neg(double x, double c) { return dbits(x) >= 0 || dbits(x) <= dbits(c); }
+__device__ __forceinline__ bool dlt_neg(double x, double c) { return !dge_neg(x, c); }
+/* x < 0 (false for -0) */
+__device__ __forceinline__ bool dneg(double x) {
+  return static_cast<unsigned long long>(dbits(x)) > 0x8000000000000000ull;
+}
+/* vmax(x, c) = (x < c) ? c : x and vmin(x, c) = (c < x) ? c : x, c > 0 */
+__device__ __forceinline__ double dmax_c(double x, double c) { return dlt(x, c) ? c : x; }
+__device__ __forceinline__ double dmin_c(double x, double c) { return dgt(x, c) ? c : x; }
+/* x > 0 */
+__device__ __forceinline__ bool dpos(double x) { return dbits(x) > 0; }
+/* vmax(x, 0.) = (x < 0) ? 0 : x, and vmax(0., x) = (0 < x) ? x : 0 (+0 for -0) */
+__device__ __forceinline__ double dmax0(double x) { return dneg(x) ? 0.0 : x; }
+__device__ __forceinline__ double dmax_0x(double x) { return dpos(x) ? x : 0.0; }
+
+/* Double-float accumulators on the FP32 pipe: a value is the unevaluated sum
+ * hi + lo of two floats with |lo| <= ulp(hi) / 2 (about 48 significant bits).
+ * Additions use Knuth's TwoSum followed by Dekker's Fast2Sum renormalisation;
+ * the product of a float by a double-float uses the FMA error-free product.
+ * Every step is a correctly rounded FP32 operation written with the _rn
+ * intrinsics, so the compiler can neither contract nor reorder it.  One update
+ * costs ~14 FP32 instructions, against one FP64 FMA that occupies the FP64
+ * pipe for the issue time of ~64 FP32 instructions on this part. */
+struct dfloat {
+  float hi, lo;
+};
+
+/* the double-float nearest x (hi = x rounded to float, lo = the remainder) */
+__device__ __forceinline__ dfloat dfloat_of(double x) {
+  const float h = float(x);
+  return {h, float(x - double(h))};
+}
+
+/* exact value as a double: |lo| <= ulp(hi)/2, so hi + lo spans <= 48 bits */
+__device__ __forceinline__ double dfloat_value(float2 g) { return f2d(g.x) + f2d(g.y); }
+
+__device__ __forceinline__ float2 dfloat_renorm(float s, float e) {
+  const float hi = __fadd_rn(s, e);
+  return make_float2(hi, __fsub_rn(e, __fsub_rn(hi, s)));
+}
+
+/* g += a */
+__device__ __forceinline__ void dfloat_add(float2& g, float a) {
+  const float s = __fadd_rn(g.x, a);
+  const float bb = __fsub_rn(s, g.x);
+  const float e = __fadd_rn(__fsub_rn(g.x, __fsub_rn(s, bb)), __fsub_rn(a, bb));
+  g = dfloat_renorm(s, __fadd_rn(e, g.y));
+}
+
+/* g += a * t */
+__device__ __forceinline__ void dfloat_add_prod(float2& g, float a, dfloat t) {
+  const float ph = __fmul_rn(a, t.hi);
+  const float pl = __fmaf_rn(a, t.lo, __fmaf_rn(a, t.hi, -ph));
+  const float s = __fadd_rn(g.x, ph);
+  const float bb = __fsub_rn(s, g.x);
+  const float e = __fadd_rn(__fsub_rn(g.x, __fsub_rn(s, bb)), __fsub_rn(ph, bb));
+  g = dfloat_renorm(s, __fadd_rn(e, __fadd_rn(g.y, pl)));
+}
+
 /* std::max / std::min semantics ((a < b) ? b : a), as the CPU reference. */
 template <class T> __device__ __forceinline__ T vmax(T a, T b) { return (a < b) ? b : a; }
 template <class T> __device__ __forceinline__ T vmin(T a, T b) { return (b < a) ? b : a; }
@@ -139,10 +216,10 @@ constexpr double kSvpT0 = 150.0, kSvpInvH = 64.0;
 constexpr int kSvpIntervals = 12800;
 __device__ __forceinline__ double svp_tabulated(const double* tab, double t, bool ice, uint32_t& err) {
   const double x = (t - kSvpT0) * kSvpInvH;
-  if (!(x >= 0.0 && x < double(kSvpIntervals))) return murphy_koop_svp<double>(t, ice, err);
+  if (!(!dneg(x) && dlt(x, double(kSvpIntervals)))) return murphy_koop_svp<double>(t, ice, err);
   const int i = int(x);
   const double u = x - double(i);
-  const int row = (ice && t < C::Tmelt) ? kSvpIntervals + i : i;
+  const int row = (ice && dlt(t, C::Tmelt)) ? kSvpIntervals + i : i;
   const double2* c = reinterpret_cast<const double2*>(tab) + size_t(row) * 2;
   const double2 c01 = __ldg(c), c23 = __ldg(c + 1);
   return c01.x + u * (c01.y + u * (c23.x + u * c23.y));
@@ -376,20 +453,20 @@ struct Incld {
 __device__ __forceinline__ void calc_incloud(double qc, double qr, double qi, double qm, double nc,
                                              double nr, double ni, double bm, double inv_cld_l,
                                              double inv_cld_i, double inv_cld_r, Incld& o) {
-  if (qc >= C::QSMALL) { o.qc = qc * inv_cld_l; o.nc = vmax(nc * inv_cld_l, 0.); }
+  if (dge(qc, C::QSMALL)) { o.qc = qc * inv_cld_l; o.nc = dmax0(nc * inv_cld_l); }
   else { o.qc = 0; o.nc = 0; }
-  if (qi >= C::QSMALL) { o.qi = qi * inv_cld_i; o.ni = vmax(ni * inv_cld_i, 0.); }
+  if (dge(qi, C::QSMALL)) { o.qi = qi * inv_cld_i; o.ni = dmax0(ni * inv_cld_i); }
   else { o.qi = 0; o.ni = 0; }
-  if (qi >= C::QSMALL && qm >= C::QSMALL) { o.qm = qm * inv_cld_i; o.bm = vmax(bm * inv_cld_l, 0.); }
+  if (dge(qi, C::QSMALL) && dge(qm, C::QSMALL)) { o.qm = qm * inv_cld_i; o.bm = dmax0(bm * inv_cld_l); }
   else { o.qm = 0; o.bm = 0; }
-  if (qr >= C::QSMALL) { o.qr = qr * inv_cld_r; o.nr = vmax(nr * inv_cld_r, 0.); }
+  if (dge(qr, C::QSMALL)) { o.qr = qr * inv_cld_r; o.nr = dmax0(nr * inv_cld_r); }
   else { o.qr = 0; o.nr = 0; }
-  if (o.qc > C::incloud_limit || o.qi > C::incloud_limit || o.qr > C::precip_limit ||
-      o.bm > C::incloud_limit) {
-    o.qc = vmin(o.qc, C::incloud_limit);
-    o.qi = vmin(o.qi, C::incloud_limit);
-    o.bm = vmin(o.bm, C::incloud_limit);
-    o.qr = vmin(o.qr, C::precip_limit);
+  if (dgt(o.qc, C::incloud_limit) || dgt(o.qi, C::incloud_limit) || dgt(o.qr, C::precip_limit) ||
+      dgt(o.bm, C::incloud_limit)) {
+    o.qc = dmin_c(o.qc, C::incloud_limit);
+    o.qi = dmin_c(o.qi, C::incloud_limit);
+    o.bm = dmin_c(o.bm, C::incloud_limit);
+    o.qr = dmin_c(o.qr, C::precip_limit);
   }
 }
 
@@ -519,7 +596,7 @@ template <class TR>
 __device__ __forceinline__ void ice_cldliq_collection(TR rho, double temp, TR rhofaci, TR tv, TR qi_incld,
                                                       TR qc_incld, TR ni_incld, TR nc_incld,
                                                       Rates<TR>& r, const RuntimeDev& rt) {
-  const bool t_neg = temp <= C::Tmelt;
+  const bool t_neg = dle(temp, C::Tmelt);
   const bool both = qi_incld >= TR(C::QSMALL) && qc_incld >= TR(C::QSMALL);
   const TR f = TR(rt.cldliq_to_ice_collection_factor);
   if (both && t_neg) r.qc2qi_collect_tend = rhofaci * tv * qc_incld * f * rho * ni_incld;
@@ -536,7 +613,7 @@ template <class TR>
 __device__ __forceinline__ void ice_rain_collection(TR rho, double temp, TR rhofaci, TR logn0r, TR tv_nr,
                                                     TR tv_qr, TR qi_incld, TR ni_incld, TR qr_incld,
                                                     Rates<TR>& r, const RuntimeDev& rt) {
-  const bool t_neg = temp <= C::Tmelt;
+  const bool t_neg = dle(temp, C::Tmelt);
   const bool both = qi_incld >= TR(C::QSMALL) && qr_incld >= TR(C::QSMALL);
   const TR f = TR(rt.rain_to_ice_collection_factor);
   if (both && t_neg) {
@@ -570,7 +647,7 @@ template <class TR>
 __device__ __forceinline__ void ice_melting(TR rho, double dT0, double dqv0, TR rhofaci, TR tv_melt,
                                             TR tv_vent, const PhysVars<TR>& v, TR qi_incld,
                                             TR ni_incld, Rates<TR>& r) {
-  if (qi_incld >= TR(C::QSMALL) && dT0 > 0) {
+  if (qi_incld >= TR(C::QSMALL) && dpos(dT0)) {
     TR t = ((tv_melt + tv_vent * m_cbrt(v.sc) * m_sqrt(rhofaci * rho / v.mu)) *
             (TR(dT0) * v.kap - rho * TR(C::LatVap) * v.dv * TR(dqv0)) * TR(2) *
             TR(C::Pi) / TR(C::LatIce)) *
@@ -587,7 +664,7 @@ __device__ __forceinline__ bool ice_cldliq_wet_growth(TR rho, double dT0, double
                                                       TR tv_vent, const PhysVars<TR>& v,
                                                       TR qc_incld, TR qi_incld, TR ni_incld, TR qr_incld,
                                                       Rates<TR>& r) {
-  const bool t_neg = dT0 < 0;
+  const bool t_neg = dneg(dT0);
   const bool any_if = qi_incld >= TR(C::QSMALL) && (qc_incld + qr_incld) >= TR(1.0e-6) && t_neg;
   const bool any_if_col = any_if && (r.qc2qi_collect_tend + r.qr2qi_collect_tend) >= TR(1.0e-10);
   bool wet = false;
@@ -601,16 +678,16 @@ __device__ __forceinline__ bool ice_cldliq_wet_growth(TR rho, double dT0, double
      * c - dum * c / (qc2qi + qr2qi), cancel almost completely when the
      * collection rate exceeds the wet-growth limit by orders of magnitude;
      * they are evaluated in FP64 (the FP64 form is unchanged by this). */
-    const double qc2qi = double(r.qc2qi_collect_tend), qr2qi = double(r.qr2qi_collect_tend);
-    const double dum = vmax(0., (qc2qi + qr2qi) - double(g));
-    const bool dum_ge_small = dum >= 1.0e-10;
+    const double qc2qi = widen(r.qc2qi_collect_tend), qr2qi = widen(r.qr2qi_collect_tend);
+    const double dum = dmax_0x((qc2qi + qr2qi) - widen(g));
+    const bool dum_ge_small = dge(dum, 1.0e-10);
     if (dum_ge_small) {
-      r.nr_ice_shed_tend = TR(double(r.nr_ice_shed_tend) + dum * 1.923e+6);
+      r.nr_ice_shed_tend = TR(widen(r.nr_ice_shed_tend) + dum * 1.923e+6);
       const double dum1 = 1.0 / (qc2qi + qr2qi);
       if (any_if_col) {
-        r.qc2qr_ice_shed_tend = TR(double(r.qc2qr_ice_shed_tend) + dum * qc2qi * dum1);
-        r.qc2qi_collect_tend = TR(vmax(0., qc2qi - dum * qc2qi * dum1));
-        r.qr2qi_collect_tend = TR(vmax(0., qr2qi - dum * qr2qi * dum1));
+        r.qc2qr_ice_shed_tend = TR(widen(r.qc2qr_ice_shed_tend) + dum * qc2qi * dum1);
+        r.qc2qi_collect_tend = TR(dmax_0x(qc2qi - dum * qc2qi * dum1));
+        r.qr2qi_collect_tend = TR(dmax_0x(qr2qi - dum * qr2qi * dum1));
       }
     }
     wet = dum_ge_small;
@@ -844,17 +921,17 @@ __device__ __forceinline__ void evaporate_rain_bulk(double qr_incld, double qc_i
   qr2qv_evap_tend = 0;
   nr_evap_tend = 0;
   const double ssat_r_d = qv - qv_sat_l;
-  const double cld_frac = ((qc_incld + qi_incld) < 1.e-6) ? 0.0 : cld_frac_l;
-  if (qr_incld >= C::QSMALL && ssat_r_d < 0 && cld_frac_r > cld_frac) {
+  const double cld_frac = dlt(qc_incld + qi_incld, 1.e-6) ? 0.0 : cld_frac_l;
+  if (dge(qr_incld, C::QSMALL) && dneg(ssat_r_d) && cld_frac_r > cld_frac) {
     const float inv_dt = float(inv_dt_d), dtf = float(dt);
     const float ssat_r = float(ssat_r_d);
     const float tau_r = 1.0f / epsr;
     const float lat_fac = 1.0f + float((C::LatVap + C::LatIce) / C::Cpair) * dqsdt;
     float eps_eff;
-    double A_c_d = (qv - qv_prev) * inv_dt_d - double(dqsdt) * (t_atm - t_atm_prev) * inv_dt_d;
-    if (t_atm < C::Tmelt) {
+    double A_c_d = (qv - qv_prev) * inv_dt_d - f2d(dqsdt) * (t_atm - t_atm_prev) * inv_dt_d;
+    if (dlt(t_atm, C::Tmelt)) {
       eps_eff = epsr + epsi_tot * lat_fac / abi;
-      A_c_d -= (qv_sat_l - qv_sat_i) * double(lat_fac / abi * epsi_tot);
+      A_c_d -= (qv_sat_l - qv_sat_i) * f2d(lat_fac / abi * epsi_tot);
     } else {
       eps_eff = epsr;
     }
@@ -862,7 +939,7 @@ __device__ __forceinline__ void evaporate_rain_bulk(double qr_incld, double qc_i
     if (eps_eff < 1e-20f) eps_eff = 1e-20f;
     const float tau_eff = 1.0f / eps_eff;
     float evap;
-    if (qr_incld < 1e-12 && qv < 0.999 * qv_sat_l) {
+    if (dlt(qr_incld, 1e-12) && qv < 0.999 * qv_sat_l) {
       evap = float(qr_incld) * inv_dt;
     } else {
       const float dt_over_tau = dtf / tau_eff;
@@ -891,7 +968,7 @@ __device__ __forceinline__ void ice_deposition_sublimation_bulk(double qi_incld,
                                                                 float& vapdep, float& sublim, float& ni_sublim,
                                                                 float& berg) {
   berg = 0; vapdep = 0; sublim = 0; ni_sublim = 0;
-  if (qi_incld > C::QSMALL) {
+  if (dgt(qi_incld, C::QSMALL)) {
     const float coef = vmin(epsi / abi, float(inv_dt));
     const float qi_tend = coef * float(qv - qv_sat_i);
     const bool neg = qi_tend < 0;
@@ -899,7 +976,7 @@ __device__ __forceinline__ void ice_deposition_sublimation_bulk(double qi_incld,
       sublim = -qi_tend;
       ni_sublim = sublim * (float(ni_incld) / float(qi_incld));
     }
-    const bool T_lt_frz = T_atm < C::T_zerodegc;
+    const bool T_lt_frz = dlt(T_atm, C::T_zerodegc);
     if (T_lt_frz && !neg) vapdep = qi_tend;
     if (T_lt_frz) berg = vmax(epsi / abi * float(qv_sat_l - qv_sat_i), 0.0f);
   }
@@ -913,16 +990,16 @@ __device__ __forceinline__ void ice_deposition_sublimation(double qi_incld, doub
                                                            double& vapdep, double& sublim, double& ni_sublim,
                                                            double& berg) {
   berg = 0; vapdep = 0; sublim = 0; ni_sublim = 0;
-  if (qi_incld > C::QSMALL) {
+  if (dgt(qi_incld, C::QSMALL)) {
     const double qi_tend = vmin(epsi / abi, inv_dt) * (qv - qv_sat_i);
-    const bool neg = qi_tend < 0;
+    const bool neg = dneg(qi_tend);
     if (neg) {
       sublim = -qi_tend;
       ni_sublim = sublim * (ni_incld / qi_incld);
     }
-    const bool T_lt_frz = T_atm < C::T_zerodegc;
+    const bool T_lt_frz = dlt(T_atm, C::T_zerodegc);
     if (T_lt_frz && !neg) vapdep = qi_tend;
-    if (T_lt_frz) berg = vmax(epsi / abi * (qv_sat_l - qv_sat_i), 0.);
+    if (T_lt_frz) berg = dmax0(epsi / abi * (qv_sat_l - qv_sat_i));
   }
 }
 
@@ -1028,10 +1105,10 @@ __device__ __forceinline__ void ice_supersat_conservation(Rates<double>& r, doub
                                                           double qv_sat_i, double t_atm, double dt) {
   const double latsublim2 = (C::LatVap + C::LatIce) * (C::LatVap + C::LatIce);
   const double qv_sink = r.qv2qi_vapdep_tend + r.qv2qi_nucleat_tend;
-  if (qv_sink > C::QSMALL && cld_frac_i > 1e-20) {
+  if (dgt(qv_sink, C::QSMALL) && dgt(cld_frac_i, 1e-20)) {
     double qv_avail = (qv + (r.qi2qv_sublim_tend + r.qr2qv_evap_tend) * dt - qv_sat_i) /
                       (1 + latsublim2 * qv_sat_i / (C::CP * C::RH2O * sq(t_atm))) / dt;
-    qv_avail = vmax(qv_avail, 0.);
+    qv_avail = dmax0(qv_avail);
     if (qv_sink > qv_avail) {
       const double fract = qv_avail / qv_sink;
       r.qv2qi_nucleat_tend *= fract;
@@ -1052,8 +1129,8 @@ __device__ __forceinline__ void prevent_liq_supersaturation(double pres, double 
   const double A = C::LatVap * qsl * dt * C::INV_CP / (C::RV * T_endstep * T_endstep) *
                    ((C::LatVap + C::LatIce) * r.qi2qv_sublim_tend + C::LatVap * r.qr2qv_evap_tend);
   double frac = (qsl - qv + qv_sinks * dt + A) / (qv_sources * dt + A);
-  frac = vmax(0., frac);
-  frac = vmin(1., frac);
+  frac = dmax_0x(frac);
+  frac = dlt(frac, 1.) ? frac : 1.;
   r.qi2qv_sublim_tend = frac * r.qi2qv_sublim_tend;
   r.qr2qv_evap_tend = frac * r.qr2qv_evap_tend;
 }
@@ -1064,9 +1141,9 @@ __device__ __forceinline__ void prevent_liq_supersaturation(double pres, double 
 __device__ __forceinline__ void ice_supersat_conservation_bulk(Rates<float>& r, double cld_frac_i, double qv,
                                                                double qv_sat_i, double t_atm, double dt) {
   const float qv_sink = r.qv2qi_vapdep_tend + r.qv2qi_nucleat_tend;
-  if (qv_sink > float(C::QSMALL) && cld_frac_i > 1e-20) {
+  if (qv_sink > float(C::QSMALL) && dgt(cld_frac_i, 1e-20)) {
     const float dtf = float(dt);
-    const double resid = qv + double((r.qi2qv_sublim_tend + r.qr2qv_evap_tend) * dtf) - qv_sat_i;
+    const double resid = qv + f2d((r.qi2qv_sublim_tend + r.qr2qv_evap_tend) * dtf) - qv_sat_i;
     const float tf = float(t_atm);
     constexpr float latsublim2 = float((C::LatVap + C::LatIce) * (C::LatVap + C::LatIce) / (C::CP * C::RH2O));
     float qv_avail = float(resid) / (1.0f + latsublim2 * float(qv_sat_i) / (tf * tf)) / dtf;
@@ -1087,12 +1164,12 @@ __device__ __forceinline__ bool prevent_liq_supersaturation_bulk(double inv_p, d
   const float dtf = float(dt);
   const float qv_sinks = r.qv2qi_vapdep_tend + r.qv2qi_nucleat_tend;
   constexpr float lvs = float((C::LatVap + C::LatIce) * C::INV_CP), lv = float(C::LatVap * C::INV_CP);
-  const double T_endstep = t_atm + double(((qv_sinks - r.qi2qv_sublim_tend) * lvs - r.qr2qv_evap_tend * lv) * dtf);
+  const double T_endstep = t_atm + f2d(((qv_sinks - r.qi2qv_sublim_tend) * lvs - r.qr2qv_evap_tend * lv) * dtf);
   const double qsl = C::ep_2 * svp_tabulated(rt.svp_tab, T_endstep, false, err) * inv_p; /* inv_p = 1 / max(p, 1e-3) */
   const float te = float(T_endstep);
   const float A = float(C::LatVap * C::INV_CP / C::RV) * float(qsl) * dtf / (te * te) *
                   (float(C::LatVap + C::LatIce) * r.qi2qv_sublim_tend + float(C::LatVap) * r.qr2qv_evap_tend);
-  const double resid = qsl - qv + double(qv_sinks * dtf);
+  const double resid = qsl - qv + f2d(qv_sinks * dtf);
   float frac = (float(resid) + A) / (qv_sources * dtf + A);
   frac = vmax(0.0f, frac);
   frac = vmin(1.0f, frac);
@@ -1114,7 +1191,7 @@ __device__ __forceinline__ void update_prognostics(const Rates<double>& r, doubl
   s.qr = s.qr + (-r.qr2qi_collect_tend + r.qi2qr_melt_tend - r.qr2qi_immers_freeze_tend + r.qc2qr_ice_shed_tend) * dt;
   s.nr = s.nr + (-r.nr_collect_tend - r.nr2ni_immers_freeze_tend + C::nmltratio * r.ni2nr_melt_tend +
                  r.nr_ice_shed_tend + r.ncshdc) * dt;
-  if (s.qi >= C::QSMALL) {
+  if (dge(s.qi, C::QSMALL)) {
     s.bm = s.bm - ((r.qi2qv_sublim_tend + r.qi2qr_melt_tend) / s.qi) * dt * s.bm;
     s.qm = s.qm - ((r.qi2qv_sublim_tend + r.qi2qr_melt_tend) * s.qm / s.qi) * dt;
     s.qi = s.qi - (r.qi2qv_sublim_tend + r.qi2qr_melt_tend) * dt;
@@ -1127,7 +1204,7 @@ __device__ __forceinline__ void update_prognostics(const Rates<double>& r, doubl
                  (r.qr2qi_immers_freeze_tend + r.qc2qi_hetero_freeze_tend) * C::INV_RHO_RIMEMAX) * dt;
   s.ni = s.ni + (r.ni_nucleat_tend - r.ni2nr_melt_tend - r.ni_sublim_tend - r.ni_selfcollect_tend +
                  r.nr2ni_immers_freeze_tend + r.nc2ni_immers_freeze_tend) * dt;
-  if (s.qm < 0) { s.qm = 0; s.bm = 0; }
+  if (dneg(s.qm)) { s.qm = 0; s.bm = 0; }
   if (log_wetgrowth) { s.qm = s.qi; s.bm = s.qm * C::INV_RHO_RIMEMAX; }
   s.qv = s.qv + (-r.qv2qi_vapdep_tend + r.qi2qv_sublim_tend - r.qv2qi_nucleat_tend) * dt;
   s.th = s.th + inv_exner * ((r.qv2qi_vapdep_tend - r.qi2qv_sublim_tend + r.qv2qi_nucleat_tend) *
@@ -1160,7 +1237,7 @@ __device__ __forceinline__ void update_prognostics_bulk(const Rates<float>& r, d
   const float dtf = float(dt);
   const float sink_i = r.qi2qv_sublim_tend + r.qi2qr_melt_tend;
   float dqi = 0, dqm = 0, dbm = 0;
-  if (s.qi >= C::QSMALL) {
+  if (dge(s.qi, C::QSMALL)) {
     const float frac = sink_i * dtf / float(s.qi);
     dbm = -frac * float(s.bm);
     dqm = -frac * float(s.qm);
@@ -1195,31 +1272,31 @@ __device__ __forceinline__ void update_prognostics_bulk(const Rates<float>& r, d
    * leave ~1e-7 of the sources instead.  The same holds for ni and, when
    * predicted, nc, whose limiters count exactly the update's terms (the nr
    * limiter counts nc2nr_autoconv where the update adds ncautr). */
-  const double Dqc = (wlim & 1) ? -s.qc : double(dqc);
-  const double Dqr = (wlim & 2) ? -s.qr + double((r_lim.qr2qv_evap_tend - r.qr2qv_evap_tend) * dtf) : double(dqr);
-  const double Dqi = ((wlim & 4) && s.qi >= C::QSMALL)
-                         ? -s.qi + double(((r.qv2qi_vapdep_tend - r_lim.qv2qi_vapdep_tend) +
-                                           (r.qv2qi_nucleat_tend - r_lim.qv2qi_nucleat_tend) -
-                                           (r.qi2qv_sublim_tend - r_lim.qi2qv_sublim_tend)) * dtf)
-                         : double(dqi);
+  const double Dqc = (wlim & 1) ? -s.qc : f2d(dqc);
+  const double Dqr = (wlim & 2) ? -s.qr + f2d((r_lim.qr2qv_evap_tend - r.qr2qv_evap_tend) * dtf) : f2d(dqr);
+  const double Dqi = ((wlim & 4) && dge(s.qi, C::QSMALL))
+                         ? -s.qi + f2d(((r.qv2qi_vapdep_tend - r_lim.qv2qi_vapdep_tend) +
+                                        (r.qv2qi_nucleat_tend - r_lim.qv2qi_nucleat_tend) -
+                                        (r.qi2qv_sublim_tend - r_lim.qi2qv_sublim_tend)) * dtf)
+                         : f2d(dqi);
   s.qi = s.qi + Dqi;
-  s.qm = s.qm + double(dqm);
-  s.bm = s.bm + double(dbm);
-  s.ni = (nlim & 4) ? 0.0 : s.ni + double(dni);
-  if (s.qm < 0) { s.qm = 0; s.bm = 0; }
+  s.qm = s.qm + f2d(dqm);
+  s.bm = s.bm + f2d(dbm);
+  s.ni = (nlim & 4) ? 0.0 : s.ni + f2d(dni);
+  if (dneg(s.qm)) { s.qm = 0; s.bm = 0; }
   if (log_wetgrowth) { s.qm = s.qi; s.bm = s.qm * C::INV_RHO_RIMEMAX; }
   s.qc = s.qc + Dqc;
   s.qr = s.qr + Dqr;
   s.qv = s.qv - (Dqc + Dqr + Dqi);
-  s.th = s.th + inv_exner * double(dth);
+  s.th = s.th + inv_exner * f2d(dth);
   if (predictNc || prescribedCCN) {
     float dnc = (-r.nc_accret_tend - r.nc2nr_autoconv_tend + r.nc_selfcollect_tend) * dtf;
     if (predictNc) dnc += (-r.nc_collect_tend - r.nc2ni_immers_freeze_tend) * dtf;
-    s.nc = ((nlim & 1) && predictNc) ? 0.0 : s.nc + double(dnc);
+    s.nc = ((nlim & 1) && predictNc) ? 0.0 : s.nc + f2d(dnc);
   } else {
     s.nc = C::NCCNST * inv_rho;
   }
-  s.nr = s.nr + double(dnr);
+  s.nr = s.nr + f2d(dnr);
 }
 
 }  // namespace dev
