@@ -119,8 +119,8 @@ template <int LANES>
 __device__ __forceinline__ bool group_any(unsigned mask, bool p) {
   return __ballot_sync(mask, p) != 0u;
 }
-template <int LANES>
-__device__ __forceinline__ double group_max(unsigned mask, double v) {
+template <int LANES, class T>
+__device__ __forceinline__ T group_max(unsigned mask, T v) {
 #pragma unroll
   for (int o = LANES / 2; o > 0; o >>= 1) v = vmax(v, __shfl_xor_sync(mask, v, o, LANES));
   return v;
@@ -1004,7 +1004,7 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
         G[2][k] = make_float2(0.f, 0.f);
         G[3][k] = make_float2(0.f, 0.f);
       }
-      if (q >= C::QSMALL) {
+      if (dge(q, C::QSMALL)) {
         my_top = min(my_top, k);
         my_bot = max(my_bot, k);
       }
@@ -1017,10 +1017,13 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
     }
     __syncwarp(mask);
 
-    double dt_left = dt;
+    /* The substep schedule is FP32 scalar work: one dt_sub scales every face
+     * flux of a substep alike, so its rounding only changes that substep's
+     * length by ~1e-7 relative and leaves the mass budget exact. */
+    float dt_left = float(dt);
     bool first = true;
     int nsub = 0;
-    while (dt_left > C::dt_left_tol) {
+    while (dt_left > float(C::dt_left_tol)) {
       if (++nsub > kMaxSubsteps) {
         err |= kErrSubstep;
         break;
@@ -1039,7 +1042,7 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
           const float n_plain = R1f[k] * icf;
           float qc_f = R0f[k] * icf, n_in = n_plain;
           if (first) {
-            if (B0[co + k] >= C::QSMALL) {
+            if (dge(B0[co + k], C::QSMALL)) {
               n_in = vmax(n_in, 0.0f);
             } else {
               qc_f = 0;
@@ -1063,7 +1066,7 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
           const float n_plain = R1f[k] * icf;
           float qr_f = R0f[k] * icf, n_in = n_plain;
           if (first) {
-            if (B0[co + k] >= C::QSMALL) {
+            if (dge(B0[co + k], C::QSMALL)) {
               n_in = vmax(n_in, 0.0f);
             } else {
               qr_f = 0;
@@ -1088,13 +1091,13 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
           const float ni_plain = R1f[k] * icf, qm_plain = R2f[k] * icf, bm_plain = R3f[k] * icf;
           float qi_f = R0f[k] * icf, ni_f = ni_plain, qm_f = qm_plain, bm_f = bm_plain;
           if (first) {
-            if (B0[co + k] >= C::QSMALL) {
+            if (dge(B0[co + k], C::QSMALL)) {
               ni_f = vmax(ni_f, 0.0f);
             } else {
               qi_f = 0;
               ni_f = 0;
             }
-            if (B0[co + k] >= C::QSMALL && B2[co + k] >= C::QSMALL) {
+            if (dge(B0[co + k], C::QSMALL) && dge(B2[co + k], C::QSMALL)) {
               bm_f = vmax(R3f[k] * (1.0f / float(in.cld_frac_l[co + k])), 0.0f);
             } else {
               qm_f = 0;
@@ -1135,15 +1138,13 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
         V1f[k_qxbot + 1] = 0; /* the cell receiving the leading edge has no fall speed */
         V2f[k_qxbot + 1] = 0;
       }
-      const double Co_max = double(group_max<LANES>(mask, lmax)) * dt_left;
-      if (!(Co_max >= 0) || Co_max > 2.0e9) {
+      const float Co_max = group_max<LANES>(mask, lmax) * dt_left;
+      if (!(Co_max >= 0.0f) || Co_max > 2.0e9f) {
         err |= kErrNumeric;
         break;
       }
-      const int tmpint1 = static_cast<int>(Co_max + 1);
-      const double dt_sub = dt_left / tmpint1;
-      const dfloat dt_sub_d = dfloat_of(dt_sub);
-      const float dt_sub_f = dt_sub_d.hi;
+      const int tmpint1 = static_cast<int>(Co_max + 1.0f);
+      const float dt_sub = dt_left / float(tmpint1);
       const int k_temp = (k_qxbot == kbot) ? k_qxbot : k_qxbot + 1;
       /* FP32 fluxes from the shadows; double-float time-integrated face
        * fluxes; the shadows follow with the FP32 flux divergence */
@@ -1173,16 +1174,16 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
           uf0 = cf0; uf1 = cf1; uf2 = cf2; uf3 = cf3;
         }
         if (act) {
-          const float coef_f = COEFf[k] * dt_sub_f;
-          dfloat_add_prod(G[0][k], f0, dt_sub_d);
+          const float coef_f = COEFf[k] * dt_sub;
+          dfloat_add_prod(G[0][k], f0, dt_sub);
           R0f[k] += (uf0 - f0) * coef_f;
           if (nfield > 1) {
-            dfloat_add_prod(G[1][k], f1, dt_sub_d);
+            dfloat_add_prod(G[1][k], f1, dt_sub);
             R1f[k] += (uf1 - f1) * coef_f;
           }
           if (nfield > 2) {
-            dfloat_add_prod(G[2][k], f2, dt_sub_d);
-            dfloat_add_prod(G[3][k], f3, dt_sub_d);
+            dfloat_add_prod(G[2][k], f2, dt_sub);
+            dfloat_add_prod(G[3][k], f3, dt_sub);
             R2f[k] += (uf2 - f2) * coef_f;
             R3f[k] += (uf3 - f3) * coef_f;
           }

@@ -145,21 +145,11 @@ __device__ __forceinline__ double dmax_0x(double x) { return dpos(x) ? x : 0.0; 
 /* Double-float accumulators on the FP32 pipe: a value is the unevaluated sum
  * hi + lo of two floats with |lo| <= ulp(hi) / 2 (about 48 significant bits).
  * Additions use Knuth's TwoSum followed by Dekker's Fast2Sum renormalisation;
- * the product of a float by a double-float uses the FMA error-free product.
+ * the product of two floats is made exact with the FMA error-free product.
  * Every step is a correctly rounded FP32 operation written with the _rn
  * intrinsics, so the compiler can neither contract nor reorder it.  One update
  * costs ~14 FP32 instructions, against one FP64 FMA that occupies the FP64
  * pipe for the issue time of ~64 FP32 instructions on this part. */
-struct dfloat {
-  float hi, lo;
-};
-
-/* the double-float nearest x (hi = x rounded to float, lo = the remainder) */
-__device__ __forceinline__ dfloat dfloat_of(double x) {
-  const float h = float(x);
-  return {h, float(x - double(h))};
-}
-
 /* exact value as a double: |lo| <= ulp(hi)/2, so hi + lo spans <= 48 bits */
 __device__ __forceinline__ double dfloat_value(float2 g) { return f2d(g.x) + f2d(g.y); }
 
@@ -176,10 +166,10 @@ __device__ __forceinline__ void dfloat_add(float2& g, float a) {
   g = dfloat_renorm(s, __fadd_rn(e, g.y));
 }
 
-/* g += a * t */
-__device__ __forceinline__ void dfloat_add_prod(float2& g, float a, dfloat t) {
-  const float ph = __fmul_rn(a, t.hi);
-  const float pl = __fmaf_rn(a, t.lo, __fmaf_rn(a, t.hi, -ph));
+/* g += a * t, with the product a * t formed exactly (ph + pl) */
+__device__ __forceinline__ void dfloat_add_prod(float2& g, float a, float t) {
+  const float ph = __fmul_rn(a, t);
+  const float pl = __fmaf_rn(a, t, -ph);
   const float s = __fadd_rn(g.x, ph);
   const float bb = __fsub_rn(s, g.x);
   const float e = __fadd_rn(__fsub_rn(g.x, __fsub_rn(s, bb)), __fsub_rn(ph, bb));
