@@ -94,6 +94,11 @@ enum { S_TATM = 0, S_RHO, S_RHOFACR, S_RHOFACI, S_ACN, kScrFields };
 __device__ __forceinline__ double* scr_at(const Inst& in, int f, int col) {
   return in.scr + (int64_t(f) * in.ncol + col) * in.ld;
 }
+/* FP32-bulk: the float-valued hand-over fields (rho, fall-speed factors,
+ * acn) hold floats in the first half of each column's row */
+__device__ __forceinline__ float* scr_f(const Inst& in, int f, int col) {
+  return reinterpret_cast<float*>(scr_at(in, f, col));
+}
 
 /* bytes of the K1->K2/K3 scratch of an instance (doubles, then the flags) */
 __host__ __device__ inline size_t scratch_bytes(int ncol, int64_t ld) {
@@ -223,9 +228,10 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
   const double inv_dt = 1 / dt;
   const bool predictNc = in.predictNc != 0, prescribedCCN = in.prescribedCCN != 0;
   const bool do_ice = rt.do_ice_production != 0;
-  const int kbot = nk - 1, ktop = 0;
-  (void)ktop;
 #define SMA(a, k) sm[(a)*S + (k)]
+  /* FP32-bulk: the float-valued slots (rho, fall-speed factors, acn) hold
+   * floats in the first half of their slot */
+#define SMF(a) reinterpret_cast<float*>(&sm[(a)*S])
 
   /* ---------------- phase 1: p3_main_init + p3_main_part1 ---------------- */
   bool nucl = false, hydro = false;
@@ -253,6 +259,7 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
     in.vap_ice_exchange[o] = 0;
 
     double rho, inv_rho, qvsl, qvsi, qvssi, ccn_nc;
+    TR rho_t, inv_rho_t;
     const double exner = 1 / inv_exner;
     double T = th * exner;
     qv = dmax0(qv);
@@ -260,6 +267,8 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
       const double inv_cld_l = 1 / cld_l;
       rho = dpres / dz / C::gravit;
       inv_rho = 1 / rho;
+      rho_t = rho;
+      inv_rho_t = inv_rho;
       qvsl = qv_sat_dry(T, pres, false, err);
       qvsi = qv_sat_dry(T, pres, true, err);
       qvssi = qv / qvsi - 1;
@@ -267,11 +276,14 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
     } else {
       /* FP32-bulk: rho and 1/rho only feed rates, fall speeds and fluxes
        * (the sedimentation's FP64 coefficient is g / dpres), so they are
-       * FP32; one FP64 division for the pressure shared by both saturation
-       * ratios; the supersaturation ratio (threshold and rate input) in FP32 */
+       * FP32 and kept as floats in the shared slots and the hand-over; one
+       * FP64 division for the pressure shared by both saturation ratios; the
+       * supersaturation ratio (threshold and rate input) in FP32 */
       const float rho_f = float(dpres) / (float(dz) * float(C::gravit));
+      rho_t = rho_f;
       rho = f2d(rho_f);
-      inv_rho = f2d(1.0f / rho_f);
+      inv_rho_t = 1.0f / rho_f;
+      inv_rho = f2d(inv_rho_t);
       const double inv_p = 1 / dmax_c(pres, 1.e-3);
       SMA(A_INVP, k) = inv_p;
       qvsl = C::ep_2 * svp_tabulated(rt.svp_tab, T, false, err) * inv_p;
@@ -279,15 +291,21 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
       qvssi = f2d(float(qv) / float(qvsi) - 1.0f);
       ccn_nc = rt.spa_ccn_to_nc_factor * in.nccn[o] * cld_l;
     }
-    const TR rhofacr = m_pow(TR(C::RHO_1000MB) * TR(inv_rho), TR(.54));
-    const TR rhofaci = m_pow(TR(C::RHO_600MB) * TR(inv_rho), TR(.54));
+    const TR rhofacr = m_pow(TR(C::RHO_1000MB) * inv_rho_t, TR(.54));
+    const TR rhofaci = m_pow(TR(C::RHO_600MB) * inv_rho_t, TR(.54));
     const TR dum = TR(1.496e-6) * m_pow(TR(T), TR(1.5)) / (TR(T) + TR(120));
     const TR acn = TR(C::gravit) * TR(C::RHO_H2O) / (TR(18) * dum);
     if (dlt(T, C::T_zerodegc) && dge_neg(qvssi, -0.05)) nucl = true;
 
+    /* A species below qsmall goes to vapour; a +0 moves nothing, so its FP64
+     * updates are skipped (bitwise the same result). */
+    bool th_changed = false;
     if (dlt(qc, C::QSMALL)) {
-      qv = qv + qc;
-      th = th - inv_exner * qc * C::LatVap * C::INV_CP;
+      if (dnz(qc)) {
+        qv = qv + qc;
+        th = th - inv_exner * qc * C::LatVap * C::INV_CP;
+        th_changed = true;
+      }
       qc = 0;
       nc = 0;
     } else {
@@ -301,16 +319,22 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
       }
     }
     if (dlt(qr, C::QSMALL)) {
-      qv = qv + qr;
-      th = th - inv_exner * qr * C::LatVap * C::INV_CP;
+      if (dnz(qr)) {
+        qv = qv + qr;
+        th = th - inv_exner * qr * C::LatVap * C::INV_CP;
+        th_changed = true;
+      }
       qr = 0;
       nr = 0;
     } else {
       hydro = true;
     }
     if (dlt(qi, C::QSMALL) || (dlt(qi, 1.e-8) && dlt_neg(qvssi, -0.1))) {
-      qv = qv + qi;
-      th = th - inv_exner * qi * (C::LatVap + C::LatIce) * C::INV_CP;
+      if (dnz(qi)) {
+        qv = qv + qi;
+        th = th - inv_exner * qi * (C::LatVap + C::LatIce) * C::INV_CP;
+        th_changed = true;
+      }
       qi = 0; ni = 0; qm = 0; bm = 0;
     } else {
       hydro = true;
@@ -318,18 +342,26 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
     if (dge(qi, C::QSMALL) && dlt(qi, 1.e-8) && dge(T, C::T_zerodegc)) {
       qr = qr + qi;
       th = th - inv_exner * qi * C::LatIce * C::INV_CP;
+      th_changed = true;
       qi = 0; ni = 0; qm = 0; bm = 0;
     }
-    T = th * exner;
+    if (th_changed) T = th * exner;
 
     in.qc[o] = qc; in.nc[o] = nc; in.qr[o] = qr; in.nr[o] = nr;
     in.qi[o] = qi; in.ni[o] = ni; in.qm[o] = qm; in.bm[o] = bm;
     in.qv[o] = qv; in.th[o] = th;
     SMA(A_TATM, k) = T;
-    SMA(A_RHO, k) = rho;
-    SMA(A_RHOFACR, k) = widen(rhofacr);
-    SMA(A_RHOFACI, k) = widen(rhofaci);
-    SMA(A_ACN, k) = widen(acn);
+    if constexpr (kF64) {
+      SMA(A_RHO, k) = rho;
+      SMA(A_RHOFACR, k) = rhofacr;
+      SMA(A_RHOFACI, k) = rhofaci;
+      SMA(A_ACN, k) = acn;
+    } else {
+      SMF(A_RHO)[k] = rho_t;
+      SMF(A_RHOFACR)[k] = rhofacr;
+      SMF(A_RHOFACI)[k] = rhofaci;
+      SMF(A_ACN)[k] = acn;
+    }
     SMA(A_QVSL, k) = qvsl;
     SMA(A_QVSI, k) = qvsi;
     SMA(A_QVSSI, k) = qvssi;
@@ -364,11 +396,23 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
     const double pres = in.pres[o];
     const double cld_i = in.cld_frac_i[o], cld_l = in.cld_frac_l[o], cld_r = in.cld_frac_r[o];
     const double inv_exner = in.inv_exner[o];
-    const double rho = SMA(A_RHO, k);
-    const double inv_rho = kF64 ? 1 / rho : f2d(1.0f / float(rho));
     const double qvsl = SMA(A_QVSL, k), qvsi = SMA(A_QVSI, k);
-    const double rhofaci = SMA(A_RHOFACI, k);
-    const double acn = SMA(A_ACN, k);
+    TR rho_t, inv_rho_t, rhofaci_t, acn_t;
+    double inv_rho;
+    if constexpr (kF64) {
+      const double rho = SMA(A_RHO, k);
+      rho_t = rho;
+      inv_rho = 1 / rho;
+      inv_rho_t = inv_rho;
+      rhofaci_t = SMA(A_RHOFACI, k);
+      acn_t = SMA(A_ACN, k);
+    } else {
+      rho_t = SMF(A_RHO)[k];
+      inv_rho_t = 1.0f / rho_t;
+      inv_rho = f2d(inv_rho_t);
+      rhofaci_t = SMF(A_RHOFACI)[k];
+      acn_t = SMF(A_ACN)[k];
+    }
     /* In-cloud values.  FP32-bulk: reciprocal cloud fractions in FP32 (the
      * in-cloud values only feed rates) and the FP64 state is rewritten below
      * only where a DSD or rime limiter changed an in-cloud value. */
@@ -392,9 +436,9 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
     bool wet = false;
     (void)epsc;
 
-    const bool skip_micro = !(inc.qc >= C::QSMALL || inc.qr >= C::QSMALL || inc.qi >= C::QSMALL);
+    const bool skip_micro = !(dge(inc.qc, C::QSMALL) || dge(inc.qr, C::QSMALL) || dge(inc.qi, C::QSMALL));
     if (!skip_micro) {
-      const TR T_r = TR(T), rho_r = TR(rho), rhofaci_r = TR(rhofaci);
+      const TR T_r = TR(T), rho_r = rho_t, rhofaci_r = rhofaci_t;
       get_time_space_phys_variables<TR>(T_r, TR(pres), rho_r, TR(qvsl), TR(qvsi), v);
       {
         const TR n_in = TR(inc.nc);
@@ -418,7 +462,7 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
         impose_max_total_ni(inc.ni, rt.max_total_ni, inv_rho);
       } else {
         float ni_f = float(inc.ni);
-        impose_max_total_ni(ni_f, rt.max_total_ni, float(inv_rho));
+        impose_max_total_ni(ni_f, rt.max_total_ni, inv_rho_t);
         inc.ni = f2d(ni_f);
       }
       if (dge(inc.qi, C::QSMALL)) {
@@ -484,7 +528,7 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
       } else {
         epsi = TR(0);
       }
-      rho_qm_cloud = calc_rime_density<TR>(T_r, rhofaci_r, tv_fallspd, TR(acn), lamc, mu_c, qc_r,
+      rho_qm_cloud = calc_rime_density<TR>(T_r, rhofaci_r, tv_fallspd, acn_t, lamc, mu_c, qc_r,
                                            r.qc2qi_collect_tend);
       if (do_ice) {
         cldliq_immersion_freezing<TR>(T_r, lamc, mu_c, nc_r, qc_r, r, rt);
@@ -526,13 +570,13 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
       }
     }
     if (do_ice) {
-      ice_nucleation<TR>(TR(T), TR(inv_rho), TR(s.ni), TR(in.ni_activated[o]), qvssi, TR(inv_dt), predictNc,
+      ice_nucleation<TR>(TR(T), inv_rho_t, TR(s.ni), TR(in.ni_activated[o]), qvssi, TR(inv_dt), predictNc,
                          prescribedCCN, r, rt);
     }
-    cloud_water_autoconversion<TR>(TR(rho), TR(inc.qc), TR(inc.nc), r, rt);
+    cloud_water_autoconversion<TR>(rho_t, TR(inc.qc), TR(inc.nc), r, rt);
     if (dge(inc.qc, C::QSMALL)) r.nc_selfcollect_tend = TR(0);
     cloud_rain_accretion<TR>(TR(inc.qc), TR(inc.nc), TR(inc.qr), r, rt);
-    rain_self_collection<TR>(TR(rho), TR(inc.qr), TR(inc.nr), r, rt);
+    rain_self_collection<TR>(rho_t, TR(inc.qr), TR(inc.nr), r, rt);
     back_to_cell_average<TR>(TR(cld_l), TR(cld_r), TR(cld_i), r);
 
     if constexpr (sizeof(TR) == sizeof(double)) {
@@ -564,24 +608,30 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
                                     r.qc2qi_berg_tend + r.qc2qi_collect_tend + r.qr2qi_collect_tend);
 
     if (dlt(s.qc, C::QSMALL)) {
-      s.qv = s.qv + s.qc;
-      s.th = s.th - inv_exner * s.qc * C::LatVap * C::INV_CP;
+      if (dnz(s.qc)) {
+        s.qv = s.qv + s.qc;
+        s.th = s.th - inv_exner * s.qc * C::LatVap * C::INV_CP;
+      }
       s.qc = 0;
       s.nc = 0;
     } else {
       hydro = true;
     }
     if (dlt(s.qr, C::QSMALL)) {
-      s.qv = s.qv + s.qr;
-      s.th = s.th - inv_exner * s.qr * C::LatVap * C::INV_CP;
+      if (dnz(s.qr)) {
+        s.qv = s.qv + s.qr;
+        s.th = s.th - inv_exner * s.qr * C::LatVap * C::INV_CP;
+      }
       s.qr = 0;
       s.nr = 0;
     } else {
       hydro = true;
     }
     if (dlt(s.qi, C::QSMALL)) {
-      s.qv = s.qv + s.qi;
-      s.th = s.th - inv_exner * s.qi * (C::LatVap + C::LatIce) * C::INV_CP;
+      if (dnz(s.qi)) {
+        s.qv = s.qv + s.qi;
+        s.th = s.th - inv_exner * s.qi * (C::LatVap + C::LatIce) * C::INV_CP;
+      }
       s.qi = 0; s.ni = 0; s.qm = 0; s.bm = 0;
     } else {
       hydro = true;
@@ -592,7 +642,7 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
       s.ni = ni_incld * cld_i;
     } else if (dge(s.ni, 1e-20)) {
       /* impose_max_total_ni as a factor applied only when it limits */
-      const float f = vmin(float(rt.max_total_ni) * float(inv_rho) * float(cld_i) / float(s.ni), 1.0f);
+      const float f = vmin(float(rt.max_total_ni) * inv_rho_t * float(cld_i) / float(s.ni), 1.0f);
       if (f < 1.0f) s.ni = s.ni * f2d(f);
     }
     in.qc[o] = s.qc; in.nc[o] = s.nc; in.qr[o] = s.qr; in.nr[o] = s.nr;
@@ -605,13 +655,21 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
   }
   for (int k = lane; k < nk; k += LANES) {
     scr_at(in, S_TATM, col)[k] = SMA(A_TATM, k);
-    scr_at(in, S_RHO, col)[k] = SMA(A_RHO, k);
-    scr_at(in, S_RHOFACR, col)[k] = SMA(A_RHOFACR, k);
-    scr_at(in, S_RHOFACI, col)[k] = SMA(A_RHOFACI, k);
-    scr_at(in, S_ACN, col)[k] = SMA(A_ACN, k);
+    if constexpr (kF64) {
+      scr_at(in, S_RHO, col)[k] = SMA(A_RHO, k);
+      scr_at(in, S_RHOFACR, col)[k] = SMA(A_RHOFACR, k);
+      scr_at(in, S_RHOFACI, col)[k] = SMA(A_RHOFACI, k);
+      scr_at(in, S_ACN, col)[k] = SMA(A_ACN, k);
+    } else {
+      scr_f(in, S_RHO, col)[k] = SMF(A_RHO)[k];
+      scr_f(in, S_RHOFACR, col)[k] = SMF(A_RHOFACR)[k];
+      scr_f(in, S_RHOFACI, col)[k] = SMF(A_RHOFACI)[k];
+      scr_f(in, S_ACN, col)[k] = SMF(A_ACN)[k];
+    }
   }
   if (lane == 0) in.cflag[col] = 1;
 #undef SMA
+#undef SMF
 }
 
 /* K2 (FP64 form): cloud, rain and ice sedimentation of one column that went
@@ -961,7 +1019,7 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
   float2* const PF = G[2]; /* rain flux accumulator (rain has two fields) */
   for (int k = lane; k < nk; k += LANES) {
     const double coef = C::gravit / in.dpres[co + k];
-    RHOf[k] = float(scr_at(in, S_RHO, col)[k]);
+    RHOf[k] = scr_f(in, S_RHO, col)[k];
     INVDZf[k] = 1.0f / float(in.dz[co + k]);
     COEF[k] = coef;
     COEFf[k] = float(coef);
@@ -977,7 +1035,7 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
     double* const Bf[4] = {B0, B1, B2, B3};
     const double* cldp = sp == 0 ? in.cld_frac_l : (sp == 1 ? in.cld_frac_r : in.cld_frac_i);
     const int sfac = sp == 0 ? S_ACN : (sp == 1 ? S_RHOFACR : S_RHOFACI);
-    const double* const facp = scr_at(in, sfac, col);
+    const float* const facp = scr_f(in, sfac, col);
     const int nfield = sp == 0 ? (predictNc ? 2 : 1) : (sp == 1 ? 2 : 4);
     const int nstate = sp == 2 ? 4 : 2; /* fields that limiters may rewrite */
     float* const Rf[4] = {R0f, R1f, R2f, R3f};
@@ -995,7 +1053,7 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
       R0f[k] = float(q);
       R1f[k] = float(B1[co + k]);
       CLDf[k] = float(cldp[co + k]);
-      FACf[k] = float(facp[k]);
+      FACf[k] = facp[k];
       G[0][k] = make_float2(0.f, 0.f);
       G[1][k] = make_float2(0.f, 0.f);
       if (sp == 2) {
@@ -1240,7 +1298,7 @@ __device__ void p3_part3(const Inst& in, const int col, const KParams<TR>& kp, c
   const int64_t co = int64_t(col) * in.ld;
   const bool do_ice = rt.do_ice_production != 0;
   const double* const t_start = scr_at(in, S_TATM, col);
-  const double* const rho_k = scr_at(in, S_RHO, col);
+  constexpr bool kF64 = sizeof(TR) == sizeof(double);
   /* ---------------- phase 4: homogeneous freezing + p3_main_part3 ---------------- */
   for (int k = lane; k < nk; k += LANES) {
     const int64_t o = co + k;
@@ -1250,17 +1308,25 @@ __device__ void p3_part3(const Inst& in, const int col, const KParams<TR>& kp, c
     s.qv = in.qv[o]; s.th = in.th[o];
     const double inv_exner = in.inv_exner[o];
     const double cld_l = in.cld_frac_l[o], cld_r = in.cld_frac_r[o], cld_i = in.cld_frac_i[o];
-    const double rho = rho_k[k];
-    const double inv_rho = sizeof(TR) == sizeof(double) ? 1 / rho : double(1.0f / float(rho));
+    /* rho: FP64 in the plain form, a float in the FP32-bulk hand-over */
+    double rho = 0, inv_rho = 0;
+    float rho_f = 0.f, inv_rho_f = 0.f;
+    if constexpr (kF64) {
+      rho = scr_at(in, S_RHO, col)[k];
+      inv_rho = 1 / rho;
+    } else {
+      rho_f = scr_f(in, S_RHO, col)[k];
+      inv_rho_f = 1.0f / rho_f;
+    }
     double vap_liq = in.vap_liq_exchange[o];
     double eff_qc = in.diag_eff_radius_qc[o], eff_qr = in.diag_eff_radius_qr[o], eff_qi = in.diag_eff_radius_qi[o];
     double rho_qi = 0;
 
     /* homogeneous_freezing, p3/impl/p3_ice_sed_impl.hpp:207-270 */
-    if (do_ice && t_start[k] < C::T_homogfrz) {
+    if (do_ice && dlt(t_start[k], C::T_homogfrz)) {
       const double Qc_nuc = s.qc, Qr_nuc = s.qr;
-      const double Nc_nuc = vmax(s.nc, C::NSMALL), Nr_nuc = vmax(s.nr, C::NSMALL);
-      const bool qc_ge = s.qc >= C::QSMALL, qr_ge = s.qr >= C::QSMALL;
+      const double Nc_nuc = dmax_c(s.nc, C::NSMALL), Nr_nuc = dmax_c(s.nr, C::NSMALL);
+      const bool qc_ge = dge(s.qc, C::QSMALL), qr_ge = dge(s.qr, C::QSMALL);
       if (qc_ge) {
         s.qm = s.qm + Qc_nuc;
         s.qi = s.qi + Qc_nuc;
@@ -1281,7 +1347,7 @@ __device__ void p3_part3(const Inst& in, const int col, const KParams<TR>& kp, c
 
     if constexpr (sizeof(TR) == sizeof(double)) {
       /* part3: cloud */
-      if (s.qc >= C::QSMALL) {
+      if (dge(s.qc, C::QSMALL)) {
         const double qc_incld = s.qc / cld_l;
         double nc_incld = s.nc / cld_l;
         TR mu_c, lamc;
@@ -1292,14 +1358,16 @@ __device__ void p3_part3(const Inst& in, const int col, const KParams<TR>& kp, c
         s.nc = nc_incld * cld_l;
         eff_qc = double(TR(0.5) * (mu_c + TR(3)) / lamc);
       } else {
-        s.qv = s.qv + s.qc;
-        s.th = s.th - inv_exner * s.qc * C::LatVap * C::INV_CP;
-        vap_liq = vap_liq - s.qc;
+        if (dnz(s.qc)) {
+          s.qv = s.qv + s.qc;
+          s.th = s.th - inv_exner * s.qc * C::LatVap * C::INV_CP;
+          vap_liq = vap_liq - s.qc;
+        }
         s.qc = 0;
         s.nc = 0;
       }
       /* part3: rain */
-      if (s.qr >= C::QSMALL) {
+      if (dge(s.qr, C::QSMALL)) {
         const double qr_incld = s.qr / cld_r;
         double nr_incld = s.nr / cld_r;
         TR mu_r = 0, lamr;
@@ -1310,16 +1378,18 @@ __device__ void p3_part3(const Inst& in, const int col, const KParams<TR>& kp, c
         s.nr = nr_incld * cld_r;
         eff_qr = double(TR(1.5) / lamr);
       } else {
-        s.qv = s.qv + s.qr;
-        s.th = s.th - inv_exner * s.qr * C::LatVap * C::INV_CP;
-        vap_liq = vap_liq - s.qr;
+        if (dnz(s.qr)) {
+          s.qv = s.qv + s.qr;
+          s.th = s.th - inv_exner * s.qr * C::LatVap * C::INV_CP;
+          vap_liq = vap_liq - s.qr;
+        }
         s.qr = 0;
         s.nr = 0;
       }
       /* part3: ice */
       {
-        const bool qi_gt_small = s.qi >= C::QSMALL;
-        s.ni = vmax(s.ni, C::NSMALL);
+        const bool qi_gt_small = dge(s.qi, C::QSMALL);
+        s.ni = dmax_c(s.ni, C::NSMALL);
         const double qi_incld = s.qi / cld_i;
         double ni_incld = s.ni / cld_i;
         double qm_incld = s.qm / cld_i;
@@ -1347,52 +1417,58 @@ __device__ void p3_part3(const Inst& in, const int col, const KParams<TR>& kp, c
           rho_qi = double(tv_dens);
         }
         s.ni = ni_incld * cld_i;
-        if (s.qm < C::QSMALL && qi_gt_small) {
+        if (dlt(s.qm, C::QSMALL) && qi_gt_small) {
           s.qm = 0;
           s.bm = 0;
         }
         if (!qi_gt_small) {
-          s.qv = s.qv + s.qi;
-          s.th = s.th - inv_exner * s.qi * (C::LatVap + C::LatIce) * C::INV_CP;
+          if (dnz(s.qi)) {
+            s.qv = s.qv + s.qi;
+            s.th = s.th - inv_exner * s.qi * (C::LatVap + C::LatIce) * C::INV_CP;
+          }
           s.qi = 0; s.ni = 0; s.qm = 0; s.bm = 0;
         }
       }
     } else {
       /* FP32-bulk part3: in-cloud values, DSDs and the diagnostics in FP32; the
        * FP64 state is rewritten only where a limiter changed an in-cloud value */
-      if (s.qc >= C::QSMALL) {
+      if (dge(s.qc, C::QSMALL)) {
         const float icl = 1.0f / float(cld_l);
         const float qc_f = float(s.qc) * icl;
         const float n_in = float(s.nc) * icl;
         float n_out = n_in, mu_c, lamc;
-        get_cloud_dsd2<float>(qc_f, n_out, mu_c, float(rho), lamc);
-        if (n_out != n_in) s.nc = double(n_out) * cld_l;
-        eff_qc = double(0.5f * (mu_c + 3.0f) / lamc);
+        get_cloud_dsd2<float>(qc_f, n_out, mu_c, rho_f, lamc);
+        if (n_out != n_in) s.nc = f2d(n_out) * cld_l;
+        eff_qc = f2d(0.5f * (mu_c + 3.0f) / lamc);
       } else {
-        s.qv = s.qv + s.qc;
-        s.th = s.th - inv_exner * s.qc * C::LatVap * C::INV_CP;
-        vap_liq = vap_liq - s.qc;
+        if (dnz(s.qc)) {
+          s.qv = s.qv + s.qc;
+          s.th = s.th - inv_exner * s.qc * C::LatVap * C::INV_CP;
+          vap_liq = vap_liq - s.qc;
+        }
         s.qc = 0;
         s.nc = 0;
       }
-      if (s.qr >= C::QSMALL) {
+      if (dge(s.qr, C::QSMALL)) {
         const float icr = 1.0f / float(cld_r);
         const float qr_f = float(s.qr) * icr;
         const float n_in = float(s.nr) * icr;
         float n_out = n_in, mu_r = 0, lamr;
         get_rain_dsd2<float>(qr_f, n_out, mu_r, lamr, rt);
-        if (n_out != n_in) s.nr = double(n_out) * cld_r;
-        eff_qr = double(1.5f / lamr);
+        if (n_out != n_in) s.nr = f2d(n_out) * cld_r;
+        eff_qr = f2d(1.5f / lamr);
       } else {
-        s.qv = s.qv + s.qr;
-        s.th = s.th - inv_exner * s.qr * C::LatVap * C::INV_CP;
-        vap_liq = vap_liq - s.qr;
+        if (dnz(s.qr)) {
+          s.qv = s.qv + s.qr;
+          s.th = s.th - inv_exner * s.qr * C::LatVap * C::INV_CP;
+          vap_liq = vap_liq - s.qr;
+        }
         s.qr = 0;
         s.nr = 0;
       }
       {
-        const bool qi_gt_small = s.qi >= C::QSMALL;
-        s.ni = vmax(s.ni, C::NSMALL);
+        const bool qi_gt_small = dge(s.qi, C::QSMALL);
+        s.ni = dmax_c(s.ni, C::NSMALL);
         if (qi_gt_small) {
           const float ici = 1.0f / float(cld_i);
           const float qi_f = float(s.qi) * ici;
@@ -1400,10 +1476,10 @@ __device__ void p3_part3(const Inst& in, const int col, const KParams<TR>& kp, c
           const float qm0 = float(s.qm) * ici, bm0 = float(s.bm) * ici;
           float qm_f = qm0, bm_f = bm0;
           const float rhop = calc_bulk_rho_rime<float>(qi_f, qm_f, bm_f, rt);
-          if (qm_f != qm0) s.qm = double(qm_f) * cld_i;
-          if (bm_f != bm0) s.bm = double(bm_f) * cld_i;
+          if (qm_f != qm0) s.qm = f2d(qm_f) * cld_i;
+          if (bm_f != bm0) s.bm = f2d(bm_f) * cld_i;
           float ni_f = ni0;
-          impose_max_total_ni(ni_f, rt.max_total_ni, float(inv_rho));
+          impose_max_total_ni(ni_f, rt.max_total_ni, inv_rho_f);
           TableIce<float> ti;
           lookup_ice<float>(qi_f, ni_f, qm_f, rhop, ti);
           float ta[4], te[4];
@@ -1411,21 +1487,23 @@ __device__ void p3_part3(const Inst& in, const int col, const KParams<TR>& kp, c
           apply_table_ice4<float>(tb, ti, 8, te); /* columns 5, 11, 8, 10 */
           ni_f = vmin(ni_f, ta[2] * ni_f);
           ni_f = vmax(ni_f, ta[3] * ni_f);
-          eff_qi = double(te[0]);
-          rho_qi = double(te[1]);
-          if (ni_f != ni0) s.ni = double(ni_f) * cld_i;
-          if (s.qm < C::QSMALL) {
+          eff_qi = f2d(te[0]);
+          rho_qi = f2d(te[1]);
+          if (ni_f != ni0) s.ni = f2d(ni_f) * cld_i;
+          if (dlt(s.qm, C::QSMALL)) {
             s.qm = 0;
             s.bm = 0;
           }
         } else {
-          s.qv = s.qv + s.qi;
-          s.th = s.th - inv_exner * s.qi * (C::LatVap + C::LatIce) * C::INV_CP;
+          if (dnz(s.qi)) {
+            s.qv = s.qv + s.qi;
+            s.th = s.th - inv_exner * s.qi * (C::LatVap + C::LatIce) * C::INV_CP;
+          }
           s.qi = 0; s.ni = 0; s.qm = 0; s.bm = 0;
         }
       }
     }
-    if (s.qr < C::QSMALL) s.nr = 0;
+    if (dlt(s.qr, C::QSMALL)) s.nr = 0;
 
     in.qc[o] = s.qc; in.nc[o] = s.nc; in.qr[o] = s.qr; in.nr[o] = s.nr;
     in.qi[o] = s.qi; in.qm[o] = s.qm; in.ni[o] = s.ni; in.bm[o] = s.bm;

@@ -138,6 +138,8 @@ __device__ __forceinline__ double dmax_c(double x, double c) { return dlt(x, c) 
 __device__ __forceinline__ double dmin_c(double x, double c) { return dgt(x, c) ? c : x; }
 /* x > 0 */
 __device__ __forceinline__ bool dpos(double x) { return dbits(x) > 0; }
+/* x is not +0 (adding or subtracting it may change a value) */
+__device__ __forceinline__ bool dnz(double x) { return dbits(x) != 0; }
 /* vmax(x, 0.) = (x < 0) ? 0 : x, and vmax(0., x) = (0 < x) ? x : 0 (+0 for -0) */
 __device__ __forceinline__ double dmax0(double x) { return dneg(x) ? 0.0 : x; }
 __device__ __forceinline__ double dmax_0x(double x) { return dpos(x) ? x : 0.0; }
