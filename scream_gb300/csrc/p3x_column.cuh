@@ -209,6 +209,254 @@ __device__ __forceinline__ void apply_n_adjust(double& n_d, TR n_in, TR n_out) {
   if (n_out != n_in) n_d = double(n_out);
 }
 
+/* The end of p3_main_part2 (p3_main_part2_impl.hpp, after update_prognostics):
+ * a species below qsmall goes to vapour and its latent heat to theta; a +0
+ * moves nothing, so its FP64 updates are skipped (bitwise the same result).
+ * Returns whether any species remains. */
+__device__ __forceinline__ bool clip_to_vapour(State& s, double inv_exner) {
+  bool hydro = false;
+  if (dlt(s.qc, C::QSMALL)) {
+    if (dnz(s.qc)) {
+      s.qv = s.qv + s.qc;
+      s.th = s.th - inv_exner * s.qc * C::LatVap * C::INV_CP;
+    }
+    s.qc = 0;
+    s.nc = 0;
+  } else {
+    hydro = true;
+  }
+  if (dlt(s.qr, C::QSMALL)) {
+    if (dnz(s.qr)) {
+      s.qv = s.qv + s.qr;
+      s.th = s.th - inv_exner * s.qr * C::LatVap * C::INV_CP;
+    }
+    s.qr = 0;
+    s.nr = 0;
+  } else {
+    hydro = true;
+  }
+  if (dlt(s.qi, C::QSMALL)) {
+    if (dnz(s.qi)) {
+      s.qv = s.qv + s.qi;
+      s.th = s.th - inv_exner * s.qi * (C::LatVap + C::LatIce) * C::INV_CP;
+    }
+    s.qi = 0; s.ni = 0; s.qm = 0; s.bm = 0;
+  } else {
+    hydro = true;
+  }
+  return hydro;
+}
+
+/* p3_main_part2 of one level in the FP32-bulk form (p3_main_part2_impl.hpp,
+ * same order of processes).  The FP64 state is read once and shadowed in
+ * FP32; the in-cloud values, DSDs, table lookups, process rates and limiter
+ * ratios are FP32, while the thresholds test the FP64 state.  The vapour
+ * residuals, the melting / wet-growth departures and the state update are
+ * FP64.  A DSD or rime limiter that changes an in-cloud value rewrites the
+ * FP64 state and its shadow.  sm / S: the K1 shared arrays of the column. */
+__device__ __forceinline__ void part2_level_bulk(const Inst& in, const int64_t o, const int k,
+                                                 double* __restrict__ sm, const int S, const KParams<float>& kp,
+                                                 const Tabs<float>& tb, const double esat0, const float dtf,
+                                                 const float inv_dtf, bool& hydro, uint32_t& err) {
+  const RuntimeDev& rt = kp.rt;
+  const bool predictNc = in.predictNc != 0, prescribedCCN = in.prescribedCCN != 0;
+  const bool do_ice = rt.do_ice_production != 0;
+  const double inv_dt_d = f2d(inv_dtf);
+  const float* const smf_rho = reinterpret_cast<const float*>(&sm[A_RHO * S]);
+  const float* const smf_rhofaci = reinterpret_cast<const float*>(&sm[A_RHOFACI * S]);
+  const float* const smf_acn = reinterpret_cast<const float*>(&sm[A_ACN * S]);
+  State s;
+  s.qc = in.qc[o]; s.nc = in.nc[o]; s.qr = in.qr[o]; s.nr = in.nr[o];
+  s.qi = in.qi[o]; s.qm = in.qm[o]; s.ni = in.ni[o]; s.bm = in.bm[o];
+  s.qv = in.qv[o]; s.th = in.th[o];
+  const double T = sm[A_TATM * S + k];
+  const double qvssi = sm[A_QVSSI * S + k];
+  if (dlt(s.qc, C::QSMALL) && dlt(s.qr, C::QSMALL) && dlt(s.qi, C::QSMALL) && dlt(T, C::T_zerodegc) &&
+      dlt_neg(qvssi, -0.05))
+    return;
+
+  const double cld_i = in.cld_frac_i[o], cld_l = in.cld_frac_l[o], cld_r = in.cld_frac_r[o];
+  const double inv_exner = in.inv_exner[o];
+  const double qvsl = sm[A_QVSL * S + k], qvsi = sm[A_QVSI * S + k];
+  const double inv_p = sm[A_INVP * S + k];
+  const float rho = smf_rho[k], inv_rho = 1.0f / rho, rhofaci = smf_rhofaci[k], acn = smf_acn[k];
+  const float T_r = float(T), qvsi_r = float(qvsi);
+  const float cl = float(cld_l), ci = float(cld_i), cr = float(cld_r);
+  const float icl = 1.0f / cl, ici = 1.0f / ci, icr = 1.0f / cr;
+  /* FP32 shadows of the state (kept equal to float(s.x) where s.x changes) */
+  const float qc0 = float(s.qc), qr0 = float(s.qr), qi0 = float(s.qi), ni0 = float(s.ni);
+  float nc0 = float(s.nc), nr0 = float(s.nr), qm0 = float(s.qm), bm0 = float(s.bm);
+  constexpr float QS = float(C::QSMALL);
+
+  /* calculate_incloud_mixingratios (bm uses 1/cld_frac_l, p3_incloud_mixingratios_impl.hpp:49) */
+  float qc_in = 0, nc_in = 0, qr_in = 0, nr_in = 0, qi_in = 0, ni_in = 0, qm_in = 0, bm_in = 0;
+  if (dge(s.qc, C::QSMALL)) { qc_in = qc0 * icl; nc_in = vmax(nc0 * icl, 0.0f); }
+  if (dge(s.qi, C::QSMALL)) { qi_in = qi0 * ici; ni_in = vmax(ni0 * ici, 0.0f); }
+  if (dge(s.qi, C::QSMALL) && dge(s.qm, C::QSMALL)) { qm_in = qm0 * ici; bm_in = vmax(bm0 * icl, 0.0f); }
+  if (dge(s.qr, C::QSMALL)) { qr_in = qr0 * icr; nr_in = vmax(nr0 * icr, 0.0f); }
+  {
+    constexpr float il = float(C::incloud_limit), pl = float(C::precip_limit);
+    if (qc_in > il || qi_in > il || qr_in > pl || bm_in > il) {
+      qc_in = vmin(qc_in, il);
+      qi_in = vmin(qi_in, il);
+      bm_in = vmin(bm_in, il);
+      qr_in = vmin(qr_in, pl);
+    }
+  }
+
+  Rates<float> r;
+  r.zero();
+  PhysVars<float> v;
+  v.mu = v.dv = v.sc = v.dqsdt = v.dqsidt = v.ab = v.abi = v.kap = v.eii = 0.0f;
+  float tv_fallspd = 0, tv_selfcol = 0, tv_qc2qi = 0, tv_melt = 0, tv_nr = 0, tv_qr2qi = 0, tv_lammax = 0,
+        tv_lammin = 0, tv_vent = 0;
+  float mu_c = 0, lamc = 0, mu_r = 0, lamr = 0, cdistr = 0, logn0r = 0;
+  float epsi = 0, epsr = 0, epsi_tot = 0;
+  float rho_qm_cloud = 400.0f;
+  bool wet = false;
+
+  if (qc_in >= QS || qr_in >= QS || qi_in >= QS) {
+    get_time_space_phys_variables<float>(T_r, float(in.pres[o]), rho, float(qvsl), qvsi_r, v);
+    {
+      float n_out = nc_in;
+      get_cloud_dsd2<float>(qc_in, n_out, mu_c, rho, lamc);
+      if (n_out != nc_in) {
+        nc_in = n_out;
+        s.nc = f2d(n_out) * cld_l;
+        nc0 = float(s.nc);
+      }
+    }
+    {
+      float n_out = nr_in;
+      get_rain_dsd2<float>(qr_in, n_out, mu_r, lamr, rt);
+      const bool changed = n_out != nr_in;
+      nr_in = n_out;
+      if (qr_in >= QS) {
+        cdistr = nr_in / float(rt.g_mur1);
+        logn0r = m_log10(cdistr) + (mu_r + 1.0f) * m_log10(lamr);
+      }
+      if (changed) {
+        s.nr = f2d(n_out) * cld_r;
+        nr0 = float(s.nr);
+      }
+    }
+    impose_max_total_ni(ni_in, rt.max_total_ni, inv_rho);
+    if (qi_in >= QS) {
+      ni_in = vmax(ni_in, float(C::NSMALL));
+      nr_in = vmax(nr_in, float(C::NSMALL));
+      float qm_f = qm_in, bm_f = bm_in;
+      const float rhop = calc_bulk_rho_rime<float>(qi_in, qm_f, bm_f, rt);
+      if (qm_f != qm_in) {
+        qm_in = qm_f;
+        s.qm = f2d(qm_f) * cld_i;
+        qm0 = float(s.qm);
+      }
+      if (bm_f != bm_in) {
+        bm_in = bm_f;
+        s.bm = f2d(bm_f) * cld_i;
+        bm0 = float(s.bm);
+      }
+      TableIce<float> ti;
+      lookup_ice<float>(qi_in, ni_in, qm_in, rhop, ti);
+      TableRain<float> trn;
+      lookup_rain<float>(qr_in, nr_in, trn);
+      float ta[4], tc[4];
+      apply_table_ice4<float>(tb, ti, 0, ta); /* columns 0, 1, 6, 7 */
+      apply_table_ice4<float>(tb, ti, 4, tc); /* columns 2, 3, 4, 9 */
+      tv_fallspd = ta[1];
+      tv_selfcol = tc[0];
+      tv_qc2qi = tc[1];
+      tv_melt = tc[2];
+      tv_lammax = ta[2];
+      tv_lammin = ta[3];
+      tv_vent = tc[3];
+      if (qr_in >= QS) {
+        tv_nr = apply_table_coll<float>(0, tb, ti, trn);
+        tv_qr2qi = apply_table_coll<float>(1, tb, ti, trn);
+      }
+      ni_in = vmin(ni_in, tv_lammax * ni_in);
+      ni_in = vmax(ni_in, tv_lammin * ni_in);
+    }
+    const double dT0 = T - C::Tmelt;
+    const double dqv0 = C::ep_2 * esat0 * inv_p - s.qv;
+    if (do_ice) {
+      ice_cldliq_collection<float>(rho, T, rhofaci, tv_qc2qi, qi_in, qc_in, ni_in, nc_in, r, rt);
+      ice_rain_collection<float>(rho, T, rhofaci, logn0r, tv_nr, tv_qr2qi, qi_in, ni_in, qr_in, r, rt);
+      ice_self_collection<float>(rho, rhofaci, tv_selfcol, v.eii, qm_in, qi_in, ni_in, r);
+    }
+    ice_melting<float>(rho, dT0, dqv0, rhofaci, tv_melt, tv_vent, v, qi_in, ni_in, r);
+    if (do_ice) {
+      wet = ice_cldliq_wet_growth<float>(rho, dT0, dqv0, rhofaci, tv_melt, tv_vent, v, qc_in, qi_in, ni_in, qr_in,
+                                         r);
+    }
+    /* ice_relaxation_timescale, p3_ice_relaxation_timescale_impl.hpp:9-37 */
+    if (qi_in >= QS && dlt(T, C::Tmelt)) {
+      epsi = ((tv_melt + tv_vent * m_cbrt(v.sc) * m_sqrt(rhofaci * rho / v.mu)) * 2.0f * float(C::Pi) * rho *
+              v.dv) * ni_in;
+      epsi_tot = epsi_tot + epsi;
+    }
+    rho_qm_cloud = calc_rime_density<float>(T_r, rhofaci, tv_fallspd, acn, lamc, mu_c, qc_in,
+                                            r.qc2qi_collect_tend);
+    if (do_ice) {
+      cldliq_immersion_freezing<float>(T_r, lamc, mu_c, nc_in, qc_in, r, rt);
+      rain_immersion_freezing<float>(T_r, lamr, mu_r, cdistr, qr_in, r, rt);
+    }
+    /* calc_liq_relaxation_timescale, p3_calc_liq_relaxation_timescale_impl.hpp:13-43 */
+    if (qr_in >= QS) {
+      Table3<float> t3;
+      lookup3<float>(mu_r, lamr, rt, t3);
+      epsr = 2.0f * float(C::Pi) * cdistr * rho * v.dv *
+             (float(C::f1r) * float(rt.g_mur2) / lamr +
+              float(C::f2r) * m_sqrt(rho / v.mu) * m_cbrt(v.sc) * apply_table3<float>(tb, tb.revap, t3));
+    }
+    evaporate_rain_bulk(qr_in, qc_in, nr_in, qi_in, cl, cr, s.qv, in.qv_prev[o], qvsl, qvsi, v.ab, v.abi, epsr,
+                        epsi_tot, T, in.t_prev[o], v.dqsdt, dtf, inv_dtf, inv_dt_d, r.qr2qv_evap_tend,
+                        r.nr_evap_tend);
+    if (do_ice) {
+      ice_deposition_sublimation_bulk(qi_in, ni_in, T, qvsl, qvsi, epsi, v.abi, s.qv, inv_dtf, r.qv2qi_vapdep_tend,
+                                      r.qi2qv_sublim_tend, r.ni_sublim_tend, r.qc2qi_berg_tend);
+    }
+  }
+  if (do_ice) {
+    ice_nucleation<float>(T_r, inv_rho, ni0, float(in.ni_activated[o]), qvssi, inv_dtf, predictNc, prescribedCCN,
+                          r, rt);
+  }
+  cloud_water_autoconversion<float>(rho, qc_in, nc_in, r, rt);
+  if (qc_in >= QS) r.nc_selfcollect_tend = 0.0f;
+  cloud_rain_accretion<float>(qc_in, nc_in, qr_in, r, rt);
+  rain_self_collection<float>(rho, qr_in, nr_in, r, rt);
+  back_to_cell_average<float>(cl, cr, ci, r);
+
+  /* limiters on the FP32 rates (FP64 vapour residuals), one FP64
+   * application of each prognostic's FP32 tendency */
+  const int wlim = water_conservation<float>(qc0, qr0, qi0, dtf, r);
+  const int nlim = number_conservation<float>(nc0, nr0, ni0, dtf, r);
+  const Rates<float> r_lim = r;
+  ice_supersat_conservation_bulk(r, cld_i, s.qv, qvsi, qvsi_r, T_r, dtf);
+  prevent_liq_supersaturation_bulk(inv_p, T, s.qv, dtf, r, rt, err);
+  update_prognostics_bulk(r, inv_exner, predictNc, prescribedCCN, wet, dtf, rho_qm_cloud, f2d(inv_rho), wlim, nlim,
+                          r_lim, qi0, qm0, bm0, s);
+
+  in.qv2qi_depos_tend[o] = f2d(r.qv2qi_vapdep_tend - r.qi2qv_sublim_tend + r.qv2qi_nucleat_tend);
+  in.precip_total_tend[o] = f2d(r.qc2qr_accret_tend + r.qc2qr_autoconv_tend + r.qc2qr_ice_shed_tend +
+                                r.qc2qi_collect_tend);
+  in.nevapr[o] = f2d(r.qi2qv_sublim_tend + r.qr2qv_evap_tend);
+  in.vap_ice_exchange[o] = f2d(r.qv2qi_vapdep_tend - r.qi2qv_sublim_tend + r.qv2qi_nucleat_tend);
+  in.vap_liq_exchange[o] = f2d(-r.qr2qv_evap_tend);
+  in.liq_ice_exchange[o] = f2d(r.qc2qi_hetero_freeze_tend + r.qr2qi_immers_freeze_tend - r.qi2qr_melt_tend +
+                               r.qc2qi_berg_tend + r.qc2qi_collect_tend + r.qr2qi_collect_tend);
+
+  hydro |= clip_to_vapour(s, inv_exner);
+  if (dge(s.ni, 1e-20)) {
+    /* impose_max_total_ni as a factor applied only when it limits */
+    const float f = vmin(float(rt.max_total_ni) * inv_rho * ci / float(s.ni), 1.0f);
+    if (f < 1.0f) s.ni = s.ni * f2d(f);
+  }
+  in.qc[o] = s.qc; in.nc[o] = s.nc; in.qr[o] = s.qr; in.nr[o] = s.nr;
+  in.qi[o] = s.qi; in.qm[o] = s.qm; in.ni[o] = s.ni; in.bm[o] = s.bm;
+  in.qv[o] = s.qv; in.th[o] = s.th;
+}
+
 /* ------------------------------------------------------------------ */
 /* one column                                                          */
 /* ------------------------------------------------------------------ */
@@ -381,6 +629,11 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
 
   /* ---------------- phase 2: p3_main_part2 ---------------- */
   hydro = false;
+  if constexpr (!kF64) {
+    const float dtf = float(dt), inv_dtf = float(inv_dt);
+    for (int k = lane; k < nk; k += LANES)
+      part2_level_bulk(in, co + k, k, sm, S, kp, tb, esat0, dtf, inv_dtf, hydro, err);
+  } else {
   for (int k = lane; k < nk; k += LANES) {
     const int64_t o = co + k;
     State s;
@@ -397,32 +650,12 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
     const double cld_i = in.cld_frac_i[o], cld_l = in.cld_frac_l[o], cld_r = in.cld_frac_r[o];
     const double inv_exner = in.inv_exner[o];
     const double qvsl = SMA(A_QVSL, k), qvsi = SMA(A_QVSI, k);
-    TR rho_t, inv_rho_t, rhofaci_t, acn_t;
-    double inv_rho;
-    if constexpr (kF64) {
-      const double rho = SMA(A_RHO, k);
-      rho_t = rho;
-      inv_rho = 1 / rho;
-      inv_rho_t = inv_rho;
-      rhofaci_t = SMA(A_RHOFACI, k);
-      acn_t = SMA(A_ACN, k);
-    } else {
-      rho_t = SMF(A_RHO)[k];
-      inv_rho_t = 1.0f / rho_t;
-      inv_rho = f2d(inv_rho_t);
-      rhofaci_t = SMF(A_RHOFACI)[k];
-      acn_t = SMF(A_ACN)[k];
-    }
-    /* In-cloud values.  FP32-bulk: reciprocal cloud fractions in FP32 (the
-     * in-cloud values only feed rates) and the FP64 state is rewritten below
-     * only where a DSD or rime limiter changed an in-cloud value. */
+    const double rho = SMA(A_RHO, k);
+    const double inv_rho = 1 / rho;
+    const double rhofaci = SMA(A_RHOFACI, k);
+    const double acn = SMA(A_ACN, k);
     Incld inc;
-    if constexpr (kF64) {
-      calc_incloud(s.qc, s.qr, s.qi, s.qm, s.nc, s.nr, s.ni, s.bm, 1 / cld_l, 1 / cld_i, 1 / cld_r, inc);
-    } else {
-      calc_incloud(s.qc, s.qr, s.qi, s.qm, s.nc, s.nr, s.ni, s.bm, f2d(1.0f / float(cld_l)),
-                   f2d(1.0f / float(cld_i)), f2d(1.0f / float(cld_r)), inc);
-    }
+    calc_incloud(s.qc, s.qr, s.qi, s.qm, s.nc, s.nr, s.ni, s.bm, 1 / cld_l, 1 / cld_i, 1 / cld_r, inc);
 
     Rates<TR> r;
     r.zero();
@@ -431,21 +664,19 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
     TR tv_fallspd = 0, tv_selfcol = 0, tv_qc2qi = 0, tv_melt = 0, tv_nr = 0, tv_qr2qi = 0,
        tv_lammax = 0, tv_lammin = 0, tv_vent = 0;
     TR mu_c = 0, lamc = 0, mu_r = 0, lamr = 0, cdistr = 0, logn0r = 0;
-    TR epsi = 0, epsr = 0, epsc = 0, epsi_tot = 0;
+    TR epsi = 0, epsr = 0, epsi_tot = 0;
     TR rho_qm_cloud = TR(400);
     bool wet = false;
-    (void)epsc;
 
     const bool skip_micro = !(dge(inc.qc, C::QSMALL) || dge(inc.qr, C::QSMALL) || dge(inc.qi, C::QSMALL));
     if (!skip_micro) {
-      const TR T_r = TR(T), rho_r = rho_t, rhofaci_r = rhofaci_t;
-      get_time_space_phys_variables<TR>(T_r, TR(pres), rho_r, TR(qvsl), TR(qvsi), v);
+      get_time_space_phys_variables<TR>(T, pres, rho, qvsl, qvsi, v);
       {
         const TR n_in = TR(inc.nc);
         TR n_out = n_in;
-        get_cloud_dsd2<TR>(TR(inc.qc), n_out, mu_c, rho_r, lamc);
+        get_cloud_dsd2<TR>(TR(inc.qc), n_out, mu_c, rho, lamc);
         apply_n_adjust(inc.nc, n_in, n_out);
-        if (kF64 || n_out != n_in) s.nc = inc.nc * cld_l;
+        s.nc = inc.nc * cld_l;
       }
       {
         const TR n_in = TR(inc.nr);
@@ -456,36 +687,15 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
           cdistr = TR(inc.nr) / TR(rt.g_mur1);
           logn0r = m_log10(cdistr) + (mu_r + TR(1)) * m_log10(lamr);
         }
-        if (kF64 || n_out != n_in) s.nr = inc.nr * cld_r;
+        s.nr = inc.nr * cld_r;
       }
-      if constexpr (kF64) {
-        impose_max_total_ni(inc.ni, rt.max_total_ni, inv_rho);
-      } else {
-        float ni_f = float(inc.ni);
-        impose_max_total_ni(ni_f, rt.max_total_ni, inv_rho_t);
-        inc.ni = f2d(ni_f);
-      }
+      impose_max_total_ni(inc.ni, rt.max_total_ni, inv_rho);
       if (dge(inc.qi, C::QSMALL)) {
         inc.ni = dmax_c(inc.ni, C::NSMALL);
         inc.nr = dmax_c(inc.nr, C::NSMALL);
-        TR rhop;
-        if constexpr (kF64) {
-          rhop = calc_bulk_rho_rime(inc.qi, inc.qm, inc.bm, rt);
-          s.qm = inc.qm * cld_i;
-          s.bm = inc.bm * cld_i;
-        } else {
-          const float qm0 = float(inc.qm), bm0 = float(inc.bm);
-          float qm_f = qm0, bm_f = bm0;
-          rhop = calc_bulk_rho_rime<float>(float(inc.qi), qm_f, bm_f, rt);
-          if (qm_f != qm0) {
-            inc.qm = f2d(qm_f);
-            s.qm = inc.qm * cld_i;
-          }
-          if (bm_f != bm0) {
-            inc.bm = f2d(bm_f);
-            s.bm = inc.bm * cld_i;
-          }
-        }
+        const TR rhop = calc_bulk_rho_rime(inc.qi, inc.qm, inc.bm, rt);
+        s.qm = inc.qm * cld_i;
+        s.bm = inc.bm * cld_i;
         TableIce<TR> ti;
         lookup_ice<TR>(TR(inc.qi), TR(inc.ni), TR(inc.qm), rhop, ti);
         TableRain<TR> trn;
@@ -504,150 +714,80 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
           tv_nr = apply_table_coll<TR>(0, tb, ti, trn);
           tv_qr2qi = apply_table_coll<TR>(1, tb, ti, trn);
         }
-        inc.ni = vmin(inc.ni, widen(tv_lammax) * inc.ni);
-        inc.ni = vmax(inc.ni, widen(tv_lammin) * inc.ni);
+        inc.ni = vmin(inc.ni, tv_lammax * inc.ni);
+        inc.ni = vmax(inc.ni, tv_lammin * inc.ni);
       }
-      const TR qi_r = TR(inc.qi), qc_r = TR(inc.qc), ni_r = TR(inc.ni), nc_r = TR(inc.nc), qr_r = TR(inc.qr);
+      const TR qi_r = inc.qi, qc_r = inc.qc, ni_r = inc.ni, nc_r = inc.nc, qr_r = inc.qr;
       const double dT0 = T - C::Tmelt;
-      const double dqv0 = kF64 ? C::ep_2 * esat0 / vmax(pres, 1.e-3) - s.qv : C::ep_2 * esat0 * SMA(A_INVP, k) - s.qv;
+      const double dqv0 = C::ep_2 * esat0 / vmax(pres, 1.e-3) - s.qv;
       if (do_ice) {
-        ice_cldliq_collection<TR>(rho_r, T, rhofaci_r, tv_qc2qi, qi_r, qc_r, ni_r, nc_r, r, rt);
-        ice_rain_collection<TR>(rho_r, T, rhofaci_r, logn0r, tv_nr, tv_qr2qi, qi_r, ni_r, qr_r, r, rt);
-        ice_self_collection<TR>(rho_r, rhofaci_r, tv_selfcol, v.eii, TR(inc.qm), qi_r, ni_r, r);
+        ice_cldliq_collection<TR>(rho, T, rhofaci, tv_qc2qi, qi_r, qc_r, ni_r, nc_r, r, rt);
+        ice_rain_collection<TR>(rho, T, rhofaci, logn0r, tv_nr, tv_qr2qi, qi_r, ni_r, qr_r, r, rt);
+        ice_self_collection<TR>(rho, rhofaci, tv_selfcol, v.eii, TR(inc.qm), qi_r, ni_r, r);
       }
-      ice_melting<TR>(rho_r, dT0, dqv0, rhofaci_r, tv_melt, tv_vent, v, qi_r, ni_r, r);
+      ice_melting<TR>(rho, dT0, dqv0, rhofaci, tv_melt, tv_vent, v, qi_r, ni_r, r);
       if (do_ice) {
-        wet = ice_cldliq_wet_growth<TR>(rho_r, dT0, dqv0, rhofaci_r, tv_melt, tv_vent, v, qc_r, qi_r, ni_r,
-                                        qr_r, r);
+        wet = ice_cldliq_wet_growth<TR>(rho, dT0, dqv0, rhofaci, tv_melt, tv_vent, v, qc_r, qi_r, ni_r, qr_r, r);
       }
       /* ice_relaxation_timescale, p3_ice_relaxation_timescale_impl.hpp:9-37 */
       if (dge(inc.qi, C::QSMALL) && dlt(T, C::Tmelt)) {
-        epsi = ((tv_melt + tv_vent * m_cbrt(v.sc) * m_sqrt(rhofaci_r * rho_r / v.mu)) * TR(2.0) * TR(C::Pi) *
-                rho_r * v.dv) * ni_r;
+        epsi = ((tv_melt + tv_vent * m_cbrt(v.sc) * m_sqrt(rhofaci * rho / v.mu)) * TR(2.0) * TR(C::Pi) * rho *
+                v.dv) * ni_r;
         epsi_tot = epsi_tot + epsi;
       } else {
         epsi = TR(0);
       }
-      rho_qm_cloud = calc_rime_density<TR>(T_r, rhofaci_r, tv_fallspd, acn_t, lamc, mu_c, qc_r,
-                                           r.qc2qi_collect_tend);
+      rho_qm_cloud = calc_rime_density<TR>(T, rhofaci, tv_fallspd, acn, lamc, mu_c, qc_r, r.qc2qi_collect_tend);
       if (do_ice) {
-        cldliq_immersion_freezing<TR>(T_r, lamc, mu_c, nc_r, qc_r, r, rt);
-        rain_immersion_freezing<TR>(T_r, lamr, mu_r, cdistr, qr_r, r, rt);
+        cldliq_immersion_freezing<TR>(T, lamc, mu_c, nc_r, qc_r, r, rt);
+        rain_immersion_freezing<TR>(T, lamr, mu_r, cdistr, qr_r, r, rt);
       }
       /* calc_liq_relaxation_timescale, p3_calc_liq_relaxation_timescale_impl.hpp:13-43 */
       if (dge(inc.qr, C::QSMALL)) {
         Table3<TR> t3;
         lookup3<TR>(mu_r, lamr, rt, t3);
-        epsr = TR(2) * TR(C::Pi) * cdistr * rho_r * v.dv *
+        epsr = TR(2) * TR(C::Pi) * cdistr * rho * v.dv *
                (TR(C::f1r) * TR(rt.g_mur2) / lamr +
-                TR(C::f2r) * m_sqrt(rho_r / v.mu) * m_cbrt(v.sc) * apply_table3<TR>(tb, tb.revap, t3));
+                TR(C::f2r) * m_sqrt(rho / v.mu) * m_cbrt(v.sc) * apply_table3<TR>(tb, tb.revap, t3));
       }
-      if constexpr (sizeof(TR) == sizeof(double)) {
-        double evap, nevap;
-        evaporate_rain(inc.qr, inc.qc, inc.nr, inc.qi, cld_l, cld_r, s.qv, in.qv_prev[o], qvsl, qvsi,
-                       double(v.ab), double(v.abi), double(epsr), double(epsi_tot), T, in.t_prev[o],
-                       double(v.dqsdt), dt, evap, nevap);
-        r.qr2qv_evap_tend = TR(evap);
-        r.nr_evap_tend = TR(nevap);
-        if (do_ice) {
-          double vd, sb, nsb, bg;
-          ice_deposition_sublimation(inc.qi, inc.ni, T, qvsl, qvsi, double(epsi), double(v.abi), s.qv, inv_dt,
-                                     vd, sb, nsb, bg);
-          r.qv2qi_vapdep_tend = TR(vd);
-          r.qi2qv_sublim_tend = TR(sb);
-          r.ni_sublim_tend = TR(nsb);
-          r.qc2qi_berg_tend = TR(bg);
-        }
-      } else {
-        evaporate_rain_bulk(inc.qr, inc.qc, inc.nr, inc.qi, cld_l, cld_r, s.qv, in.qv_prev[o], qvsl, qvsi, v.ab,
-                            v.abi, epsr, epsi_tot, T, in.t_prev[o], v.dqsdt, dt, inv_dt, r.qr2qv_evap_tend,
-                            r.nr_evap_tend);
-        if (do_ice) {
-          ice_deposition_sublimation_bulk(inc.qi, inc.ni, T, qvsl, qvsi, epsi, v.abi, s.qv, inv_dt,
-                                          r.qv2qi_vapdep_tend, r.qi2qv_sublim_tend, r.ni_sublim_tend,
-                                          r.qc2qi_berg_tend);
-        }
+      evaporate_rain(inc.qr, inc.qc, inc.nr, inc.qi, cld_l, cld_r, s.qv, in.qv_prev[o], qvsl, qvsi, v.ab, v.abi,
+                     epsr, epsi_tot, T, in.t_prev[o], v.dqsdt, dt, r.qr2qv_evap_tend, r.nr_evap_tend);
+      if (do_ice) {
+        ice_deposition_sublimation(inc.qi, inc.ni, T, qvsl, qvsi, epsi, v.abi, s.qv, inv_dt, r.qv2qi_vapdep_tend,
+                                   r.qi2qv_sublim_tend, r.ni_sublim_tend, r.qc2qi_berg_tend);
       }
     }
     if (do_ice) {
-      ice_nucleation<TR>(TR(T), inv_rho_t, TR(s.ni), TR(in.ni_activated[o]), qvssi, TR(inv_dt), predictNc,
-                         prescribedCCN, r, rt);
+      ice_nucleation<TR>(T, inv_rho, s.ni, in.ni_activated[o], qvssi, inv_dt, predictNc, prescribedCCN, r, rt);
     }
-    cloud_water_autoconversion<TR>(rho_t, TR(inc.qc), TR(inc.nc), r, rt);
+    cloud_water_autoconversion<TR>(rho, inc.qc, inc.nc, r, rt);
     if (dge(inc.qc, C::QSMALL)) r.nc_selfcollect_tend = TR(0);
-    cloud_rain_accretion<TR>(TR(inc.qc), TR(inc.nc), TR(inc.qr), r, rt);
-    rain_self_collection<TR>(rho_t, TR(inc.qr), TR(inc.nr), r, rt);
-    back_to_cell_average<TR>(TR(cld_l), TR(cld_r), TR(cld_i), r);
+    cloud_rain_accretion<TR>(inc.qc, inc.nc, inc.qr, r, rt);
+    rain_self_collection<TR>(rho, inc.qr, inc.nr, r, rt);
+    back_to_cell_average<TR>(cld_l, cld_r, cld_i, r);
 
-    if constexpr (sizeof(TR) == sizeof(double)) {
-      Rates<double>& rd = r;
-      water_conservation<double>(s.qc, s.qr, s.qi, dt, rd);
-      number_conservation<double>(s.nc, s.nr, s.ni, dt, rd);
-      ice_supersat_conservation(rd, cld_i, s.qv, qvsi, s.th / inv_exner, dt);
-      prevent_liq_supersaturation(pres, T, s.qv, dt, rd, err);
-      update_prognostics(rd, inv_exner, predictNc, prescribedCCN, wet, dt, double(rho_qm_cloud), inv_rho, s);
-    } else {
-      /* FP32-bulk: limiters on the FP32 rates (FP64 vapour residuals), one
-       * FP64 application of each prognostic's FP32 tendency */
-      const float dtf = float(dt);
-      const int wlim = water_conservation<float>(float(s.qc), float(s.qr), float(s.qi), dtf, r);
-      const int nlim = number_conservation<float>(float(s.nc), float(s.nr), float(s.ni), dtf, r);
-      const Rates<float> r_lim = r;
-      ice_supersat_conservation_bulk(r, cld_i, s.qv, qvsi, T, dt);
-      prevent_liq_supersaturation_bulk(SMA(A_INVP, k), T, s.qv, dt, r, rt, err);
-      update_prognostics_bulk(r, inv_exner, predictNc, prescribedCCN, wet, dt, rho_qm_cloud, inv_rho, wlim, nlim,
-                              r_lim, s);
-    }
+    water_conservation<double>(s.qc, s.qr, s.qi, dt, r);
+    number_conservation<double>(s.nc, s.nr, s.ni, dt, r);
+    ice_supersat_conservation(r, cld_i, s.qv, qvsi, s.th / inv_exner, dt);
+    prevent_liq_supersaturation(pres, T, s.qv, dt, r, err);
+    update_prognostics(r, inv_exner, predictNc, prescribedCCN, wet, dt, rho_qm_cloud, inv_rho, s);
 
-    in.qv2qi_depos_tend[o] = widen(r.qv2qi_vapdep_tend - r.qi2qv_sublim_tend + r.qv2qi_nucleat_tend);
-    in.precip_total_tend[o] = widen(r.qc2qr_accret_tend + r.qc2qr_autoconv_tend + r.qc2qr_ice_shed_tend + r.qc2qi_collect_tend);
-    in.nevapr[o] = widen(r.qi2qv_sublim_tend + r.qr2qv_evap_tend);
-    in.vap_ice_exchange[o] = widen(r.qv2qi_vapdep_tend - r.qi2qv_sublim_tend + r.qv2qi_nucleat_tend);
-    in.vap_liq_exchange[o] = widen(-r.qr2qv_evap_tend);
-    in.liq_ice_exchange[o] = widen(r.qc2qi_hetero_freeze_tend + r.qr2qi_immers_freeze_tend - r.qi2qr_melt_tend +
-                                    r.qc2qi_berg_tend + r.qc2qi_collect_tend + r.qr2qi_collect_tend);
+    in.qv2qi_depos_tend[o] = r.qv2qi_vapdep_tend - r.qi2qv_sublim_tend + r.qv2qi_nucleat_tend;
+    in.precip_total_tend[o] = r.qc2qr_accret_tend + r.qc2qr_autoconv_tend + r.qc2qr_ice_shed_tend + r.qc2qi_collect_tend;
+    in.nevapr[o] = r.qi2qv_sublim_tend + r.qr2qv_evap_tend;
+    in.vap_ice_exchange[o] = r.qv2qi_vapdep_tend - r.qi2qv_sublim_tend + r.qv2qi_nucleat_tend;
+    in.vap_liq_exchange[o] = -r.qr2qv_evap_tend;
+    in.liq_ice_exchange[o] = r.qc2qi_hetero_freeze_tend + r.qr2qi_immers_freeze_tend - r.qi2qr_melt_tend +
+                             r.qc2qi_berg_tend + r.qc2qi_collect_tend + r.qr2qi_collect_tend;
 
-    if (dlt(s.qc, C::QSMALL)) {
-      if (dnz(s.qc)) {
-        s.qv = s.qv + s.qc;
-        s.th = s.th - inv_exner * s.qc * C::LatVap * C::INV_CP;
-      }
-      s.qc = 0;
-      s.nc = 0;
-    } else {
-      hydro = true;
-    }
-    if (dlt(s.qr, C::QSMALL)) {
-      if (dnz(s.qr)) {
-        s.qv = s.qv + s.qr;
-        s.th = s.th - inv_exner * s.qr * C::LatVap * C::INV_CP;
-      }
-      s.qr = 0;
-      s.nr = 0;
-    } else {
-      hydro = true;
-    }
-    if (dlt(s.qi, C::QSMALL)) {
-      if (dnz(s.qi)) {
-        s.qv = s.qv + s.qi;
-        s.th = s.th - inv_exner * s.qi * (C::LatVap + C::LatIce) * C::INV_CP;
-      }
-      s.qi = 0; s.ni = 0; s.qm = 0; s.bm = 0;
-    } else {
-      hydro = true;
-    }
-    if constexpr (kF64) {
-      double ni_incld = s.ni / cld_i;
-      impose_max_total_ni(ni_incld, rt.max_total_ni, inv_rho);
-      s.ni = ni_incld * cld_i;
-    } else if (dge(s.ni, 1e-20)) {
-      /* impose_max_total_ni as a factor applied only when it limits */
-      const float f = vmin(float(rt.max_total_ni) * inv_rho_t * float(cld_i) / float(s.ni), 1.0f);
-      if (f < 1.0f) s.ni = s.ni * f2d(f);
-    }
+    hydro |= clip_to_vapour(s, inv_exner);
+    double ni_incld = s.ni / cld_i;
+    impose_max_total_ni(ni_incld, rt.max_total_ni, inv_rho);
+    s.ni = ni_incld * cld_i;
     in.qc[o] = s.qc; in.nc[o] = s.nc; in.qr[o] = s.qr; in.nr[o] = s.nr;
     in.qi[o] = s.qi; in.qm[o] = s.qm; in.ni[o] = s.ni; in.bm[o] = s.bm;
     in.qv[o] = s.qv; in.th[o] = s.th;
+  }
   }
   if (!group_any<LANES>(mask, hydro)) {
     if (lane == 0) in.cflag[col] = 0;

@@ -901,21 +901,22 @@ __device__ __forceinline__ void evaporate_rain(double qr_incld, double qc_incld,
 
 /* evaporate_rain of the FP32-bulk form: the supersaturation residual
  * ssat_r = qv - qv_sat_l and the A_c source term (differences of the state
- * against the previous step) are formed in FP64; the relaxation weights,
- * the equilibrium / instantaneous tendencies and the limits are rate
- * arithmetic in FP32.  Same formulas and branch order as evaporate_rain. */
-__device__ __forceinline__ void evaporate_rain_bulk(double qr_incld, double qc_incld, double nr_incld,
-                                                    double qi_incld, double cld_frac_l, double cld_frac_r,
+ * against the previous step) are formed in FP64; the in-cloud values, the
+ * relaxation weights, the equilibrium / instantaneous tendencies and the
+ * limits are rate arithmetic in FP32.  Same formulas and branch order as
+ * evaporate_rain. */
+__device__ __forceinline__ void evaporate_rain_bulk(float qr_incld, float qc_incld, float nr_incld,
+                                                    float qi_incld, float cld_frac_l, float cld_frac_r,
                                                     double qv, double qv_prev, double qv_sat_l, double qv_sat_i,
                                                     float ab, float abi, float epsr, float epsi_tot,
-                                                    double t_atm, double t_atm_prev, float dqsdt, double dt,
-                                                    double inv_dt_d, float& qr2qv_evap_tend, float& nr_evap_tend) {
+                                                    double t_atm, double t_atm_prev, float dqsdt, float dtf,
+                                                    float inv_dt, double inv_dt_d, float& qr2qv_evap_tend,
+                                                    float& nr_evap_tend) {
   qr2qv_evap_tend = 0;
   nr_evap_tend = 0;
   const double ssat_r_d = qv - qv_sat_l;
-  const double cld_frac = dlt(qc_incld + qi_incld, 1.e-6) ? 0.0 : cld_frac_l;
-  if (dge(qr_incld, C::QSMALL) && dneg(ssat_r_d) && cld_frac_r > cld_frac) {
-    const float inv_dt = float(inv_dt_d), dtf = float(dt);
+  const float cld_frac = ((qc_incld + qi_incld) < 1.e-6f) ? 0.0f : cld_frac_l;
+  if (qr_incld >= float(C::QSMALL) && dneg(ssat_r_d) && cld_frac_r > cld_frac) {
     const float ssat_r = float(ssat_r_d);
     const float tau_r = 1.0f / epsr;
     const float lat_fac = 1.0f + float((C::LatVap + C::LatIce) / C::Cpair) * dqsdt;
@@ -931,8 +932,8 @@ __device__ __forceinline__ void evaporate_rain_bulk(double qr_incld, double qc_i
     if (eps_eff < 1e-20f) eps_eff = 1e-20f;
     const float tau_eff = 1.0f / eps_eff;
     float evap;
-    if (dlt(qr_incld, 1e-12) && qv < 0.999 * qv_sat_l) {
-      evap = float(qr_incld) * inv_dt;
+    if (qr_incld < 1e-12f && qv < 0.999 * qv_sat_l) {
+      evap = qr_incld * inv_dt;
     } else {
       const float dt_over_tau = dtf / tau_eff;
       const float w = -expm1f(-dt_over_tau) / dt_over_tau;
@@ -943,30 +944,30 @@ __device__ __forceinline__ void evaporate_rain_bulk(double qr_incld, double qc_i
     const float lim = -ssat_r * inv_dt / ab;
     if (evap > lim) evap = lim;
     if (evap < 0.0f) evap = 0.0f;
-    const float qlim = float(qr_incld) * inv_dt;
+    const float qlim = qr_incld * inv_dt;
     if (evap > qlim) evap = qlim;
-    evap = evap * (float(cld_frac_r - cld_frac) / float(cld_frac_r));
+    evap = evap * ((cld_frac_r - cld_frac) / cld_frac_r);
     qr2qv_evap_tend = evap;
-    nr_evap_tend = evap * (float(nr_incld) / float(qr_incld));
+    nr_evap_tend = evap * (nr_incld / qr_incld);
   }
 }
 
 /* ice_deposition_sublimation of the FP32-bulk form: the vapour residuals
- * qv - qv_sat_i and qv_sat_l - qv_sat_i are FP64, the relaxation coefficient
- * FP32. */
-__device__ __forceinline__ void ice_deposition_sublimation_bulk(double qi_incld, double ni_incld, double T_atm,
+ * qv - qv_sat_i and qv_sat_l - qv_sat_i are FP64, the in-cloud values and the
+ * relaxation coefficient FP32. */
+__device__ __forceinline__ void ice_deposition_sublimation_bulk(float qi_incld, float ni_incld, double T_atm,
                                                                 double qv_sat_l, double qv_sat_i, float epsi,
-                                                                float abi, double qv, double inv_dt,
+                                                                float abi, double qv, float inv_dt,
                                                                 float& vapdep, float& sublim, float& ni_sublim,
                                                                 float& berg) {
   berg = 0; vapdep = 0; sublim = 0; ni_sublim = 0;
-  if (dgt(qi_incld, C::QSMALL)) {
-    const float coef = vmin(epsi / abi, float(inv_dt));
+  if (qi_incld > float(C::QSMALL)) {
+    const float coef = vmin(epsi / abi, inv_dt);
     const float qi_tend = coef * float(qv - qv_sat_i);
     const bool neg = qi_tend < 0;
     if (neg) {
       sublim = -qi_tend;
-      ni_sublim = sublim * (float(ni_incld) / float(qi_incld));
+      ni_sublim = sublim * (ni_incld / qi_incld);
     }
     const bool T_lt_frz = dlt(T_atm, C::T_zerodegc);
     if (T_lt_frz && !neg) vapdep = qi_tend;
@@ -1131,14 +1132,13 @@ __device__ __forceinline__ void prevent_liq_supersaturation(double pres, double 
  * form: the vapour residuals (qv + sources dt - qv_sat) are FP64, the
  * limiting fractions FP32. */
 __device__ __forceinline__ void ice_supersat_conservation_bulk(Rates<float>& r, double cld_frac_i, double qv,
-                                                               double qv_sat_i, double t_atm, double dt) {
+                                                               double qv_sat_i, float qv_sat_i_f, float tf,
+                                                               float dtf) {
   const float qv_sink = r.qv2qi_vapdep_tend + r.qv2qi_nucleat_tend;
   if (qv_sink > float(C::QSMALL) && dgt(cld_frac_i, 1e-20)) {
-    const float dtf = float(dt);
     const double resid = qv + f2d((r.qi2qv_sublim_tend + r.qr2qv_evap_tend) * dtf) - qv_sat_i;
-    const float tf = float(t_atm);
     constexpr float latsublim2 = float((C::LatVap + C::LatIce) * (C::LatVap + C::LatIce) / (C::CP * C::RH2O));
-    float qv_avail = float(resid) / (1.0f + latsublim2 * float(qv_sat_i) / (tf * tf)) / dtf;
+    float qv_avail = float(resid) / (1.0f + latsublim2 * qv_sat_i_f / (tf * tf)) / dtf;
     qv_avail = vmax(qv_avail, 0.0f);
     if (qv_sink > qv_avail) {
       const float fract = qv_avail / qv_sink;
@@ -1148,12 +1148,11 @@ __device__ __forceinline__ void ice_supersat_conservation_bulk(Rates<float>& r, 
   }
 }
 
-__device__ __forceinline__ bool prevent_liq_supersaturation_bulk(double inv_p, double t_atm, double qv, double dt,
+__device__ __forceinline__ bool prevent_liq_supersaturation_bulk(double inv_p, double t_atm, double qv, float dtf,
                                                                  Rates<float>& r, const RuntimeDev& rt,
                                                                  uint32_t& err) {
   const float qv_sources = r.qi2qv_sublim_tend + r.qr2qv_evap_tend;
   if (!(qv_sources >= float(C::QSMALL))) return false;
-  const float dtf = float(dt);
   const float qv_sinks = r.qv2qi_vapdep_tend + r.qv2qi_nucleat_tend;
   constexpr float lvs = float((C::LatVap + C::LatIce) * C::INV_CP), lv = float(C::LatVap * C::INV_CP);
   const double T_endstep = t_atm + f2d(((qv_sinks - r.qi2qv_sublim_tend) * lvs - r.qr2qv_evap_tend * lv) * dtf);
@@ -1221,18 +1220,19 @@ __device__ __forceinline__ void update_prognostics(const Rates<double>& r, doubl
  * each prognostic's tendency is summed in FP32 from the FP32 rates (same
  * terms as update_prognostics) and applied to the FP64 state once; the
  * vapour change is minus the condensate changes, formed in FP64, so the
- * water of every cell is conserved to FP64 round-off. */
+ * water of every cell is conserved to FP64 round-off.  qi_f, qm_f, bm_f are
+ * the FP32 shadows of the current s.qi, s.qm, s.bm. */
 __device__ __forceinline__ void update_prognostics_bulk(const Rates<float>& r, double inv_exner, bool predictNc,
-                                                        bool prescribedCCN, bool log_wetgrowth, double dt,
+                                                        bool prescribedCCN, bool log_wetgrowth, float dtf,
                                                         float rho_qm_cloud, double inv_rho, int wlim, int nlim,
-                                                        const Rates<float>& r_lim, State& s) {
-  const float dtf = float(dt);
+                                                        const Rates<float>& r_lim, float qi_f, float qm_f,
+                                                        float bm_f, State& s) {
   const float sink_i = r.qi2qv_sublim_tend + r.qi2qr_melt_tend;
   float dqi = 0, dqm = 0, dbm = 0;
   if (dge(s.qi, C::QSMALL)) {
-    const float frac = sink_i * dtf / float(s.qi);
-    dbm = -frac * float(s.bm);
-    dqm = -frac * float(s.qm);
+    const float frac = sink_i * dtf / qi_f;
+    dbm = -frac * bm_f;
+    dqm = -frac * qm_f;
     dqi = -sink_i * dtf;
   }
   const float dum = (r.qr2qi_collect_tend + r.qc2qi_collect_tend + r.qr2qi_immers_freeze_tend +
