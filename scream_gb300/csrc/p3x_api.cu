@@ -155,8 +155,10 @@ int sm_stride_for(int nlev_max) {
 bool spec_fits(int precision, const LaunchSpec& ls, int stride) {
   if (ls.lanes != 8 && ls.lanes != 16 && ls.lanes != 32) return false;
   if (ls.groups_per_block <= 0 || ls.groups_per_block * ls.lanes > 256) return false;
-  const size_t k1 = precision == P3X_FP32_BULK ? p3_smem_bytes<float>(ls, stride) : p3_smem_bytes<double>(ls, stride);
-  return k1 <= size_t(227 * 1024) && sed_smem_bytes(ls, stride) <= size_t(227 * 1024);
+  const bool f32 = precision == P3X_FP32_BULK;
+  const size_t k1 = f32 ? p3_smem_bytes<float>(ls, stride) : p3_smem_bytes<double>(ls, stride);
+  const size_t k2 = f32 ? sed_smem_bytes<float>(ls, stride) : sed_smem_bytes<double>(ls, stride);
+  return k1 <= size_t(227 * 1024) && k2 <= size_t(227 * 1024);
 }
 
 /* Falls back to tables in global memory and then to fewer columns per CTA

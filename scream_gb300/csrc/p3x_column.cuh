@@ -88,6 +88,13 @@ enum { A_TATM = 0, A_RHO, A_RHOFACR, A_RHOFACI, A_ACN, A_QVSL, A_QVSI, A_QVSSI, 
  * the species being sedimented (acn, rhofacr or rhofaci), the rain flux
  * accumulator re-uses R2 (rain has two fields) */
 enum { B_RHO = 0, B_INVRHO, B_INVDZ, B_FAC, B_CLD, B_V1, B_V2, B_R0, B_R1, B_R2, B_R3, B_NARR };
+/* slots (of S doubles) of one column group in K2: B_NARR in the FP64 form,
+ * kSedBulkSlots in the FP32-bulk form (p3_sed_bulk) */
+constexpr int kSedBulkSlots = 10;
+template <class TR>
+__host__ __device__ constexpr int sed_slots() {
+  return sizeof(TR) == sizeof(float) ? kSedBulkSlots : B_NARR;
+}
 /* hand-over fields K1 -> K2/K3 */
 enum { S_TATM = 0, S_RHO, S_RHOFACR, S_RHOFACI, S_ACN, kScrFields };
 
@@ -1140,26 +1147,27 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
   const bool predictNc = in.predictNc != 0;
   const int kbot = nk - 1;
 #define SMA(a, k) sm[(a)*S + (k)]
-  /* 11 slots of S doubles; two float arrays share a slot */
-  float* const RHOf = reinterpret_cast<float*>(&SMA(0, 0));
-  float* const FACf = RHOf + S;
+  /* kSedBulkSlots slots of S doubles; two float arrays share a slot.  The
+   * density is read from the hand-over row (a float per level, L1-resident
+   * during the walk) rather than held in a slot. */
+  const float* const RHOf = scr_f(in, S_RHO, col);
+  float* const FACf = reinterpret_cast<float*>(&SMA(0, 0));
+  float* const CLDf = FACf + S;
   double* const COEF = &SMA(1, 0); /* g / dpres */
   float* const INVDZf = reinterpret_cast<float*>(&SMA(2, 0));
   float* const COEFf = INVDZf + S;
   float* const R2f = reinterpret_cast<float*>(&SMA(3, 0));
   float* const R3f = R2f + S;
-  float* const CLDf = reinterpret_cast<float*>(&SMA(4, 0));
-  float* const V1f = reinterpret_cast<float*>(&SMA(5, 0));
+  float* const V1f = reinterpret_cast<float*>(&SMA(4, 0));
   float* const V2f = V1f + S;
-  float* const R0f = reinterpret_cast<float*>(&SMA(6, 0));
+  float* const R0f = reinterpret_cast<float*>(&SMA(5, 0));
   float* const R1f = R0f + S;
   /* time-integrated face fluxes and the rain flux sum, as double-floats */
-  float2* const G[4] = {reinterpret_cast<float2*>(&SMA(7, 0)), reinterpret_cast<float2*>(&SMA(8, 0)),
-                        reinterpret_cast<float2*>(&SMA(9, 0)), reinterpret_cast<float2*>(&SMA(10, 0))};
+  float2* const G[4] = {reinterpret_cast<float2*>(&SMA(6, 0)), reinterpret_cast<float2*>(&SMA(7, 0)),
+                        reinterpret_cast<float2*>(&SMA(8, 0)), reinterpret_cast<float2*>(&SMA(9, 0))};
   float2* const PF = G[2]; /* rain flux accumulator (rain has two fields) */
   for (int k = lane; k < nk; k += LANES) {
     const double coef = C::gravit / in.dpres[co + k];
-    RHOf[k] = scr_f(in, S_RHO, col)[k];
     INVDZf[k] = 1.0f / float(in.dz[co + k]);
     COEF[k] = coef;
     COEFf[k] = float(coef);
@@ -1731,21 +1739,39 @@ __global__ void __launch_bounds__(256, sizeof(TR) == sizeof(float) ? 2 : 1)
 
 template <class TR, int LANES>
 __global__ void __launch_bounds__(256) p3_sed_kernel(const Inst inst0, const KParams<TR> kp) {
+  static_assert(sizeof(TR) == sizeof(double), "the FP32-bulk sedimentation kernel is p3_sed_bulk_kernel");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint32_t err = 0;
   Tabs<TR> tb;
   setup_tables<TR>(kp, false, smem_raw, tb, err);
   const int g_in_block = threadIdx.x / LANES;
-  double* sm = reinterpret_cast<double*>(smem_raw) + size_t(g_in_block) * B_NARR * kp.sm_stride;
+  double* sm = reinterpret_cast<double*>(smem_raw) + size_t(g_in_block) * sed_slots<TR>() * kp.sm_stride;
   const int groups_total = gridDim.x * kp.groups_per_block;
   for (int w = blockIdx.x * kp.groups_per_block + g_in_block; w < kp.nwork; w += groups_total) {
     int col;
     const Inst& in = work_inst(inst0, kp, w, col);
-    if constexpr (sizeof(TR) == sizeof(float)) {
-      p3_sed_bulk<LANES>(in, col, kp, tb, sm, err);
-    } else {
-      p3_sed<TR, LANES>(in, col, kp, tb, sm, err);
-    }
+    p3_sed<TR, LANES>(in, col, kp, tb, sm, err);
+  }
+  if (err) atomicOr(kp.err, err);
+}
+
+/* K2 of the FP32-bulk form.  Held to 96 registers: with its 10 shared slots
+ * per column that is five 4-column CTAs (20 warps) per SM, where the
+ * latency-bound substep walk gains from every resident warp.  At most 256
+ * threads per CTA (the launch checks it). */
+template <int LANES>
+__global__ void __maxnreg__(96) p3_sed_bulk_kernel(const Inst inst0, const KParams<float> kp) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint32_t err = 0;
+  Tabs<float> tb;
+  setup_tables<float>(kp, false, smem_raw, tb, err);
+  const int g_in_block = threadIdx.x / LANES;
+  double* sm = reinterpret_cast<double*>(smem_raw) + size_t(g_in_block) * kSedBulkSlots * kp.sm_stride;
+  const int groups_total = gridDim.x * kp.groups_per_block;
+  for (int w = blockIdx.x * kp.groups_per_block + g_in_block; w < kp.nwork; w += groups_total) {
+    int col;
+    const Inst& in = work_inst(inst0, kp, w, col);
+    p3_sed_bulk<LANES>(in, col, kp, tb, sm, err);
   }
   if (err) atomicOr(kp.err, err);
 }

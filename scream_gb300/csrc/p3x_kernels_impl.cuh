@@ -39,8 +39,13 @@ cudaError_t launch_p3_lanes(const dev::Inst& inst0, const dev::KParams<TR>& kp_i
                                         p3_smem_bytes<TR>(ls, kp.sm_stride), ls.blocks_per_sm, num_sms, stream);
   if (e != cudaSuccess) return e;
   if (ls.marks) cudaEventRecord(ls.marks[1], stream);
-  e = launch_persistent<TR>(dev::p3_sed_kernel<TR, LANES>, inst0, kp, threads, sed_smem_bytes(ls, kp.sm_stride),
-                            0, num_sms, stream);
+  if constexpr (sizeof(TR) == sizeof(float)) {
+    e = launch_persistent<TR>(dev::p3_sed_bulk_kernel<LANES>, inst0, kp, threads,
+                              sed_smem_bytes<TR>(ls, kp.sm_stride), 0, num_sms, stream);
+  } else {
+    e = launch_persistent<TR>(dev::p3_sed_kernel<TR, LANES>, inst0, kp, threads,
+                              sed_smem_bytes<TR>(ls, kp.sm_stride), 0, num_sms, stream);
+  }
   if (e != cudaSuccess) return e;
   if (ls.marks) cudaEventRecord(ls.marks[2], stream);
   e = launch_persistent<TR>(dev::p3_part3_kernel<TR, LANES>, inst0, kp, threads, 0, 0, num_sms, stream);

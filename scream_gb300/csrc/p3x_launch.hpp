@@ -26,8 +26,9 @@ inline size_t p3_smem_bytes(const LaunchSpec& ls, int sm_stride) {
   const size_t tables = ls.staged ? dev::table_smem_bytes<TR>() : 0;
   return tables + size_t(ls.groups_per_block) * dev::A_NARR * size_t(sm_stride) * sizeof(double);
 }
+template <class TR>
 inline size_t sed_smem_bytes(const LaunchSpec& ls, int sm_stride) {
-  return size_t(ls.groups_per_block) * dev::B_NARR * size_t(sm_stride) * sizeof(double);
+  return size_t(ls.groups_per_block) * dev::sed_slots<TR>() * size_t(sm_stride) * sizeof(double);
 }
 
 /* Persistent launches of the three column kernels (K1 part1+part2, K2
