@@ -515,7 +515,7 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
 
     double rho, inv_rho, qvsl, qvsi, qvssi, ccn_nc;
     TR rho_t, inv_rho_t;
-    const double exner = 1 / inv_exner;
+    const double exner = kF64 ? 1 / inv_exner : rcp_newton(inv_exner);
     double T = th * exner;
     qv = dmax0(qv);
     if constexpr (kF64) {
@@ -539,7 +539,7 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
       rho = f2d(rho_f);
       inv_rho_t = 1.0f / rho_f;
       inv_rho = f2d(inv_rho_t);
-      const double inv_p = 1 / dmax_c(pres, 1.e-3);
+      const double inv_p = rcp_newton(dmax_c(pres, 1.e-3));
       SMA(A_INVP, k) = inv_p;
       qvsl = C::ep_2 * svp_tabulated(rt.svp_tab, T, false, err) * inv_p;
       qvsi = C::ep_2 * svp_tabulated(rt.svp_tab, T, true, err) * inv_p;
@@ -1167,7 +1167,7 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
                         reinterpret_cast<float2*>(&SMA(8, 0)), reinterpret_cast<float2*>(&SMA(9, 0))};
   float2* const PF = G[2]; /* rain flux accumulator (rain has two fields) */
   for (int k = lane; k < nk; k += LANES) {
-    const double coef = C::gravit / in.dpres[co + k];
+    const double coef = C::gravit * rcp_newton(in.dpres[co + k]);
     INVDZf[k] = 1.0f / float(in.dz[co + k]);
     COEF[k] = coef;
     COEFf[k] = float(coef);

@@ -109,6 +109,19 @@ __device__ __forceinline__ double f2d(float x) {
   return __hiloint2double(int(hi), int(lo));
 }
 
+/* 1/x for the FP32-bulk form by Newton-Raphson from the FP32 reciprocal:
+ * each step r <- r + r (1 - x r) squares the relative error (~2^-22 from
+ * the FP32 seed, ~2^-44 after one step, below the FP64 rounding after two),
+ * so the result is within an ulp or two of 1/x.  Four FP64 FMAs replace the
+ * FP64 division sequence.  For positive normal x inside the float range
+ * (pressures, Exner factors, layer thicknesses). */
+__device__ __forceinline__ double rcp_newton(double x) {
+  double r = f2d(__fdividef(1.0f, float(x)));
+  r = fma(r, fma(-x, r, 1.0), r);
+  r = fma(r, fma(-x, r, 1.0), r);
+  return r;
+}
+
 /* widen(x): exact conversion to double (identity for doubles) */
 __device__ __forceinline__ double widen(double x) { return x; }
 __device__ __forceinline__ double widen(float x) { return f2d(x); }
@@ -207,7 +220,7 @@ __device__ __forceinline__ TR murphy_koop_svp(TR t, bool ice, uint32_t& err) {
 constexpr double kSvpT0 = 150.0, kSvpInvH = 64.0;
 constexpr int kSvpIntervals = 12800;
 __device__ __forceinline__ double svp_tabulated(const double* tab, double t, bool ice, uint32_t& err) {
-  const double x = (t - kSvpT0) * kSvpInvH;
+  const double x = fma(t, kSvpInvH, -kSvpT0 * kSvpInvH); /* = (t - T0) * 64, both exact here */
   if (!(!dneg(x) && dlt(x, double(kSvpIntervals)))) return murphy_koop_svp<double>(t, ice, err);
   const int i = int(x);
   const double u = x - double(i);
