@@ -176,6 +176,10 @@ cudaError_t launch_postamble(const dev::Inst* insts_d, const dev::WorkItem* work
 
 /* Exhaustive check of the integer-pipe float -> double conversion against
  * the hardware conversion: every one of the 2^32 float bit patterns. */
+/* Every float bit pattern: the integer-pipe float -> double conversion
+ * against the hardware one, and the FP32-pipe table index against the
+ * hardware truncation after the callers' clamps ([1, hi - 1] and [1, hi]);
+ * every integer below 2^22 in magnitude: its float on the FP32 pipe. */
 __global__ void f2d_selftest_kernel(unsigned long long* mismatches) {
   unsigned long long bad = 0;
   const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
@@ -183,6 +187,14 @@ __global__ void f2d_selftest_kernel(unsigned long long* mismatches) {
     const float x = __uint_as_float(uint32_t(i));
     const double a = dev::f2d(x), b = double(x);
     if (__double_as_longlong(a) != __double_as_longlong(b)) ++bad;
+    const int tz = __float2int_rz(x);
+    for (const int hi : {4, 5, 20, 30, 50, 300}) {
+      const int ti = dev::table_index(x, hi);
+      if (min(hi - 1, max(1, ti)) != min(hi - 1, max(1, tz))) ++bad;
+      if (min(hi, max(1, ti)) != min(hi, max(1, tz))) ++bad;
+    }
+    const int j = int(uint32_t(i));
+    if (j > -(1 << 22) && j < (1 << 22) && dev::i2f_small(j) != __int2float_rn(j)) ++bad;
   }
   if (bad) atomicAdd(mismatches, bad);
 }

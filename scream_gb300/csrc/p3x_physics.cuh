@@ -122,6 +122,34 @@ __device__ __forceinline__ double rcp_newton(double x) {
   return r;
 }
 
+/* Float <-> small integer on the FP32 and integer pipes (the hardware
+ * conversions execute on the FP64 pipe on this part).  Magic-number method:
+ * adding 1.5 * 2^23 with rounding toward minus infinity leaves floor(x) in
+ * the low significand bits for |x| < 2^22; the reverse subtraction gives the
+ * exact float of an integer |i| < 2^22. */
+__device__ __forceinline__ int ffloor_small(float x) {
+  return __float_as_int(__fadd_rd(x, 12582912.0f)) - 0x4B400000;
+}
+__device__ __forceinline__ float i2f_small(int i) { return __int_as_float(i + 0x4B400000) - 12582912.0f; }
+
+/* Table index of a coordinate: the reference truncates to int and then
+ * clamps the index to [1, hi - 1] (or a narrower range); truncating x
+ * clamped to [0, hi] gives the same index for every x, NaN included (0, as
+ * the hardware conversion gives).  The FP64 form keeps the conversion. */
+__device__ __forceinline__ int table_index(float x, int hi) {
+  return ffloor_small(fminf(fmaxf(x, 0.0f), float(hi)));
+}
+__device__ __forceinline__ int table_index(double x, int) { return static_cast<int>(x); }
+/* a table index as the rate type */
+__device__ __forceinline__ void index_value(int i, float& v) { v = i2f_small(i); }
+__device__ __forceinline__ void index_value(int i, double& v) { v = double(i); }
+template <class TR>
+__device__ __forceinline__ TR ival(int i) {
+  TR v;
+  index_value(i, v);
+  return v;
+}
+
 /* widen(x): exact conversion to double (identity for doubles) */
 __device__ __forceinline__ double widen(double x) { return x; }
 __device__ __forceinline__ double widen(float x) { return f2d(x); }
@@ -302,13 +330,13 @@ struct Table3 {
 template <class TR>
 __device__ __forceinline__ void lookup_ice(TR qi, TR ni, TR qm, TR rhop, TableIce<TR>& tab) {
   tab.dum1 = (m_log10(qi / ni) + TR(18)) * TR(C::lookup_table_1a_dum1_c) - TR(10);
-  tab.dumi = static_cast<int>(tab.dum1);
+  tab.dumi = table_index(tab.dum1, kIsize);
   tab.dum1 = vmin(tab.dum1, TR(kIsize));
   tab.dum1 = vmax(tab.dum1, TR(1.));
   tab.dumi = max(1, tab.dumi);
   tab.dumi = min(kIsize - 1, tab.dumi);
   tab.dum4 = (qm / qi) * TR(3) + TR(1);
-  tab.dumii = static_cast<int>(tab.dum4);
+  tab.dumii = table_index(tab.dum4, kRimsize);
   tab.dum4 = vmin(tab.dum4, TR(kRimsize));
   tab.dum4 = vmax(tab.dum4, TR(1.));
   tab.dumii = max(1, tab.dumii);
@@ -318,7 +346,7 @@ __device__ __forceinline__ void lookup_ice(TR qi, TR ni, TR qm, TR rhop, TableIc
   } else {
     tab.dum5 = (rhop - TR(650)) * TR(0.004) + TR(4);
   }
-  tab.dumjj = static_cast<int>(tab.dum5);
+  tab.dumjj = table_index(tab.dum5, kDensize);
   tab.dum5 = vmin(tab.dum5, TR(kDensize));
   tab.dum5 = vmax(tab.dum5, TR(1.));
   tab.dumjj = max(1, tab.dumjj);
@@ -335,7 +363,7 @@ __device__ __forceinline__ void lookup_rain(TR qr, TR nr, TableRain<TR>& tab) {
   TR dumlr = TR(1);
   if (gt_small) dumlr = m_cbrt(qr / (TR(C::Pi) * TR(C::RHO_H2O) * nr));
   tab.dum3 = (m_log10(TR(1) * dumlr) + TR(5)) * TR(10.70415);
-  tab.dumj = static_cast<int>(tab.dum3);
+  tab.dumj = table_index(tab.dum3, kRcollsize);
   tab.dum3 = vmin(tab.dum3, TR(kRcollsize));
   tab.dum3 = vmax(tab.dum3, TR(1));
   tab.dumj = max(1, tab.dumj);
@@ -352,9 +380,9 @@ __device__ __forceinline__ void lookup_rain(TR qr, TR nr, TableRain<TR>& tab) {
  * reference's order of operations. */
 template <class TR>
 __device__ __forceinline__ void apply_table_ice4(const Tabs<TR>& t, const TableIce<TR>& tab, int s0, TR out[4]) {
-  const TR w1 = tab.dum1 - TR(tab.dumi) - TR(1);
-  const TR w4 = tab.dum4 - TR(tab.dumii) - TR(1);
-  const TR w5 = tab.dum5 - TR(tab.dumjj) - TR(1);
+  const TR w1 = tab.dum1 - ival<TR>(tab.dumi) - TR(1);
+  const TR w4 = tab.dum4 - ival<TR>(tab.dumii) - TR(1);
+  const TR w5 = tab.dum5 - ival<TR>(tab.dumjj) - TR(1);
   TR a00[4], a01[4], a10[4], a11[4], b00[4], b01[4], b10[4], b11[4];
   ld4(ice_row(t, tab.dumjj, tab.dumii, tab.dumi) + s0, a00);
   ld4(ice_row(t, tab.dumjj, tab.dumii, tab.dumi + 1) + s0, a01);
@@ -380,10 +408,10 @@ __device__ __forceinline__ void apply_table_ice4(const Tabs<TR>& t, const TableI
 template <class TR>
 __device__ __forceinline__ TR apply_table_coll(int idx, const Tabs<TR>& t, const TableIce<TR>& ti,
                                                const TableRain<TR>& tr) {
-  const TR w1 = ti.dum1 - TR(ti.dumi) - TR(1);
-  const TR w3 = tr.dum3 - TR(tr.dumj) - TR(1);
-  const TR w4 = ti.dum4 - TR(ti.dumii) - TR(1);
-  const TR w5 = ti.dum5 - TR(ti.dumjj) - TR(1);
+  const TR w1 = ti.dum1 - ival<TR>(ti.dumi) - TR(1);
+  const TR w3 = tr.dum3 - ival<TR>(tr.dumj) - TR(1);
+  const TR w4 = ti.dum4 - ival<TR>(ti.dumii) - TR(1);
+  const TR w5 = ti.dum5 - ival<TR>(ti.dumjj) - TR(1);
   TR tmp[2];
 #pragma unroll
   for (int dj = 0; dj < 2; ++dj) {
@@ -415,7 +443,7 @@ __device__ __forceinline__ void lookup3(TR mu_r, TR lamr, const RuntimeDev& rt, 
     TR rdumii = (dum1 * TR(1.e6) + TR(5)) * inv_dum3;
     rdumii = vmax(rdumii, TR(1.0));
     rdumii = vmin(rdumii, TR(20.0));
-    int dumii = static_cast<int>(rdumii);
+    int dumii = table_index(rdumii, 20);
     dumii = max(dumii, 1);
     dumii = min(dumii, 20);
     tab.rdumii = rdumii;
@@ -425,7 +453,7 @@ __device__ __forceinline__ void lookup3(TR mu_r, TR lamr, const RuntimeDev& rt, 
     TR rdumii = (dum1 * TR(1.e+6) - TR(195)) * inv_dum3 + TR(20);
     rdumii = vmax(rdumii, TR(20.0));
     rdumii = vmin(rdumii, TR(300.0));
-    int dumii = static_cast<int>(rdumii);
+    int dumii = table_index(rdumii, 300);
     dumii = max(dumii, 20);
     dumii = min(dumii, 299);
     tab.rdumii = rdumii;
@@ -438,12 +466,12 @@ __device__ __forceinline__ void lookup3(TR mu_r, TR lamr, const RuntimeDev& rt, 
 /* apply_table (Table3), p3_table3_impl.hpp:66-83 */
 template <class TR>
 __device__ __forceinline__ TR apply_table3(const Tabs<TR>& t, const TR* table, const Table3<TR>& t3) {
-  const TR rdumii_m_dumii = t3.rdumii - TR(t3.dumii);
+  const TR rdumii_m_dumii = t3.rdumii - ival<TR>(t3.dumii);
   const TR t_im1_jm1 = t3_at(t, table, t3.dumii - 1, t3.dumjj - 1);
   const TR dum1 = (t_im1_jm1 + rdumii_m_dumii * (t3_at(t, table, t3.dumii, t3.dumjj - 1) - t_im1_jm1));
   const TR t_im1_j = t3_at(t, table, t3.dumii - 1, t3.dumjj);
   const TR dum2 = (t_im1_j + rdumii_m_dumii * (t3_at(t, table, t3.dumii, t3.dumjj) - t_im1_j));
-  return dum1 + (t3.rdumjj - TR(t3.dumjj)) * (dum2 - dum1);
+  return dum1 + (t3.rdumjj - ival<TR>(t3.dumjj)) * (dum2 - dum1);
 }
 
 /* ------------------------------------------------------------------ */

@@ -321,7 +321,9 @@ def test_fp32_bulk_precision_form(gpu_ctx, tables, built):
 
 def test_integer_float_to_double_conversion_is_exact(gpu_ctx):
     """The FP32-bulk form's float -> double conversion on the integer pipes
-    agrees bitwise with the hardware conversion for every float bit pattern."""
+    agrees bitwise with the hardware conversion for every float bit pattern;
+    its table indices on the FP32 pipe equal the hardware truncation after the
+    lookups' clamps for every float, and its small-integer floats are exact."""
     from scream_gb300 import _lib as L
     n = C.c_uint64(123)
     assert gpu_ctx.lib.p3x_selftest(C.byref(n)) == 0
