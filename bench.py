@@ -8,9 +8,11 @@ all columns.  Inputs (15.9 GB per step) are larger than L2, so no flush is
 needed between steps.
 
   value       column-levels/s of the FP32-bulk step, inputs resident in HBM
-  e2e         the same step through the public API with pinned HOST buffers:
-              every step copies the 23 input fields host->device and the
-              20 per-level outputs + 2 interface fluxes + 2 surface fields back
+  e2e         the same step through the public API on pinned HOST arrays
+              (p3x_main_host): every step copies the 23 input fields
+              host->device and the 20 per-level outputs + 2 interface fluxes +
+              2 surface fields back, in column chunks overlapped with the
+              kernels
   roofline    HBM roofline of the P3 step (three kernels: part1+part2,
               sedimentation, part3) at 360 algorithmic bytes per column-level
               (23 FP64 inputs read, 22 FP64 outputs written), with each
@@ -385,18 +387,15 @@ def run_gpu(args):
     # e2e: pinned host buffers through the public API
     h2d_fields = L.INPUT_FIELDS
     d2h_fields = [n for n in L.ALL_FIELDS if n not in L.DIAG_IN_FIELDS]
-    f = p3.P3Fields.allocate(ncol, NLEV)
-    host_in = {n: torch.from_numpy(np.ascontiguousarray(inputs[n])).pin_memory() for n in h2d_fields}
-    host_out = {n: torch.empty(f.t[n].shape, dtype=torch.float64).pin_memory() for n in d2h_fields}
-    h2d_bytes = sum(v.numel() * 8 for v in host_in.values())
-    d2h_bytes = sum(v.numel() * 8 for v in host_out.values())
+    hf = p3.P3Fields.allocate_host(ncol, NLEV)
+    for n in h2d_fields:
+        hf.t[n].copy_(torch.from_numpy(np.ascontiguousarray(inputs[n])))
+    h2d_bytes = sum(hf.t[n].numel() * 8 for n in h2d_fields)
+    d2h_bytes = sum(hf.t[n].numel() * 8 for n in d2h_fields)
 
     def e2e_step(it):
-        for n in h2d_fields:
-            f.t[n].copy_(host_in[n], non_blocking=True)
-        ctx.p3_main(f, DT, L.P3X_FP32_BULK, it=it, sync=False)
-        for n in d2h_fields:
-            host_out[n].copy_(f.t[n], non_blocking=True)
+        # host arrays in, host arrays out (state carried in host memory)
+        ctx.p3_main_host(hf, DT, L.P3X_FP32_BULK, it=it)
 
     e2e_steps = max(2, min(args.steps, 5))
     for s in range(min(args.warmup, 2)):
@@ -409,7 +408,7 @@ def run_gpu(args):
     e2e_wall = maxr(time.perf_counter() - t0)
     ctx.check()
     e2e_value = weak_value(ws, cl_step, e2e_steps, e2e_wall)
-    del f, host_in, host_out
+    del hf
     torch.cuda.empty_cache()
 
     batched = run_batched(ctx, args) if not args.no_batched else None
@@ -453,7 +452,9 @@ def run_gpu(args):
         "roofline": roof,
         "e2e": {"value": e2e_value, "unit": "column-levels/s", "h2d_bytes_per_step": h2d_bytes,
                 "d2h_bytes_per_step": d2h_bytes, "steps": e2e_steps,
-                "path": "pinned host tensors -> P3Context.p3_main (libp3x C ABI) -> pinned host"},
+                "path": "pinned host arrays -> P3Context.p3_main_host (libp3x C ABI p3x_main_host: column "
+                        "chunks through three device buffers, uploads/kernels/downloads overlapped) -> "
+                        "pinned host arrays"},
         "gpu_launches": 3 * args.steps,
         "batched": batched,
         "serving": serving,

@@ -180,6 +180,23 @@ int p3x_main(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_state
              const p3x_infrastructure* infra, const p3x_history_only* hist, int32_t nj, int32_t nk,
              const p3x_layout* layout, int32_t precision, void* stream, double* elapsed_us);
 
+/* Same step on HOST buffers: every pointer of prog / din / dout / hist is a
+ * host array in the same (nj, ld) layout (page-locked memory for full
+ * speed).  The columns are processed in chunks of chunk_cols (0: an eighth
+ * of nj, at least 8192) through a ring of three device chunk buffers on the
+ * context's own streams, so one chunk's upload, another's kernels and a
+ * third's download run at once.  Uploads the prognostic state and the
+ * diagnostic inputs, downloads the prognostic state, the diagnostic outputs
+ * and the history fields.  Synchronous: returns when the host arrays hold
+ * the results; *elapsed_us (may be NULL) receives the time from the first
+ * upload to the last download.  Results are bitwise those of p3x_main on the
+ * same data.  The reference's host drivers pass host views to p3_main
+ * through its own deep copies; this entry is that path without them. */
+int p3x_main_host(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_state* prog,
+                  const p3x_diagnostic_inputs* din, const p3x_diagnostic_outputs* dout,
+                  const p3x_infrastructure* infra, const p3x_history_only* hist, int32_t nj, int32_t nk,
+                  const p3x_layout* layout, int32_t precision, int32_t chunk_cols, double* elapsed_us);
+
 /* Same, stream-ordered and asynchronous: no host synchronisation.  The
  * per-step hand-over scratch between the three kernels (40 B per
  * column-level + 4 B per column) is taken from and returned to the

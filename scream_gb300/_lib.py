@@ -136,6 +136,10 @@ PROTOTYPES = {
                            C.POINTER(DiagnosticInputs), C.POINTER(DiagnosticOutputs),
                            C.POINTER(Infrastructure), C.POINTER(HistoryOnly), _I, _I,
                            C.POINTER(Layout), _I, _V, C.POINTER(C.c_double)]),
+    "p3x_main_host": (C.c_int, [_V, C.POINTER(Runtime), C.POINTER(PrognosticState),
+                                C.POINTER(DiagnosticInputs), C.POINTER(DiagnosticOutputs),
+                                C.POINTER(Infrastructure), C.POINTER(HistoryOnly), _I, _I,
+                                C.POINTER(Layout), _I, _I, C.POINTER(C.c_double)]),
     "p3x_main_async": (C.c_int, [_V, C.POINTER(Runtime), C.POINTER(PrognosticState),
                                  C.POINTER(DiagnosticInputs), C.POINTER(DiagnosticOutputs),
                                  C.POINTER(Infrastructure), C.POINTER(HistoryOnly), _I, _I,

@@ -42,6 +42,12 @@ struct p3x_context {
   int64_t fbuf_elems = 0;
   double* fstage = nullptr;
   int64_t fstage_elems = 0;
+  /* host-buffer entry: a ring of device chunk buffers, one stream each
+   * (grown on demand) */
+  static constexpr int kHostRing = 3;
+  cudaStream_t hstream[kHostRing] = {nullptr, nullptr, nullptr};
+  double* hbuf[kHostRing] = {nullptr, nullptr, nullptr};
+  size_t hbuf_bytes = 0;
 };
 
 namespace p3x {
@@ -253,11 +259,12 @@ void bind_scratch(dev::Inst& in, unsigned char* base) {
                                         sizeof(double));
 }
 
-int launch_kernels(p3x_context* ctx, const p3x_runtime* rt, const dev::Inst& in, cudaStream_t st) {
+int launch_kernels(p3x_context* ctx, const p3x_runtime* rt, const dev::Inst& in, cudaStream_t st,
+                   bool marks = true) {
   const dev::RuntimeDev rtd = make_runtime(*rt);
   const int stride = sm_stride_for(in.nlev);
   LaunchSpec ls = fit_spec(in.precision, spec_of(ctx->cfg[in.precision]), stride);
-  if (ctx->ktime) ls.marks = ctx->kev;
+  if (ctx->ktime && marks) ls.marks = ctx->kev;
   if (!spec_fits(in.precision, ls, stride)) return P3X_EINVAL;
   cudaError_t e;
   if (in.precision == P3X_FP32_BULK) {
@@ -280,13 +287,14 @@ int launch_kernels(p3x_context* ctx, const p3x_runtime* rt, const dev::Inst& in,
 
 /* One step of one instance: the K1->K2/K3 scratch comes from the context's
  * stream-ordered pool and returns to it behind the three kernels. */
-int launch_single(p3x_context* ctx, const p3x_runtime* rt, const dev::Inst& in_, cudaStream_t st) {
+int launch_single(p3x_context* ctx, const p3x_runtime* rt, const dev::Inst& in_, cudaStream_t st,
+                  bool marks = true) {
   if (in_.ncol == 0) return P3X_OK;
   dev::Inst in = in_;
   void* scr = nullptr;
   P3X_CUDA(cudaMallocFromPoolAsync(&scr, dev::scratch_bytes(in.ncol, in.ld), ctx->pool, st));
   bind_scratch(in, static_cast<unsigned char*>(scr));
-  const int rc = launch_kernels(ctx, rt, in, st);
+  const int rc = launch_kernels(ctx, rt, in, st, marks);
   const cudaError_t fe = cudaFreeAsync(scr, st);
   if (rc) return rc;
   return cuda_status(fe);
@@ -476,6 +484,10 @@ int p3x_context_destroy(p3x_context* ctx) {
   }
   for (cudaEvent_t e : ctx->kev)
     if (e) cudaEventDestroy(e);
+  for (int i = 0; i < p3x_context::kHostRing; ++i) {
+    if (ctx->hbuf[i]) cudaFree(ctx->hbuf[i]);
+    if (ctx->hstream[i]) cudaStreamDestroy(ctx->hstream[i]);
+  }
   delete ctx;
   return P3X_OK;
 }
@@ -579,6 +591,157 @@ int p3x_main(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_state
   if (se != cudaSuccess) return cuda_status(se);
   if (elapsed_us) *elapsed_us = double(ms) * 1000.0;
   return read_and_clear_err(ctx, s);
+}
+
+/* ------------------------------------------------------------------ */
+/* Host-buffer entry: chunked, copies overlapped with the kernels       */
+/* ------------------------------------------------------------------ */
+namespace {
+
+/* The fields of one call in the order of dev::Inst, with their row length
+ * (0: one value per column, 1: ld, 2: ld_int) and direction (1 = uploaded,
+ * 2 = downloaded, 3 = both). */
+struct HostField {
+  int rows;
+  int dir;
+};
+constexpr int kNumHostFields = 37;
+constexpr HostField kHostFields[kNumHostFields] = {
+    {1, 3}, {1, 3}, {1, 3}, {1, 3}, {1, 3}, {1, 3}, {1, 3}, {1, 3}, {1, 3}, {1, 3},  /* prognostic state */
+    {1, 1}, {1, 1}, {1, 1}, {1, 1}, {1, 1}, {1, 1}, {1, 1}, {1, 1}, {1, 1}, {1, 1},  /* diagnostic inputs */
+    {1, 1}, {1, 1}, {1, 1},
+    {1, 2}, {0, 2}, {0, 2}, {1, 2}, {1, 2}, {1, 2}, {1, 2}, {2, 2}, {2, 2}, {1, 2},  /* diagnostic outputs */
+    {1, 2},
+    {1, 2}, {1, 2}, {1, 2}};                                                          /* history */
+
+/* the addresses of an Inst's field pointers, in kHostFields order */
+void field_addrs(dev::Inst& in, const double** a[kNumHostFields]) {
+  const double** v[kNumHostFields] = {
+      const_cast<const double**>(&in.qc), const_cast<const double**>(&in.nc),
+      const_cast<const double**>(&in.qr), const_cast<const double**>(&in.nr),
+      const_cast<const double**>(&in.qi), const_cast<const double**>(&in.qm),
+      const_cast<const double**>(&in.ni), const_cast<const double**>(&in.bm),
+      const_cast<const double**>(&in.qv), const_cast<const double**>(&in.th),
+      &in.nc_nuceat_tend, &in.nccn, &in.ni_activated, &in.inv_qc_relvar, &in.cld_frac_i, &in.cld_frac_l,
+      &in.cld_frac_r, &in.pres, &in.dz, &in.dpres, &in.inv_exner, &in.qv_prev, &in.t_prev,
+      const_cast<const double**>(&in.qv2qi_depos_tend), const_cast<const double**>(&in.precip_liq_surf),
+      const_cast<const double**>(&in.precip_ice_surf), const_cast<const double**>(&in.diag_eff_radius_qc),
+      const_cast<const double**>(&in.diag_eff_radius_qi), const_cast<const double**>(&in.diag_eff_radius_qr),
+      const_cast<const double**>(&in.rho_qi), const_cast<const double**>(&in.precip_liq_flux),
+      const_cast<const double**>(&in.precip_ice_flux), const_cast<const double**>(&in.precip_total_tend),
+      const_cast<const double**>(&in.nevapr), const_cast<const double**>(&in.liq_ice_exchange),
+      const_cast<const double**>(&in.vap_liq_exchange), const_cast<const double**>(&in.vap_ice_exchange)};
+  for (int i = 0; i < kNumHostFields; ++i) a[i] = v[i];
+}
+
+int64_t row_len(const dev::Inst& in, int rows) { return rows == 0 ? 1 : (rows == 1 ? in.ld : in.ld_int); }
+
+/* doubles of one chunk of `cols` columns of every field */
+size_t chunk_elems(const dev::Inst& in, int64_t cols) {
+  size_t n = 0;
+  for (const HostField& f : kHostFields) n += size_t(cols) * size_t(row_len(in, f.rows));
+  return n;
+}
+
+}  // namespace
+
+int p3x_main_host(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_state* prog,
+                  const p3x_diagnostic_inputs* din, const p3x_diagnostic_outputs* dout,
+                  const p3x_infrastructure* infra, const p3x_history_only* hist, int32_t nj, int32_t nk,
+                  const p3x_layout* layout, int32_t precision, int32_t chunk_cols, double* elapsed_us) {
+  if (!ctx || !rt || !infra || !valid_runtime(*rt) || chunk_cols < 0) return P3X_EINVAL;
+  dev::Inst host;
+  int st = fill_inst(prog, din, dout, hist, layout, nj, nk, infra->dt, infra->predictNc, infra->prescribedCCN,
+                     precision, host);
+  if (st) return st;
+  if (nj == 0) {
+    if (elapsed_us) *elapsed_us = 0;
+    return P3X_OK;
+  }
+  /* chunks: an eighth of the columns (at least 8192, and all of them when
+   * fewer), so that three chunks in flight overlap upload, kernels and
+   * download */
+  int64_t cols = chunk_cols > 0 ? chunk_cols : std::max<int64_t>((int64_t(nj) + 7) / 8, 8192);
+  cols = std::min<int64_t>(cols, nj);
+  const size_t slot_bytes = chunk_elems(host, cols) * sizeof(double);
+  if (slot_bytes > ctx->hbuf_bytes) {
+    for (int i = 0; i < p3x_context::kHostRing; ++i) {
+      if (ctx->hstream[i]) P3X_CUDA(cudaStreamSynchronize(ctx->hstream[i]));
+      if (ctx->hbuf[i]) {
+        cudaFree(ctx->hbuf[i]);
+        ctx->hbuf[i] = nullptr;
+      }
+    }
+    ctx->hbuf_bytes = 0;
+    for (int i = 0; i < p3x_context::kHostRing; ++i) {
+      if (cudaMalloc(&ctx->hbuf[i], slot_bytes) != cudaSuccess) {
+        cudaGetLastError();
+        for (int j = 0; j <= i; ++j) {
+          if (ctx->hbuf[j]) cudaFree(ctx->hbuf[j]);
+          ctx->hbuf[j] = nullptr;
+        }
+        return P3X_ENOMEM;
+      }
+    }
+    ctx->hbuf_bytes = slot_bytes;
+  }
+  for (int i = 0; i < p3x_context::kHostRing; ++i)
+    if (!ctx->hstream[i]) P3X_CUDA(cudaStreamCreateWithFlags(&ctx->hstream[i], cudaStreamNonBlocking));
+
+  cudaEvent_t e0, e1;
+  P3X_CUDA(cudaEventCreate(&e0));
+  P3X_CUDA(cudaEventCreate(&e1));
+  cudaEventRecord(e0, ctx->hstream[0]);
+  for (int i = 1; i < p3x_context::kHostRing; ++i) cudaStreamWaitEvent(ctx->hstream[i], e0, 0);
+  int nchunk = 0;
+  for (int64_t c0 = 0; c0 < nj && st == P3X_OK; c0 += cols, ++nchunk) {
+    const int slot = nchunk % p3x_context::kHostRing;
+    cudaStream_t s = ctx->hstream[slot];
+    const int64_t n = std::min<int64_t>(cols, int64_t(nj) - c0);
+    dev::Inst chunk = host;
+    chunk.ncol = int32_t(n);
+    const double** ha[kNumHostFields];
+    const double** ca[kNumHostFields];
+    field_addrs(host, ha);
+    field_addrs(chunk, ca);
+    double* d = ctx->hbuf[slot];
+    for (int i = 0; i < kNumHostFields && st == P3X_OK; ++i) {
+      const int64_t len = row_len(host, kHostFields[i].rows);
+      *ca[i] = d;
+      if (kHostFields[i].dir & 1) {
+        const cudaError_t e = cudaMemcpyAsync(d, *ha[i] + c0 * len, size_t(n * len) * sizeof(double),
+                                              cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) st = cuda_status(e);
+      }
+      d += size_t(cols) * size_t(len);
+    }
+    if (st == P3X_OK) st = launch_single(ctx, rt, chunk, s, false);
+    for (int i = 0; i < kNumHostFields && st == P3X_OK; ++i) {
+      if (!(kHostFields[i].dir & 2)) continue;
+      const int64_t len = row_len(host, kHostFields[i].rows);
+      const cudaError_t e = cudaMemcpyAsync(const_cast<double*>(*ha[i]) + c0 * len, *ca[i],
+                                            size_t(n * len) * sizeof(double), cudaMemcpyDeviceToHost, s);
+      if (e != cudaSuccess) st = cuda_status(e);
+    }
+  }
+  for (int i = 1; i < p3x_context::kHostRing; ++i) {
+    cudaEvent_t ei;
+    if (cudaEventCreateWithFlags(&ei, cudaEventDisableTiming) == cudaSuccess) {
+      cudaEventRecord(ei, ctx->hstream[i]);
+      cudaStreamWaitEvent(ctx->hstream[0], ei, 0);
+      cudaEventDestroy(ei);
+    }
+  }
+  cudaEventRecord(e1, ctx->hstream[0]);
+  const cudaError_t se = cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  if (se != cudaSuccess) return cuda_status(se);
+  if (elapsed_us) *elapsed_us = double(ms) * 1000.0;
+  return read_and_clear_err(ctx, ctx->hstream[0]);
 }
 
 /* ------------------------------------------------------------------ */

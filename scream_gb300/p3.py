@@ -94,6 +94,15 @@ class P3Fields:
     def hist(self):
         return L.HistoryOnly(*[_ptr(self.t[n]) for n in L.HIST_FIELDS])
 
+    @classmethod
+    def allocate_host(cls, ncol: int, nlev: int, pinned: bool = True):
+        """Host (page-locked by default) arrays of one call, for
+        :meth:`P3Context.p3_main_host`."""
+        f = cls(ncol, nlev)
+        for n in L.ALL_FIELDS:
+            f.t[n] = torch.zeros(field_shape(n, ncol, nlev), dtype=torch.float64, pin_memory=pinned)
+        return f
+
     def to_host(self) -> Dict[str, np.ndarray]:
         return {n: v.detach().cpu().numpy() for n, v in self.t.items()}
 
@@ -165,6 +174,20 @@ class P3Context:
                                      precision, sh)
         L.check("p3x_main_async", rc)
         return 0.0
+
+    def p3_main_host(self, f: P3Fields, dt: float, precision: int = L.P3X_FP64, runtime: L.Runtime = None,
+                     predictNc=True, prescribedCCN=True, it=1, chunk_cols=0) -> float:
+        """One P3 step on HOST arrays (``P3Fields.allocate_host``), copies
+        overlapped with the kernels chunk by chunk (p3x_main_host); returns
+        the time from first upload to last download in microseconds."""
+        rt = runtime if runtime is not None else L.default_runtime()
+        infra = L.Infrastructure(dt, it, 1, f.ncol, 1, f.nlev, int(predictNc), int(prescribedCCN), None)
+        us = C.c_double(0)
+        rc = self.lib.p3x_main_host(self.h, C.byref(rt), C.byref(f.prog()), C.byref(f.din()), C.byref(f.dout()),
+                                    C.byref(infra), C.byref(f.hist()), f.ncol, f.nlev,
+                                    C.byref(L.Layout(f.nlev, f.nlev + 1)), precision, chunk_cols, C.byref(us))
+        L.check("p3x_main_host", rc)
+        return us.value
 
     def _interface(self, host_fields: Dict[str, "torch.Tensor"]):
         return L.InterfaceFields(*[(_ptr(host_fields[n]) if host_fields.get(n) is not None else None)
