@@ -21,6 +21,7 @@ BUILD = PKG / "_build"
 LIB = PKG / "libp3x.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+FP32_BULK_FLAGS = ["--use_fast_math", "-ftz=false"]
 
 
 def _nvcc() -> str:
@@ -31,7 +32,7 @@ def _nvcc() -> str:
 
 
 def _deps_mtime() -> float:
-    files = list(CSRC.glob("*")) + list(INCLUDE.glob("*.h"))
+    files = list(CSRC.glob("*")) + list(INCLUDE.glob("*.h")) + [Path(__file__)]
     return max(f.stat().st_mtime for f in files)
 
 
@@ -43,6 +44,13 @@ def _compile(src: Path, newest: float) -> Path:
     if src.suffix == ".cu":
         cmd = [nvcc, "-std=c++17", "-O3", *ARCH, "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp",
                f"-I{INCLUDE}", f"-I{CSRC}", "-c", str(src), "-o", str(obj)]
+        if src.name.startswith("p3x_k_f"):
+            # FP32-bulk kernels: FP32 rates through the hardware approximations
+            # (approximate division, square root and transcendentals); FP64
+            # arithmetic is unaffected, denormals are kept, and the exact
+            # building blocks (double-float sums, table indices) use
+            # correctly rounded intrinsics.
+            cmd[3:3] = FP32_BULK_FLAGS
     else:
         cmd = ["g++", "-std=c++17", "-O3", "-fPIC", "-fopenmp", f"-I{INCLUDE}", f"-I{CSRC}",
                "-I/usr/local/cuda/include", "-c", str(src), "-o", str(obj)]
