@@ -182,7 +182,7 @@ int p3x_main(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_state
 
 /* Same step on HOST buffers: every pointer of prog / din / dout / hist is a
  * host array in the same (nj, ld) layout (page-locked memory for full
- * speed).  The columns are processed in chunks of chunk_cols (0: a twelfth
+ * speed).  The columns are processed in chunks of chunk_cols (0: a sixteenth
  * of nj, at least 8192) through a ring of three device chunk buffers on the
  * context's own streams, so one chunk's upload, another's kernels and a
  * third's download run at once.  Uploads the prognostic state and the

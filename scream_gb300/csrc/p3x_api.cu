@@ -658,11 +658,13 @@ int p3x_main_host(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_
     if (elapsed_us) *elapsed_us = 0;
     return P3X_OK;
   }
-  /* chunks: a twelfth of the columns (at least 8192, and all of them when
+  /* chunks: a sixteenth of the columns (at least 8192, and all of them when
    * fewer), so that three chunks in flight overlap upload, kernels and
-   * download; at 345,600 x 128 on GB300 twelve chunks measured 59 ms per
-   * step against 63 ms for eight and 60 ms for sixteen */
-  int64_t cols = chunk_cols > 0 ? chunk_cols : std::max<int64_t>((int64_t(nj) + 11) / 12, 8192);
+   * download.  At 345,600 x 128 on GB300 the step is then bound by the
+   * host link (15.9 GB moved at ~290 GB/s both ways): 54.2 ms per step for
+   * 16 chunks, 54.8 for 12, 56.8 for 8; a ring of 4 or 6 buffers measured
+   * the same as 3. */
+  int64_t cols = chunk_cols > 0 ? chunk_cols : std::max<int64_t>((int64_t(nj) + 15) / 16, 8192);
   cols = std::min<int64_t>(cols, nj);
   const size_t slot_bytes = chunk_elems(host, cols) * sizeof(double);
   if (slot_bytes > ctx->hbuf_bytes) {
