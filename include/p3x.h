@@ -266,8 +266,10 @@ int p3x_postamble(const p3x_interface_fields* f, const p3x_prognostic_state* pro
  * reference): for all 2^32 float bit patterns, compares the FP32-bulk form's
  * integer-pipe float -> double conversion with the hardware conversion and
  * its FP32-pipe table indices with the hardware truncation (after the table
- * lookups' clamps), and checks its small-integer floats; *mismatches
- * receives the number of disagreements (0 expected). */
+ * lookups' clamps), and checks its small-integer floats; for 2^32 doubles
+ * covering every high word, compares its integer-pipe narrowing toward zero
+ * with the hardware conversion; *mismatches receives the number of
+ * disagreements (0 expected). */
 int p3x_selftest(uint64_t* mismatches);
 
 /* Per-kernel timing of single-instance steps (no counterpart in the

@@ -136,6 +136,32 @@ dev::RuntimeDev make_runtime(const p3x_runtime& r) {
   d.g_mur2 = std::tgamma(mu_r + 2.0);
   d.lg_mur4 = std::log(std::tgamma(mu_r + 4.0));
   d.lg_mur7 = std::log(std::tgamma(mu_r + 7.0));
+  d.accretion_same_exponent = r.accretion_qc_exponent == r.accretion_qr_exponent ? 1 : 0;
+  /* float copies for the FP32-bulk rates (round to nearest, as a device
+   * conversion gives) */
+  d.f.max_total_ni = float(d.max_total_ni);
+  d.f.autoconversion_prefactor = float(d.autoconversion_prefactor);
+  d.f.autoconversion_qc_exponent = float(d.autoconversion_qc_exponent);
+  d.f.autoconversion_nc_exponent = float(d.autoconversion_nc_exponent);
+  d.f.accretion_prefactor = float(d.accretion_prefactor);
+  d.f.accretion_qc_exponent = float(d.accretion_qc_exponent);
+  d.f.accretion_qr_exponent = float(d.accretion_qr_exponent);
+  d.f.rain_selfcollection_prefactor = float(d.rain_selfcollection_prefactor);
+  d.f.rain_selfcollection_breakup_diameter = float(d.rain_selfcollection_breakup_diameter);
+  d.f.constant_mu_rain = float(d.constant_mu_rain);
+  d.f.cldliq_to_ice_collection_factor = float(d.cldliq_to_ice_collection_factor);
+  d.f.rain_to_ice_collection_factor = float(d.rain_to_ice_collection_factor);
+  d.f.min_rime_rho = float(d.min_rime_rho);
+  d.f.max_rime_rho = float(d.max_rime_rho);
+  d.f.immersion_freezing_exponent = float(d.immersion_freezing_exponent);
+  d.f.deposition_nucleation_exponent = float(d.deposition_nucleation_exponent);
+  d.f.ice_sedimentation_factor = float(d.ice_sedimentation_factor);
+  d.f.cons3 = float(d.cons3);
+  d.f.t3_rdumjj = float(d.t3_rdumjj);
+  d.f.g_mur1 = float(d.g_mur1);
+  d.f.g_mur2 = float(d.g_mur2);
+  d.f.lg_mur4 = float(d.lg_mur4);
+  d.f.lg_mur7 = float(d.lg_mur7);
   return d;
 }
 

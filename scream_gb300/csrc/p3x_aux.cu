@@ -179,7 +179,9 @@ cudaError_t launch_postamble(const dev::Inst* insts_d, const dev::WorkItem* work
 /* Every float bit pattern: the integer-pipe float -> double conversion
  * against the hardware one, and the FP32-pipe table index against the
  * hardware truncation after the callers' clamps ([1, hi - 1] and [1, hi]);
- * every integer below 2^22 in magnitude: its float on the FP32 pipe. */
+ * every integer below 2^22 in magnitude: its float on the FP32 pipe; 2^32
+ * doubles covering every high word: the integer-pipe narrowing toward zero
+ * against the hardware conversion. */
 __global__ void f2d_selftest_kernel(unsigned long long* mismatches) {
   unsigned long long bad = 0;
   const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
@@ -195,6 +197,14 @@ __global__ void f2d_selftest_kernel(unsigned long long* mismatches) {
     }
     const int j = int(uint32_t(i));
     if (j > -(1 << 22) && j < (1 << 22) && dev::i2f_small(j) != __int2float_rn(j)) ++bad;
+    /* a double with this pattern as its high word and a hashed low word:
+     * every sign, exponent and leading significand */
+    const double y = __hiloint2double(int(uint32_t(i)), int(uint32_t(i) * 2654435761u));
+    const double ay = fabs(y);
+    const float want = !(ay < 0x1p128) ? __double2float_rn(y)
+                                        : (ay < 0x1p-126 ? (signbit(y) ? -0.0f : 0.0f) : __double2float_rz(y));
+    const float got = dev::d2f_rz(y);
+    if (__float_as_uint(got) != __float_as_uint(want) && !(isnan(got) && isnan(want))) ++bad;
   }
   if (bad) atomicAdd(mismatches, bad);
 }

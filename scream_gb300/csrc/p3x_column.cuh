@@ -339,7 +339,7 @@ __device__ __forceinline__ void part2_level_bulk(const Inst& in, const int64_t o
       const bool changed = n_out != nr_in;
       nr_in = n_out;
       if (qr_in >= QS) {
-        cdistr = nr_in / float(rt.g_mur1);
+        cdistr = nr_in / rt.f.g_mur1;
         logn0r = m_log10(cdistr) + (mu_r + 1.0f) * m_log10(lamr);
       }
       if (changed) {
@@ -347,7 +347,7 @@ __device__ __forceinline__ void part2_level_bulk(const Inst& in, const int64_t o
         nr0 = float(s.nr);
       }
     }
-    impose_max_total_ni(ni_in, rt.max_total_ni, inv_rho);
+    impose_max_total_ni(ni_in, rt.f.max_total_ni, inv_rho);
     if (qi_in >= QS) {
       ni_in = vmax(ni_in, float(C::NSMALL));
       nr_in = vmax(nr_in, float(C::NSMALL));
@@ -413,7 +413,7 @@ __device__ __forceinline__ void part2_level_bulk(const Inst& in, const int64_t o
       Table3<float> t3;
       lookup3<float>(mu_r, lamr, rt, t3);
       epsr = 2.0f * float(C::Pi) * cdistr * rho * v.dv *
-             (float(C::f1r) * float(rt.g_mur2) / lamr +
+             (float(C::f1r) * rt.f.g_mur2 / lamr +
               float(C::f2r) * m_sqrt(rho / v.mu) * m_cbrt(v.sc) * apply_table3<float>(tb, tb.revap, t3));
     }
     evaporate_rain_bulk(qr_in, qc_in, nr_in, qi_in, cl, cr, s.qv, in.qv_prev[o], qvsl, qvsi, v.ab, v.abi, epsr,
@@ -456,7 +456,7 @@ __device__ __forceinline__ void part2_level_bulk(const Inst& in, const int64_t o
   hydro |= clip_to_vapour(s, inv_exner);
   if (dge(s.ni, 1e-20)) {
     /* impose_max_total_ni as a factor applied only when it limits */
-    const float f = vmin(float(rt.max_total_ni) * inv_rho * ci / float(s.ni), 1.0f);
+    const float f = vmin(rt.f.max_total_ni * inv_rho * ci / float(s.ni), 1.0f);
     if (f < 1.0f) s.ni = s.ni * f2d(f);
   }
   in.qc[o] = s.qc; in.nc[o] = s.nc; in.qr[o] = s.qr; in.nr[o] = s.nr;
@@ -1330,7 +1330,7 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
             if (n2 != ni_plain) {
               set_state(1, k, f2d(n2) * f2d(cldf));
             }
-            const float f = float(rt.ice_sedimentation_factor) * FACf[k];
+            const float f = rt.f.ice_sedimentation_factor * FACf[k];
             v1 = f * tv[1];
             v2 = f * tv[0];
             fall = true;
@@ -1627,7 +1627,7 @@ __device__ void p3_part3(const Inst& in, const int col, const KParams<TR>& kp, c
           if (qm_f != qm0) s.qm = f2d(qm_f) * cld_i;
           if (bm_f != bm0) s.bm = f2d(bm_f) * cld_i;
           float ni_f = ni0;
-          impose_max_total_ni(ni_f, rt.max_total_ni, inv_rho_f);
+          impose_max_total_ni(ni_f, rt.f.max_total_ni, inv_rho_f);
           TableIce<float> ti;
           lookup_ice<float>(qi_f, ni_f, qm_f, rhop, ti);
           float ta[4], te[4];

@@ -66,7 +66,30 @@ struct RuntimeDev {
   double lg_mur7;     /* log Gamma(mu_r + 7)   */
   /* FP32-bulk saturation table (layout of build_svp_table) */
   const double* svp_tab;
+  /* accretion_qc_exponent == accretion_qr_exponent (the single-power form) */
+  int accretion_same_exponent;
+  /* float copies (rounded to nearest on the host) of the parameters the
+   * FP32-bulk rates read, so no kernel converts them */
+  struct F32 {
+    float max_total_ni, autoconversion_prefactor, autoconversion_qc_exponent, autoconversion_nc_exponent,
+        accretion_prefactor, accretion_qc_exponent, accretion_qr_exponent, rain_selfcollection_prefactor,
+        rain_selfcollection_breakup_diameter, constant_mu_rain, cldliq_to_ice_collection_factor,
+        rain_to_ice_collection_factor, min_rime_rho, max_rime_rho, immersion_freezing_exponent,
+        deposition_nucleation_exponent, ice_sedimentation_factor, cons3, t3_rdumjj, g_mur1, g_mur2, lg_mur4,
+        lg_mur7;
+  } f;
 };
+
+/* a runtime parameter in the rate type: the FP64 value, or its float copy */
+template <class TR>
+__device__ __forceinline__ TR rtp(double d, float f) {
+  if constexpr (sizeof(TR) == sizeof(float)) {
+    return f;
+  } else {
+    return d;
+  }
+}
+#define P3X_RTP(TR, name) rtp<TR>(rt.name, rt.f.name)
 
 /* ------------------------------------------------------------------ */
 /* math wrappers (explicit precision)                                  */
@@ -120,6 +143,23 @@ __device__ __forceinline__ double rcp_newton(double x) {
   r = fma(r, fma(-x, r, 1.0), r);
   r = fma(r, fma(-x, r, 1.0), r);
   return r;
+}
+
+/* Double -> float on the integer pipes, rounding toward zero.  The top 23
+ * significand bits are funnel-shifted under the re-biased exponent
+ * (exponent - 896, taken mod 2^9 in the 32-bit word); |x| below 2^-126
+ * becomes a signed zero, and |x| >= 2^128, infinities and NaN take the
+ * hardware conversion.  Truncation is monotone and exact on integers, so
+ * floor(d2f_rz(x)) = floor(x) for 0 <= x < 2^22: the saturation table's
+ * interval index uses it.  (As a general narrowing of state values it was
+ * slower than the hardware conversion, and its one-sided rounding biased the
+ * sedimentation's substep counts.) */
+__device__ __forceinline__ float d2f_rz(double x) {
+  const uint32_t hi = uint32_t(__double2hiint(x)), lo = uint32_t(__double2loint(x));
+  const uint32_t ahi = hi & 0x7fffffffu;
+  if (ahi >= 0x47f00000u) return float(x);
+  const uint32_t m = __funnelshift_l(lo, ahi, 3) - (896u << 23);
+  return __uint_as_float((ahi < 0x38100000u ? 0u : m) | (hi & 0x80000000u));
 }
 
 /* Float <-> small integer on the FP32 and integer pipes (the hardware
@@ -250,8 +290,10 @@ constexpr int kSvpIntervals = 12800;
 __device__ __forceinline__ double svp_tabulated(const double* tab, double t, bool ice, uint32_t& err) {
   const double x = fma(t, kSvpInvH, -kSvpT0 * kSvpInvH); /* = (t - T0) * 64, both exact here */
   if (!(!dneg(x) && dlt(x, double(kSvpIntervals)))) return murphy_koop_svp<double>(t, ice, err);
-  const int i = int(x);
-  const double u = x - double(i);
+  /* floor(x) through the truncated float (exact, see d2f_rz) and its exact
+   * double, off the FP64 pipe */
+  const int i = ffloor_small(d2f_rz(x));
+  const double u = x - f2d(i2f_small(i));
   const int row = (ice && dlt(t, C::Tmelt)) ? kSvpIntervals + i : i;
   const double2* c = reinterpret_cast<const double2*>(tab) + size_t(row) * 2;
   const double2 c01 = __ldg(c), c23 = __ldg(c + 1);
@@ -459,7 +501,7 @@ __device__ __forceinline__ void lookup3(TR mu_r, TR lamr, const RuntimeDev& rt, 
     tab.rdumii = rdumii;
     tab.dumii = dumii;
   }
-  tab.rdumjj = TR(rt.t3_rdumjj);
+  tab.rdumjj = P3X_RTP(TR, t3_rdumjj);
   tab.dumjj = rt.t3_dumjj;
 }
 
@@ -536,7 +578,7 @@ __device__ __forceinline__ void get_rain_dsd2(TR qr, TR& nr, TR& mu_r, TR& lamr,
   lamr = 0;
   if (qr >= TR(C::QSMALL)) {
     const TR nr_lim = vmax(nr, TR(C::NSMALL));
-    mu_r = TR(rt.constant_mu_rain);
+    mu_r = P3X_RTP(TR, constant_mu_rain);
     const TR f = TR(C::CONS1) * (mu_r + TR(3)) * (mu_r + TR(2)) * (mu_r + TR(1));
     lamr = m_cbrt(f * nr_lim / qr);
     const TR lammax = (mu_r + TR(1.)) * TR(1.e+5);
@@ -553,8 +595,8 @@ __device__ __forceinline__ void get_rain_dsd2(TR qr, TR& nr, TR& mu_r, TR& lamr,
 
 /* impose_max_total_ni, p3_impose_max_total_ni_impl.hpp:9-27 */
 template <class T>
-__device__ __forceinline__ void impose_max_total_ni(T& ni_local, double max_total_ni, T inv_rho_local) {
-  if (ni_local >= T(1e-20)) ni_local = ni_local * vmin(T(max_total_ni) * inv_rho_local / ni_local, T(1.));
+__device__ __forceinline__ void impose_max_total_ni(T& ni_local, T max_total_ni, T inv_rho_local) {
+  if (ni_local >= T(1e-20)) ni_local = ni_local * vmin(max_total_ni * inv_rho_local / ni_local, T(1.));
 }
 
 /* calc_bulk_rho_rime, p3/impl/p3_ice_sed_impl.hpp:14-64 */
@@ -564,10 +606,10 @@ __device__ __forceinline__ T calc_bulk_rho_rime(T qi_tot, T& qi_rim, T& bi_rim, 
   const bool gt = bi_rim >= T(C::BSMALL);
   const bool lt = bi_rim < T(C::BSMALL);
   if (gt) rho_rime = qi_rim / bi_rim;
-  const bool rr_lt_min = rho_rime < T(rt.min_rime_rho);
-  const bool rr_gt_max = rho_rime > T(rt.max_rime_rho);
-  if (gt && rr_lt_min) rho_rime = T(rt.min_rime_rho);
-  if (gt && rr_gt_max) rho_rime = T(rt.max_rime_rho);
+  const bool rr_lt_min = rho_rime < P3X_RTP(T, min_rime_rho);
+  const bool rr_gt_max = rho_rime > P3X_RTP(T, max_rime_rho);
+  if (gt && rr_lt_min) rho_rime = P3X_RTP(T, min_rime_rho);
+  if (gt && rr_gt_max) rho_rime = P3X_RTP(T, max_rime_rho);
   if (gt && (rr_gt_max || rr_lt_min)) bi_rim = qi_rim / rho_rime;
   if (lt) { qi_rim = 0; bi_rim = 0; rho_rime = 0; }
   if (qi_rim > qi_tot && rho_rime > T(0)) { qi_rim = qi_tot; bi_rim = qi_rim / rho_rime; }
@@ -631,7 +673,7 @@ __device__ __forceinline__ void ice_cldliq_collection(TR rho, double temp, TR rh
                                                       Rates<TR>& r, const RuntimeDev& rt) {
   const bool t_neg = dle(temp, C::Tmelt);
   const bool both = qi_incld >= TR(C::QSMALL) && qc_incld >= TR(C::QSMALL);
-  const TR f = TR(rt.cldliq_to_ice_collection_factor);
+  const TR f = P3X_RTP(TR, cldliq_to_ice_collection_factor);
   if (both && t_neg) r.qc2qi_collect_tend = rhofaci * tv * qc_incld * f * rho * ni_incld;
   if (both) r.nc_collect_tend = rhofaci * tv * nc_incld * f * rho * ni_incld;
   if (both && !t_neg) {
@@ -648,7 +690,7 @@ __device__ __forceinline__ void ice_rain_collection(TR rho, double temp, TR rhof
                                                     Rates<TR>& r, const RuntimeDev& rt) {
   const bool t_neg = dle(temp, C::Tmelt);
   const bool both = qi_incld >= TR(C::QSMALL) && qr_incld >= TR(C::QSMALL);
-  const TR f = TR(rt.rain_to_ice_collection_factor);
+  const TR f = P3X_RTP(TR, rain_to_ice_collection_factor);
   if (both && t_neg) {
     r.qr2qi_collect_tend = m_pow(TR(10.0), tv_qr + logn0r) * rho * rhofaci * f * ni_incld;
     r.nr_collect_tend = m_pow(TR(10.0), tv_nr + logn0r) * rho * rhofaci * f * ni_incld;
@@ -760,7 +802,7 @@ template <class TR>
 __device__ __forceinline__ void cldliq_immersion_freezing(TR T_atm, TR lamc, TR mu_c, TR nc_incld, TR qc_incld,
                                                           Rates<TR>& r, const RuntimeDev& rt) {
   if (qc_incld >= TR(C::QSMALL) && T_atm <= TR(C::T_rainfrz)) {
-    const TR expAimmDt = m_exp(TR(rt.immersion_freezing_exponent) * (TR(C::T_zerodegc) - T_atm));
+    const TR expAimmDt = m_exp(P3X_RTP(TR, immersion_freezing_exponent) * (TR(C::T_zerodegc) - T_atm));
     const TR inv_lamc = TR(1) / lamc;
     const TR inv_lamc3 = inv_lamc * inv_lamc * inv_lamc;
     const TR p3 = (TR(1) + mu_c) * (TR(2) + mu_c) * (TR(3) + mu_c);
@@ -780,14 +822,14 @@ template <class TR>
 __device__ __forceinline__ void rain_immersion_freezing(TR T_atm, TR lamr, TR mu_r, TR cdistr, TR qr_incld,
                                                         Rates<TR>& r, const RuntimeDev& rt) {
   if (qr_incld >= TR(C::QSMALL) && T_atm <= TR(C::T_rainfrz)) {
-    const TR e = m_exp(TR(rt.immersion_freezing_exponent) * (TR(C::T_zerodegc) - T_atm));
+    const TR e = m_exp(P3X_RTP(TR, immersion_freezing_exponent) * (TR(C::T_zerodegc) - T_atm));
     /* mu_r is the runtime constant here: log(Gamma(7+mu_r)) and
      * log(Gamma(4+mu_r)) are precomputed on the host */
     (void)mu_r;
     r.qr2qi_immers_freeze_tend =
-        TR(C::CONS6) * m_exp(m_log(cdistr) + TR(rt.lg_mur7) - TR(6.) * m_log(lamr)) * e;
+        TR(C::CONS6) * m_exp(m_log(cdistr) + P3X_RTP(TR, lg_mur7) - TR(6.) * m_log(lamr)) * e;
     r.nr2ni_immers_freeze_tend =
-        TR(C::CONS5) * m_exp(m_log(cdistr) + TR(rt.lg_mur4) - TR(3.) * m_log(lamr)) * e;
+        TR(C::CONS5) * m_exp(m_log(cdistr) + P3X_RTP(TR, lg_mur4) - TR(3.) * m_log(lamr)) * e;
   }
 }
 
@@ -800,7 +842,7 @@ __device__ __forceinline__ void ice_nucleation(TR temp, TR inv_rho, TR ni, TR ni
   const bool do_log = (!do_predict_nc || do_prescribed_CCN);
   const bool base = temp < TR(C::Tmelt - 15.0) && qv_supersat_i >= 0.05;
   if (base && do_log) {
-    TR dum = TR(0.005) * m_exp(TR(rt.deposition_nucleation_exponent) * (TR(C::Tmelt) - temp)) * TR(1.0e3) * inv_rho;
+    TR dum = TR(0.005) * m_exp(P3X_RTP(TR, deposition_nucleation_exponent) * (TR(C::Tmelt) - temp)) * TR(1.0e3) * inv_rho;
     dum = vmin(dum, TR(1.0e5) * inv_rho);
     const TR N_nuc = vmax(TR(0.), (dum - ni) * inv_dt);
     if (N_nuc >= TR(C::NSMALL)) {
@@ -819,9 +861,9 @@ template <class TR>
 __device__ __forceinline__ void cloud_water_autoconversion(TR rho, TR qc_incld, TR nc_incld, Rates<TR>& r,
                                                            const RuntimeDev& rt) {
   if (qc_incld >= TR(1e-8)) {
-    r.qc2qr_autoconv_tend = TR(rt.autoconversion_prefactor) * m_pow(qc_incld, TR(rt.autoconversion_qc_exponent)) *
-                            m_pow(nc_incld * TR(1.e-6) * rho, TR(-rt.autoconversion_nc_exponent));
-    r.ncautr = r.qc2qr_autoconv_tend * TR(rt.cons3);
+    r.qc2qr_autoconv_tend = P3X_RTP(TR, autoconversion_prefactor) * m_pow(qc_incld, P3X_RTP(TR, autoconversion_qc_exponent)) *
+                            m_pow(nc_incld * TR(1.e-6) * rho, (-P3X_RTP(TR, autoconversion_nc_exponent)));
+    r.ncautr = r.qc2qr_autoconv_tend * P3X_RTP(TR, cons3);
     r.nc2nr_autoconv_tend = r.qc2qr_autoconv_tend * nc_incld / qc_incld;
   }
   if (r.qc2qr_autoconv_tend == TR(0)) r.nc2nr_autoconv_tend = 0;
@@ -833,11 +875,11 @@ template <class TR>
 __device__ __forceinline__ void cloud_rain_accretion(TR qc_incld, TR nc_incld, TR qr_incld, Rates<TR>& r,
                                                      const RuntimeDev& rt) {
   if (qr_incld >= TR(C::QSMALL) && qc_incld >= TR(C::QSMALL)) {
-    if (rt.accretion_qc_exponent == rt.accretion_qr_exponent) {
-      r.qc2qr_accret_tend = TR(rt.accretion_prefactor) * m_pow(qc_incld * qr_incld, TR(rt.accretion_qr_exponent));
+    if (rt.accretion_same_exponent) {
+      r.qc2qr_accret_tend = P3X_RTP(TR, accretion_prefactor) * m_pow(qc_incld * qr_incld, P3X_RTP(TR, accretion_qr_exponent));
     } else {
-      r.qc2qr_accret_tend = TR(rt.accretion_prefactor) * m_pow(qc_incld, TR(rt.accretion_qc_exponent)) *
-                            m_pow(qr_incld, TR(rt.accretion_qr_exponent));
+      r.qc2qr_accret_tend = P3X_RTP(TR, accretion_prefactor) * m_pow(qc_incld, P3X_RTP(TR, accretion_qc_exponent)) *
+                            m_pow(qr_incld, P3X_RTP(TR, accretion_qr_exponent));
     }
     r.nc_accret_tend = r.qc2qr_accret_tend * nc_incld / qc_incld;
     if (r.nc_accret_tend == TR(0)) r.qc2qr_accret_tend = 0;
@@ -851,9 +893,9 @@ __device__ __forceinline__ void rain_self_collection(TR rho, TR qr_incld, TR nr_
                                                      const RuntimeDev& rt) {
   if (qr_incld >= TR(C::QSMALL)) {
     const TR dum2 = m_cbrt((qr_incld) / (TR(C::Pi) * TR(C::RHO_H2O) * nr_incld));
-    const TR dbr = TR(rt.rain_selfcollection_breakup_diameter);
+    const TR dbr = P3X_RTP(TR, rain_selfcollection_breakup_diameter);
     const TR dum = (dum2 < dbr) ? TR(1) : TR(2) - m_exp(TR(2300) * (dum2 - dbr));
-    r.nr_selfcollect_tend = dum * TR(rt.rain_selfcollection_prefactor) * nr_incld * qr_incld * rho;
+    r.nr_selfcollect_tend = dum * P3X_RTP(TR, rain_selfcollection_prefactor) * nr_incld * qr_incld * rho;
   }
 }
 

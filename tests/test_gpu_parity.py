@@ -323,7 +323,8 @@ def test_integer_float_to_double_conversion_is_exact(gpu_ctx):
     """The FP32-bulk form's float -> double conversion on the integer pipes
     agrees bitwise with the hardware conversion for every float bit pattern;
     its table indices on the FP32 pipe equal the hardware truncation after the
-    lookups' clamps for every float, and its small-integer floats are exact."""
+    lookups' clamps for every float, its small-integer floats are exact, and
+    its integer-pipe narrowing toward zero matches the hardware conversion."""
     from scream_gb300 import _lib as L
     n = C.c_uint64(123)
     assert gpu_ctx.lib.p3x_selftest(C.byref(n)) == 0
