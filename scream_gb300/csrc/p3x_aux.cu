@@ -181,7 +181,8 @@ cudaError_t launch_postamble(const dev::Inst* insts_d, const dev::WorkItem* work
  * hardware truncation after the callers' clamps ([1, hi - 1] and [1, hi]);
  * every integer below 2^22 in magnitude: its float on the FP32 pipe; 2^32
  * doubles covering every high word: the integer-pipe narrowing toward zero
- * against the hardware conversion. */
+ * against the hardware conversion; 2^24 hashed operand sets: the packed
+ * double-float accumulation against the scalar one. */
 __global__ void f2d_selftest_kernel(unsigned long long* mismatches) {
   unsigned long long bad = 0;
   const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
@@ -205,6 +206,23 @@ __global__ void f2d_selftest_kernel(unsigned long long* mismatches) {
                                         : (ay < 0x1p-126 ? (signbit(y) ? -0.0f : 0.0f) : __double2float_rz(y));
     const float got = dev::d2f_rz(y);
     if (__float_as_uint(got) != __float_as_uint(want) && !(isnan(got) && isnan(want))) ++bad;
+    /* the packed double-float accumulation against two scalar ones, on
+     * hashed operands spanning many magnitudes */
+    if ((i & 255u) == 0u) {
+      const uint32_t h1 = uint32_t(i) * 747796405u + 2891336453u, h2 = h1 * 277803737u + 1u;
+      const float s1 = __uint_as_float(0x30000000u + (h1 >> 4)), s2 = __uint_as_float(0x30000000u + (h2 >> 4));
+      const float lo1 = s1 * 1.0e-8f, lo2 = -s2 * 3.0e-8f;
+      const float a1 = __uint_as_float(0x34000000u + (h2 >> 5)), a2 = __uint_as_float(0x36000000u + (h1 >> 5));
+      const float tt = __uint_as_float(0x3f800000u + (h1 & 0x7fffffu)) * 37.0f;
+      float4 g = make_float4(s1, s2, lo1, lo2);
+      float2 g1 = make_float2(s1, lo1), g2 = make_float2(s2, lo2);
+      dev::dfloat2_add_prod(g, make_float2(a1, a2), tt);
+      dev::dfloat_add_prod(g1, a1, tt);
+      dev::dfloat_add_prod(g2, a2, tt);
+      if (__float_as_uint(g.x) != __float_as_uint(g1.x) || __float_as_uint(g.z) != __float_as_uint(g1.y) ||
+          __float_as_uint(g.y) != __float_as_uint(g2.x) || __float_as_uint(g.w) != __float_as_uint(g2.y))
+        ++bad;
+    }
   }
   if (bad) atomicAdd(mismatches, bad);
 }

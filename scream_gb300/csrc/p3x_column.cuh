@@ -1156,16 +1156,29 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
   double* const COEF = &SMA(1, 0); /* g / dpres */
   float* const INVDZf = reinterpret_cast<float*>(&SMA(2, 0));
   float* const COEFf = INVDZf + S;
-  float* const R2f = reinterpret_cast<float*>(&SMA(3, 0));
-  float* const R3f = R2f + S;
-  float* const V1f = reinterpret_cast<float*>(&SMA(4, 0));
-  float* const V2f = V1f + S;
-  float* const R0f = reinterpret_cast<float*>(&SMA(5, 0));
-  float* const R1f = R0f + S;
-  /* time-integrated face fluxes and the rain flux sum, as double-floats */
-  float2* const G[4] = {reinterpret_cast<float2*>(&SMA(6, 0)), reinterpret_cast<float2*>(&SMA(7, 0)),
-                        reinterpret_cast<float2*>(&SMA(8, 0)), reinterpret_cast<float2*>(&SMA(9, 0))};
-  float2* const PF = G[2]; /* rain flux accumulator (rain has two fields) */
+  /* Fields in pairs for the packed FP32 instructions: FP32 shadows of
+   * fields (0, 1) and (2, 3), the fall speeds (V1, V2), and the time-
+   * integrated face fluxes of fields (0, 1) and (2, 3) as double-floats
+   * {hi_a, hi_b, lo_a, lo_b} (two slots each). */
+  float2* const R23 = reinterpret_cast<float2*>(&SMA(3, 0));
+  float2* const V12 = reinterpret_cast<float2*>(&SMA(4, 0));
+  float2* const R01 = reinterpret_cast<float2*>(&SMA(5, 0));
+  float4* const G01 = reinterpret_cast<float4*>(&SMA(6, 0));
+  float4* const G23 = reinterpret_cast<float4*>(&SMA(8, 0));
+  float2* const PF = reinterpret_cast<float2*>(G23); /* rain flux sum (rain has two fields) */
+  /* the double-float G of field f at level k, as a double */
+  auto g_value = [&](int f, int k) -> double {
+    const float4 g = (f < 2 ? G01 : G23)[k];
+    return (f & 1) ? dfloat_value(make_float2(g.y, g.w)) : dfloat_value(make_float2(g.x, g.z));
+  };
+  auto r_set = [&](int f, int k, float v) {
+    float2& r = (f < 2 ? R01 : R23)[k];
+    if (f & 1) {
+      r.y = v;
+    } else {
+      r.x = v;
+    }
+  };
   for (int k = lane; k < nk; k += LANES) {
     const double coef = C::gravit * rcp_newton(in.dpres[co + k]);
     INVDZf[k] = 1.0f / float(in.dz[co + k]);
@@ -1186,29 +1199,24 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
     const float* const facp = scr_f(in, sfac, col);
     const int nfield = sp == 0 ? (predictNc ? 2 : 1) : (sp == 1 ? 2 : 4);
     const int nstate = sp == 2 ? 4 : 2; /* fields that limiters may rewrite */
-    float* const Rf[4] = {R0f, R1f, R2f, R3f};
     /* R_k := x now (k owned by this lane; G_{k-1} belongs to the lane above
      * and is final for this substep after the warp barrier) */
     auto set_state = [&](int f, int k, double x) {
-      const double gin = k > 0 ? dfloat_value(G[f][k - 1]) : 0.0;
-      Bf[f][co + k] = x - COEF[k] * (gin - dfloat_value(G[f][k]));
-      Rf[f][k] = float(x);
+      const double gin = k > 0 ? g_value(f, k - 1) : 0.0;
+      Bf[f][co + k] = x - COEF[k] * (gin - g_value(f, k));
+      r_set(f, k, float(x));
     };
 
     int my_top = 1 << 30, my_bot = -1;
     for (int k = lane; k < nk; k += LANES) {
       const double q = B0[co + k];
-      R0f[k] = float(q);
-      R1f[k] = float(B1[co + k]);
+      R01[k] = make_float2(float(q), float(B1[co + k]));
       CLDf[k] = float(cldp[co + k]);
       FACf[k] = facp[k];
-      G[0][k] = make_float2(0.f, 0.f);
-      G[1][k] = make_float2(0.f, 0.f);
+      G01[k] = make_float4(0.f, 0.f, 0.f, 0.f);
       if (sp == 2) {
-        R2f[k] = float(B2[co + k]);
-        R3f[k] = float(B3[co + k]);
-        G[2][k] = make_float2(0.f, 0.f);
-        G[3][k] = make_float2(0.f, 0.f);
+        R23[k] = make_float2(float(B2[co + k]), float(B3[co + k]));
+        G23[k] = make_float4(0.f, 0.f, 0.f, 0.f);
       }
       if (dge(q, C::QSMALL)) {
         my_top = min(my_top, k);
@@ -1245,8 +1253,9 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
         const float cldf = CLDf[k];
         const float icf = 1.0f / cldf;
         if (sp == 0) {
-          const float n_plain = R1f[k] * icf;
-          float qc_f = R0f[k] * icf, n_in = n_plain;
+          const float2 r01 = R01[k];
+          const float n_plain = r01.y * icf;
+          float qc_f = r01.x * icf, n_in = n_plain;
           if (first) {
             if (dge(B0[co + k], C::QSMALL)) {
               n_in = vmax(n_in, 0.0f);
@@ -1269,8 +1278,9 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
             fall = true;
           }
         } else if (sp == 1) {
-          const float n_plain = R1f[k] * icf;
-          float qr_f = R0f[k] * icf, n_in = n_plain;
+          const float2 r01 = R01[k];
+          const float n_plain = r01.y * icf;
+          float qr_f = r01.x * icf, n_in = n_plain;
           if (first) {
             if (dge(B0[co + k], C::QSMALL)) {
               n_in = vmax(n_in, 0.0f);
@@ -1294,8 +1304,9 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
             fall = true;
           }
         } else {
-          const float ni_plain = R1f[k] * icf, qm_plain = R2f[k] * icf, bm_plain = R3f[k] * icf;
-          float qi_f = R0f[k] * icf, ni_f = ni_plain, qm_f = qm_plain, bm_f = bm_plain;
+          const float2 r01 = R01[k], r23 = R23[k];
+          const float ni_plain = r01.y * icf, qm_plain = r23.x * icf, bm_plain = r23.y * icf;
+          float qi_f = r01.x * icf, ni_f = ni_plain, qm_f = qm_plain, bm_f = bm_plain;
           if (first) {
             if (dge(B0[co + k], C::QSMALL)) {
               ni_f = vmax(ni_f, 0.0f);
@@ -1304,7 +1315,7 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
               ni_f = 0;
             }
             if (dge(B0[co + k], C::QSMALL) && dge(B2[co + k], C::QSMALL)) {
-              bm_f = vmax(R3f[k] * (1.0f / float(in.cld_frac_l[co + k])), 0.0f);
+              bm_f = vmax(r23.y * (1.0f / float(in.cld_frac_l[co + k])), 0.0f);
             } else {
               qm_f = 0;
               bm_f = 0;
@@ -1336,13 +1347,11 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
             fall = true;
           }
         }
-        V1f[k] = v1;
-        V2f[k] = v2;
+        V12[k] = make_float2(v1, v2);
         if (fall) lmax = vmax(lmax, v1 * INVDZf[k]);
       }
       if (k_qxbot < kbot && lane == (k_qxbot + 1 - k_qxtop) % LANES) {
-        V1f[k_qxbot + 1] = 0; /* the cell receiving the leading edge has no fall speed */
-        V2f[k_qxbot + 1] = 0;
+        V12[k_qxbot + 1] = make_float2(0.f, 0.f); /* the cell receiving the leading edge has no fall speed */
       }
       const float Co_max = group_max<LANES>(mask, lmax) * dt_left;
       if (!(Co_max >= 0.0f) || Co_max > 2.0e9f) {
@@ -1353,53 +1362,47 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
       const float dt_sub = dt_left / float(tmpint1);
       const int k_temp = (k_qxbot == kbot) ? k_qxbot : k_qxbot + 1;
       /* FP32 fluxes from the shadows; double-float time-integrated face
-       * fluxes; the shadows follow with the FP32 flux divergence */
-      float cf0 = 0, cf1 = 0, cf2 = 0, cf3 = 0;
+       * fluxes; the shadows follow with the FP32 flux divergence.  Fields go
+       * in pairs through the packed FP32 instructions (same operations and
+       * rounding as the scalar form). */
+      float2 c01 = make_float2(0.f, 0.f), c23 = make_float2(0.f, 0.f);
       for (int base = k_qxtop; base <= k_temp; base += LANES) {
         const int k = base + lane;
         const bool act = k <= k_temp;
-        float f0 = 0, f1 = 0, f2 = 0, f3 = 0;
+        float2 f01 = make_float2(0.f, 0.f), f23 = make_float2(0.f, 0.f);
         if (act) {
-          const float rho = RHOf[k];
-          const float v1 = V1f[k];
-          f0 = v1 * R0f[k] * rho;
-          if (nfield > 1) f1 = V2f[k] * R1f[k] * rho;
-          if (nfield > 2) {
-            f2 = v1 * R2f[k] * rho;
-            f3 = v1 * R3f[k] * rho;
-          }
+          const float2 rho2 = f2splat(RHOf[k]);
+          const float2 v = V12[k];
+          f01 = __fmul2_rn(__fmul2_rn(v, R01[k]), rho2);
+          if (nfield < 2) f01.y = 0.f;
+          if (nfield > 2) f23 = __fmul2_rn(__fmul2_rn(f2splat(v.x), R23[k]), rho2);
         }
-        float uf0 = __shfl_up_sync(mask, f0, 1, LANES);
-        float uf1 = 0, uf2 = 0, uf3 = 0;
-        if (nfield > 1) uf1 = __shfl_up_sync(mask, f1, 1, LANES);
+        float2 u01, u23 = make_float2(0.f, 0.f);
+        u01.x = __shfl_up_sync(mask, f01.x, 1, LANES);
+        u01.y = nfield > 1 ? __shfl_up_sync(mask, f01.y, 1, LANES) : 0.f;
         if (nfield > 2) {
-          uf2 = __shfl_up_sync(mask, f2, 1, LANES);
-          uf3 = __shfl_up_sync(mask, f3, 1, LANES);
+          u23.x = __shfl_up_sync(mask, f23.x, 1, LANES);
+          u23.y = __shfl_up_sync(mask, f23.y, 1, LANES);
         }
         if (lane == 0) {
-          uf0 = cf0; uf1 = cf1; uf2 = cf2; uf3 = cf3;
+          u01 = c01;
+          u23 = c23;
         }
         if (act) {
-          const float coef_f = COEFf[k] * dt_sub;
-          dfloat_add_prod(G[0][k], f0, dt_sub);
-          R0f[k] += (uf0 - f0) * coef_f;
-          if (nfield > 1) {
-            dfloat_add_prod(G[1][k], f1, dt_sub);
-            R1f[k] += (uf1 - f1) * coef_f;
-          }
+          const float2 coef2 = f2splat(COEFf[k] * dt_sub);
+          dfloat2_add_prod(G01[k], f01, dt_sub);
+          R01[k] = __ffma2_rn(__fadd2_rn(u01, f2neg(f01)), coef2, R01[k]);
           if (nfield > 2) {
-            dfloat_add_prod(G[2][k], f2, dt_sub);
-            dfloat_add_prod(G[3][k], f3, dt_sub);
-            R2f[k] += (uf2 - f2) * coef_f;
-            R3f[k] += (uf3 - f3) * coef_f;
+            dfloat2_add_prod(G23[k], f23, dt_sub);
+            R23[k] = __ffma2_rn(__fadd2_rn(u23, f2neg(f23)), coef2, R23[k]);
           }
-          if (sp == 1) dfloat_add(PF[k + 1], f0);
+          if (sp == 1) dfloat_add(PF[k + 1], f01.x);
         }
-        cf0 = __shfl_sync(mask, f0, LANES - 1, LANES);
-        if (nfield > 1) cf1 = __shfl_sync(mask, f1, LANES - 1, LANES);
+        c01.x = __shfl_sync(mask, f01.x, LANES - 1, LANES);
+        c01.y = nfield > 1 ? __shfl_sync(mask, f01.y, LANES - 1, LANES) : 0.f;
         if (nfield > 2) {
-          cf2 = __shfl_sync(mask, f2, LANES - 1, LANES);
-          cf3 = __shfl_sync(mask, f3, LANES - 1, LANES);
+          c23.x = __shfl_sync(mask, f23.x, LANES - 1, LANES);
+          c23.y = __shfl_sync(mask, f23.y, LANES - 1, LANES);
         }
       }
       if (k_qxbot < kbot) k_qxbot += 1;
@@ -1411,7 +1414,7 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
     /* the bottom face's integral is what left the column: V is zero at the
      * leading edge, so G_kbot gains only in substeps where the species
      * reaches the surface */
-    const double prt_accum = dfloat_value(G[0][kbot]);
+    const double prt_accum = g_value(0, kbot);
     if (sp == 0) precip_liq_surf = prt_accum * C::INV_RHO_H2O * inv_dt;
     else if (sp == 1) precip_liq_surf += prt_accum * C::INV_RHO_H2O * inv_dt;
     else precip_ice_surf += prt_accum * C::INV_RHO_H2O * inv_dt;
@@ -1419,8 +1422,8 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
     /* FP64 state: R_k = B_k + (g / dpres_k) (G_{k-1} - G_k) */
     for (int k = lane; k < nk; k += LANES) {
       for (int f = 0; f < nstate; ++f) {
-        const double gin = k > 0 ? dfloat_value(G[f][k - 1]) : 0.0;
-        Bf[f][co + k] = Bf[f][co + k] + COEF[k] * (gin - dfloat_value(G[f][k]));
+        const double gin = k > 0 ? g_value(f, k - 1) : 0.0;
+        Bf[f][co + k] = Bf[f][co + k] + COEF[k] * (gin - g_value(f, k));
       }
     }
     if (sp == 1) {

@@ -259,6 +259,32 @@ __device__ __forceinline__ void dfloat_add_prod(float2& g, float a, float t) {
   g = dfloat_renorm(s, __fadd_rn(e, __fadd_rn(g.y, pl)));
 }
 
+/* Packed FP32 (Blackwell FFMA2/FADD2/FMUL2): two correctly rounded FP32
+ * operations per lane and instruction, each component exactly the scalar
+ * operation. */
+__device__ __forceinline__ float2 f2neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 f2splat(float a) { return make_float2(a, a); }
+/* a + w (b - a), as the scalar code evaluates it: fma(w, b - a, a) */
+__device__ __forceinline__ float2 lerp2(float2 a, float2 b, float2 w) {
+  return __ffma2_rn(w, __fadd2_rn(b, f2neg(a)), a);
+}
+
+/* Two double-floats side by side, g = {hi0, hi1, lo0, lo1}: g += a * t per
+ * component, with the same steps as dfloat_add_prod. */
+__device__ __forceinline__ void dfloat2_add_prod(float4& g, float2 a, float t) {
+  const float2 tt = f2splat(t);
+  const float2 hi = make_float2(g.x, g.y), lo = make_float2(g.z, g.w);
+  const float2 ph = __fmul2_rn(a, tt);
+  const float2 pl = __ffma2_rn(a, tt, f2neg(ph));
+  const float2 s = __fadd2_rn(hi, ph);
+  const float2 bb = __fadd2_rn(s, f2neg(hi));
+  const float2 e = __fadd2_rn(__fadd2_rn(hi, f2neg(__fadd2_rn(s, f2neg(bb)))), __fadd2_rn(ph, f2neg(bb)));
+  const float2 e2 = __fadd2_rn(e, __fadd2_rn(lo, pl));
+  const float2 nh = __fadd2_rn(s, e2);
+  const float2 nl = __fadd2_rn(e2, f2neg(__fadd2_rn(nh, f2neg(s))));
+  g = make_float4(nh.x, nh.y, nl.x, nl.y);
+}
+
 /* std::max / std::min semantics ((a < b) ? b : a), as the CPU reference. */
 template <class T> __device__ __forceinline__ T vmax(T a, T b) { return (a < b) ? b : a; }
 template <class T> __device__ __forceinline__ T vmin(T a, T b) { return (b < a) ? b : a; }
@@ -444,6 +470,33 @@ __device__ __forceinline__ void apply_table_ice4(const Tabs<TR>& t, const TableI
     const TR tmp2 = iproc1 + w4 * (gproc1 - iproc1);
     out[c] = tmp1 + w5 * (tmp2 - tmp1);
   }
+}
+
+/* The FP32 form of apply_table_ice4 on packed pairs of columns (s0..s0+1
+ * and s0+2..s0+3): the same interpolations in the same order. */
+template <>
+__device__ __forceinline__ void apply_table_ice4<float>(const Tabs<float>& t, const TableIce<float>& tab, int s0,
+                                                       float out[4]) {
+  const float w1 = tab.dum1 - ival<float>(tab.dumi) - 1.0f;
+  const float w4 = tab.dum4 - ival<float>(tab.dumii) - 1.0f;
+  const float w5 = tab.dum5 - ival<float>(tab.dumjj) - 1.0f;
+  const float2 W1 = f2splat(w1), W4 = f2splat(w4), W5 = f2splat(w5);
+  const float4 a00 = *reinterpret_cast<const float4*>(ice_row(t, tab.dumjj, tab.dumii, tab.dumi) + s0);
+  const float4 a01 = *reinterpret_cast<const float4*>(ice_row(t, tab.dumjj, tab.dumii, tab.dumi + 1) + s0);
+  const float4 a10 = *reinterpret_cast<const float4*>(ice_row(t, tab.dumjj, tab.dumii + 1, tab.dumi) + s0);
+  const float4 a11 = *reinterpret_cast<const float4*>(ice_row(t, tab.dumjj, tab.dumii + 1, tab.dumi + 1) + s0);
+  const float4 b00 = *reinterpret_cast<const float4*>(ice_row(t, tab.dumjj + 1, tab.dumii, tab.dumi) + s0);
+  const float4 b01 = *reinterpret_cast<const float4*>(ice_row(t, tab.dumjj + 1, tab.dumii, tab.dumi + 1) + s0);
+  const float4 b10 = *reinterpret_cast<const float4*>(ice_row(t, tab.dumjj + 1, tab.dumii + 1, tab.dumi) + s0);
+  const float4 b11 = *reinterpret_cast<const float4*>(ice_row(t, tab.dumjj + 1, tab.dumii + 1, tab.dumi + 1) + s0);
+  auto lo = [](float4 v) { return make_float2(v.x, v.y); };
+  auto hi = [](float4 v) { return make_float2(v.z, v.w); };
+  const float2 t1l = lerp2(lerp2(lo(a00), lo(a01), W1), lerp2(lo(a10), lo(a11), W1), W4);
+  const float2 t2l = lerp2(lerp2(lo(b00), lo(b01), W1), lerp2(lo(b10), lo(b11), W1), W4);
+  const float2 t1h = lerp2(lerp2(hi(a00), hi(a01), W1), lerp2(hi(a10), hi(a11), W1), W4);
+  const float2 t2h = lerp2(lerp2(hi(b00), hi(b01), W1), lerp2(hi(b10), hi(b11), W1), W4);
+  const float2 rl = lerp2(t1l, t2l, W5), rh = lerp2(t1h, t2h, W5);
+  out[0] = rl.x; out[1] = rl.y; out[2] = rh.x; out[3] = rh.y;
 }
 
 /* apply_table_coll, p3_table_ice_impl.hpp:214-297 */
