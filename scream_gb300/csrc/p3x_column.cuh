@@ -83,7 +83,7 @@ constexpr long long kWaitSpinLimit = 1ll << 26;
 constexpr uint64_t kWaitNanosLimit = 2000000000ull; /* 2 s */
 
 /* shared arrays of one column group in K1 */
-enum { A_TATM = 0, A_RHO, A_RHOFACR, A_RHOFACI, A_ACN, A_QVSL, A_QVSI, A_QVSSI, A_INVP, A_NARR };
+enum { A_TATM = 0, A_RHO, A_RHOFACR, A_RHOFACI, A_ACN, A_QVSL, A_QVSI, A_QVSSI, A_EPINVP, A_NARR };
 /* shared arrays of one column group in K2; FAC is the fall-speed factor of
  * the species being sedimented (acn, rhofacr or rhofaci), the rain flux
  * accumulator re-uses R2 (rain has two fields) */
@@ -285,7 +285,7 @@ __device__ __forceinline__ void part2_level_bulk(const Inst& in, const int64_t o
   const double cld_i = in.cld_frac_i[o], cld_l = in.cld_frac_l[o], cld_r = in.cld_frac_r[o];
   const double inv_exner = in.inv_exner[o];
   const double qvsl = sm[A_QVSL * S + k], qvsi = sm[A_QVSI * S + k];
-  const double inv_p = sm[A_INVP * S + k];
+  const double ep_inv_p = sm[A_EPINVP * S + k]; /* ep_2 / max(p, 1e-3) */
   const float rho = smf_rho[k], inv_rho = 1.0f / rho, rhofaci = smf_rhofaci[k], acn = smf_acn[k];
   const float T_r = float(T), qvsi_r = float(qvsi);
   const float cl = float(cld_l), ci = float(cld_i), cr = float(cld_r);
@@ -385,7 +385,7 @@ __device__ __forceinline__ void part2_level_bulk(const Inst& in, const int64_t o
       ni_in = vmax(ni_in, tv_lammin * ni_in);
     }
     const double dT0 = T - C::Tmelt;
-    const double dqv0 = C::ep_2 * esat0 * inv_p - s.qv;
+    const double dqv0 = esat0 * ep_inv_p - s.qv;
     if (do_ice) {
       ice_cldliq_collection<float>(rho, T, rhofaci, tv_qc2qi, qi_in, qc_in, ni_in, nc_in, r, rt);
       ice_rain_collection<float>(rho, T, rhofaci, logn0r, tv_nr, tv_qr2qi, qi_in, ni_in, qr_in, r, rt);
@@ -440,7 +440,7 @@ __device__ __forceinline__ void part2_level_bulk(const Inst& in, const int64_t o
   const int nlim = number_conservation<float>(nc0, nr0, ni0, dtf, r);
   const Rates<float> r_lim = r;
   ice_supersat_conservation_bulk(r, cld_i, s.qv, qvsi, qvsi_r, T_r, dtf);
-  prevent_liq_supersaturation_bulk(inv_p, T, s.qv, dtf, r, rt, err);
+  prevent_liq_supersaturation_bulk(ep_inv_p, T, s.qv, dtf, r, rt, err);
   update_prognostics_bulk(r, inv_exner, predictNc, prescribedCCN, wet, dtf, rho_qm_cloud, f2d(inv_rho), wlim, nlim,
                           r_lim, qi0, qm0, bm0, s);
 
@@ -515,7 +515,7 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
 
     double rho, inv_rho, qvsl, qvsi, qvssi, ccn_nc;
     TR rho_t, inv_rho_t;
-    const double exner = kF64 ? 1 / inv_exner : rcp_newton(inv_exner);
+    const double exner = kF64 ? 1 / inv_exner : rcp_newton1(inv_exner);
     double T = th * exner;
     qv = dmax0(qv);
     if constexpr (kF64) {
@@ -532,17 +532,19 @@ __device__ void p3_part12(const Inst& in, const int col, const KParams<TR>& kp, 
       /* FP32-bulk: rho and 1/rho only feed rates, fall speeds and fluxes
        * (the sedimentation's FP64 coefficient is g / dpres), so they are
        * FP32 and kept as floats in the shared slots and the hand-over; one
-       * FP64 division for the pressure shared by both saturation ratios; the
-       * supersaturation ratio (threshold and rate input) in FP32 */
+       * Newton reciprocal of the pressure, times ep_2, shared by both
+       * saturation ratios (and kept for part2's melting departure and
+       * supersaturation limiter); the supersaturation ratio (threshold and
+       * rate input) in FP32 */
       const float rho_f = float(dpres) / (float(dz) * float(C::gravit));
       rho_t = rho_f;
       rho = f2d(rho_f);
       inv_rho_t = 1.0f / rho_f;
       inv_rho = f2d(inv_rho_t);
-      const double inv_p = rcp_newton(dmax_c(pres, 1.e-3));
-      SMA(A_INVP, k) = inv_p;
-      qvsl = C::ep_2 * svp_tabulated(rt.svp_tab, T, false, err) * inv_p;
-      qvsi = C::ep_2 * svp_tabulated(rt.svp_tab, T, true, err) * inv_p;
+      const double ep_inv_p = C::ep_2 * rcp_newton1(dmax_c(pres, 1.e-3));
+      SMA(A_EPINVP, k) = ep_inv_p;
+      qvsl = svp_tabulated(rt.svp_tab, T, false, err) * ep_inv_p;
+      qvsi = svp_tabulated(rt.svp_tab, T, true, err) * ep_inv_p;
       qvssi = f2d(float(qv) / float(qvsi) - 1.0f);
       ccn_nc = rt.spa_ccn_to_nc_factor * in.nccn[o] * cld_l;
     }

@@ -144,6 +144,12 @@ __device__ __forceinline__ double rcp_newton(double x) {
   r = fma(r, fma(-x, r, 1.0), r);
   return r;
 }
+/* One step only: relative error ~2^-44 (~1e-14), used where that is below
+ * the other errors of the quantity (the saturation table's 1e-12). */
+__device__ __forceinline__ double rcp_newton1(double x) {
+  const double r = f2d(__fdividef(1.0f, float(x)));
+  return fma(r, fma(-x, r, 1.0), r);
+}
 
 /* Double -> float on the integer pipes, rounding toward zero.  The top 23
  * significand bits are funnel-shifted under the re-biased exponent
@@ -1284,7 +1290,7 @@ __device__ __forceinline__ void ice_supersat_conservation_bulk(Rates<float>& r, 
   }
 }
 
-__device__ __forceinline__ bool prevent_liq_supersaturation_bulk(double inv_p, double t_atm, double qv, float dtf,
+__device__ __forceinline__ bool prevent_liq_supersaturation_bulk(double ep_inv_p, double t_atm, double qv, float dtf,
                                                                  Rates<float>& r, const RuntimeDev& rt,
                                                                  uint32_t& err) {
   const float qv_sources = r.qi2qv_sublim_tend + r.qr2qv_evap_tend;
@@ -1292,7 +1298,7 @@ __device__ __forceinline__ bool prevent_liq_supersaturation_bulk(double inv_p, d
   const float qv_sinks = r.qv2qi_vapdep_tend + r.qv2qi_nucleat_tend;
   constexpr float lvs = float((C::LatVap + C::LatIce) * C::INV_CP), lv = float(C::LatVap * C::INV_CP);
   const double T_endstep = t_atm + f2d(((qv_sinks - r.qi2qv_sublim_tend) * lvs - r.qr2qv_evap_tend * lv) * dtf);
-  const double qsl = C::ep_2 * svp_tabulated(rt.svp_tab, T_endstep, false, err) * inv_p; /* inv_p = 1 / max(p, 1e-3) */
+  const double qsl = svp_tabulated(rt.svp_tab, T_endstep, false, err) * ep_inv_p; /* ep_2 / max(p, 1e-3) */
   const float te = float(T_endstep);
   const float A = float(C::LatVap * C::INV_CP / C::RV) * float(qsl) * dtf / (te * te) *
                   (float(C::LatVap + C::LatIce) * r.qi2qv_sublim_tend + float(C::LatVap) * r.qr2qv_evap_tend);
