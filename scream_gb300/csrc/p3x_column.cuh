@@ -137,6 +137,13 @@ __device__ __forceinline__ T group_max(unsigned mask, T v) {
   for (int o = LANES / 2; o > 0; o >>= 1) v = vmax(v, __shfl_xor_sync(mask, v, o, LANES));
   return v;
 }
+/* maximum over the group of non-negative doubles (dmax_nn) */
+template <int LANES>
+__device__ __forceinline__ double group_max_nn(unsigned mask, double v) {
+#pragma unroll
+  for (int o = LANES / 2; o > 0; o >>= 1) v = dmax_nn(v, __shfl_xor_sync(mask, v, o, LANES));
+  return v;
+}
 template <int LANES>
 __device__ __forceinline__ int group_min_int(unsigned mask, int v) {
 #pragma unroll
@@ -887,7 +894,7 @@ __device__ void p3_sed(const Inst& in, const int col, const KParams<TR>& kp, con
         R2[k] = in.qm[co + k];
         R3[k] = in.bm[co + k];
       }
-      if (q >= C::QSMALL) {
+      if (dge(q, C::QSMALL)) {
         my_top = min(my_top, k);
         my_bot = max(my_bot, k);
       }
@@ -905,7 +912,7 @@ __device__ void p3_sed(const Inst& in, const int col, const KParams<TR>& kp, con
     double dt_left = dt, prt_accum = 0.0;
     bool first = true;
     int nsub = 0;
-    while (dt_left > C::dt_left_tol) {
+    while (dgt(dt_left, C::dt_left_tol)) {
       if (++nsub > kMaxSubsteps) {
         err |= kErrSubstep;
         break;
@@ -919,19 +926,19 @@ __device__ void p3_sed(const Inst& in, const int col, const KParams<TR>& kp, con
           double qc_incld, nc_incld;
           if (first) {
             const double inv_cld = 1 / cld;
-            if (R0[k] >= C::QSMALL) {
+            if (dge(R0[k], C::QSMALL)) {
               qc_incld = R0[k] * inv_cld;
-              nc_incld = vmax(R1[k] * inv_cld, 0.);
+              nc_incld = dmax0(R1[k] * inv_cld);
             } else {
               qc_incld = 0;
               nc_incld = 0;
             }
-            qc_incld = vmin(qc_incld, C::incloud_limit);
+            qc_incld = dmin_c(qc_incld, C::incloud_limit);
           } else {
             qc_incld = R0[k] / cld;
             nc_incld = R1[k] / cld;
           }
-          if (qc_incld > C::QSMALL) {
+          if (dgt(qc_incld, C::QSMALL)) {
             TR mu_c, lamc;
             const TR n_in = TR(nc_incld);
             TR n_out = n_in;
@@ -944,25 +951,25 @@ __device__ void p3_sed(const Inst& in, const int col, const KParams<TR>& kp, con
             const TR acn = TR(FAC[k]);
             v1 = double(acn * ((TR(5) + mu_c) * (TR(4) + mu_c)) * dum);
             if (predictNc) v2 = double(acn * ((TR(2) + mu_c) * (TR(1) + mu_c)) * dum);
-            lmax = vmax(lmax, v1 * dt_left * INVDZ[k]);
+            lmax = dmax_nn(lmax, v1 * dt_left * INVDZ[k]);
           }
         } else if (sp == 1) {
           double qr_incld, nr_incld;
           if (first) {
             const double inv_cld = 1 / cld;
-            if (R0[k] >= C::QSMALL) {
+            if (dge(R0[k], C::QSMALL)) {
               qr_incld = R0[k] * inv_cld;
-              nr_incld = vmax(R1[k] * inv_cld, 0.);
+              nr_incld = dmax0(R1[k] * inv_cld);
             } else {
               qr_incld = 0;
               nr_incld = 0;
             }
-            qr_incld = vmin(qr_incld, C::precip_limit);
+            qr_incld = dmin_c(qr_incld, C::precip_limit);
           } else {
             qr_incld = R0[k] / cld;
             nr_incld = R1[k] / cld;
           }
-          if (qr_incld > C::QSMALL) {
+          if (dgt(qr_incld, C::QSMALL)) {
             TR mu_r = 0, lamr;
             const TR n_in = TR(nr_incld);
             TR n_out = n_in;
@@ -973,37 +980,37 @@ __device__ void p3_sed(const Inst& in, const int col, const KParams<TR>& kp, con
             v1 = double(apply_table3<TR>(tb, tb.vm, t3) * rhofacr);
             v2 = double(apply_table3<TR>(tb, tb.vn, t3) * rhofacr);
             R1[k] = double(n_out) * cld;
-            lmax = vmax(lmax, v1 * dt_left * INVDZ[k]);
+            lmax = dmax_nn(lmax, v1 * dt_left * INVDZ[k]);
           }
         } else {
           {
             double qi_incld, ni_incld, qm_incld, bm_incld;
             if (first) {
               const double inv_cld = 1 / cld;
-              if (R0[k] >= C::QSMALL) {
+              if (dge(R0[k], C::QSMALL)) {
                 qi_incld = R0[k] * inv_cld;
-                ni_incld = vmax(R1[k] * inv_cld, 0.);
+                ni_incld = dmax0(R1[k] * inv_cld);
               } else {
                 qi_incld = 0;
                 ni_incld = 0;
               }
-              if (R0[k] >= C::QSMALL && R2[k] >= C::QSMALL) {
+              if (dge(R0[k], C::QSMALL) && dge(R2[k], C::QSMALL)) {
                 qm_incld = R2[k] * inv_cld;
-                bm_incld = vmax(R3[k] * (1 / in.cld_frac_l[co + k]), 0.);
+                bm_incld = dmax0(R3[k] * (1 / in.cld_frac_l[co + k]));
               } else {
                 qm_incld = 0;
                 bm_incld = 0;
               }
-              qi_incld = vmin(qi_incld, C::incloud_limit);
-              bm_incld = vmin(bm_incld, C::incloud_limit);
+              qi_incld = dmin_c(qi_incld, C::incloud_limit);
+              bm_incld = dmin_c(bm_incld, C::incloud_limit);
             } else {
               qi_incld = R0[k] / cld;
               ni_incld = R1[k] / cld;
               qm_incld = R2[k] / cld;
               bm_incld = R3[k] / cld;
             }
-            if (qi_incld > C::QSMALL) {
-              ni_incld = vmax(ni_incld, C::NSMALL);
+            if (dgt(qi_incld, C::QSMALL)) {
+              ni_incld = dmax_c(ni_incld, C::NSMALL);
               const double rhop = calc_bulk_rho_rime(qi_incld, qm_incld, bm_incld, rt);
               R2[k] = qm_incld * cld;
               R3[k] = bm_incld * cld;
@@ -1017,7 +1024,7 @@ __device__ void p3_sed(const Inst& in, const int col, const KParams<TR>& kp, con
               const TR rhofaci = TR(FAC[k]);
               v1 = double(TR(rt.ice_sedimentation_factor) * tv[1] * rhofaci);
               v2 = double(TR(rt.ice_sedimentation_factor) * tv[0] * rhofaci);
-              lmax = vmax(lmax, v1 * dt_left * INVDZ[k]);
+              lmax = dmax_nn(lmax, v1 * dt_left * INVDZ[k]);
             }
           }
         }
@@ -1028,7 +1035,7 @@ __device__ void p3_sed(const Inst& in, const int col, const KParams<TR>& kp, con
         V1[k_qxbot + 1] = 0; /* the cell receiving the leading edge has no fall speed */
         V2[k_qxbot + 1] = 0;
       }
-      const double Co_max = group_max<LANES>(mask, lmax);
+      const double Co_max = group_max_nn<LANES>(mask, lmax);
       if (!(Co_max >= 0) || Co_max > 2.0e9) {
         err |= kErrNumeric;
         break;

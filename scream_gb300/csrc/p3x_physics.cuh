@@ -225,6 +225,10 @@ __device__ __forceinline__ double dmax_c(double x, double c) { return dlt(x, c) 
 __device__ __forceinline__ double dmin_c(double x, double c) { return dgt(x, c) ? c : x; }
 /* x > 0 */
 __device__ __forceinline__ bool dpos(double x) { return dbits(x) > 0; }
+/* vmax(a, b) = (a < b) ? b : a for non-negative a and b (Courant numbers): the
+ * bit patterns order as the values; a NaN b propagates (it would be dropped by
+ * the IEEE form) and is then caught by the Courant check */
+__device__ __forceinline__ double dmax_nn(double a, double b) { return dbits(a) < dbits(b) ? b : a; }
 /* x is not +0 (adding or subtracting it may change a value) */
 __device__ __forceinline__ bool dnz(double x) { return dbits(x) != 0; }
 /* vmax(x, 0.) = (x < 0) ? 0 : x, and vmax(0., x) = (0 < x) ? x : 0 (+0 for -0) */
