@@ -190,7 +190,8 @@ int p3x_main(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_state
  * and the history fields.  Synchronous: returns when the host arrays hold
  * the results; *elapsed_us (may be NULL) receives the time from the first
  * upload to the last download.  Results are bitwise those of p3x_main on the
- * same data.  The reference's host drivers pass host views to p3_main
+ * same data.  Calls on one context are serialised (they share its chunk
+ * buffers); calls on different contexts run concurrently.  The reference's host drivers pass host views to p3_main
  * through its own deep copies; this entry is that path without them. */
 int p3x_main_host(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_state* prog,
                   const p3x_diagnostic_inputs* din, const p3x_diagnostic_outputs* dout,

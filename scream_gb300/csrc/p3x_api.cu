@@ -48,6 +48,7 @@ struct p3x_context {
   cudaStream_t hstream[kHostRing] = {nullptr, nullptr, nullptr};
   double* hbuf[kHostRing] = {nullptr, nullptr, nullptr};
   size_t hbuf_bytes = 0;
+  std::mutex hmu; /* one host-entry call at a time per context (the ring is shared) */
 };
 
 namespace p3x {
@@ -684,6 +685,7 @@ int p3x_main_host(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_
     if (elapsed_us) *elapsed_us = 0;
     return P3X_OK;
   }
+  std::lock_guard<std::mutex> lock(ctx->hmu);
   /* chunks: a sixteenth of the columns (at least 8192, and all of them when
    * fewer), so that three chunks in flight overlap upload, kernels and
    * download.  At 345,600 x 128 on GB300 the step is then bound by the
