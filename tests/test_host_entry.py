@@ -48,3 +48,35 @@ def test_host_entry_arguments(gpu_ctx):
     assert e.value.code == L.P3X_EINVAL
     empty = p3.P3Fields.allocate_host(0, 16)
     assert gpu_ctx.p3_main_host(empty, 300.0, 1) == 0.0
+
+
+def test_host_entry_concurrent_calls_on_one_context(gpu_ctx):
+    """Two threads stepping different host arrays through one context (the
+    calls are serialised on its chunk buffers) each get the device entry's
+    result."""
+    import threading
+    import scream_gb300 as p3
+    ins = [p3.generate_inputs(1, 900 + s, 700, 72) for s in range(2)]
+    hosts = [_host_fields(i) for i in ins]
+    errors = []
+
+    def work(h):
+        try:
+            for it in (1, 2):
+                gpu_ctx.p3_main_host(h, 300.0, 1, it=it, chunk_cols=128)
+        except Exception as e:  # reported below
+            errors.append(e)
+
+    threads = [threading.Thread(target=work, args=(h,)) for h in hosts]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    assert not errors, errors
+    for inp, h in zip(ins, hosts):
+        dev = p3.P3Fields.from_inputs(inp)
+        for it in (1, 2):
+            gpu_ctx.p3_main(dev, 300.0, 1, it=it)
+        a = dev.to_host()
+        for name, v in h.t.items():
+            assert np.array_equal(a[name], v.numpy()), name
