@@ -80,3 +80,20 @@ def test_host_entry_concurrent_calls_on_one_context(gpu_ctx):
         a = dev.to_host()
         for name, v in h.t.items():
             assert np.array_equal(a[name], v.numpy()), name
+
+
+def test_host_entry_pageable_arrays(gpu_ctx):
+    """Pageable (not page-locked) host arrays give the same result."""
+    import torch
+    import scream_gb300 as p3
+    from scream_gb300 import _lib as L
+    inputs = p3.generate_inputs(1, 77, 600, 72)
+    dev = p3.P3Fields.from_inputs(inputs)
+    host = p3.P3Fields.allocate_host(600, 72, pinned=False)
+    for n in L.INPUT_FIELDS:
+        host.t[n].copy_(torch.from_numpy(np.ascontiguousarray(inputs[n])))
+    gpu_ctx.p3_main(dev, 300.0, 1)
+    gpu_ctx.p3_main_host(host, 300.0, 1, chunk_cols=200)
+    a = dev.to_host()
+    for name, v in host.t.items():
+        assert np.array_equal(a[name], v.numpy()), name
