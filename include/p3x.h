@@ -200,7 +200,7 @@ int p3x_main_host(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_
 
 /* Same, stream-ordered and asynchronous: no host synchronisation.  The
  * per-step hand-over scratch between the three kernels (40 B per
- * column-level + 4 B per column) is taken from and returned to the
+ * column-level + 4 B per column + 16 B of work counters) is taken from and returned to the
  * context's stream-ordered memory pool on `stream`, so concurrent calls on
  * different streams do not share scratch.  Device-side error bits accumulate
  * in the context; read them with p3x_context_check. */
@@ -215,7 +215,7 @@ int p3x_main_async(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic
  * hosts that reserve the device's memory for themselves at start-up and
  * cannot let a library allocate during their time loop.  No counterpart in
  * the reference.
- *   - Limit: 40 * ncol * ld + 4 * ncol bytes (rounded up to 256) must fit in
+ *   - Limit: 40 * ncol * ld + 4 * ncol + 16 bytes (rounded up) must fit in
  *     64 MiB, e.g. 13,000 columns of 128 levels; larger calls return
  *     P3X_ENOMEM and launch nothing.
  *   - The array is one per device and shared by every context: calls that
@@ -224,7 +224,8 @@ int p3x_main_async(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic
  *   - The first call on each device looks the array's address up
  *     (cudaGetSymbolAddress, once per device with that device current); make
  *     that first call before any stream capture begins.
- *   - Nothing in the array has to be zeroed. */
+ *   - Nothing in the array has to be zeroed (the step zeroes its work
+ *     counters on the stream). */
 int p3x_main_fixed_scratch(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_state* prog,
                            const p3x_diagnostic_inputs* din, const p3x_diagnostic_outputs* dout,
                            const p3x_infrastructure* infra, const p3x_history_only* hist, int32_t nj,

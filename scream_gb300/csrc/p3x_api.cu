@@ -286,6 +286,11 @@ void bind_scratch(dev::Inst& in, unsigned char* base) {
                                         sizeof(double));
 }
 
+uint32_t* work_counters(const dev::Inst& in) {
+  return reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(in.scr) +
+                                     dev::work_counter_offset(in.ncol, in.ld));
+}
+
 int launch_kernels(p3x_context* ctx, const p3x_runtime* rt, const dev::Inst& in, cudaStream_t st,
                    bool marks = true) {
   const dev::RuntimeDev rtd = make_runtime(*rt);
@@ -300,6 +305,7 @@ int launch_kernels(p3x_context* ctx, const p3x_runtime* rt, const dev::Inst& in,
     kp.nwork = in.ncol;
     kp.work = nullptr;
     kp.insts = nullptr;
+    kp.wctr = work_counters(in);
     e = launch_p3<float>(in, kp, ls, ctx->num_sms, st);
   } else {
     dev::KParams<double> kp = make_kparams<double>(ctx, rtd);
@@ -307,6 +313,7 @@ int launch_kernels(p3x_context* ctx, const p3x_runtime* rt, const dev::Inst& in,
     kp.nwork = in.ncol;
     kp.work = nullptr;
     kp.insts = nullptr;
+    kp.wctr = work_counters(in);
     e = launch_p3<double>(in, kp, ls, ctx->num_sms, st);
   }
   return cuda_status(e);
@@ -965,6 +972,7 @@ struct p3x_batch {
   dev::RuntimeDev rtd{};
   dev::Inst* insts_d = nullptr;
   void* scratch = nullptr; /* every instance's K1->K2/K3 scratch */
+  uint32_t* ctr_d = nullptr; /* work counters, kWorkCounters per group */
   struct Group {
     int precision = 0;
     dev::WorkItem* work_d = nullptr;
@@ -981,7 +989,7 @@ namespace p3x {
 namespace {
 template <class TR>
 int launch_work_t(p3x_context* ctx, const dev::RuntimeDev& rtd, const LaunchSpec& ls0, const dev::Inst* insts_d,
-                  const dev::WorkItem* work_d, int nwork, int nlev_max, cudaStream_t st) {
+                  const dev::WorkItem* work_d, int nwork, int nlev_max, uint32_t* wctr, cudaStream_t st) {
   if (nwork == 0) return P3X_OK;
   const int stride = sm_stride_for(nlev_max);
   const int prec = sizeof(TR) == sizeof(double) ? P3X_FP64 : P3X_FP32_BULK;
@@ -992,6 +1000,7 @@ int launch_work_t(p3x_context* ctx, const dev::RuntimeDev& rtd, const LaunchSpec
   kp.nwork = nwork;
   kp.work = work_d;
   kp.insts = insts_d;
+  kp.wctr = wctr;
   dev::Inst dummy{};
   return cuda_status(launch_p3<TR>(dummy, kp, ls, ctx->num_sms, st));
 }
@@ -999,9 +1008,11 @@ int launch_work_t(p3x_context* ctx, const dev::RuntimeDev& rtd, const LaunchSpec
 int batch_launch(p3x_batch* b, cudaStream_t st) {
   for (int g = 0; g < b->ngroups; ++g) {
     auto& G = b->groups[g];
-    const int rc = G.precision == P3X_FP32_BULK
-                       ? launch_work_t<float>(b->ctx, b->rtd, G.ls, b->insts_d, G.work_d, G.nwork, G.nlev_max, st)
-                       : launch_work_t<double>(b->ctx, b->rtd, G.ls, b->insts_d, G.work_d, G.nwork, G.nlev_max, st);
+    uint32_t* ctr = b->ctr_d + size_t(g) * dev::kWorkCounters;
+    const int rc =
+        G.precision == P3X_FP32_BULK
+            ? launch_work_t<float>(b->ctx, b->rtd, G.ls, b->insts_d, G.work_d, G.nwork, G.nlev_max, ctr, st)
+            : launch_work_t<double>(b->ctx, b->rtd, G.ls, b->insts_d, G.work_d, G.nwork, G.nlev_max, ctr, st);
     if (rc) return rc;
   }
   return P3X_OK;
@@ -1015,12 +1026,13 @@ void drop_graph(p3x_batch* b) {
 }  // namespace
 
 int launch_work(p3x_context* ctx, const p3x_runtime& rt, int precision, const dev::Inst* insts_d,
-                const dev::WorkItem* work_d, int nwork, int nlev_max, cudaStream_t st) {
+                const dev::WorkItem* work_d, int nwork, int nlev_max, uint32_t* wctr, cudaStream_t st) {
   if (!ctx || (precision != P3X_FP64 && precision != P3X_FP32_BULK)) return P3X_EINVAL;
   const dev::RuntimeDev rtd = make_runtime(rt);
   const LaunchSpec ls = spec_of(ctx->cfg[precision]);
-  return precision == P3X_FP32_BULK ? launch_work_t<float>(ctx, rtd, ls, insts_d, work_d, nwork, nlev_max, st)
-                                    : launch_work_t<double>(ctx, rtd, ls, insts_d, work_d, nwork, nlev_max, st);
+  return precision == P3X_FP32_BULK
+             ? launch_work_t<float>(ctx, rtd, ls, insts_d, work_d, nwork, nlev_max, wctr, st)
+             : launch_work_t<double>(ctx, rtd, ls, insts_d, work_d, nwork, nlev_max, wctr, st);
 }
 
 }  // namespace p3x
@@ -1044,6 +1056,7 @@ int p3x_batch_create(p3x_context* ctx, const p3x_runtime* rt, const p3x_instance
   size_t scr_total = 0;
   for (int i = 0; i < n; ++i) scr_total += dev::scratch_bytes(insts[i].ncol, insts[i].ld);
   if (scr_total) P3X_CUDA(cudaMalloc(&b->scratch, scr_total));
+  P3X_CUDA(cudaMalloc(&b->ctr_d, 2 * dev::kWorkCounters * sizeof(uint32_t)));
   {
     size_t off = 0;
     for (int i = 0; i < n; ++i) {
@@ -1123,6 +1136,7 @@ int p3x_batch_destroy(p3x_batch* b) {
   drop_graph(b);
   if (b->insts_d) cudaFree(b->insts_d);
   if (b->scratch) cudaFree(b->scratch);
+  if (b->ctr_d) cudaFree(b->ctr_d);
   for (int g = 0; g < b->ngroups; ++g)
     if (b->groups[g].work_d) cudaFree(b->groups[g].work_d);
   delete b;
@@ -1194,11 +1208,12 @@ int p3x_autotune_batch(p3x_batch* b, void* stream, int32_t reps, p3x_launch_conf
  * start-up, or one that must keep a fixed, audited device footprint for a
  * whole simulation, has no memory to give and no way to account for a pool
  * that grows behind its back.  For them the three kernels' hand-over scratch
- * (40 bytes per column-level plus 4 bytes per column) lives in one array of
- * static device storage, reserved when the library's module is loaded.
- * Nothing in the array needs to start at zero: part1+part2 writes every
- * column's continue flag, and the hand-over values of every column that
- * goes on, before sedimentation and part3 read them. */
+ * (40 bytes per column-level, 4 bytes per column and 16 bytes of work
+ * counters) lives in one array of static device storage, reserved when the
+ * library's module is loaded.  Nothing in the array needs to start at zero:
+ * the step zeroes its work counters on the stream, and part1+part2 writes
+ * every column's continue flag, and the hand-over values of every column
+ * that goes on, before sedimentation and part3 read them. */
 static __device__ __align__(256) unsigned char g_step_scratch[p3x::kFixedScratchBytes];
 
 namespace p3x {

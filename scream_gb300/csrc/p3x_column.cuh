@@ -74,6 +74,9 @@ struct KParams {
   const WorkItem* work;
   const Inst* insts;
   uint32_t* err;
+  /* kWorkCounters zeroed counters: groups take work items from them as they
+   * finish the last ones.  Null: groups stride the list statically. */
+  uint32_t* wctr;
 };
 
 constexpr int kIceTableElems = kDensize * kRimsize * kIsize * kIceCols; /* 12000 */
@@ -107,10 +110,17 @@ __device__ __forceinline__ float* scr_f(const Inst& in, int f, int col) {
   return reinterpret_cast<float*>(scr_at(in, f, col));
 }
 
-/* bytes of the K1->K2/K3 scratch of an instance (doubles, then the flags) */
-__host__ __device__ inline size_t scratch_bytes(int ncol, int64_t ld) {
+/* Launch-wide work counters of one step (K1, K2, K3, spare), zeroed on the
+ * stream before K1.  They follow the hand-over doubles and the flags in an
+ * instance's scratch. */
+constexpr int kWorkCounters = 4;
+__host__ __device__ inline size_t work_counter_offset(int ncol, int64_t ld) {
   const size_t d = size_t(kScrFields) * size_t(ncol) * size_t(ld) * sizeof(double);
-  return ((d + size_t(ncol) * sizeof(int32_t) + 255) / 256) * 256;
+  return ((d + size_t(ncol) * sizeof(int32_t) + 15) / 16) * 16;
+}
+/* bytes of the K1->K2/K3 scratch of an instance (doubles, flags, counters) */
+__host__ __device__ inline size_t scratch_bytes(int ncol, int64_t ld) {
+  return ((work_counter_offset(ncol, ld) + kWorkCounters * sizeof(uint32_t) + 255) / 256) * 256;
 }
 
 template <class TR>
@@ -1709,6 +1719,34 @@ __device__ __forceinline__ unsigned char* setup_tables(const KParams<TR>& kp, bo
   return smem_raw;
 }
 
+/* Runs f(w) for the work items of this column group.  With a counter, a warp
+ * takes the next 32/LANES items whenever it has finished its last ones, so a
+ * warp that drew cheap columns takes more of them and no SM idles behind the
+ * slowest column list (a static stride gives every warp a fixed share, and an
+ * even stride gives it columns of one parity only).  Without one, groups
+ * stride the list. */
+template <int LANES, class F>
+__device__ __forceinline__ void for_each_work(uint32_t* ctr, int nwork, int groups_per_block, F&& f) {
+  if (ctr) {
+    const int lane = threadIdx.x & 31;
+    const int nthr = min(32, int(blockDim.x) - int(threadIdx.x & ~31u));
+    const unsigned wmask = nthr == 32 ? 0xffffffffu : ((1u << nthr) - 1u);
+    const uint32_t per_warp = uint32_t(nthr / LANES);
+    const uint32_t g_in_warp = uint32_t(lane / LANES);
+    for (;;) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(ctr, per_warp);
+      base = __shfl_sync(wmask, base, 0);
+      if (base >= uint32_t(nwork)) break;
+      const uint32_t w = base + g_in_warp;
+      if (w < uint32_t(nwork)) f(int(w));
+    }
+  } else {
+    const int groups_total = gridDim.x * groups_per_block;
+    for (int w = blockIdx.x * groups_per_block + int(threadIdx.x) / LANES; w < nwork; w += groups_total) f(w);
+  }
+}
+
 /* Column of work item w (single instance or batched work list). */
 template <class TR>
 __device__ __forceinline__ const Inst& work_inst(const Inst& inst0, const KParams<TR>& kp, int w, int& col) {
@@ -1740,12 +1778,11 @@ __global__ void __launch_bounds__(256, sizeof(TR) == sizeof(float) ? 2 : 1)
   /* liquid saturation vapour pressure at 0 C (qsat0 of ice_melting and
    * ice_cldliq_wet_growth), evaluated once */
   const double esat0 = murphy_koop_svp<double>(C::Tmelt, false, err);
-  const int groups_total = gridDim.x * kp.groups_per_block;
-  for (int w = blockIdx.x * kp.groups_per_block + g_in_block; w < kp.nwork; w += groups_total) {
+  for_each_work<LANES>(kp.wctr ? kp.wctr + 0 : nullptr, kp.nwork, kp.groups_per_block, [&](int w) {
     int col;
     const Inst& in = work_inst(inst0, kp, w, col);
     p3_part12<TR, LANES>(in, col, kp, tb, sm, esat0, err);
-  }
+  });
   if (err) atomicOr(kp.err, err);
 }
 
@@ -1758,12 +1795,11 @@ __global__ void __launch_bounds__(256) p3_sed_kernel(const Inst inst0, const KPa
   setup_tables<TR>(kp, false, smem_raw, tb, err);
   const int g_in_block = threadIdx.x / LANES;
   double* sm = reinterpret_cast<double*>(smem_raw) + size_t(g_in_block) * sed_slots<TR>() * kp.sm_stride;
-  const int groups_total = gridDim.x * kp.groups_per_block;
-  for (int w = blockIdx.x * kp.groups_per_block + g_in_block; w < kp.nwork; w += groups_total) {
+  for_each_work<LANES>(kp.wctr ? kp.wctr + 1 : nullptr, kp.nwork, kp.groups_per_block, [&](int w) {
     int col;
     const Inst& in = work_inst(inst0, kp, w, col);
     p3_sed<TR, LANES>(in, col, kp, tb, sm, err);
-  }
+  });
   if (err) atomicOr(kp.err, err);
 }
 
@@ -1779,12 +1815,11 @@ __global__ void __maxnreg__(96) p3_sed_bulk_kernel(const Inst inst0, const KPara
   setup_tables<float>(kp, false, smem_raw, tb, err);
   const int g_in_block = threadIdx.x / LANES;
   double* sm = reinterpret_cast<double*>(smem_raw) + size_t(g_in_block) * kSedBulkSlots * kp.sm_stride;
-  const int groups_total = gridDim.x * kp.groups_per_block;
-  for (int w = blockIdx.x * kp.groups_per_block + g_in_block; w < kp.nwork; w += groups_total) {
+  for_each_work<LANES>(kp.wctr ? kp.wctr + 1 : nullptr, kp.nwork, kp.groups_per_block, [&](int w) {
     int col;
     const Inst& in = work_inst(inst0, kp, w, col);
     p3_sed_bulk<LANES>(in, col, kp, tb, sm, err);
-  }
+  });
   if (err) atomicOr(kp.err, err);
 }
 
@@ -1794,13 +1829,11 @@ __global__ void __launch_bounds__(256) p3_part3_kernel(const Inst inst0, const K
   uint32_t err = 0;
   Tabs<TR> tb;
   setup_tables<TR>(kp, false, smem_raw, tb, err);
-  const int g_in_block = threadIdx.x / LANES;
-  const int groups_total = gridDim.x * kp.groups_per_block;
-  for (int w = blockIdx.x * kp.groups_per_block + g_in_block; w < kp.nwork; w += groups_total) {
+  for_each_work<LANES>(kp.wctr ? kp.wctr + 2 : nullptr, kp.nwork, kp.groups_per_block, [&](int w) {
     int col;
     const Inst& in = work_inst(inst0, kp, w, col);
     p3_part3<TR, LANES>(in, col, kp, tb);
-  }
+  });
 }
 
 }  // namespace dev

@@ -34,6 +34,10 @@ cudaError_t launch_p3_lanes(const dev::Inst& inst0, const dev::KParams<TR>& kp_i
   kp.staged = ls.staged;
   const int threads = ls.groups_per_block * LANES;
   if (threads <= 0 || threads > 256) return cudaErrorInvalidValue;
+  if (kp.wctr) {
+    const cudaError_t z = cudaMemsetAsync(kp.wctr, 0, dev::kWorkCounters * sizeof(uint32_t), stream);
+    if (z != cudaSuccess) return z;
+  }
   if (ls.marks) cudaEventRecord(ls.marks[0], stream);
   cudaError_t e = launch_persistent<TR>(dev::p3_part12_kernel<TR, LANES>, inst0, kp, threads,
                                         p3_smem_bytes<TR>(ls, kp.sm_stride), ls.blocks_per_sm, num_sms, stream);

@@ -60,9 +60,10 @@ cudaError_t launch_transpose_to_columns(const double* src, double* dst, int ncol
 /* One step of a work list of (instance, column) items whose instances all
  * have the given precision: K1, K2, K3 with the context's launch
  * configuration for that precision (p3x_api.cu).  Every instance's scratch
- * must be bound. */
+ * must be bound.  wctr: dev::kWorkCounters device words used by no other
+ * launch in flight (zeroed on the stream), or null for a static stride. */
 int launch_work(p3x_context* ctx, const p3x_runtime& rt, int precision, const dev::Inst* insts_d,
-                const dev::WorkItem* work_d, int nwork, int nlev_max, cudaStream_t st);
+                const dev::WorkItem* work_d, int nwork, int nlev_max, uint32_t* wctr, cudaStream_t st);
 
 /* The state hand-over of the P3 process interface between steps
  * (eamxx_p3_process_interface.hpp:218,237 with dry = wet mixing ratios):
