@@ -86,7 +86,6 @@ struct Slot {
   WorkItem* h_work = nullptr;
   Inst* d_insts = nullptr;
   WorkItem* d_work = nullptr;
-  uint32_t* d_ctr = nullptr; /* this slot's work counters */
   int cap_insts = 0, cap_work = 0;
 };
 
@@ -326,7 +325,12 @@ int dispatch(p3x_server* s, Slot& sl) {
   }
   SRV_CUDA(cudaMemcpyAsync(sl.d_insts, sl.h_insts, sizeof(Inst) * take.size(), cudaMemcpyHostToDevice, sl.st));
   SRV_CUDA(cudaMemcpyAsync(sl.d_work, sl.h_work, sizeof(WorkItem) * w, cudaMemcpyHostToDevice, sl.st));
-  rc = p3x::launch_work(s->ctx, s->rt, prec, sl.d_insts, sl.d_work, w, nlev_max, sl.d_ctr, sl.st);
+  /* Static stride, no work counters: a launch that hands out work from a
+   * counter keeps every CTA resident until its whole list is done, so the
+   * other slots' launches find no free SM until then (measured at 80 % load:
+   * p50 1.4 -> 1.75 ms, p90 30 -> 47 ms for 2.5 % more capacity).  With a
+   * static stride CTAs retire one by one and the slots interleave. */
+  rc = p3x::launch_work(s->ctx, s->rt, prec, sl.d_insts, sl.d_work, w, nlev_max, nullptr, sl.st);
   if (rc) return rc;
   SRV_CUDA(p3x::launch_postamble(sl.d_insts, sl.d_work, w, sl.st));
   SRV_CUDA(cudaEventRecord(sl.ev, sl.st));
@@ -532,7 +536,6 @@ int p3x_server_create(p3x_context* ctx, const p3x_runtime* rt, int64_t budget_by
   for (auto& sl : s->slots) {
     SRV_CUDA(cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking));
     SRV_CUDA(cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming));
-    SRV_CUDA(cudaMalloc(&sl.d_ctr, p3x::dev::kWorkCounters * sizeof(uint32_t)));
   }
   s->t0 = Clock::now();
   *out = s.release();
@@ -552,7 +555,6 @@ int p3x_server_destroy(p3x_server* s) {
     if (sl.h_work) cudaFreeHost(sl.h_work);
     if (sl.d_insts) cudaFree(sl.d_insts);
     if (sl.d_work) cudaFree(sl.d_work);
-    if (sl.d_ctr) cudaFree(sl.d_ctr);
   }
   for (double* t : s->tmpl)
     if (t) cudaFree(t);
