@@ -156,16 +156,26 @@ def test_outputs_are_fully_written(gpu_ctx, case0):
 
 @pytest.mark.parametrize("precision", [0, 1])
 def test_launch_configs_bitwise_identical(gpu_ctx, case0, precision):
+    """Every launch shape gives the same bits, including CTAs narrower than a
+    warp (8 and 16 threads) and partial last warps (24 and 48 threads), where
+    a warp's groups take their work items from the launch-wide counter
+    together."""
+    orig = gpu_ctx.launch_config(precision)
     base = None
-    for lanes, cols, staged in [(32, 8, 1), (32, 4, 0), (16, 8, 1), (8, 16, 0), (8, 4, 1)]:
-        gpu_ctx.set_launch_config(precision, lanes=lanes, columns_per_block=cols, table_staging=staged)
-        g = run_gpu(gpu_ctx, case0, precision=precision)
-        if base is None:
-            base = g
-        else:
-            for n in ALLF:
-                np.testing.assert_array_equal(g[n], base[n], err_msg=f"{lanes}/{cols}/{staged} {n}")
-    gpu_ctx.set_launch_config(precision, lanes=32, columns_per_block=8, table_staging=1)
+    try:
+        for lanes, cols, staged in [(32, 8, 1), (32, 4, 0), (16, 8, 1), (8, 16, 0), (8, 4, 1),
+                                    (8, 1, 0), (16, 1, 0), (8, 3, 0), (16, 3, 1)]:
+            gpu_ctx.set_launch_config(precision, lanes=lanes, columns_per_block=cols, table_staging=staged)
+            g = run_gpu(gpu_ctx, case0, precision=precision)
+            if base is None:
+                base = g
+            else:
+                for n in ALLF:
+                    np.testing.assert_array_equal(g[n], base[n], err_msg=f"{lanes}/{cols}/{staged} {n}")
+    finally:
+        gpu_ctx.set_launch_config(precision, lanes=orig["lanes_per_column"],
+                                  columns_per_block=orig["columns_per_block"],
+                                  table_staging=orig["table_staging"], blocks_per_sm=orig["blocks_per_sm"])
 
 
 @pytest.mark.parametrize("precision", [0, 1])
