@@ -1760,7 +1760,7 @@ __device__ __forceinline__ const Inst& work_inst(const Inst& inst0, const KParam
 }
 
 /* The FP32-bulk instantiation is held to 128 registers (two CTAs of 256
- * threads per SM; 64 bytes spill), which measured 25 % faster than 176
+ * threads per SM; a few dozen bytes spill), which measured 25 % faster than 176
  * registers at one CTA per SM. */
 template <class TR, int LANES>
 __global__ void __launch_bounds__(256, sizeof(TR) == sizeof(float) ? 2 : 1)
