@@ -47,7 +47,7 @@ sys.path.insert(0, str(ROOT))
 
 NCOL, NLEV, DT = 345_600, 128, 300.0
 ALG_BYTES_PER_CL = 360.0
-SEED = 1002  # config 2 seed (1000 + config index)
+SEED = 1002  # seed of the 345,600-column RH-stress workload
 
 
 def _dist():
@@ -196,7 +196,7 @@ def cpu_baseline(seconds_target=15.0, nlev=NLEV, keep=None):
             O.p3_main(pert, tab, DT, it=s + 1, nthreads=cores)
         keep.update(inputs=inp, oracle=final, oracle_1ulp=pert)
     return {"value": value, "unit": "column-levels/s", "cores": cores, "kind": "port",
-            "sample": f"{ncol} columns x {nlev} levels (RH-stress workload, config-2 distributions), "
+            "sample": f"{ncol} columns x {nlev} levels (RH-stress workload: RH ~ U(0.9, 1.05) in even columns), "
                       f"{runs} runs of 10 steps from the initial state, oracle p3_main (C++ restatement of "
                       f"the reference) with OpenMP over columns on {cores} threads"}
 

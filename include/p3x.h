@@ -399,7 +399,7 @@ int p3x_server_destroy(p3x_server* s);
 
 /* Submits a request: instance `instance_id` (created on first use, nlev 72
  * or 128, ncol <= 65536) advances by one step.  Its initial state is columns
- * [c0, c0 + ncol) of the server's synthetic workload (config-0 distributions,
+ * [c0, c0 + ncol) of the server's synthetic workload (standard-atmosphere columns,
  * workload seed 5000) with c0 = seed mod (65536 - ncol + 1).  The instance
  * stays resident, readable with p3x_server_read_field, until the server is
  * destroyed.  arrival_s is the request's arrival time on the server clock

@@ -28,7 +28,7 @@
  * for memory that cannot come free.
  *
  * Instance workloads are column slices of synthetic templates (65536
- * columns of the config-0 distributions per level count), generated once per
+ * standard-atmosphere columns, RH ~ U(0.3, 1.05), per level count), generated once per
  * server and kept on the device: instance `seed` starts at template column
  * seed mod (65536 - ncol + 1), so a request's data does not cross PCIe on the
  * latency path and the same instance has the same data alone and in a mix.
@@ -57,7 +57,7 @@ using p3x::dev::Inst;
 using p3x::dev::WorkItem;
 
 constexpr int kTemplateCols = 65536;
-constexpr uint64_t kTemplateSeed = 5000;   /* config-4 instance seeds start at 1000 * (4 + 1) */
+constexpr uint64_t kTemplateSeed = 5000;   /* seed of the serving workload's templates */
 constexpr int kMidOutputs = 10;             /* 7 per-level diagnostics + 3 history fields */
 constexpr int kBatchColumnCap = 1 << 18;    /* columns per dispatched work list */
 

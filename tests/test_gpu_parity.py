@@ -1,6 +1,6 @@
 """GPU parity of the P3 step against the CPU oracle, through the C ABI.
 
-How parity is judged.  P3 contains complete-depletion cancellations (e.g. a
+How parity is decided.  P3 contains complete-depletion cancellations (e.g. a
 number-conservation limiter that sets ni + (sources - sinks) dt to a
 round-off residue) whose residue then feeds a table lookup on qi/ni.  A 1-ulp
 change of a single input moves the ice fields of the oracle itself by ~1e-2

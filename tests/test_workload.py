@@ -1,4 +1,4 @@
-"""CPU checks of the synthetic workload generator (configs 0-4 distributions)."""
+"""CPU checks of the synthetic workload generator (standard, RH-stress and mixed-IC columns)."""
 import numpy as np
 import pytest
 
