@@ -126,7 +126,8 @@ typedef struct p3x_layout {
 
 /* Launch configuration (chosen by p3x_autotune or set by hand). */
 typedef struct p3x_launch_config {
-  int32_t lanes_per_column;  /* 8, 16 or 32                                    */
+  int32_t lanes_per_column;  /* 8, 16 or 32 (part1+2 and part3; sedimentation  */
+                             /*    always runs 32 lanes per column)            */
   int32_t columns_per_block; /* columns handled concurrently by one CTA        */
   int32_t table_staging;     /* 0: tables read through L1/L2; 1: staged into   */
                              /*    shared memory by bulk copies (cp.async.bulk) */

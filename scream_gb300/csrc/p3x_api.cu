@@ -190,7 +190,8 @@ bool spec_fits(int precision, const LaunchSpec& ls, int stride) {
   if (ls.groups_per_block <= 0 || ls.groups_per_block * ls.lanes > 256) return false;
   const bool f32 = precision == P3X_FP32_BULK;
   const size_t k1 = f32 ? p3_smem_bytes<float>(ls, stride) : p3_smem_bytes<double>(ls, stride);
-  const size_t k2 = f32 ? sed_smem_bytes<float>(ls, stride) : sed_smem_bytes<double>(ls, stride);
+  const LaunchSpec ls2 = sed_spec(ls);
+  const size_t k2 = f32 ? sed_smem_bytes<float>(ls2, stride) : sed_smem_bytes<double>(ls2, stride);
   return k1 <= size_t(227 * 1024) && k2 <= size_t(227 * 1024);
 }
 
@@ -496,8 +497,10 @@ int p3x_context_create(const char* table_file, p3x_context** out, int* info) {
   }
   /* 4 columns per CTA with the tables read through L1: part1+part2 then fits
    * two CTAs per SM (staging the tables in shared memory leaves room for one),
-   * measured faster in both forms; staging remains a launch option */
-  ctx->cfg[P3X_FP64] = p3x_launch_config{32, 4, 0, 0};
+   * measured faster in both forms; staging remains a launch option.  The FP64
+   * part1+part2 (254 registers) keeps twice the columns in flight at 16 lanes
+   * per column and ran 7 % faster there (sedimentation stays at 32). */
+  ctx->cfg[P3X_FP64] = p3x_launch_config{16, 4, 0, 0};
   ctx->cfg[P3X_FP32_BULK] = p3x_launch_config{32, 4, 0, 0};
   *out = ctx.release();
   return P3X_OK;

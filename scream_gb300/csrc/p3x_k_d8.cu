@@ -2,6 +2,6 @@
 #include "p3x_kernels_impl.cuh"
 
 namespace p3x {
-template cudaError_t launch_p3_lanes<double, 8>(const dev::Inst&, const dev::KParams<double>&,
-                                                  const LaunchSpec&, int, cudaStream_t);
+template cudaError_t launch_p3_part<double, 8>(const dev::Inst&, const dev::KParams<double>&,
+                                                 const LaunchSpec&, int, int, cudaStream_t);
 }  // namespace p3x

@@ -2,6 +2,6 @@
 #include "p3x_kernels_impl.cuh"
 
 namespace p3x {
-template cudaError_t launch_p3_lanes<float, 16>(const dev::Inst&, const dev::KParams<float>&,
-                                                  const LaunchSpec&, int, cudaStream_t);
+template cudaError_t launch_p3_part<float, 16>(const dev::Inst&, const dev::KParams<float>&,
+                                                 const LaunchSpec&, int, int, cudaStream_t);
 }  // namespace p3x

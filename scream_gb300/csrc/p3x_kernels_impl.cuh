@@ -27,35 +27,39 @@ cudaError_t launch_persistent(Kern kern, const dev::Inst& inst0, const dev::KPar
 }
 
 template <class TR, int LANES>
-cudaError_t launch_p3_lanes(const dev::Inst& inst0, const dev::KParams<TR>& kp_in, const LaunchSpec& ls,
-                            int num_sms, cudaStream_t stream) {
+cudaError_t launch_p3_part(const dev::Inst& inst0, const dev::KParams<TR>& kp_in, const LaunchSpec& ls, int part,
+                           int num_sms, cudaStream_t stream) {
   dev::KParams<TR> kp = kp_in;
   kp.groups_per_block = ls.groups_per_block;
   kp.staged = ls.staged;
   const int threads = ls.groups_per_block * LANES;
   if (threads <= 0 || threads > 256) return cudaErrorInvalidValue;
-  if (kp.wctr) {
-    const cudaError_t z = cudaMemsetAsync(kp.wctr, 0, dev::kWorkCounters * sizeof(uint32_t), stream);
-    if (z != cudaSuccess) return z;
+  cudaError_t e = cudaErrorInvalidValue;
+  if (part == kPartK1) {
+    if (kp.wctr) {
+      e = cudaMemsetAsync(kp.wctr, 0, dev::kWorkCounters * sizeof(uint32_t), stream);
+      if (e != cudaSuccess) return e;
+    }
+    if (ls.marks) cudaEventRecord(ls.marks[0], stream);
+    e = launch_persistent<TR>(dev::p3_part12_kernel<TR, LANES>, inst0, kp, threads,
+                              p3_smem_bytes<TR>(ls, kp.sm_stride), ls.blocks_per_sm, num_sms, stream);
+    if (e == cudaSuccess && ls.marks) cudaEventRecord(ls.marks[1], stream);
+  } else if (part == kPartK2) {
+    if constexpr (LANES == 32) {
+      if constexpr (sizeof(TR) == sizeof(float)) {
+        e = launch_persistent<TR>(dev::p3_sed_bulk_kernel<LANES>, inst0, kp, threads,
+                                  sed_smem_bytes<TR>(ls, kp.sm_stride), 0, num_sms, stream);
+      } else {
+        e = launch_persistent<TR>(dev::p3_sed_kernel<TR, LANES>, inst0, kp, threads,
+                                  sed_smem_bytes<TR>(ls, kp.sm_stride), 0, num_sms, stream);
+      }
+      if (e == cudaSuccess && ls.marks) cudaEventRecord(ls.marks[2], stream);
+    }
+  } else if (part == kPartK3) {
+    e = launch_persistent<TR>(dev::p3_part3_kernel<TR, LANES>, inst0, kp, threads, 0, 0, num_sms, stream);
+    if (e == cudaSuccess && ls.marks) cudaEventRecord(ls.marks[3], stream);
   }
-  if (ls.marks) cudaEventRecord(ls.marks[0], stream);
-  cudaError_t e = launch_persistent<TR>(dev::p3_part12_kernel<TR, LANES>, inst0, kp, threads,
-                                        p3_smem_bytes<TR>(ls, kp.sm_stride), ls.blocks_per_sm, num_sms, stream);
-  if (e != cudaSuccess) return e;
-  if (ls.marks) cudaEventRecord(ls.marks[1], stream);
-  if constexpr (sizeof(TR) == sizeof(float)) {
-    e = launch_persistent<TR>(dev::p3_sed_bulk_kernel<LANES>, inst0, kp, threads,
-                              sed_smem_bytes<TR>(ls, kp.sm_stride), 0, num_sms, stream);
-  } else {
-    e = launch_persistent<TR>(dev::p3_sed_kernel<TR, LANES>, inst0, kp, threads,
-                              sed_smem_bytes<TR>(ls, kp.sm_stride), 0, num_sms, stream);
-  }
-  if (e != cudaSuccess) return e;
-  if (ls.marks) cudaEventRecord(ls.marks[2], stream);
-  e = launch_persistent<TR>(dev::p3_part3_kernel<TR, LANES>, inst0, kp, threads, 0, 0, num_sms, stream);
-  if (e != cudaSuccess) return e;
-  if (ls.marks) cudaEventRecord(ls.marks[3], stream);
-  return cudaSuccess;
+  return e;
 }
 
 }  // namespace p3x

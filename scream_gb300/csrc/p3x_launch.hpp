@@ -31,24 +31,53 @@ inline size_t sed_smem_bytes(const LaunchSpec& ls, int sm_stride) {
   return size_t(ls.groups_per_block) * dev::sed_slots<TR>() * size_t(sm_stride) * sizeof(double);
 }
 
-/* Persistent launches of the three column kernels (K1 part1+part2, K2
- * sedimentation, K3 part3) for one lane count, in order on one stream
- * (defined in p3x_kernels_impl.cuh, instantiated in p3x_k_*.cu).  kp.nwork,
- * kp.work, kp.insts and kp.sm_stride are set by the caller, and every
- * instance's scratch (Inst::scr, Inst::cflag) is bound. */
-template <class TR, int LANES>
-cudaError_t launch_p3_lanes(const dev::Inst& inst0, const dev::KParams<TR>& kp, const LaunchSpec& ls,
-                            int num_sms, cudaStream_t stream);
+/* Launch shape of K2.  Sedimentation always runs 32 lanes per column,
+ * whatever lane count K1 and K3 use: its substeps walk the levels chunk by
+ * chunk, so a narrower group only lengthens the walk (measured at 65,536 x
+ * 128 with 16 lanes: FP64 K2 +17 %, FP32-bulk K2 +95 %), while K1 in the
+ * FP64 form runs 7 % faster at 16 lanes.  Columns per CTA as configured, at
+ * most 8 (256 threads). */
+inline LaunchSpec sed_spec(const LaunchSpec& ls) {
+  LaunchSpec s = ls;
+  s.lanes = 32;
+  s.groups_per_block = ls.groups_per_block < 8 ? ls.groups_per_block : 8;
+  s.staged = 0;
+  return s;
+}
 
+/* Kernel parts of one step, launched in order on one stream: K1
+ * (part1+part2; zeroes the work counters first), K2 (sedimentation), K3
+ * (part3). */
+enum : int { kPartK1 = 1, kPartK2 = 2, kPartK3 = 4 };
+
+/* Persistent launch of one part for one lane count (defined in
+ * p3x_kernels_impl.cuh, instantiated in p3x_k_*.cu; K2 only for 32 lanes).
+ * kp.nwork, kp.work, kp.insts and kp.sm_stride are set by the caller, and
+ * every instance's scratch (Inst::scr, Inst::cflag) is bound. */
+template <class TR, int LANES>
+cudaError_t launch_p3_part(const dev::Inst& inst0, const dev::KParams<TR>& kp, const LaunchSpec& ls, int part,
+                           int num_sms, cudaStream_t stream);
+
+template <class TR>
+inline cudaError_t launch_p3_part_lanes(const dev::Inst& inst0, const dev::KParams<TR>& kp, const LaunchSpec& ls,
+                                        int part, int num_sms, cudaStream_t stream) {
+  switch (ls.lanes) {
+    case 8: return launch_p3_part<TR, 8>(inst0, kp, ls, part, num_sms, stream);
+    case 16: return launch_p3_part<TR, 16>(inst0, kp, ls, part, num_sms, stream);
+    case 32: return launch_p3_part<TR, 32>(inst0, kp, ls, part, num_sms, stream);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+/* The three column kernels of one step (K1, K2, K3) in order on one stream. */
 template <class TR>
 inline cudaError_t launch_p3(const dev::Inst& inst0, const dev::KParams<TR>& kp, const LaunchSpec& ls,
                              int num_sms, cudaStream_t stream) {
-  switch (ls.lanes) {
-    case 8: return launch_p3_lanes<TR, 8>(inst0, kp, ls, num_sms, stream);
-    case 16: return launch_p3_lanes<TR, 16>(inst0, kp, ls, num_sms, stream);
-    case 32: return launch_p3_lanes<TR, 32>(inst0, kp, ls, num_sms, stream);
-    default: return cudaErrorInvalidValue;
-  }
+  cudaError_t e = launch_p3_part_lanes<TR>(inst0, kp, ls, kPartK1, num_sms, stream);
+  if (e != cudaSuccess) return e;
+  e = launch_p3_part<TR, 32>(inst0, kp, sed_spec(ls), kPartK2, num_sms, stream);
+  if (e != cudaSuccess) return e;
+  return launch_p3_part_lanes<TR>(inst0, kp, ls, kPartK3, num_sms, stream);
 }
 
 /* (nlev, ncol) column-fastest <-> (ncol, ld) level-contiguous transposes. */
