@@ -286,7 +286,10 @@ int p3x_kernel_times(p3x_context* ctx, float* ms3);
 /* Synchronises `stream`, returns and clears the accumulated device status. */
 int p3x_context_check(p3x_context* ctx, void* stream);
 
-/* Overrides the launch configuration used by p3x_main for a precision form. */
+/* Overrides the launch configuration used by p3x_main (and the host and
+ * fixed-scratch entries, new batches and served requests) for a precision
+ * form.  Defaults:
+ * FP64 {16, 4, 0, 0}, FP32-bulk {32, 4, 0, 0}. */
 int p3x_set_launch_config(p3x_context* ctx, int32_t precision, const p3x_launch_config* cfg);
 int p3x_get_launch_config(const p3x_context* ctx, int32_t precision, p3x_launch_config* cfg);
 
