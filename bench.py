@@ -48,6 +48,17 @@ sys.path.insert(0, str(ROOT))
 NCOL, NLEV, DT = 345_600, 128, 300.0
 ALG_BYTES_PER_CL = 360.0
 SEED = 1002  # seed of the 345,600-column RH-stress workload
+METRIC = "P3 column-levels/sec at nlev=128 (FP32-bulk; FP64 beside it)"
+DATA = "synthetic (seeded standard-atmosphere columns, RH~U(0.9,1.05) in even columns)"
+
+
+def workload_config(ncol):
+    """The `config` object of both arms' lines."""
+    gb = ALG_BYTES_PER_CL * ncol * NLEV / 1e9  # interface fields read and written per step
+    l2 = f"interface fields {gb:.1f} GB/step > L2 (no flush needed)" if gb > 0.129 else \
+        f"interface fields {gb:.3f} GB/step < L2"
+    return {"workload": f"P3 p3_main ncol={ncol} nlev={NLEV} dt={DT}s, state carried", "l2": l2,
+            "columns_per_gpu": ncol}
 
 
 def _dist():
@@ -206,11 +217,10 @@ def run_reference(args):
     if rank != 0:
         return 0
     cb = cpu_baseline(seconds_target=max(5.0, 2.0 * args.steps))
-    line = {"metric": "P3 column-levels/sec at nlev=128", "value": cb["value"], "unit": "column-levels/s",
+    line = {"metric": METRIC, "value": cb["value"], "unit": "column-levels/s",
             "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded standard-atmosphere columns)",
-            "config": {"workload": f"P3 p3_main ncol={NCOL} nlev={NLEV} dt={DT} (sampled on CPU)"},
+            "data": DATA, "config": workload_config(args.ncol or NCOL),
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "column-levels/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -439,13 +449,12 @@ def run_gpu(args):
     cb = cpu_baseline(seconds_target=args.cpu_seconds, keep=sample) if not args.no_cpu else None
     precision = precision_report(ctx, sample) if sample else None
     line = {
-        "metric": "P3 column-levels/sec at nlev=128 (FP32-bulk; FP64 beside it)",
+        "metric": METRIC,
         "value": value, "unit": "column-levels/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": wall32 / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32-bulk (f64 state/residuals/fluxes)",
-        "data": "synthetic (seeded standard-atmosphere columns, RH~U(0.9,1.05) in even columns)",
-        "config": {"workload": f"P3 p3_main ncol={ncol} nlev={NLEV} dt={DT}s, state carried",
-                   "l2": "inputs 15.9 GB/step > L2 (no flush needed)", "columns_per_gpu": ncol},
+        "data": DATA,
+        "config": workload_config(ncol),
         "fp64": {"value": value64, "unit": "column-levels/s", "ms_per_step": wall64 / args.steps * 1e3,
                  "kernel_ms": kmean64 * 1e3,
                  "hbm_gbs_alg": ALG_BYTES_PER_CL * cl_step / kmean64 / 1e9,
