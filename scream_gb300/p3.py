@@ -143,9 +143,15 @@ class P3Context:
         L.check("p3x_context_get_tables", self.lib.p3x_context_get_tables(self.h, *args))
         return out
 
-    def set_launch_config(self, precision: int, lanes=32, columns_per_block=8, table_staging=1,
-                          blocks_per_sm=0):
-        cfg = L.LaunchConfig(lanes, columns_per_block, table_staging, blocks_per_sm)
+    def set_launch_config(self, precision: int, lanes=None, columns_per_block=None, table_staging=None,
+                          blocks_per_sm=None):
+        """Launch configuration of a precision form; arguments left at None keep
+        their current value (defaults: FP64 16 lanes, FP32-bulk 32, both 4
+        columns per CTA, tables through L1)."""
+        cur = self.launch_config(precision)
+        pick = lambda v, k: cur[k] if v is None else v  # noqa: E731
+        cfg = L.LaunchConfig(pick(lanes, "lanes_per_column"), pick(columns_per_block, "columns_per_block"),
+                             pick(table_staging, "table_staging"), pick(blocks_per_sm, "blocks_per_sm"))
         L.check("p3x_set_launch_config", self.lib.p3x_set_launch_config(self.h, precision, C.byref(cfg)))
 
     def launch_config(self, precision: int) -> dict:
