@@ -31,6 +31,7 @@
 #ifndef P3X_H
 #define P3X_H
 
+#include <stdbool.h>
 #include <stddef.h>
 #include <stdint.h>
 
@@ -222,15 +223,22 @@ int p3x_main_async(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic
  *   - The array is one per device and shared by every context: calls that
  *     overlap on the device (different streams or host threads) race on it
  *     and must be serialised by the caller.
- *   - The first call on each device looks the array's address up
- *     (cudaGetSymbolAddress, once per device with that device current); make
- *     that first call before any stream capture begins.
+ *   - p3x_context_create reserves the array on the context's device and
+ *     looks its address up there (cudaGetSymbolAddress, once per device), so
+ *     the reservation happens at start-up, before any stream capture.  Call
+ *     this entry with the context's device current; otherwise it returns
+ *     P3X_EINVAL.
  *   - Nothing in the array has to be zeroed (the step zeroes its work
  *     counters on the stream). */
 int p3x_main_fixed_scratch(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_state* prog,
                            const p3x_diagnostic_inputs* din, const p3x_diagnostic_outputs* dout,
                            const p3x_infrastructure* infra, const p3x_history_only* hist, int32_t nj,
                            int32_t nk, const p3x_layout* layout, int32_t precision, void* stream);
+
+/* Capacity in bytes of the static scratch of p3x_main_fixed_scratch, and
+ * whether it is reserved on the context's device (1 once the context
+ * exists).  No counterpart in the reference. */
+int p3x_fixed_scratch_info(const p3x_context* ctx, int64_t* capacity_bytes, int32_t* reserved);
 
 /* ------------------------------------------------------------------ */
 /* Process interface around the step (P3Microphysics pre/postamble)    */
@@ -293,11 +301,13 @@ int p3x_context_check(p3x_context* ctx, void* stream);
 int p3x_set_launch_config(p3x_context* ctx, int32_t precision, const p3x_launch_config* cfg);
 int p3x_get_launch_config(const p3x_context* ctx, int32_t precision, p3x_launch_config* cfg);
 
-/* p3_main_c (physics/p3/p3_iso_c.f90:132-183), same argument order and
- * meaning: HOST arrays in the Fortran (its:ite, kts:kte) layout (column index
- * fastest), precip fluxes (its:ite, kts:kte+1).  Uses the default context
- * created by p3x_init.  Runs FP64 on the current device.  elapsed_s receives
- * the step time in seconds. */
+/* p3_main_c (physics/p3/p3_iso_c.f90:132-183), same argument order, types
+ * and meaning: HOST arrays in the Fortran (its:ite, kts:kte) layout (column
+ * index fastest), precip fluxes (its:ite, kts:kte+1); its/ite/kts/kte/it are
+ * c_int and do_predict_nc/do_prescribed_CCN are logical(c_bool), all by
+ * value.  Unlike the reference subroutine it returns a status.  Uses the
+ * default context created by p3x_init.  Runs FP64 on the current device.
+ * elapsed_s receives the step time in seconds. */
 int p3x_init(const char* table_file, int* info);
 int p3x_finalize(void);
 int p3x_main_f(double* qc, double* nc, double* qr, double* nr, double* th_atm, double* qv,
@@ -306,8 +316,8 @@ int p3x_main_f(double* qc, double* nc, double* qr, double* nr, double* th_atm, d
                double* inv_qc_relvar, int32_t it, double* precip_liq_surf,
                double* precip_ice_surf, int32_t its, int32_t ite, int32_t kts, int32_t kte,
                double* diag_eff_radius_qc, double* diag_eff_radius_qi,
-               double* diag_eff_radius_qr, double* rho_qi, int32_t do_predict_nc,
-               int32_t do_prescribed_CCN, double* dpres, double* inv_exner,
+               double* diag_eff_radius_qr, double* rho_qi, bool do_predict_nc,
+               bool do_prescribed_CCN, double* dpres, double* inv_exner,
                double* qv2qi_depos_tend, double* precip_liq_flux, double* precip_ice_flux,
                double* cld_frac_r, double* cld_frac_l, double* cld_frac_i,
                double* liq_ice_exchange, double* vap_liq_exchange, double* vap_ice_exchange,

@@ -12,7 +12,7 @@
 ! the lookup tables in-process, or the address of a NUL-terminated path of a
 ! "VERSION 4.1.1" ice-table file.  info receives 0 or the negative status.
 module p3x_mod
-  use iso_c_binding, only: c_int, c_int32_t, c_double, c_ptr
+  use iso_c_binding, only: c_int, c_bool, c_double, c_ptr
   implicit none
   private
   public :: p3x_init, p3x_finalize, p3x_main_f
@@ -37,8 +37,9 @@ module p3x_mod
                         precip_liq_flux, precip_ice_flux, cld_frac_r, cld_frac_l, cld_frac_i, &
                         liq_ice_exchange, vap_liq_exchange, vap_ice_exchange, qv_prev, t_prev, elapsed_s) &
         bind(C, name="p3x_main_f") result(status)
-      import :: c_int, c_int32_t, c_double
-      integer(c_int32_t), value :: its, ite, kts, kte, it, do_predict_nc, do_prescribed_ccn
+      import :: c_int, c_bool, c_double
+      integer(c_int), value :: its, ite, kts, kte, it
+      logical(c_bool), value :: do_predict_nc, do_prescribed_ccn
       real(c_double), value :: dt
       real(c_double), intent(inout), dimension(its:ite, kts:kte) :: qc, nc, qr, nr, th_atm, qv, qi, qm, &
                                                                     ni, bm

@@ -154,7 +154,8 @@ PROTOTYPES = {
     "p3x_init": (C.c_int, [C.c_char_p, C.POINTER(C.c_int)]),
     "p3x_finalize": (C.c_int, []),
     "p3x_main_f": (C.c_int, [_dp] * 6 + [C.c_double] + [_dp] * 10 + [_I, _dp, _dp, _I, _I, _I, _I]
-                   + [_dp] * 4 + [_I, _I] + [_dp] * 13 + [_dp]),
+                   + [_dp] * 4 + [C.c_bool, C.c_bool] + [_dp] * 13 + [_dp]),
+    "p3x_fixed_scratch_info": (C.c_int, [_V, C.POINTER(C.c_int64), C.POINTER(C.c_int32)]),
     "p3x_batch_create": (C.c_int, [_V, C.POINTER(Runtime), C.POINTER(InstanceDesc), _I, C.POINTER(_V)]),
     "p3x_batch_run": (C.c_int, [_V, _V]),
     "p3x_batch_capture_graph": (C.c_int, [_V, _V]),

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -346,7 +347,49 @@ int read_and_clear_err(p3x_context* ctx, cudaStream_t st) {
 
 p3x_context* g_default_ctx = nullptr;
 
+struct OccKey {
+  int device;
+  const void* func;
+  int threads;
+  size_t smem;
+  bool operator<(const OccKey& o) const {
+    if (device != o.device) return device < o.device;
+    if (func != o.func) return func < o.func;
+    if (threads != o.threads) return threads < o.threads;
+    return smem < o.smem;
+  }
+};
+std::mutex g_occ_mu;
+std::map<OccKey, int> g_occ;
+std::map<std::pair<int, const void*>, size_t> g_smem_limit;
+
 }  // namespace
+
+cudaError_t kernel_occupancy(const void* func, int threads, size_t smem, int* per_sm) {
+  int device = 0;
+  cudaError_t e = cudaGetDevice(&device);
+  if (e != cudaSuccess) return e;
+  const OccKey key{device, func, threads, smem};
+  std::lock_guard<std::mutex> lk(g_occ_mu);
+  const auto it = g_occ.find(key);
+  if (it != g_occ.end()) {
+    *per_sm = it->second;
+    return cudaSuccess;
+  }
+  /* the limit only grows, so shapes cached earlier stay launchable */
+  size_t& limit = g_smem_limit[{device, func}];
+  if (smem > limit) {
+    e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    limit = smem;
+  }
+  int n = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, func, threads, smem);
+  if (e != cudaSuccess) return e;
+  g_occ[key] = n;
+  *per_sm = n;
+  return cudaSuccess;
+}
 }  // namespace p3x
 
 using namespace p3x;
@@ -421,6 +464,61 @@ int p3x_write_ice_table(const char* path, const char* version) {
   if (!path) return P3X_EINVAL;
   return write_ice_table_file(path, version ? version : "4.1.1") == 0 ? P3X_OK : P3X_ETABLE;
 }
+
+}  // extern "C"
+
+/* ------------------------------------------------------------------ */
+/* Fixed, pre-reserved hand-over scratch (p3x_main_fixed_scratch)     */
+/* ------------------------------------------------------------------ */
+/* Some hosts cannot let a library take device memory while their time loop
+ * runs: a model that reserves nearly all of HBM for its own pool at
+ * start-up, or one that must keep a fixed, audited device footprint for a
+ * whole simulation, has no memory to give and no way to account for a pool
+ * that grows behind its back.  For them the three kernels' hand-over scratch
+ * (40 bytes per column-level, 4 bytes per column and 16 bytes of work
+ * counters) lives in one array of static device storage.  This translation
+ * unit holds no kernel, so with lazy module loading the array is only
+ * reserved on a device when its address is first looked up; context
+ * creation does that, on the context's device, so the reservation happens at
+ * start-up and never inside a caller's time loop.  Nothing in the array needs
+ * to start at zero: the step zeroes its work counters on the stream, and
+ * part1+part2 writes every column's continue flag, and the hand-over values
+ * of every column that goes on, before sedimentation and part3 read them. */
+static __device__ __align__(256) unsigned char g_step_scratch[p3x::kFixedScratchBytes];
+
+namespace p3x {
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_step_scratch_mu;
+void* g_step_scratch_ptr[kMaxDevices] = {};
+
+/* Address of the array on `device`, which must be the current device (a
+ * symbol's address is looked up on the current one).  Looked up once per
+ * device; the lookup loads this module there and so reserves the array. */
+int step_scratch_address(int device, void** out) {
+  int cur = -1;
+  P3X_CUDA(cudaGetDevice(&cur));
+  if (device < 0 || device >= kMaxDevices || cur != device) return P3X_EINVAL;
+  std::lock_guard<std::mutex> lk(g_step_scratch_mu);
+  if (!g_step_scratch_ptr[device]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_step_scratch);
+    if (e != cudaSuccess) return cuda_status(e);
+    g_step_scratch_ptr[device] = p;
+  }
+  *out = g_step_scratch_ptr[device];
+  return P3X_OK;
+}
+
+bool step_scratch_reserved(int device) {
+  if (device < 0 || device >= kMaxDevices) return false;
+  std::lock_guard<std::mutex> lk(g_step_scratch_mu);
+  return g_step_scratch_ptr[device] != nullptr;
+}
+}  // namespace
+}  // namespace p3x
+
+extern "C" {
 
 int p3x_context_create(const char* table_file, p3x_context** out, int* info) {
   if (info) *info = 0;
@@ -502,6 +600,16 @@ int p3x_context_create(const char* table_file, p3x_context** out, int* info) {
    * per column and ran 7 % faster there (sedimentation stays at 32). */
   ctx->cfg[P3X_FP64] = p3x_launch_config{16, 4, 0, 0};
   ctx->cfg[P3X_FP32_BULK] = p3x_launch_config{32, 4, 0, 0};
+  /* reserve the fixed hand-over scratch of p3x_main_fixed_scratch on this
+   * device now (see g_step_scratch) */
+  {
+    void* scr = nullptr;
+    if ((st = step_scratch_address(ctx->device, &scr))) {
+      if (info) *info = st;
+      p3x_context_destroy(ctx.release());
+      return st;
+    }
+  }
   *out = ctx.release();
   return P3X_OK;
 }
@@ -805,7 +913,7 @@ int p3x_main_f(double* qc, double* nc, double* qr, double* nr, double* th_atm, d
                double* nc_nuceat_tend, double* nccn_prescribed, double* ni_activated, double* inv_qc_relvar,
                int32_t it, double* precip_liq_surf, double* precip_ice_surf, int32_t its, int32_t ite,
                int32_t kts, int32_t kte, double* diag_eff_radius_qc, double* diag_eff_radius_qi,
-               double* diag_eff_radius_qr, double* rho_qi, int32_t do_predict_nc, int32_t do_prescribed_CCN,
+               double* diag_eff_radius_qr, double* rho_qi, bool do_predict_nc, bool do_prescribed_CCN,
                double* dpres, double* inv_exner, double* qv2qi_depos_tend, double* precip_liq_flux,
                double* precip_ice_flux, double* cld_frac_r, double* cld_frac_l, double* cld_frac_i,
                double* liq_ice_exchange, double* vap_liq_exchange, double* vap_ice_exchange, double* qv_prev,
@@ -860,7 +968,7 @@ int p3x_main_f(double* qc, double* nc, double* qr, double* nr, double* th_atm, d
   p3x_diagnostic_outputs dout{B[23], B[nmid + 4], B[nmid + 5], B[24], B[25], B[26], B[27],
                               B[nmid + 2], B[nmid + 3], B[nmid], B[nmid + 1]};
   p3x_history_only hist{B[28], B[29], B[30]};
-  p3x_infrastructure infra{dt, it, its, ite, kts, kte, do_predict_nc, do_prescribed_CCN, nullptr};
+  p3x_infrastructure infra{dt, it, its, ite, kts, kte, do_predict_nc ? 1 : 0, do_prescribed_CCN ? 1 : 0, nullptr};
   p3x_layout lay{ld, ldi};
   p3x_runtime rt;
   p3x_runtime_defaults(&rt);
@@ -1125,11 +1233,11 @@ int p3x_batch_capture_graph(p3x_batch* b, void* stream) {
 
 int p3x_batch_set_launch_config(p3x_batch* b, const p3x_launch_config* cfg) {
   if (!b || !cfg) return P3X_EINVAL;
-  for (int g = 0; g < b->ngroups; ++g) {
-    const LaunchSpec ls = spec_of(*cfg);
+  const LaunchSpec ls = spec_of(*cfg);
+  /* every group must accept the configuration before any group takes it */
+  for (int g = 0; g < b->ngroups; ++g)
     if (!spec_fits(b->groups[g].precision, ls, sm_stride_for(1))) return P3X_EINVAL;
-    b->groups[g].ls = ls;
-  }
+  for (int g = 0; g < b->ngroups; ++g) b->groups[g].ls = ls;
   drop_graph(b);
   return P3X_OK;
 }
@@ -1203,45 +1311,12 @@ int p3x_autotune_batch(p3x_batch* b, void* stream, int32_t reps, p3x_launch_conf
 
 }  // extern "C"
 
-/* ------------------------------------------------------------------ */
-/* P3 step with a fixed, pre-reserved hand-over scratch               */
-/* ------------------------------------------------------------------ */
-/* Some hosts cannot let a library take device memory while their time loop
- * runs: a model that reserves nearly all of HBM for its own pool at
- * start-up, or one that must keep a fixed, audited device footprint for a
- * whole simulation, has no memory to give and no way to account for a pool
- * that grows behind its back.  For them the three kernels' hand-over scratch
- * (40 bytes per column-level, 4 bytes per column and 16 bytes of work
- * counters) lives in one array of static device storage, reserved when the
- * library's module is loaded.  Nothing in the array needs to start at zero:
- * the step zeroes its work counters on the stream, and part1+part2 writes
- * every column's continue flag, and the hand-over values of every column
- * that goes on, before sedimentation and part3 read them. */
-static __device__ __align__(256) unsigned char g_step_scratch[p3x::kFixedScratchBytes];
-
-namespace p3x {
-namespace {
-constexpr int kMaxDevices = 64;
-std::mutex g_step_scratch_mu;
-void* g_step_scratch_ptr[kMaxDevices] = {};
-
-/* Address of the array on the current device, looked up once per device. */
-int step_scratch_address(void** out) {
-  int dev = 0;
-  P3X_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return P3X_EINVAL;
-  std::lock_guard<std::mutex> lk(g_step_scratch_mu);
-  if (!g_step_scratch_ptr[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_step_scratch);
-    if (e != cudaSuccess) return cuda_status(e);
-    g_step_scratch_ptr[dev] = p;
-  }
-  *out = g_step_scratch_ptr[dev];
+extern "C" int p3x_fixed_scratch_info(const p3x_context* ctx, int64_t* capacity_bytes, int32_t* reserved) {
+  if (!ctx) return P3X_EINVAL;
+  if (capacity_bytes) *capacity_bytes = int64_t(kFixedScratchBytes);
+  if (reserved) *reserved = step_scratch_reserved(ctx->device) ? 1 : 0;
   return P3X_OK;
 }
-}  // namespace
-}  // namespace p3x
 
 extern "C" int p3x_main_fixed_scratch(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_state* prog,
                                       const p3x_diagnostic_inputs* din, const p3x_diagnostic_outputs* dout,
@@ -1255,7 +1330,9 @@ extern "C" int p3x_main_fixed_scratch(p3x_context* ctx, const p3x_runtime* rt, c
   if (in.ncol == 0) return P3X_OK;
   if (dev::scratch_bytes(in.ncol, in.ld) > kFixedScratchBytes) return P3X_ENOMEM;
   void* scr = nullptr;
-  const int rc = step_scratch_address(&scr);
+  /* the context reserved the array on its device; a call made while another
+   * device is current is rejected (P3X_EINVAL) */
+  const int rc = step_scratch_address(ctx->device, &scr);
   if (rc) return rc;
   bind_scratch(in, static_cast<unsigned char*>(scr));
   return launch_kernels(ctx, rt, in, static_cast<cudaStream_t>(stream));

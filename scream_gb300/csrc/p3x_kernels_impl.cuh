@@ -7,14 +7,14 @@ namespace p3x {
 
 /* Persistent launch of one kernel: the grid is the number of CTAs that fit on
  * all SMs at once (capped by blocks_per_sm when given, and by the amount of
- * work); groups walk the work list with a grid stride. */
+ * work); groups walk the work list with a grid stride.  The occupancy comes
+ * from a per-device cache, so a launch makes no attribute or occupancy query
+ * after the first one of its shape. */
 template <class TR, class Kern>
 cudaError_t launch_persistent(Kern kern, const dev::Inst& inst0, const dev::KParams<TR>& kp, int threads,
                               size_t smem, int blocks_per_sm, int num_sms, cudaStream_t stream) {
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-  if (e != cudaSuccess) return e;
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+  cudaError_t e = kernel_occupancy(reinterpret_cast<const void*>(kern), threads, smem, &per_sm);
   if (e != cudaSuccess) return e;
   if (per_sm <= 0) return cudaErrorInvalidConfiguration;
   if (blocks_per_sm > 0) per_sm = per_sm < blocks_per_sm ? per_sm : blocks_per_sm;

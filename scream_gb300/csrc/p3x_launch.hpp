@@ -45,6 +45,13 @@ inline LaunchSpec sed_spec(const LaunchSpec& ls) {
   return s;
 }
 
+/* CTAs of kernel `func` that fit on one SM with `threads` threads and `smem`
+ * bytes of dynamic shared memory on the current device.  The first query of
+ * a (device, kernel, threads, smem) shape raises the kernel's
+ * dynamic-shared-memory limit as needed and asks the occupancy calculator;
+ * later ones read the cache (p3x_api.cu). */
+cudaError_t kernel_occupancy(const void* func, int threads, size_t smem, int* per_sm);
+
 /* Kernel parts of one step, launched in order on one stream: K1
  * (part1+part2; zeroes the work counters first), K2 (sedimentation), K3
  * (part3). */

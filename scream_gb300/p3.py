@@ -256,6 +256,8 @@ class P3Batch:
         self.h = C.c_void_p()
         L.check("p3x_batch_create", ctx.lib.p3x_batch_create(ctx.h, C.byref(rt), descs, len(self.fields),
                                                              C.byref(self.h)))
+        # a new batch starts from the context's configuration for its precision
+        self._cfg = ctx.launch_config(precision)
 
     def run(self, stream=None):
         L.check("p3x_batch_run", self.ctx.lib.p3x_batch_run(self.h, _stream_handle(stream)))
@@ -263,15 +265,23 @@ class P3Batch:
     def capture_graph(self, stream):
         L.check("p3x_batch_capture_graph", self.ctx.lib.p3x_batch_capture_graph(self.h, _stream_handle(stream)))
 
-    def set_launch_config(self, lanes=32, columns_per_block=8, table_staging=1, blocks_per_sm=0):
-        cfg = L.LaunchConfig(lanes, columns_per_block, table_staging, blocks_per_sm)
+    def set_launch_config(self, lanes=None, columns_per_block=None, table_staging=None, blocks_per_sm=None):
+        """Launch configuration of the batch; arguments left at None keep their
+        current value (initially the context's configuration for the batch's
+        precision)."""
+        cur = self._cfg
+        pick = lambda v, k: cur[k] if v is None else v  # noqa: E731
+        cfg = L.LaunchConfig(pick(lanes, "lanes_per_column"), pick(columns_per_block, "columns_per_block"),
+                             pick(table_staging, "table_staging"), pick(blocks_per_sm, "blocks_per_sm"))
         L.check("p3x_batch_set_launch_config", self.ctx.lib.p3x_batch_set_launch_config(self.h, C.byref(cfg)))
+        self._cfg = cfg.as_dict()
 
     def autotune(self, reps=3, stream=None):
         cfg = L.LaunchConfig()
         ms = C.c_double(0)
         L.check("p3x_autotune_batch", self.ctx.lib.p3x_autotune_batch(self.h, _stream_handle(stream), reps,
                                                                       C.byref(cfg), C.byref(ms)))
+        self._cfg = cfg.as_dict()
         return cfg.as_dict(), ms.value
 
     def close(self):

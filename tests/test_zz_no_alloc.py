@@ -43,6 +43,21 @@ def test_fixed_scratch_matches_pooled_entry_two_steps(gpu_ctx, precision):
             assert np.array_equal(a[name], b[name]), (it, name)
 
 
+def test_fixed_scratch_reserved_at_context_creation(gpu_ctx):
+    """The static array is reserved, and its address looked up, when the
+    context is created, so a host that fills the device right after creating
+    the context cannot meet an out-of-memory error on the first call."""
+    import scream_gb300 as p3
+    cap, res = C.c_int64(0), C.c_int32(0)
+    ctx = p3.P3Context()
+    try:
+        assert ctx.lib.p3x_fixed_scratch_info(ctx.h, C.byref(cap), C.byref(res)) == 0
+        assert cap.value == FIXED_SCRATCH_BYTES
+        assert res.value == 1
+    finally:
+        ctx.close()
+
+
 def test_fixed_scratch_rejects_oversize_call(gpu_ctx):
     import scream_gb300 as p3
     from scream_gb300 import _lib as L
