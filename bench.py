@@ -25,11 +25,17 @@ needed between steps.
               [1,65536], nlev 72/128, FP64/FP32-bulk 50/50, 1-20 steps) at
               80% of the capacity measured in the same run, 120 GB budget
   cpu_baseline  the CPU oracle (a C++/OpenMP restatement of the reference
-              p3_main) on a bounded sample, all host cores
+              p3_main) on the whole workload, 10 steps with the state
+              carried, all host cores
+  precision   per-field rel-L2 / max-abs of both GPU forms against that
+              oracle run over all columns after 1 and 10 steps, the
+              oracle's own 1-ulp spread, domain-total precipitation per step
+              and every column's 10-step water budget
 
---impl reference times the CPU oracle alone (the reference itself cannot be
-built: its EKAT/Kokkos submodules are empty).  Multi-GPU (torchrun): each rank
-runs its own 345,600 columns (weak scaling, no collective on the data path).
+--impl reference times the CPU oracle alone on the same whole workload (the
+reference itself cannot be built: its EKAT/Kokkos submodules are empty).
+Multi-GPU (torchrun): each rank runs its own 345,600 columns (weak scaling,
+no collective on the data path).
 """
 from __future__ import annotations
 
@@ -167,60 +173,95 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(seconds_target=15.0, nlev=NLEV, keep=None):
-    """CPU oracle on a bounded sample of the same workload (all host cores):
-    runs of 10 steps with state carried, each run restarting from the initial
-    state (as the GPU runs do), until the time budget is spent."""
+PRECISION_FIELDS = ["qc", "nc", "qr", "nr", "qi", "qm", "ni", "bm", "qv", "th", "precip_liq_surf",
+                    "precip_ice_surf", "precip_liq_flux", "diag_eff_radius_qc", "diag_eff_radius_qr",
+                    "diag_eff_radius_qi", "rho_qi", "qv2qi_depos_tend", "precip_total_tend", "nevapr",
+                    "liq_ice_exchange", "vap_liq_exchange", "vap_ice_exchange"]
+RHO_W = 1000.0
+GRAV = 9.80616
+
+
+def carry_host(state):
+    """State hand-over of the process interface between steps
+    (eamxx_p3_process_interface.hpp:218,237): qv_prev <- qv, t_prev <- T."""
+    state["qv_prev"][...] = state["qv"]
+    state["t_prev"][...] = state["th"] / state["inv_exner"]
+
+
+def column_water(st):
+    return ((st["qv"] + st["qc"] + st["qr"] + st["qi"]) * st["dpres"] / GRAV).sum(axis=1)
+
+
+def cpu_baseline(inputs, steps=10, keep=None, warmup=0):
+    """The CPU oracle (C++/OpenMP restatement of the reference p3_main) on the
+    whole workload: `steps` steps of all columns with the state carried, on
+    all host cores; `warmup` untimed steps first (on the same state, then the
+    state restarts from the inputs).  Timed like the reference times p3_main
+    (the column loop, init excluded).  With `keep`, also stores the state after
+    step 1 and after the last step, the domain-total surface precipitation of
+    every step, and the same run with th moved by one ulp (the oracle's own
+    round-off spread)."""
     import numpy as np
     from scream_gb300 import _lib as L
-    from scream_gb300.p3 import generate_inputs
     from oracle import p3_oracle as O
     tab = L.host_tables()
     cores = os.cpu_count() or 1
-    ncol = max(256, 64 * cores)
-    inp = generate_inputs(1, SEED, ncol, nlev)
+    ncol, nlev = inputs["qc"].shape
 
-    def fresh():
-        st = {k: np.array(v, copy=True) for k, v in inp.items()}
+    def fresh(perturb=False):
+        st = {k: np.array(v, copy=True) for k, v in inputs.items()}
         st.update(O.empty_outputs(ncol, nlev))
+        if perturb:
+            st["th"] = np.nextafter(st["th"], np.inf)
         return st
 
-    O.p3_main(fresh(), tab, DT, nthreads=cores)  # warm-up step
-    total_us, steps, runs = 0.0, 0, 0
-    t_end = time.time() + seconds_target
-    final = None
-    while time.time() < t_end or runs < 1:
+    if warmup:
         st = fresh()
-        for s in range(10):
-            err, us = O.p3_main(st, tab, DT, it=s + 1, nthreads=cores)
-            total_us += us
-            steps += 1
-        runs += 1
-        final = st
+        for s in range(warmup):
+            O.p3_main(st, tab, DT, it=s + 1, nthreads=cores)
+            carry_host(st)
+        del st
+    st = fresh()
+    total_us, totals = 0.0, []
+    for s in range(steps):
+        err, us = O.p3_main(st, tab, DT, it=s + 1, nthreads=cores)
+        if err:
+            raise RuntimeError(f"oracle step {s + 1} returned error bits {err}")
+        total_us += us
+        totals.append(float(np.sum(st["precip_liq_surf"] + st["precip_ice_surf"])))
+        if keep is not None and s == 0:
+            keep["step1"] = {n: st[n].copy() for n in PRECISION_FIELDS}
+        carry_host(st)
     value = ncol * nlev * steps / (total_us * 1e-6)
     if keep is not None:
-        # the oracle's own round-off envelope: the same 10 steps with th
-        # moved by one ulp
-        pert = fresh()
-        pert["th"] = np.nextafter(pert["th"], np.inf)
-        for s in range(10):
+        keep.update(oracle=st, oracle_totals=totals)
+        pert = fresh(perturb=True)
+        ptot = []
+        for s in range(steps):
             O.p3_main(pert, tab, DT, it=s + 1, nthreads=cores)
-        keep.update(inputs=inp, oracle=final, oracle_1ulp=pert)
+            ptot.append(float(np.sum(pert["precip_liq_surf"] + pert["precip_ice_surf"])))
+            carry_host(pert)
+        keep.update(oracle_1ulp=pert, oracle_1ulp_totals=ptot)
     return {"value": value, "unit": "column-levels/s", "cores": cores, "kind": "port",
-            "sample": f"{ncol} columns x {nlev} levels (RH-stress workload: RH ~ U(0.9, 1.05) in even columns), "
-                      f"{runs} runs of 10 steps from the initial state, oracle p3_main (C++ restatement of "
-                      f"the reference) with OpenMP over columns on {cores} threads"}
+            "sample": f"the whole workload: {ncol} columns x {nlev} levels (RH ~ U(0.9, 1.05) in even columns), "
+                      f"{steps} steps with the state carried" + (f" after {warmup} untimed steps" if warmup else "")
+                      + f"; oracle p3_main (scalar FP64 C++ restatement of the reference, -O2) with OpenMP "
+                        f"over columns on {cores} threads; elapsed time of the column loops"}
 
 
 def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
         return 0
-    cb = cpu_baseline(seconds_target=max(5.0, 2.0 * args.steps))
+    from scream_gb300.p3 import generate_inputs
+    ncol = args.ncol or NCOL
+    inputs = generate_inputs(1, rank_seed(0), ncol, NLEV)
+    cb = cpu_baseline(inputs, steps=args.steps, warmup=args.warmup)
     line = {"metric": METRIC, "value": cb["value"], "unit": "column-levels/s",
             "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ncol * NLEV / cb["value"] * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": DATA, "config": workload_config(args.ncol or NCOL),
+            "data": DATA, "config": workload_config(ncol),
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "column-levels/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -228,39 +269,63 @@ def run_reference(args):
     return 0
 
 
-def precision_report(ctx, sample):
-    """Per-field rel-L2 and max-abs error of the GPU forms against the FP64
-    oracle after 10 steps on the CPU baseline's column sample (the oracle run
-    the baseline just timed).  The FP64 row is the round-off envelope: P3's
-    ice fields respond at ~1e-2 to 1-ulp input changes."""
+def _errors(g, ref):
+    import numpy as np
+    rows = {}
+    for n in PRECISION_FIELDS:
+        den = float(np.linalg.norm(ref[n]))
+        d = g[n] - ref[n]
+        num = float(np.linalg.norm(d))
+        rows[n] = {"rel_l2": num / den if den > 0 else num, "max_abs": float(np.max(np.abs(d)))}
+    tot_g = g["precip_liq_surf"] + g["precip_ice_surf"]
+    tot_r = ref["precip_liq_surf"] + ref["precip_ice_surf"]
+    rows["surface_precip_total"] = {"rel_l2": float(np.linalg.norm(tot_g - tot_r) / np.linalg.norm(tot_r)),
+                                    "max_abs": float(np.max(np.abs(tot_g - tot_r)))}
+    return rows
+
+
+def precision_report(ctx, inputs, sample, steps=10):
+    """Per-field rel-L2 and max-abs error of both GPU forms against the FP64
+    oracle over the whole workload, after one step and after `steps` steps
+    (the oracle run the CPU baseline just timed), with two well-conditioned
+    aggregates: the domain-total surface precipitation of every step, and
+    every column's water budget over all steps (W_end + precipitated mass =
+    W_0).  The oracle's own run with th moved by one ulp is the round-off
+    spread: P3's ice fields respond at ~1e-2 to 1-ulp input changes, so
+    multi-step per-field figures measure the problem's conditioning."""
     import numpy as np
     import scream_gb300 as p3
-    inp, ref = sample["inputs"], sample["oracle"]
-    names = ["qc", "nc", "qr", "nr", "qi", "qm", "ni", "bm", "qv", "th", "precip_liq_surf", "precip_ice_surf",
-             "precip_liq_flux", "diag_eff_radius_qc", "diag_eff_radius_qr", "diag_eff_radius_qi", "rho_qi",
-             "qv2qi_depos_tend", "precip_total_tend", "nevapr", "liq_ice_exchange", "vap_liq_exchange",
-             "vap_ice_exchange"]
-    out = {"sample": f"{inp['qc'].shape[0]} columns x {inp['qc'].shape[1]} levels, 10 steps, RH-stress workload",
-           "note": "oracle_1ulp: the oracle itself after th moved by one ulp (round-off envelope)"}
-    for prec, tag in ((p3.P3X_FP32_BULK, "fp32_bulk"), (p3.P3X_FP64, "fp64"), (None, "oracle_1ulp")):
-        if prec is None:
-            g = sample["oracle_1ulp"]
-        else:
-            f = p3.P3Fields.from_inputs(inp)
-            for s in range(10):
-                ctx.p3_main(f, DT, prec, it=s + 1)
-            g = f.to_host()
-        rows = {}
-        for n in names:
-            den = np.linalg.norm(ref[n])
-            diff = g[n] - ref[n]
-            rows[n] = {"rel_l2": float(np.linalg.norm(diff) / den) if den > 0 else float(np.linalg.norm(diff)),
-                       "max_abs": float(np.max(np.abs(diff)))}
-        tot_g = g["precip_liq_surf"] + g["precip_ice_surf"]
-        tot_r = ref["precip_liq_surf"] + ref["precip_ice_surf"]
-        rows["surface_precip_total"] = {"rel_l2": float(np.linalg.norm(tot_g - tot_r) / np.linalg.norm(tot_r)),
-                                        "max_abs": float(np.max(np.abs(tot_g - tot_r)))}
-        out[tag] = rows
+    ncol, nlev = inputs["qc"].shape
+    w0 = column_water(inputs)
+    ref, ref1 = sample["oracle"], sample["step1"]
+    o_tot = sample["oracle_totals"]
+    out = {"workload": f"all {ncol} columns x {nlev} levels, {steps} steps, state carried "
+                       "(qv_prev <- qv, t_prev <- T between steps), RH-stress inputs",
+           "note": "oracle_1ulp: the oracle itself with th moved by one ulp (round-off spread)",
+           "step1": {}, f"step{steps}": {}, "domain_total_precip_rel_diff": {},
+           "column_water_residual_max": {}}
+    for prec, tag in ((p3.P3X_FP32_BULK, "fp32_bulk"), (p3.P3X_FP64, "fp64")):
+        f = p3.P3Fields.from_inputs(inputs)
+        acc = np.zeros(ncol)
+        rel_tot = []
+        for s in range(steps):
+            ctx.p3_main(f, DT, prec, it=s + 1)
+            pl = f.t["precip_liq_surf"].cpu().numpy()
+            pi = f.t["precip_ice_surf"].cpu().numpy()
+            acc += (pl + pi) * RHO_W * DT
+            rel_tot.append(abs(float(np.sum(pl + pi)) - o_tot[s]) / o_tot[s])
+            if s == 0:
+                out["step1"][tag] = _errors({n: f.t[n].cpu().numpy() for n in PRECISION_FIELDS}, ref1)
+            f.t["qv_prev"].copy_(f.t["qv"])
+            f.t["t_prev"].copy_(f.t["th"] / f.t["inv_exner"])
+        g = {n: f.t[n].cpu().numpy() for n in PRECISION_FIELDS + ["dpres"]}
+        out[f"step{steps}"][tag] = _errors(g, ref)
+        out["domain_total_precip_rel_diff"][tag] = rel_tot
+        out["column_water_residual_max"][tag] = float(np.max(np.abs(column_water(g) + acc - w0) / w0))
+        del f, g
+    out[f"step{steps}"]["oracle_1ulp"] = _errors(sample["oracle_1ulp"], ref)
+    out["domain_total_precip_rel_diff"]["oracle_1ulp"] = [abs(a - b) / b for a, b in
+                                                          zip(sample["oracle_1ulp_totals"], o_tot)]
     return out
 
 
@@ -446,8 +511,9 @@ def run_gpu(args):
             "kernels": shares(parts32, names32)}
     kmean64 = sum(k64) / len(k64) * 1e-3
     sample = {}
-    cb = cpu_baseline(seconds_target=args.cpu_seconds, keep=sample) if not args.no_cpu else None
-    precision = precision_report(ctx, sample) if sample else None
+    cb = cpu_baseline(inputs, steps=10, keep=sample) if not args.no_cpu else None
+    precision = precision_report(ctx, inputs, sample) if sample else None
+    sample.clear()
     line = {
         "metric": METRIC,
         "value": value, "unit": "column-levels/s", "n_gpus": ws, "steps": args.steps,
@@ -486,7 +552,6 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ncol", type=int, default=0)
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serving", action="store_true")

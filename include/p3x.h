@@ -273,6 +273,38 @@ int p3x_postamble(const p3x_interface_fields* f, const p3x_prognostic_state* pro
                   const p3x_diagnostic_inputs* din, const p3x_diagnostic_outputs* dout, int32_t nj,
                   int32_t nk, const p3x_layout* layout, double dt, void* stream);
 
+/* ------------------------------------------------------------------ */
+/* The step in stages (stage-by-stage checks against a CPU restatement) */
+/* ------------------------------------------------------------------ */
+/* No counterpart in the reference, whose p3_main runs its stages inside one
+ * kernel (p3_main_impl.hpp:108-325).  The step is three kernels in a row:
+ *   P3X_STAGE_PART12  p3_main_init + p3_main_part1 + p3_main_part2
+ *   P3X_STAGE_SED     cloud, rain and ice sedimentation
+ *   P3X_STAGE_PART3   homogeneous freezing + p3_main_part3
+ * p3x_main_stages runs the subset `stages` (OR of the bits) in that order on
+ * `stream`, asynchronously, with the hand-over between them in the caller's
+ * DEVICE buffer `handover` (16-byte aligned, p3x_handover_bytes(nj, ld)
+ * bytes) instead of the context's pool, so a caller can stop after part2,
+ * inspect or replace the hand-over and the state, and resume.  All three
+ * stages in one call give exactly p3x_main_async.  Hand-over layout (ld as in
+ * the call's layout):
+ *   doubles [5][nj][ld]: the temperature after part1 (homogeneous freezing
+ *     reads it), the air density, rhofacr, rhofaci and acn; in the FP32-bulk
+ *     form the last four hold floats in the first half of each column's row;
+ *   then int32 [nj]: 1 where the column goes on past part2, 0 where it took
+ *     one of the step's early exits (later stages skip it);
+ *   then the stages' work counters (zeroed by the call).
+ * Only the rows of columns that go on are written by P3X_STAGE_PART12. */
+#define P3X_STAGE_PART12 1
+#define P3X_STAGE_SED 2
+#define P3X_STAGE_PART3 4
+int p3x_handover_bytes(int32_t nj, int64_t ld, int64_t* bytes);
+int p3x_main_stages(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_state* prog,
+                    const p3x_diagnostic_inputs* din, const p3x_diagnostic_outputs* dout,
+                    const p3x_infrastructure* infra, const p3x_history_only* hist, int32_t nj, int32_t nk,
+                    const p3x_layout* layout, int32_t precision, int32_t stages, void* handover,
+                    void* stream);
+
 /* Device self-test of numeric building blocks (no counterpart in the
  * reference): for all 2^32 float bit patterns, compares the FP32-bulk form's
  * integer-pipe float -> double conversion with the hardware conversion and

@@ -1141,10 +1141,13 @@ struct Col {
       *precip_total_tend, *nevapr, *liq_ice_exchange, *vap_liq_exchange, *vap_ice_exchange;
 };
 
-void p3_column(const Col& c, int nk, Real dt, bool predictNc, bool prescribedCCN,
-               const p3o_runtime& rt, const p3o_tables* tab, Work& w, Err& e) {
+/* p3_main_init, p3_main_part1 and p3_main_part2 of one column.  Returns
+ * false when the column takes one of the two early exits of
+ * p3_main_internal (p3_main_impl.hpp:237-239 after part1, :260 after part2),
+ * which skip everything after them. */
+bool p3_column_part12(const Col& c, int nk, Real dt, bool predictNc, bool prescribedCCN,
+                      const p3o_runtime& rt, const p3o_tables* tab, Work& w, Err& e) {
   const Real inv_dt = 1 / dt;
-  const int kdir = -1, ktop = 0, kbot = nk - 1;
   const bool do_ice_production = rt.do_ice_production != 0;
 
   /* p3_main_init: p3_main_impl.hpp:18-72 */
@@ -1243,7 +1246,7 @@ void p3_column(const Col& c, int nk, Real dt, bool predictNc, bool prescribedCCN
                                    w.nc_incld[k], w.nr_incld[k], w.ni_incld[k], w.bm_incld[k]);
   }
 
-  if (!(nucleationPossible || hydrometeorsPresent)) return;
+  if (!(nucleationPossible || hydrometeorsPresent)) return false;
 
   /* p3_main_part2: p3_main_impl_part2.hpp:18-526 */
   hydrometeorsPresent = false;
@@ -1422,8 +1425,20 @@ void p3_column(const Col& c, int nk, Real dt, bool predictNc, bool prescribedCCN
                                    w.nc_incld[k], w.nr_incld[k], w.ni_incld[k], w.bm_incld[k]);
   }
 
-  if (!hydrometeorsPresent) return;
+  return hydrometeorsPresent;
+}
 
+/* Cloud, rain and ice sedimentation, homogeneous freezing and
+ * p3_main_part3 of a column that went on past part2
+ * (p3_main_impl.hpp:262-325).  Reads from the workspace the per-level
+ * density, its inverse, 1/dz, the fall-speed factors (rhofacr, rhofaci,
+ * acn), the temperature after part1 (homogeneous freezing uses it) and the
+ * in-cloud mixing ratios of the state left by part2. */
+void p3_column_sed_part3(const Col& c, int nk, Real dt, bool predictNc, const p3o_runtime& rt,
+                         const p3o_tables* tab, Work& w, Err& e) {
+  const Real inv_dt = 1 / dt;
+  const int kdir = -1, ktop = 0, kbot = nk - 1;
+  const bool do_ice_production = rt.do_ice_production != 0;
   const Real* rho = w.rho.data();
   const Real* inv_rho = w.inv_rho.data();
   const Real* inv_dz = w.inv_dz.data();
@@ -1674,6 +1689,40 @@ void p3_column(const Col& c, int nk, Real dt, bool predictNc, bool prescribedCCN
   }
 }
 
+/* One column, in the stage order of p3_main_internal (p3_main_impl.hpp:108-325). */
+void p3_column(const Col& c, int nk, Real dt, bool predictNc, bool prescribedCCN,
+               const p3o_runtime& rt, const p3o_tables* tab, Work& w, Err& e) {
+  if (p3_column_part12(c, nk, dt, predictNc, prescribedCCN, rt, tab, w, e))
+    p3_column_sed_part3(c, nk, dt, predictNc, rt, tab, w, e);
+}
+
+/* Field pointers of column i. */
+Col column_of(const p3o_fields* f, int i, int64_t ld, int64_t li) {
+  Col c;
+  const int64_t o = i * ld, oi = i * li;
+  c.qc = f->qc + o; c.nc = f->nc + o; c.qr = f->qr + o; c.nr = f->nr + o;
+  c.qi = f->qi + o; c.qm = f->qm + o; c.ni = f->ni + o; c.bm = f->bm + o;
+  c.qv = f->qv + o; c.th = f->th + o;
+  c.nc_nuceat_tend = f->nc_nuceat_tend + o; c.nccn = f->nccn + o;
+  c.ni_activated = f->ni_activated + o; c.inv_qc_relvar = f->inv_qc_relvar + o;
+  c.cld_frac_i = f->cld_frac_i + o; c.cld_frac_l = f->cld_frac_l + o;
+  c.cld_frac_r = f->cld_frac_r + o; c.pres = f->pres + o; c.dz = f->dz + o;
+  c.dpres = f->dpres + o; c.inv_exner = f->inv_exner + o; c.qv_prev = f->qv_prev + o;
+  c.t_prev = f->t_prev + o;
+  c.qv2qi_depos_tend = f->qv2qi_depos_tend + o;
+  c.precip_liq_surf = f->precip_liq_surf + i; c.precip_ice_surf = f->precip_ice_surf + i;
+  c.diag_eff_radius_qc = f->diag_eff_radius_qc + o; c.diag_eff_radius_qi = f->diag_eff_radius_qi + o;
+  c.diag_eff_radius_qr = f->diag_eff_radius_qr + o; c.rho_qi = f->rho_qi + o;
+  c.precip_liq_flux = f->precip_liq_flux + oi; c.precip_ice_flux = f->precip_ice_flux + oi;
+  c.precip_total_tend = f->precip_total_tend + o; c.nevapr = f->nevapr + o;
+  c.liq_ice_exchange = f->liq_ice_exchange + o; c.vap_liq_exchange = f->vap_liq_exchange + o;
+  c.vap_ice_exchange = f->vap_ice_exchange + o;
+  return c;
+}
+
+/* The hand-over rows of the staged entry points, [kHandover][ncol][ld]. */
+enum { H_TATM = 0, H_RHO, H_RHOFACR, H_RHOFACI, H_ACN, kHandover };
+
 }  // namespace
 
 extern "C" {
@@ -1720,31 +1769,92 @@ int p3o_main(const p3o_call* call, const p3o_runtime* rt, const p3o_tables* tab,
 #pragma omp for schedule(dynamic, 16)
 #endif
     for (int i = 0; i < ncol; ++i) {
-      Col c;
-      const int64_t o = i * ld, oi = i * li;
-      c.qc = f->qc + o; c.nc = f->nc + o; c.qr = f->qr + o; c.nr = f->nr + o;
-      c.qi = f->qi + o; c.qm = f->qm + o; c.ni = f->ni + o; c.bm = f->bm + o;
-      c.qv = f->qv + o; c.th = f->th + o;
-      c.nc_nuceat_tend = f->nc_nuceat_tend + o; c.nccn = f->nccn + o;
-      c.ni_activated = f->ni_activated + o; c.inv_qc_relvar = f->inv_qc_relvar + o;
-      c.cld_frac_i = f->cld_frac_i + o; c.cld_frac_l = f->cld_frac_l + o;
-      c.cld_frac_r = f->cld_frac_r + o; c.pres = f->pres + o; c.dz = f->dz + o;
-      c.dpres = f->dpres + o; c.inv_exner = f->inv_exner + o; c.qv_prev = f->qv_prev + o;
-      c.t_prev = f->t_prev + o;
-      c.qv2qi_depos_tend = f->qv2qi_depos_tend + o;
-      c.precip_liq_surf = f->precip_liq_surf + i; c.precip_ice_surf = f->precip_ice_surf + i;
-      c.diag_eff_radius_qc = f->diag_eff_radius_qc + o; c.diag_eff_radius_qi = f->diag_eff_radius_qi + o;
-      c.diag_eff_radius_qr = f->diag_eff_radius_qr + o; c.rho_qi = f->rho_qi + o;
-      c.precip_liq_flux = f->precip_liq_flux + oi; c.precip_ice_flux = f->precip_ice_flux + oi;
-      c.precip_total_tend = f->precip_total_tend + o; c.nevapr = f->nevapr + o;
-      c.liq_ice_exchange = f->liq_ice_exchange + o; c.vap_liq_exchange = f->vap_liq_exchange + o;
-      c.vap_ice_exchange = f->vap_ice_exchange + o;
+      const Col c = column_of(f, i, ld, li);
       p3_column(c, nk, call->dt, call->predictNc != 0, call->prescribedCCN != 0, *rt, tab, w, e);
     }
     err |= e.bits;
   }
   const auto t1 = std::chrono::steady_clock::now();
   if (elapsed_us) *elapsed_us = std::chrono::duration<double, std::micro>(t1 - t0).count();
+  return err;
+}
+
+int p3o_main_part12(const p3o_call* call, const p3o_runtime* rt, const p3o_tables* tab, const p3o_fields* f,
+                    double* handover, int32_t* cflag) {
+  const int ncol = call->ncol, nk = call->nlev;
+  const int64_t ld = call->ld, li = call->ld_int;
+  int err = 0;
+#ifdef _OPENMP
+  const int nthr = call->nthreads > 0 ? call->nthreads : omp_get_max_threads();
+#pragma omp parallel num_threads(nthr) reduction(| : err)
+#endif
+  {
+    Work w;
+    w.resize(nk);
+    Err e;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 16)
+#endif
+    for (int i = 0; i < ncol; ++i) {
+      const Col c = column_of(f, i, ld, li);
+      const bool go_on = p3_column_part12(c, nk, call->dt, call->predictNc != 0, call->prescribedCCN != 0, *rt,
+                                          tab, w, e);
+      cflag[i] = go_on ? 1 : 0;
+      if (!go_on) continue;
+      const std::vector<Real>* rows[kHandover] = {&w.T_atm, &w.rho, &w.rhofacr, &w.rhofaci, &w.acn};
+      for (int h = 0; h < kHandover; ++h) {
+        double* dst = handover + (int64_t(h) * ncol + i) * ld;
+        for (int k = 0; k < nk; ++k) dst[k] = (*rows[h])[k];
+      }
+    }
+    err |= e.bits;
+  }
+  return err;
+}
+
+int p3o_main_sed_part3(const p3o_call* call, const p3o_runtime* rt, const p3o_tables* tab, const p3o_fields* f,
+                       const double* handover, const int32_t* cflag) {
+  const int ncol = call->ncol, nk = call->nlev;
+  const int64_t ld = call->ld, li = call->ld_int;
+  int err = 0;
+#ifdef _OPENMP
+  const int nthr = call->nthreads > 0 ? call->nthreads : omp_get_max_threads();
+#pragma omp parallel num_threads(nthr) reduction(| : err)
+#endif
+  {
+    Work w;
+    w.resize(nk);
+    Err e;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 16)
+#endif
+    for (int i = 0; i < ncol; ++i) {
+      if (!cflag[i]) continue;
+      const Col c = column_of(f, i, ld, li);
+      w.resize(nk); /* nothing of the previous column is carried over */
+      std::vector<Real>* rows[kHandover] = {&w.T_atm, &w.rho, &w.rhofacr, &w.rhofaci, &w.acn};
+      for (int h = 0; h < kHandover; ++h) {
+        const double* src = handover + (int64_t(h) * ncol + i) * ld;
+        for (int k = 0; k < nk; ++k) (*rows[h])[k] = src[k];
+      }
+      /* what part1 and part2 leave in the workspace for the later stages
+       * (p3_main_impl_part1.hpp, p3_main_impl_part2.hpp:516-523): 1/rho,
+       * 1/dz and the in-cloud values of the state */
+      for (int k = 0; k < nk; ++k) {
+        w.inv_rho[k] = 1 / w.rho[k];
+        w.inv_dz[k] = 1 / c.dz[k];
+        w.inv_cld_frac_l[k] = 1 / c.cld_frac_l[k];
+        w.inv_cld_frac_i[k] = 1 / c.cld_frac_i[k];
+        w.inv_cld_frac_r[k] = 1 / c.cld_frac_r[k];
+        calculate_incloud_mixingratios(c.qc[k], c.qr[k], c.qi[k], c.qm[k], c.nc[k], c.nr[k], c.ni[k], c.bm[k],
+                                       w.inv_cld_frac_l[k], w.inv_cld_frac_i[k], w.inv_cld_frac_r[k],
+                                       w.qc_incld[k], w.qr_incld[k], w.qi_incld[k], w.qm_incld[k],
+                                       w.nc_incld[k], w.nr_incld[k], w.ni_incld[k], w.bm_incld[k]);
+      }
+      p3_column_sed_part3(c, nk, call->dt, call->predictNc != 0, *rt, tab, w, e);
+    }
+    err |= e.bits;
+  }
   return err;
 }
 

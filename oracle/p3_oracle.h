@@ -103,6 +103,19 @@ void p3o_runtime_defaults(p3o_runtime* rt);
 int p3o_main(const p3o_call* call, const p3o_runtime* rt, const p3o_tables* tab,
              const p3o_fields* f, double* elapsed_us);
 
+/* The step in two stages, for stage-by-stage parity checks.
+ * p3o_main_part12 runs p3_main_init, part1 and part2 in place and writes,
+ * for every column that goes on (cflag[i] = 1; 0 after an early exit), the
+ * hand-over the later stages read: rows [5][ncol][ld] of the temperature
+ * after part1, the density, rhofacr, rhofaci and acn.  p3o_main_sed_part3
+ * runs sedimentation, homogeneous freezing and part3 in place on the columns
+ * with cflag[i] = 1, from the given state and hand-over.  Both stages in a
+ * row give exactly p3o_main.  Return the OR of error bits. */
+int p3o_main_part12(const p3o_call* call, const p3o_runtime* rt, const p3o_tables* tab,
+                    const p3o_fields* f, double* handover, int32_t* cflag);
+int p3o_main_sed_part3(const p3o_call* call, const p3o_runtime* rt, const p3o_tables* tab,
+                       const p3o_fields* f, const double* handover, const int32_t* cflag);
+
 /* Single-function entry points used by the invariant tests. */
 void p3o_calc_first_order_upwind_step(int nk, int k_bot, int k_top, int kdir,
                                       double dt_sub, const double* rho,

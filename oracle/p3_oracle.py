@@ -59,6 +59,12 @@ def load():
         lib.p3o_runtime_defaults.argtypes = [C.POINTER(Runtime)]
         lib.p3o_main.argtypes = [C.POINTER(Call), C.POINTER(Runtime), C.POINTER(Tables), C.POINTER(Fields), dp]
         lib.p3o_main.restype = C.c_int
+        lib.p3o_main_part12.argtypes = [C.POINTER(Call), C.POINTER(Runtime), C.POINTER(Tables), C.POINTER(Fields),
+                                        dp, C.POINTER(C.c_int32)]
+        lib.p3o_main_part12.restype = C.c_int
+        lib.p3o_main_sed_part3.argtypes = [C.POINTER(Call), C.POINTER(Runtime), C.POINTER(Tables),
+                                           C.POINTER(Fields), dp, C.POINTER(C.c_int32)]
+        lib.p3o_main_sed_part3.restype = C.c_int
         lib.p3o_calc_first_order_upwind_step.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                                          dp, dp, dp, C.c_int, C.POINTER(dp),
                                                          C.POINTER(dp), C.POINTER(dp)]
@@ -120,3 +126,49 @@ def p3_main(state: Dict[str, np.ndarray], tables: Dict[str, np.ndarray], dt: flo
     err = lib.p3o_main(C.byref(call), C.byref(rt), C.byref(t), C.byref(f), C.byref(us))
     del keep
     return err, us.value
+
+
+HANDOVER_ROWS = ["T_atm", "rho", "rhofacr", "rhofaci", "acn"]
+
+
+def _stage_args(state, tables, dt, runtime, predictNc, prescribedCCN, it, nthreads):
+    ncol, nlev = state["qc"].shape
+    for n in ALL:
+        a = state[n]
+        assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"], n
+    f = Fields(*[state[n].ctypes.data for n in ALL])
+    t, keep = make_tables(tables)
+    rt = runtime if runtime is not None else default_runtime()
+    call = Call(ncol, nlev, nlev, nlev + 1, dt, it, int(predictNc), int(prescribedCCN),
+                int(nthreads or os.cpu_count() or 1))
+    return f, t, keep, rt, call
+
+
+def p3_main_part12(state, tables, dt, runtime=None, predictNc=True, prescribedCCN=True, it=1, nthreads=0):
+    """p3_main_init + part1 + part2 in place on ``state``.  Returns (error bits,
+    hand-over (5, ncol, nlev) float64 in HANDOVER_ROWS order, cflag (ncol,)
+    int32: 1 where the column goes on to sedimentation and part3)."""
+    lib = load()
+    ncol, nlev = state["qc"].shape
+    f, t, keep, rt, call = _stage_args(state, tables, dt, runtime, predictNc, prescribedCCN, it, nthreads)
+    ho = np.zeros((len(HANDOVER_ROWS), ncol, nlev))
+    cflag = np.zeros(ncol, dtype=np.int32)
+    err = lib.p3o_main_part12(C.byref(call), C.byref(rt), C.byref(t), C.byref(f),
+                              ho.ctypes.data_as(C.POINTER(C.c_double)), cflag.ctypes.data_as(C.POINTER(C.c_int32)))
+    del keep
+    return err, ho, cflag
+
+
+def p3_main_sed_part3(state, tables, dt, handover, cflag, runtime=None, predictNc=True, prescribedCCN=True, it=1,
+                      nthreads=0):
+    """Sedimentation + homogeneous freezing + part3 in place on ``state`` for
+    the columns with cflag = 1, from ``handover`` ((5, ncol, nlev),
+    HANDOVER_ROWS order).  Returns the error bits."""
+    lib = load()
+    f, t, keep, rt, call = _stage_args(state, tables, dt, runtime, predictNc, prescribedCCN, it, nthreads)
+    ho = np.ascontiguousarray(handover, dtype=np.float64)
+    cf = np.ascontiguousarray(cflag, dtype=np.int32)
+    err = lib.p3o_main_sed_part3(C.byref(call), C.byref(rt), C.byref(t), C.byref(f),
+                                 ho.ctypes.data_as(C.POINTER(C.c_double)), cf.ctypes.data_as(C.POINTER(C.c_int32)))
+    del keep
+    return err

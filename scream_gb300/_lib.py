@@ -20,6 +20,9 @@ P3X_ECUDA = -5
 P3X_ETABLE = -6
 P3X_FP64 = 0
 P3X_FP32_BULK = 1
+P3X_STAGE_PART12 = 1
+P3X_STAGE_SED = 2
+P3X_STAGE_PART3 = 4
 
 STATUS_NAMES = {0: "P3X_OK", -1: "P3X_EINVAL", -2: "P3X_ENOMEM", -3: "P3X_ENUMERIC",
                 -4: "P3X_ETIMEOUT", -5: "P3X_ECUDA", -6: "P3X_ETABLE"}
@@ -156,6 +159,11 @@ PROTOTYPES = {
     "p3x_main_f": (C.c_int, [_dp] * 6 + [C.c_double] + [_dp] * 10 + [_I, _dp, _dp, _I, _I, _I, _I]
                    + [_dp] * 4 + [C.c_bool, C.c_bool] + [_dp] * 13 + [_dp]),
     "p3x_fixed_scratch_info": (C.c_int, [_V, C.POINTER(C.c_int64), C.POINTER(C.c_int32)]),
+    "p3x_handover_bytes": (C.c_int, [_I, C.c_int64, C.POINTER(C.c_int64)]),
+    "p3x_main_stages": (C.c_int, [_V, C.POINTER(Runtime), C.POINTER(PrognosticState),
+                                  C.POINTER(DiagnosticInputs), C.POINTER(DiagnosticOutputs),
+                                  C.POINTER(Infrastructure), C.POINTER(HistoryOnly), _I, _I,
+                                  C.POINTER(Layout), _I, _I, _V, _V]),
     "p3x_batch_create": (C.c_int, [_V, C.POINTER(Runtime), C.POINTER(InstanceDesc), _I, C.POINTER(_V)]),
     "p3x_batch_run": (C.c_int, [_V, _V]),
     "p3x_batch_capture_graph": (C.c_int, [_V, _V]),

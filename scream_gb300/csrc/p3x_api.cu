@@ -294,7 +294,7 @@ uint32_t* work_counters(const dev::Inst& in) {
 }
 
 int launch_kernels(p3x_context* ctx, const p3x_runtime* rt, const dev::Inst& in, cudaStream_t st,
-                   bool marks = true) {
+                   bool marks = true, int parts = kPartK1 | kPartK2 | kPartK3) {
   const dev::RuntimeDev rtd = make_runtime(*rt);
   const int stride = sm_stride_for(in.nlev);
   LaunchSpec ls = fit_spec(in.precision, spec_of(ctx->cfg[in.precision]), stride);
@@ -308,7 +308,7 @@ int launch_kernels(p3x_context* ctx, const p3x_runtime* rt, const dev::Inst& in,
     kp.work = nullptr;
     kp.insts = nullptr;
     kp.wctr = work_counters(in);
-    e = launch_p3<float>(in, kp, ls, ctx->num_sms, st);
+    e = launch_p3<float>(in, kp, ls, ctx->num_sms, st, parts);
   } else {
     dev::KParams<double> kp = make_kparams<double>(ctx, rtd);
     kp.sm_stride = stride;
@@ -316,7 +316,7 @@ int launch_kernels(p3x_context* ctx, const p3x_runtime* rt, const dev::Inst& in,
     kp.work = nullptr;
     kp.insts = nullptr;
     kp.wctr = work_counters(in);
-    e = launch_p3<double>(in, kp, ls, ctx->num_sms, st);
+    e = launch_p3<double>(in, kp, ls, ctx->num_sms, st, parts);
   }
   return cuda_status(e);
 }
@@ -675,6 +675,28 @@ int p3x_main_async(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic
                            infra->prescribedCCN, precision, in);
   if (st) return st;
   return launch_single(ctx, rt, in, static_cast<cudaStream_t>(stream));
+}
+
+int p3x_handover_bytes(int32_t nj, int64_t ld, int64_t* bytes) {
+  if (nj < 0 || ld <= 0 || !bytes) return P3X_EINVAL;
+  *bytes = int64_t(dev::scratch_bytes(nj, ld));
+  return P3X_OK;
+}
+
+int p3x_main_stages(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic_state* prog,
+                    const p3x_diagnostic_inputs* din, const p3x_diagnostic_outputs* dout,
+                    const p3x_infrastructure* infra, const p3x_history_only* hist, int32_t nj, int32_t nk,
+                    const p3x_layout* layout, int32_t precision, int32_t stages, void* handover, void* stream) {
+  if (!ctx || !rt || !infra || !valid_runtime(*rt)) return P3X_EINVAL;
+  if (stages <= 0 || (stages & ~(kPartK1 | kPartK2 | kPartK3))) return P3X_EINVAL;
+  dev::Inst in;
+  const int st = fill_inst(prog, din, dout, hist, layout, nj, nk, infra->dt, infra->predictNc,
+                           infra->prescribedCCN, precision, in);
+  if (st) return st;
+  if (in.ncol == 0) return P3X_OK;
+  if (!handover || (reinterpret_cast<uintptr_t>(handover) & 15)) return P3X_EINVAL;
+  bind_scratch(in, static_cast<unsigned char*>(handover));
+  return launch_kernels(ctx, rt, in, static_cast<cudaStream_t>(stream), false, stages);
 }
 
 int p3x_selftest(uint64_t* mismatches) {

@@ -76,15 +76,26 @@ inline cudaError_t launch_p3_part_lanes(const dev::Inst& inst0, const dev::KPara
   }
 }
 
-/* The three column kernels of one step (K1, K2, K3) in order on one stream. */
+/* The column kernels of one step in order on one stream: all three (K1, K2,
+ * K3) by default, or the subset `parts` (kPartK* bits).  K1 zeroes the work
+ * counters; a subset without K1 zeroes them here. */
 template <class TR>
 inline cudaError_t launch_p3(const dev::Inst& inst0, const dev::KParams<TR>& kp, const LaunchSpec& ls,
-                             int num_sms, cudaStream_t stream) {
-  cudaError_t e = launch_p3_part_lanes<TR>(inst0, kp, ls, kPartK1, num_sms, stream);
-  if (e != cudaSuccess) return e;
-  e = launch_p3_part<TR, 32>(inst0, kp, sed_spec(ls), kPartK2, num_sms, stream);
-  if (e != cudaSuccess) return e;
-  return launch_p3_part_lanes<TR>(inst0, kp, ls, kPartK3, num_sms, stream);
+                             int num_sms, cudaStream_t stream, int parts = kPartK1 | kPartK2 | kPartK3) {
+  cudaError_t e = cudaSuccess;
+  if (parts & kPartK1) {
+    e = launch_p3_part_lanes<TR>(inst0, kp, ls, kPartK1, num_sms, stream);
+    if (e != cudaSuccess) return e;
+  } else if (kp.wctr) {
+    e = cudaMemsetAsync(kp.wctr, 0, dev::kWorkCounters * sizeof(uint32_t), stream);
+    if (e != cudaSuccess) return e;
+  }
+  if (parts & kPartK2) {
+    e = launch_p3_part<TR, 32>(inst0, kp, sed_spec(ls), kPartK2, num_sms, stream);
+    if (e != cudaSuccess) return e;
+  }
+  if (parts & kPartK3) e = launch_p3_part_lanes<TR>(inst0, kp, ls, kPartK3, num_sms, stream);
+  return e;
 }
 
 /* (nlev, ncol) column-fastest <-> (ncol, ld) level-contiguous transposes. */

@@ -181,6 +181,39 @@ class P3Context:
         L.check("p3x_main_async", rc)
         return 0.0
 
+    def handover_bytes(self, ncol: int, nlev: int) -> int:
+        n = C.c_int64(0)
+        L.check("p3x_handover_bytes", self.lib.p3x_handover_bytes(int(ncol), int(nlev), C.byref(n)))
+        return n.value
+
+    def allocate_handover(self, ncol: int, nlev: int, device="cuda"):
+        """A zeroed device buffer for :meth:`p3_main_stages` (uint8 tensor)."""
+        return torch.zeros(self.handover_bytes(ncol, nlev), dtype=torch.uint8, device=device)
+
+    @staticmethod
+    def handover_views(buf, ncol: int, nlev: int):
+        """(rows, cflag) views of a hand-over buffer: rows (5, ncol, nlev)
+        float64 (temperature after part1, density, rhofacr, rhofaci, acn),
+        cflag (ncol,) int32."""
+        nd = 5 * ncol * nlev
+        rows = buf[: nd * 8].view(torch.float64).view(5, ncol, nlev)
+        cflag = buf[nd * 8: nd * 8 + ncol * 4].view(torch.int32)
+        return rows, cflag
+
+    def p3_main_stages(self, f: P3Fields, dt: float, stages: int, handover, precision: int = L.P3X_FP64,
+                       runtime: L.Runtime = None, predictNc=True, prescribedCCN=True, it=1, stream=None):
+        """Runs the subset ``stages`` (P3X_STAGE_* bits) of the step's three
+        kernels on ``f`` with the hand-over in ``handover`` (p3x_main_stages),
+        then synchronises and checks the device status."""
+        rt = runtime if runtime is not None else L.default_runtime()
+        infra = L.Infrastructure(dt, it, 1, f.ncol, 1, f.nlev, int(predictNc), int(prescribedCCN), None)
+        rc = self.lib.p3x_main_stages(self.h, C.byref(rt), C.byref(f.prog()), C.byref(f.din()),
+                                      C.byref(f.dout()), C.byref(infra), C.byref(f.hist()), f.ncol, f.nlev,
+                                      C.byref(L.Layout(f.nlev, f.nlev + 1)), precision, int(stages),
+                                      _ptr(handover), _stream_handle(stream))
+        L.check("p3x_main_stages", rc)
+        self.check(stream)
+
     def p3_main_host(self, f: P3Fields, dt: float, precision: int = L.P3X_FP64, runtime: L.Runtime = None,
                      predictNc=True, prescribedCCN=True, it=1, chunk_cols=0) -> float:
         """One P3 step on HOST arrays (``P3Fields.allocate_host``), copies
