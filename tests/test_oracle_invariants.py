@@ -230,3 +230,54 @@ def test_mixed_ic_matches_committed_oracle_fixture(O, tables):
                   "precip_ice_surf", "diag_eff_radius_qc", "diag_eff_radius_qr", "diag_eff_radius_qi"]:
             a, b = st[n], ref[f"p{pn}{pc}_{n}"]
             assert np.allclose(a, b, rtol=1e-9, atol=0.0), (pn, pc, n)
+
+
+# Murphy & Koop (2005), Table C1, "values recommended for checking computer
+# codes" -- the check points the reference's saturation test names
+# (components/eamxx/src/physics/share/tests/physics_saturation_run_and_cmp.cpp:91-101),
+# whose expected values live in a generated baseline file, not in the source.
+# Published to five significant figures: (T in K, over ice?, vapour pressure in Pa as printed).
+MK_TABLE_C1 = [
+    (150.0, True, "6.1061e-6"), (180.0, True, "0.0053975"), (210.0, True, "0.70202"),
+    (240.0, True, "27.272"), (273.16, True, "611.66"),
+    (240.0, False, "37.667"), (273.16, False, "611.66"), (300.0, False, "3536.8"),
+]
+
+
+def _half_unit(printed):
+    """Half a unit in the last printed significant digit."""
+    low = printed.lower()
+    mant = low.split("e")[0]
+    exp = int(low.split("e")[1]) if "e" in low else 0
+    decimals = len(mant.split(".")[1]) if "." in mant else 0
+    return 0.5 * 10.0 ** (exp - decimals)
+
+
+@pytest.mark.parametrize("T,ice,printed", MK_TABLE_C1)
+def test_saturation_matches_published_check_values(O, T, ice, printed):
+    """The oracle's Murphy-Koop vapour pressure rounds to the published
+    five-figure check values (e = qv_sat p / ep_2 at p = 1e5 Pa)."""
+    lib = O.load()
+    ep2 = 18.016 / 28.966
+    e = lib.p3o_qv_sat_dry(T, 1e5, int(ice)) * 1e5 / ep2
+    assert abs(e - float(printed)) <= _half_unit(printed), (T, ice, e, printed)
+
+
+@pytest.mark.parametrize("T,ice,printed", MK_TABLE_C1)
+def test_saturation_table_matches_published_check_values(built, T, ice, printed):
+    """The FP32-bulk form's tabulated vapour pressure (cubic per 1/64 K) at
+    the same check points."""
+    import ctypes as C
+    from scream_gb300 import _lib as L
+    lib = L.load()
+    n, t0, inv_h = C.c_int32(0), C.c_double(0), C.c_double(0)
+    assert lib.p3x_saturation_table(None, C.byref(n), C.byref(t0), C.byref(inv_h)) == 0
+    coef = np.zeros(2 * n.value * 4)
+    lib.p3x_saturation_table(coef.ctypes.data_as(C.POINTER(C.c_double)), C.byref(n), C.byref(t0), C.byref(inv_h))
+    x = (T - t0.value) * inv_h.value
+    i = int(np.floor(x))
+    u = x - i
+    row = n.value + i if (ice and T < 273.15) else i
+    c = coef[row * 4: row * 4 + 4]
+    e = c[0] + u * (c[1] + u * (c[2] + u * c[3]))
+    assert abs(e - float(printed)) <= _half_unit(printed), (T, ice, e, printed)
