@@ -49,6 +49,7 @@ extern "C" {
 #define P3X_ETIMEOUT (-4) /* sedimentation substep cap or a bounded wait ran out   */
 #define P3X_ECUDA (-5)    /* a CUDA runtime call failed                            */
 #define P3X_ETABLE (-6)   /* lookup table file missing / malformed / wrong version */
+#define P3X_ERANGE (-7)   /* check_values in fail mode: T outside (173, 323) K      */
 
 /* p3_init info codes (physics/p3/p3_iso_c.f90:43-130 returns 0 or -1..-6). */
 
@@ -322,6 +323,33 @@ int p3x_selftest(uint64_t* mismatches);
  * returns the three durations in ms. */
 int p3x_set_kernel_timing(p3x_context* ctx, int32_t on);
 int p3x_kernel_times(p3x_context* ctx, float* ms3);
+
+/* check_values (physics/p3/impl/p3_check_values_impl.hpp:26-81, called after
+ * part3 at p3_main_impl.hpp:316-323 in the reference's debug builds only): a
+ * range check of every level of every column that went on past part2, T =
+ * th / inv_exner in (173, 323) K and qv in (0, 0.04) kg/kg.  Modes:
+ *   P3X_CHECK_OFF     no check (default; the reference's release build);
+ *   P3X_CHECK_RECORD  out-of-range levels are counted (the reference's debug
+ *                     build, which prints them and goes on);
+ *   P3X_CHECK_FAIL    also, a temperature out of range makes the step
+ *                     return P3X_ERANGE (the reference's debug abort; qv out
+ *                     of range is only counted there too).  Nothing traps.
+ * The mode applies to steps launched after the call, including new batches,
+ * served requests and graphs captured afterwards.  p3x_check_values_report
+ * synchronises `stream`, returns the counts and the smallest (instance,
+ * column, level) of each kind since the previous report (-1 when none;
+ * instance is 0 for single-instance steps), and clears them. */
+#define P3X_CHECK_OFF 0
+#define P3X_CHECK_RECORD 1
+#define P3X_CHECK_FAIL 2
+typedef struct p3x_check_report {
+  int64_t t_out_of_range;  /* levels with T not in (173, 323) K    */
+  int64_t qv_out_of_range; /* levels with qv not in (0, 0.04) kg/kg */
+  int32_t t_first_instance, t_first_column, t_first_level;
+  int32_t qv_first_instance, qv_first_column, qv_first_level;
+} p3x_check_report;
+int p3x_set_check_values(p3x_context* ctx, int32_t mode);
+int p3x_check_values_report(p3x_context* ctx, void* stream, p3x_check_report* out);
 
 /* Synchronises `stream`, returns and clears the accumulated device status. */
 int p3x_context_check(p3x_context* ctx, void* stream);

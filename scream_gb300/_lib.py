@@ -18,6 +18,10 @@ P3X_ENUMERIC = -3
 P3X_ETIMEOUT = -4
 P3X_ECUDA = -5
 P3X_ETABLE = -6
+P3X_ERANGE = -7
+P3X_CHECK_OFF = 0
+P3X_CHECK_RECORD = 1
+P3X_CHECK_FAIL = 2
 P3X_FP64 = 0
 P3X_FP32_BULK = 1
 P3X_STAGE_PART12 = 1
@@ -25,7 +29,7 @@ P3X_STAGE_SED = 2
 P3X_STAGE_PART3 = 4
 
 STATUS_NAMES = {0: "P3X_OK", -1: "P3X_EINVAL", -2: "P3X_ENOMEM", -3: "P3X_ENUMERIC",
-                -4: "P3X_ETIMEOUT", -5: "P3X_ECUDA", -6: "P3X_ETABLE"}
+                -4: "P3X_ETIMEOUT", -5: "P3X_ECUDA", -6: "P3X_ETABLE", -7: "P3X_ERANGE"}
 
 # field order of the 23 inputs (P3X_F_*)
 INPUT_FIELDS = ["qc", "nc", "qr", "nr", "qi", "qm", "ni", "bm", "qv", "th",
@@ -109,6 +113,15 @@ class InstanceDesc(C.Structure):
                 ("prescribedCCN", C.c_int32), ("precision", C.c_int32)]
 
 
+class CheckReport(C.Structure):
+    _fields_ = [("t_out_of_range", C.c_int64), ("qv_out_of_range", C.c_int64),
+                ("t_first_instance", C.c_int32), ("t_first_column", C.c_int32), ("t_first_level", C.c_int32),
+                ("qv_first_instance", C.c_int32), ("qv_first_column", C.c_int32), ("qv_first_level", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class ServeStats(C.Structure):
     _fields_ = [("completed", C.c_int64), ("rejected", C.c_int64), ("p50_ms", C.c_double),
                 ("p90_ms", C.c_double), ("p99_ms", C.c_double), ("max_ms", C.c_double),
@@ -160,6 +173,8 @@ PROTOTYPES = {
                    + [_dp] * 4 + [C.c_bool, C.c_bool] + [_dp] * 13 + [_dp]),
     "p3x_fixed_scratch_info": (C.c_int, [_V, C.POINTER(C.c_int64), C.POINTER(C.c_int32)]),
     "p3x_handover_bytes": (C.c_int, [_I, C.c_int64, C.POINTER(C.c_int64)]),
+    "p3x_set_check_values": (C.c_int, [_V, _I]),
+    "p3x_check_values_report": (C.c_int, [_V, _V, C.POINTER(CheckReport)]),
     "p3x_main_stages": (C.c_int, [_V, C.POINTER(Runtime), C.POINTER(PrognosticState),
                                   C.POINTER(DiagnosticInputs), C.POINTER(DiagnosticOutputs),
                                   C.POINTER(Infrastructure), C.POINTER(HistoryOnly), _I, _I,

@@ -31,6 +31,9 @@ struct p3x_context {
   float* f_t3slices = nullptr;
   double* d_svp = nullptr; /* FP32-bulk saturation table */
   uint32_t* d_err = nullptr;
+  /* check_values words (dev::kCheckWords) and mode (P3X_CHECK_*) */
+  unsigned long long* d_check = nullptr;
+  int check_mode = 0;
   /* stream-ordered pool of the per-call K1->K2/K3 scratch (memory is kept
    * for reuse; released with the context) */
   cudaMemPool_t pool = nullptr;
@@ -69,7 +72,14 @@ int cuda_status(cudaError_t e) {
 int status_from_bits(uint32_t bits) {
   if (bits & dev::kErrNumeric) return P3X_ENUMERIC;
   if (bits & (dev::kErrSubstep | dev::kErrWait)) return P3X_ETIMEOUT;
+  if (bits & dev::kErrRange) return P3X_ERANGE;
   return P3X_OK;
+}
+
+/* check_values words after a reset: counts 0, first keys "none" */
+int reset_check_words(unsigned long long* d, cudaStream_t st) {
+  const unsigned long long init[dev::kCheckWords] = {0ull, 0ull, ~0ull, ~0ull};
+  return cuda_status(cudaMemcpyAsync(d, init, sizeof(init), cudaMemcpyHostToDevice, st));
 }
 
 std::mutex g_tables_mu;
@@ -220,6 +230,8 @@ dev::KParams<double> make_kparams<double>(p3x_context* ctx, const dev::RuntimeDe
   kp.t3slice = ctx->d_t3slices + size_t(rtd.t3_dumjj - 1) * dev::kT3SliceElems;
   kp.rt.svp_tab = ctx->d_svp;
   kp.err = ctx->d_err;
+  kp.check = ctx->check_mode ? ctx->d_check : nullptr;
+  kp.check_fail = ctx->check_mode == P3X_CHECK_FAIL ? 1 : 0;
   return kp;
 }
 template <>
@@ -234,6 +246,8 @@ dev::KParams<float> make_kparams<float>(p3x_context* ctx, const dev::RuntimeDev&
   kp.t3slice = ctx->f_t3slices + size_t(rtd.t3_dumjj - 1) * dev::kT3SliceElems;
   kp.rt.svp_tab = ctx->d_svp;
   kp.err = ctx->d_err;
+  kp.check = ctx->check_mode ? ctx->d_check : nullptr;
+  kp.check_fail = ctx->check_mode == P3X_CHECK_FAIL ? 1 : 0;
   return kp;
 }
 
@@ -575,7 +589,9 @@ int p3x_context_create(const char* table_file, p3x_context** out, int* info) {
     return st;
   }
   if (cudaMalloc(&ctx->d_err, sizeof(uint32_t)) != cudaSuccess ||
-      cudaMemset(ctx->d_err, 0, sizeof(uint32_t)) != cudaSuccess) {
+      cudaMemset(ctx->d_err, 0, sizeof(uint32_t)) != cudaSuccess ||
+      cudaMalloc(&ctx->d_check, dev::kCheckWords * sizeof(unsigned long long)) != cudaSuccess ||
+      reset_check_words(ctx->d_check, nullptr) != P3X_OK || cudaDeviceSynchronize() != cudaSuccess) {
     if (info) *info = P3X_ENOMEM;
     p3x_context_destroy(ctx.release());
     return P3X_ENOMEM;
@@ -618,7 +634,7 @@ int p3x_context_destroy(p3x_context* ctx) {
   if (!ctx) return P3X_EINVAL;
   void* ptrs[] = {ctx->d_ice, ctx->d_coll, ctx->d_vn, ctx->d_vm, ctx->d_revap, ctx->f_ice, ctx->f_coll,
                   ctx->f_vn, ctx->f_vm, ctx->f_revap, ctx->d_t3slices, ctx->f_t3slices, ctx->d_svp, ctx->d_err,
-                  ctx->fstage};
+                  ctx->d_check, ctx->fstage};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (double* p : ctx->fbuf)
@@ -675,6 +691,37 @@ int p3x_main_async(p3x_context* ctx, const p3x_runtime* rt, const p3x_prognostic
                            infra->prescribedCCN, precision, in);
   if (st) return st;
   return launch_single(ctx, rt, in, static_cast<cudaStream_t>(stream));
+}
+
+int p3x_set_check_values(p3x_context* ctx, int32_t mode) {
+  if (!ctx || mode < P3X_CHECK_OFF || mode > P3X_CHECK_FAIL) return P3X_EINVAL;
+  ctx->check_mode = mode;
+  return P3X_OK;
+}
+
+int p3x_check_values_report(p3x_context* ctx, void* stream, p3x_check_report* out) {
+  if (!ctx || !out) return P3X_EINVAL;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned long long w[dev::kCheckWords];
+  P3X_CUDA(cudaMemcpyAsync(w, ctx->d_check, sizeof(w), cudaMemcpyDeviceToHost, st));
+  P3X_CUDA(cudaStreamSynchronize(st));
+  const int rc = reset_check_words(ctx->d_check, st);
+  if (rc) return rc;
+  P3X_CUDA(cudaStreamSynchronize(st));
+  auto unpack = [](unsigned long long key, int32_t& inst, int32_t& col, int32_t& lev) {
+    if (key == ~0ull) {
+      inst = col = lev = -1;
+    } else {
+      inst = int32_t(key >> 40);
+      col = int32_t((key >> 16) & 0xffffffull);
+      lev = int32_t(key & 0xffffull);
+    }
+  };
+  out->t_out_of_range = int64_t(w[dev::kChkTCount]);
+  out->qv_out_of_range = int64_t(w[dev::kChkQvCount]);
+  unpack(w[dev::kChkTFirst], out->t_first_instance, out->t_first_column, out->t_first_level);
+  unpack(w[dev::kChkQvFirst], out->qv_first_instance, out->qv_first_column, out->qv_first_level);
+  return P3X_OK;
 }
 
 int p3x_handover_bytes(int32_t nj, int64_t ld, int64_t* bytes) {

@@ -77,7 +77,19 @@ struct KParams {
   /* kWorkCounters zeroed counters: groups take work items from them as they
    * finish the last ones.  Null: groups stride the list statically. */
   uint32_t* wctr;
+  /* check_values after part3 (null: off): kCheckWords words of CheckWord */
+  unsigned long long* check;
+  int check_fail; /* a temperature out of range also sets kErrRange */
 };
+
+/* check_values (p3_check_values_impl.hpp): counts of levels with T outside
+ * (173, 323) K and with qv outside (0, 0.04), and the smallest packed
+ * (instance, column, level) key of each kind. */
+enum CheckWord { kChkTCount = 0, kChkQvCount, kChkTFirst, kChkQvFirst, kCheckWords };
+__host__ __device__ inline unsigned long long check_key(int inst, int col, int k) {
+  return (static_cast<unsigned long long>(inst) << 40) | (static_cast<unsigned long long>(col) << 16) |
+         static_cast<unsigned long long>(k);
+}
 
 constexpr int kIceTableElems = kDensize * kRimsize * kIsize * kIceCols; /* 12000 */
 constexpr int kT3SliceElems = 3 * 300 * 2;
@@ -1198,7 +1210,25 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
       r.x = v;
     }
   };
+  /* Top and bottom of the three species (p3_find_impl.hpp) in one pass on
+   * the integer pipes.  A species only ever changes the levels from its top
+   * down to its final leading edge, so conversions, flux coefficients and the
+   * FP64 state rebuild are limited to those levels; the levels above the top
+   * and below the leading edge keep their values. */
+  int top_c = 1 << 30, top_r = 1 << 30, top_i = 1 << 30, bot_c = -1, bot_r = -1, bot_i = -1;
   for (int k = lane; k < nk; k += LANES) {
+    if (dge(in.qc[co + k], C::QSMALL)) { top_c = min(top_c, k); bot_c = k; }
+    if (dge(in.qr[co + k], C::QSMALL)) { top_r = min(top_r, k); bot_r = k; }
+    if (dge(in.qi[co + k], C::QSMALL)) { top_i = min(top_i, k); bot_i = k; }
+  }
+  top_c = group_min_int<LANES>(mask, top_c);
+  top_r = group_min_int<LANES>(mask, top_r);
+  top_i = group_min_int<LANES>(mask, top_i);
+  bot_c = group_max_int<LANES>(mask, bot_c);
+  bot_r = group_max_int<LANES>(mask, bot_r);
+  bot_i = group_max_int<LANES>(mask, bot_i);
+  const int k_first = min(top_c, min(top_r, top_i));
+  for (int k = k_first + lane; k < nk; k += LANES) {
     const double coef = C::gravit * rcp_newton(in.dpres[co + k]);
     INVDZf[k] = 1.0f / float(in.dz[co + k]);
     COEF[k] = coef;
@@ -1226,27 +1256,22 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
       r_set(f, k, float(x));
     };
 
-    int my_top = 1 << 30, my_bot = -1;
-    for (int k = lane; k < nk; k += LANES) {
-      const double q = B0[co + k];
-      R01[k] = make_float2(float(q), float(B1[co + k]));
-      CLDf[k] = float(cldp[co + k]);
-      FACf[k] = facp[k];
+    const int k_qxtop = sp == 0 ? top_c : (sp == 1 ? top_r : top_i);
+    int k_qxbot = sp == 0 ? bot_c : (sp == 1 ? bot_r : bot_i);
+    if (k_qxbot < 0) continue; /* species absent (group-uniform) */
+    /* the walk and the rebuild read G one level above the top */
+    for (int k = max(k_qxtop - 1, 0) + lane; k < nk; k += LANES) {
       G01[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (sp == 2) {
-        R23[k] = make_float2(float(B2[co + k]), float(B3[co + k]));
-        G23[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-      }
-      if (dge(q, C::QSMALL)) {
-        my_top = min(my_top, k);
-        my_bot = max(my_bot, k);
+      if (sp == 2) G23[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (k >= k_qxtop) {
+        R01[k] = make_float2(float(B0[co + k]), float(B1[co + k]));
+        CLDf[k] = float(cldp[co + k]);
+        FACf[k] = facp[k];
+        if (sp == 2) R23[k] = make_float2(float(B2[co + k]), float(B3[co + k]));
       }
     }
-    const int k_qxtop = group_min_int<LANES>(mask, my_top);
-    int k_qxbot = group_max_int<LANES>(mask, my_bot);
-    if (k_qxbot < 0) continue; /* species absent (group-uniform) */
     if (sp == 1) {
-      for (int k = lane; k <= nk; k += LANES) PF[k] = make_float2(0.f, 0.f);
+      for (int k = k_qxtop + 1 + lane; k <= nk; k += LANES) PF[k] = make_float2(0.f, 0.f);
     }
     __syncwarp(mask);
 
@@ -1438,15 +1463,17 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
     else if (sp == 1) precip_liq_surf += prt_accum * C::INV_RHO_H2O * inv_dt;
     else precip_ice_surf += prt_accum * C::INV_RHO_H2O * inv_dt;
 
-    /* FP64 state: R_k = B_k + (g / dpres_k) (G_{k-1} - G_k) */
-    for (int k = lane; k < nk; k += LANES) {
+    /* FP64 state: R_k = B_k + (g / dpres_k) (G_{k-1} - G_k), on the levels
+     * from the top to the final leading edge (G is zero elsewhere) */
+    for (int k = k_qxtop + lane; k <= k_qxbot; k += LANES) {
       for (int f = 0; f < nstate; ++f) {
         const double gin = k > 0 ? g_value(f, k - 1) : 0.0;
         Bf[f][co + k] = Bf[f][co + k] + COEF[k] * (gin - g_value(f, k));
       }
     }
     if (sp == 1) {
-      for (int k = lane; k <= nk; k += LANES) in.precip_liq_flux[ci + k] = dfloat_value(PF[k]);
+      /* interfaces above the top stay at part1's zero */
+      for (int k = k_qxtop + 1 + lane; k <= nk; k += LANES) in.precip_liq_flux[ci + k] = dfloat_value(PF[k]);
     }
     __syncwarp(mask);
   }
@@ -1460,7 +1487,8 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
 /* K3: homogeneous freezing and p3_main_part3 of one column that went on past
  * part2. */
 template <class TR, int LANES>
-__device__ void p3_part3(const Inst& in, const int col, const KParams<TR>& kp, const Tabs<TR>& tb) {
+__device__ void p3_part3(const Inst& in, const int col, const KParams<TR>& kp, const Tabs<TR>& tb, const int inst_idx,
+                         uint32_t& err) {
   if (in.cflag[col] == 0) return;
   const RuntimeDev& rt = kp.rt;
   const int lane = threadIdx.x & (LANES - 1);
@@ -1683,6 +1711,23 @@ __device__ void p3_part3(const Inst& in, const int col, const KParams<TR>& kp, c
     in.diag_eff_radius_qr[o] = eff_qr;
     in.diag_eff_radius_qi[o] = eff_qi;
     in.rho_qi[o] = rho_qi;
+    if (kp.check) {
+      /* check_values (p3_check_values_impl.hpp:26-81, called at
+       * p3_main_impl.hpp:316-323 with T = th exner): T must lie in
+       * (173, 323) K and qv in (0, 0.04); the reference traps only on T, and
+       * only when its debug abort is on.  Recorded, never trapped. */
+      const double T = s.th * (1 / inv_exner);
+      const unsigned long long key = check_key(inst_idx, col, k);
+      if (!(dgt(T, 173.0) && dlt(T, 323.0))) {
+        atomicAdd(&kp.check[kChkTCount], 1ull);
+        atomicMin(&kp.check[kChkTFirst], key);
+        if (kp.check_fail) err |= kErrRange;
+      }
+      if (!(dpos(s.qv) && dlt(s.qv, 0.04))) {
+        atomicAdd(&kp.check[kChkQvCount], 1ull);
+        atomicMin(&kp.check[kChkQvFirst], key);
+      }
+    }
   }
 }
 
@@ -1832,8 +1877,9 @@ __global__ void __launch_bounds__(256) p3_part3_kernel(const Inst inst0, const K
   for_each_work<LANES>(kp.wctr ? kp.wctr + 2 : nullptr, kp.nwork, kp.groups_per_block, [&](int w) {
     int col;
     const Inst& in = work_inst(inst0, kp, w, col);
-    p3_part3<TR, LANES>(in, col, kp, tb);
+    p3_part3<TR, LANES>(in, col, kp, tb, kp.work ? kp.work[w].inst : 0, err);
   });
+  if (err) atomicOr(kp.err, err);
 }
 
 }  // namespace dev

@@ -44,7 +44,7 @@ constexpr int kDensize = 5, kRimsize = 4, kIsize = 50, kIceCols = 12, kRcollsize
               kCollCols = 2, kVT1 = 10;
 
 /* status bits accumulated on the device */
-enum : uint32_t { kErrNumeric = 1u, kErrSubstep = 2u, kErrWait = 4u };
+enum : uint32_t { kErrNumeric = 1u, kErrSubstep = 2u, kErrWait = 4u, kErrRange = 8u };
 
 /* Runtime options, P3Runtime (p3/p3_functions.hpp:112-133). */
 struct RuntimeDev {
@@ -1422,8 +1422,15 @@ __device__ __forceinline__ void update_prognostics_bulk(const Rates<float>& r, d
    * nucleation.  The FP64 update reaches this up to a round-off residue
    * (< qsmall, clipped to zero); an FP32 sum of the cancelling terms would
    * leave ~1e-7 of the sources instead.  The same holds for ni and, when
-   * predicted, nc, whose limiters count exactly the update's terms (the nr
-   * limiter counts nc2nr_autoconv where the update adds ncautr). */
+   * predicted, nc, whose limiters count exactly the update's terms.  The nr
+   * limiter (p3_nr_conservation_impl.hpp:12-25) counts nc2nr_autoconv among
+   * the sources where the update (p3_update_prognostics_impl.hpp) adds
+   * ncautr, and no later limiter changes a rain-number rate, so a limited nr
+   * becomes exactly (ncautr - nc2nr_autoconv) dt.  Near the melting level,
+   * where shedding and collection both reach ~1e7 /kg/s, the FP32 sum of the
+   * cancelling terms (~1e10 /kg, FP32 spacing ~1e3) would otherwise leave a
+   * residue of ~1e3 /kg in place of that value, and rain sedimentation turns
+   * it into a different drop size and fall speed. */
   const double Dqc = (wlim & 1) ? -s.qc : f2d(dqc);
   const double Dqr = (wlim & 2) ? -s.qr + f2d((r_lim.qr2qv_evap_tend - r.qr2qv_evap_tend) * dtf) : f2d(dqr);
   const double Dqi = ((wlim & 4) && dge(s.qi, C::QSMALL))
@@ -1448,7 +1455,7 @@ __device__ __forceinline__ void update_prognostics_bulk(const Rates<float>& r, d
   } else {
     s.nc = C::NCCNST * inv_rho;
   }
-  s.nr = s.nr + f2d(dnr);
+  s.nr = (nlim & 2) ? f2d((r.ncautr - r.nc2nr_autoconv_tend) * dtf) : s.nr + f2d(dnr);
 }
 
 }  // namespace dev

@@ -262,6 +262,17 @@ class P3Context:
         L.check("p3x_kernel_times", self.lib.p3x_kernel_times(self.h, ms))
         return [float(x) for x in ms]
 
+    def set_check_values(self, mode: int):
+        """check_values after part3: L.P3X_CHECK_OFF / _RECORD / _FAIL."""
+        L.check("p3x_set_check_values", self.lib.p3x_set_check_values(self.h, int(mode)))
+
+    def check_values_report(self, stream=None) -> dict:
+        """Out-of-range counts and first locations since the last report (cleared)."""
+        rep = L.CheckReport()
+        L.check("p3x_check_values_report",
+                self.lib.p3x_check_values_report(self.h, _stream_handle(stream), C.byref(rep)))
+        return rep.as_dict()
+
     def check(self, stream=None):
         L.check("p3x_context_check", self.lib.p3x_context_check(self.h, _stream_handle(stream)))
 
