@@ -449,6 +449,46 @@ int p3x_column_budgets(const p3x_prognostic_state* prog, const double* dpres,
                        const double* inv_exner, int32_t ncol, int32_t nlev, int64_t ld,
                        double* water_out, double* energy_out, void* stream);
 
+/* Column mass and energy conservation check around the P3 process
+ * (share/property_checks/mass_and_energy_column_conservation_check.cpp):
+ * host-model fields after the process (device pointers; per-level
+ * (ncol, nlev) with leading dimension ld, horiz_winds (ncol, 2, nlev) with
+ * the same ld, per-column (ncol)).  horiz_winds, ps, phis and the fluxes may
+ * be NULL (kinetic energy, phis ps / g and that flux are then left out). */
+typedef struct p3x_conservation_fields {
+  const double *pseudo_density, *T_mid, *qv, *qc, *qi, *qr;
+  const double* horiz_winds;
+  const double *ps, *phis;
+  const double *vapor_flux, *water_flux, *ice_flux, *heat_flux;
+} p3x_conservation_fields;
+
+/* Column totals, device arrays of ncol (either may be NULL):
+ * mass = sum_k (qv+qc+qi+qr) pseudo_density / g (:281-298), energy =
+ * sum_k (cp T + (u^2+v^2)/2 + (Lv+Lf) qv + Lf (qc+qr)) pseudo_density / g
+ * + phis ps / g (:314-347).  Call it before the process (the reference's
+ * compute_current_mass / compute_current_energy).  Asynchronous. */
+int p3x_column_mass_energy(const p3x_conservation_fields* f, int32_t ncol, int32_t nlev, int64_t ld, double* mass,
+                           double* energy, void* stream);
+
+/* The check (:110-208): per column the relative error of the mass against
+ * mass_before + (vapor_flux - water_flux rho_w) dt and of the energy against
+ * energy_before + (vapor_flux (Lv+Lf) - (water_flux - ice_flux) rho_w Lf
+ * + heat_flux) dt, into the caller's device arrays mass_err / energy_err
+ * (ncol each); then the largest of each with its column (the smallest
+ * column among equal maxima) into *out, and pass = both below their
+ * tolerances (the reference driver's defaults are 1e-10 for mass and 1e-14
+ * for energy, atmosphere_driver.cpp:428-429).  Synchronises `stream`;
+ * allocates nothing. */
+typedef struct p3x_conservation_report {
+  double max_mass_err, max_energy_err;
+  int32_t mass_col, energy_col;
+  int32_t pass, pad_;
+} p3x_conservation_report;
+int p3x_conservation_check(p3x_context* ctx, const p3x_conservation_fields* f, const double* mass_before,
+                           const double* energy_before, int32_t ncol, int32_t nlev, int64_t ld, double dt,
+                           double mass_tol, double energy_tol, double* mass_err, double* energy_err,
+                           p3x_conservation_report* out, void* stream);
+
 /* ------------------------------------------------------------------ */
 /* Serving: continuous batching of P3 steps under a memory budget      */
 /* ------------------------------------------------------------------ */
@@ -463,9 +503,24 @@ typedef struct p3x_serve_stats {
   double offered_rate_hz;
   int64_t peak_bytes;
   int32_t peak_inflight;
+  int32_t pad_;
+  /* per size class, ncol in [1,10), [10,100), [100,1000), [1000,10000),
+   * [10000, 65536]: completed requests and latency percentiles */
+  int64_t class_count[5];
+  double class_p50_ms[5], class_p99_ms[5];
+  /* latency / isolated service time of the same request (0 until
+   * p3x_server_calibrate has run) */
+  double slowdown_p50, slowdown_p99;
+  /* bytes copied host -> device (first-step state uploads) and device ->
+   * host (every step's result) */
+  int64_t h2d_bytes, d2h_bytes;
 } p3x_serve_stats;
 
-/* budget_bytes: device memory the server may hold for resident instances.
+/* Requests carry data: an instance's first step uploads its 23 input fields
+ * from page-locked host memory, and every step downloads its result (the 10
+ * prognostic fields and the two surface precipitation rates) to page-locked
+ * host memory before it completes; latency covers both copies.
+ * budget_bytes: device memory the server may hold for resident instances.
  * max_inflight: concurrent steps (one CUDA stream each). */
 int p3x_server_create(p3x_context* ctx, const p3x_runtime* rt, int64_t budget_bytes,
                       int32_t max_inflight, p3x_server** out);
@@ -501,6 +556,30 @@ int p3x_server_read_field(p3x_server* s, int64_t instance_id, int32_t field, dou
                           int64_t n);
 /* Waits until every submitted request has finished. */
 int p3x_server_drain(p3x_server* s, p3x_serve_stats* stats);
+
+/* Measures isolated service times: one request at a time on an otherwise
+ * idle server, first steps (upload included) of fresh instances with ncol in
+ * {1, 8, 64, 512, 4096, 32768, 65536}, both level counts and both precision
+ * forms, best of two.  Later statistics then report the slowdown (latency
+ * over the request's isolated time, log-log interpolated in ncol).
+ * p3x_server_isolated_ms returns that interpolated time.  No counterpart in
+ * the reference. */
+int p3x_server_calibrate(p3x_server* s);
+int p3x_server_isolated_ms(p3x_server* s, int32_t precision, int32_t nlev, int32_t ncol, double* ms);
+
+/* Checkpoint / resume of a resident instance (no counterpart in the
+ * reference's interface; its restart carries the same state, including
+ * qv_prev and T_prev: eamxx_p3_process_interface.cpp:93-94).
+ * export: copies the instance's 23 input fields, [P3X_NUM_INPUTS][ncol][nlev]
+ * in P3X_F_* order (n >= 23 ncol nlev doubles), to host memory; the instance
+ * must be idle (drained).  import: makes instance `instance_id` (which must
+ * not exist) resident with that state; later p3x_server_submit calls step
+ * it, bitwise as if it had never left.  Like an explicit instance after its
+ * last step, an idle imported instance may be evicted when admission needs
+ * its memory. */
+int p3x_server_export_instance(p3x_server* s, int64_t instance_id, double* host_state, int64_t n);
+int p3x_server_import_instance(p3x_server* s, int64_t instance_id, int32_t ncol, int32_t nlev, int32_t precision,
+                               double dt, const double* host_state, int64_t n);
 
 /* Version string of the library build. */
 const char* p3x_version(void);

@@ -122,15 +122,48 @@ class CheckReport(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+CONS_FIELDS = ["pseudo_density", "T_mid", "qv", "qc", "qi", "qr", "horiz_winds", "ps", "phis", "vapor_flux",
+               "water_flux", "ice_flux", "heat_flux"]
+
+
+class ConservationFields(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in CONS_FIELDS]
+
+
+class ConservationReport(C.Structure):
+    _fields_ = [("max_mass_err", C.c_double), ("max_energy_err", C.c_double), ("mass_col", C.c_int32),
+                ("energy_col", C.c_int32), ("pass_", C.c_int32), ("pad_", C.c_int32)]
+
+    def as_dict(self):
+        return {"max_mass_err": self.max_mass_err, "mass_col": self.mass_col,
+                "max_energy_err": self.max_energy_err, "energy_col": self.energy_col, "pass": bool(self.pass_)}
+
+
+SIZE_CLASSES = ["1-9", "10-99", "100-999", "1000-9999", "10000-65536"]
+
+
 class ServeStats(C.Structure):
     _fields_ = [("completed", C.c_int64), ("rejected", C.c_int64), ("p50_ms", C.c_double),
                 ("p90_ms", C.c_double), ("p99_ms", C.c_double), ("max_ms", C.c_double),
                 ("mean_ms", C.c_double), ("wall_s", C.c_double),
                 ("column_levels_per_s", C.c_double), ("offered_rate_hz", C.c_double),
-                ("peak_bytes", C.c_int64), ("peak_inflight", C.c_int32)]
+                ("peak_bytes", C.c_int64), ("peak_inflight", C.c_int32), ("pad_", C.c_int32),
+                ("class_count", C.c_int64 * 5), ("class_p50_ms", C.c_double * 5),
+                ("class_p99_ms", C.c_double * 5), ("slowdown_p50", C.c_double), ("slowdown_p99", C.c_double),
+                ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {}
+        for k, _ in self._fields_:
+            if k == "pad_":
+                continue
+            v = getattr(self, k)
+            d[k] = list(v) if k.startswith("class_") else v
+        d["by_size_class"] = {c: {"count": d["class_count"][i], "p50_ms": d["class_p50_ms"][i],
+                                  "p99_ms": d["class_p99_ms"][i]} for i, c in enumerate(SIZE_CLASSES)}
+        for k in ("class_count", "class_p50_ms", "class_p99_ms"):
+            del d[k]
+        return d
 
 
 # name -> (restype, argtypes)
@@ -186,6 +219,10 @@ PROTOTYPES = {
     "p3x_batch_destroy": (C.c_int, [_V]),
     "p3x_autotune_batch": (C.c_int, [_V, _V, _I, C.POINTER(LaunchConfig), C.POINTER(C.c_double)]),
     "p3x_workload_generate": (C.c_int, [_I, C.c_uint64, _I, _I, _I, C.POINTER(_V), C.c_int64]),
+    "p3x_column_mass_energy": (C.c_int, [C.POINTER(ConservationFields), _I, _I, C.c_int64, _V, _V, _V]),
+    "p3x_conservation_check": (C.c_int, [_V, C.POINTER(ConservationFields), _V, _V, _I, _I, C.c_int64,
+                                         C.c_double, C.c_double, C.c_double, _V, _V,
+                                         C.POINTER(ConservationReport), _V]),
     "p3x_column_budgets": (C.c_int, [C.POINTER(PrognosticState), _V, _V, _I, _I, C.c_int64, _V, _V, _V]),
     "p3x_preamble": (C.c_int, [C.POINTER(InterfaceFields), C.POINTER(PrognosticState),
                                C.POINTER(DiagnosticInputs), _I, _I, C.POINTER(Layout), _V]),
@@ -198,6 +235,10 @@ PROTOTYPES = {
     "p3x_server_run_poisson": (C.c_int, [_V, C.c_double, _I, _I, C.c_uint64, C.POINTER(ServeStats)]),
     "p3x_server_read_field": (C.c_int, [_V, C.c_int64, _I, _dp, C.c_int64]),
     "p3x_server_drain": (C.c_int, [_V, C.POINTER(ServeStats)]),
+    "p3x_server_calibrate": (C.c_int, [_V]),
+    "p3x_server_isolated_ms": (C.c_int, [_V, _I, _I, _I, _dp]),
+    "p3x_server_export_instance": (C.c_int, [_V, C.c_int64, _dp, C.c_int64]),
+    "p3x_server_import_instance": (C.c_int, [_V, C.c_int64, _I, _I, _I, C.c_double, _dp, C.c_int64]),
 }
 
 _lib = None

@@ -34,6 +34,8 @@ struct p3x_context {
   /* check_values words (dev::kCheckWords) and mode (P3X_CHECK_*) */
   unsigned long long* d_check = nullptr;
   int check_mode = 0;
+  /* conservation check: {max mass err, column, max energy err, column} */
+  double* d_maxloc = nullptr;
   /* stream-ordered pool of the per-call K1->K2/K3 scratch (memory is kept
    * for reuse; released with the context) */
   cudaMemPool_t pool = nullptr;
@@ -591,6 +593,7 @@ int p3x_context_create(const char* table_file, p3x_context** out, int* info) {
   if (cudaMalloc(&ctx->d_err, sizeof(uint32_t)) != cudaSuccess ||
       cudaMemset(ctx->d_err, 0, sizeof(uint32_t)) != cudaSuccess ||
       cudaMalloc(&ctx->d_check, dev::kCheckWords * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc(&ctx->d_maxloc, 4 * sizeof(double)) != cudaSuccess ||
       reset_check_words(ctx->d_check, nullptr) != P3X_OK || cudaDeviceSynchronize() != cudaSuccess) {
     if (info) *info = P3X_ENOMEM;
     p3x_context_destroy(ctx.release());
@@ -634,7 +637,7 @@ int p3x_context_destroy(p3x_context* ctx) {
   if (!ctx) return P3X_EINVAL;
   void* ptrs[] = {ctx->d_ice, ctx->d_coll, ctx->d_vn, ctx->d_vm, ctx->d_revap, ctx->f_ice, ctx->f_coll,
                   ctx->f_vn, ctx->f_vm, ctx->f_revap, ctx->d_t3slices, ctx->f_t3slices, ctx->d_svp, ctx->d_err,
-                  ctx->d_check, ctx->fstage};
+                  ctx->d_check, ctx->d_maxloc, ctx->fstage};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (double* p : ctx->fbuf)
@@ -1131,6 +1134,58 @@ int p3x_postamble(const p3x_interface_fields* f, const p3x_prognostic_state* pro
 int p3x_workload_generate(int32_t kind, uint64_t seed, int32_t col0, int32_t ncol, int32_t nlev,
                           double* const* fields, int64_t ld) {
   return workload_generate(kind, seed, col0, ncol, nlev, fields, ld);
+}
+
+static int cons_ptrs(const p3x_conservation_fields* f, p3x::ConsPtrs& p) {
+  if (!f || !f->pseudo_density || !f->T_mid || !f->qv || !f->qc || !f->qi || !f->qr) return P3X_EINVAL;
+  p = p3x::ConsPtrs{};
+  p.pd = f->pseudo_density; p.T = f->T_mid; p.qv = f->qv; p.qc = f->qc; p.qi = f->qi; p.qr = f->qr;
+  p.winds = f->horiz_winds; p.ps = f->ps; p.phis = f->phis;
+  p.vapor_flux = f->vapor_flux; p.water_flux = f->water_flux; p.ice_flux = f->ice_flux; p.heat_flux = f->heat_flux;
+  return P3X_OK;
+}
+
+int p3x_column_mass_energy(const p3x_conservation_fields* f, int32_t ncol, int32_t nlev, int64_t ld, double* mass,
+                           double* energy, void* stream) {
+  if (ncol < 0 || nlev <= 0 || (!mass && !energy)) return P3X_EINVAL;
+  if (ld <= 0) ld = nlev;
+  if (ld < nlev) return P3X_EINVAL;
+  p3x::ConsPtrs p;
+  const int st = cons_ptrs(f, p);
+  if (st) return st;
+  p.mass = mass;
+  p.energy = energy;
+  return cuda_status(p3x::launch_conservation(p, ncol, nlev, ld, 0.0, nullptr, static_cast<cudaStream_t>(stream)));
+}
+
+int p3x_conservation_check(p3x_context* ctx, const p3x_conservation_fields* f, const double* mass_before,
+                           const double* energy_before, int32_t ncol, int32_t nlev, int64_t ld, double dt,
+                           double mass_tol, double energy_tol, double* mass_err, double* energy_err,
+                           p3x_conservation_report* out, void* stream) {
+  if (!ctx || !mass_before || !energy_before || !mass_err || !energy_err || !out || ncol <= 0 || nlev <= 0 ||
+      !(dt > 0))
+    return P3X_EINVAL;
+  if (ld <= 0) ld = nlev;
+  if (ld < nlev) return P3X_EINVAL;
+  p3x::ConsPtrs p;
+  const int st = cons_ptrs(f, p);
+  if (st) return st;
+  p.mass_before = mass_before;
+  p.energy_before = energy_before;
+  p.mass_err = mass_err;
+  p.energy_err = energy_err;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  P3X_CUDA(p3x::launch_conservation(p, ncol, nlev, ld, dt, ctx->d_maxloc, s));
+  double h[4];
+  P3X_CUDA(cudaMemcpyAsync(h, ctx->d_maxloc, sizeof(h), cudaMemcpyDeviceToHost, s));
+  P3X_CUDA(cudaStreamSynchronize(s));
+  out->max_mass_err = h[0];
+  out->mass_col = int32_t(h[1]);
+  out->max_energy_err = h[2];
+  out->energy_col = int32_t(h[3]);
+  out->pass = (h[0] < mass_tol && h[2] < energy_tol) ? 1 : 0;
+  out->pad_ = 0;
+  return P3X_OK;
 }
 
 int p3x_column_budgets(const p3x_prognostic_state* prog, const double* dpres, const double* inv_exner,

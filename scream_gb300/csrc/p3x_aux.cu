@@ -70,7 +70,99 @@ __global__ void column_budgets(const double* __restrict__ qv, const double* __re
   }
 }
 
+/* Column totals of the mass and energy conservation check
+ * (share/property_checks/mass_and_energy_column_conservation_check.cpp:281-298
+ * compute_total_mass_on_column, :314-347 compute_total_energy_on_column),
+ * one warp per column; with the totals before the process, also the relative
+ * errors against the totals expected from the boundary fluxes (:140-200,
+ * :300-312, :349-363).  Kinetic energy is included when winds are given,
+ * phis ps / g when both are given. */
+__global__ void conservation_kernel(ConsPtrs p, int ncol, int nlev, int64_t ld, double dt) {
+  constexpr double g = 9.80616, cp = 1004.64, Lv = 2501000.0, Lf = 333700.0, rho_w = 1000.0;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= ncol) return;
+  const int64_t o = int64_t(warp) * ld;
+  double m = 0, e = 0;
+  for (int k = lane; k < nlev; k += 32) {
+    const double pd = p.pd[o + k];
+    m += (p.qv[o + k] + p.qc[o + k] + p.qi[o + k] + p.qr[o + k]) * pd / g;
+    double ke = 0;
+    if (p.winds) {
+      const double u = p.winds[int64_t(warp) * 2 * ld + k], v = p.winds[int64_t(warp) * 2 * ld + ld + k];
+      ke = 0.5 * (u * u + v * v);
+    }
+    e += (p.T[o + k] * cp + ke + (Lv + Lf) * p.qv[o + k] + Lf * (p.qc[o + k] + p.qr[o + k])) * pd / g;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    m += __shfl_xor_sync(0xffffffffu, m, off);
+    e += __shfl_xor_sync(0xffffffffu, e, off);
+  }
+  if (lane != 0) return;
+  if (p.ps && p.phis) e += p.phis[warp] * p.ps[warp] / g;
+  if (p.mass) p.mass[warp] = m;
+  if (p.energy) p.energy[warp] = e;
+  if (p.mass_before) {
+    const double vf = p.vapor_flux ? p.vapor_flux[warp] : 0.0, wf = p.water_flux ? p.water_flux[warp] : 0.0;
+    const double inf = p.ice_flux ? p.ice_flux[warp] : 0.0, hf = p.heat_flux ? p.heat_flux[warp] : 0.0;
+    const double m0 = p.mass_before[warp], e0 = p.energy_before[warp];
+    const double m_exp = m0 + (vf - wf * rho_w) * dt;
+    const double e_exp = e0 + (vf * (Lv + Lf) - (wf - inf) * rho_w * Lf + hf) * dt;
+    p.mass_err[warp] = fabs(m - m_exp) / m0;
+    p.energy_err[warp] = fabs(e - e_exp) / e0;
+  }
+}
+
+/* Largest relative error and its column (the smallest column among equal
+ * maxima), one block; errors are non-negative, so their bit patterns order
+ * as the values (a NaN error sorts above every number). */
+__global__ void maxloc_kernel(const double* __restrict__ a, const double* __restrict__ b, int n,
+                              double* __restrict__ out) {
+  __shared__ unsigned long long best_a[32], best_b[32];
+  __shared__ int loc_a[32], loc_b[32];
+  unsigned long long va = 0, vb = 0;
+  int la = -1, lb = -1;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const unsigned long long xa = __double_as_longlong(a[i]), xb = __double_as_longlong(b[i]);
+    if (la < 0 || xa > va) { va = xa; la = i; }
+    if (lb < 0 || xb > vb) { vb = xb; lb = i; }
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    const unsigned long long oa = __shfl_down_sync(0xffffffffu, va, off), ob = __shfl_down_sync(0xffffffffu, vb, off);
+    const int ola = __shfl_down_sync(0xffffffffu, la, off), olb = __shfl_down_sync(0xffffffffu, lb, off);
+    if (ola >= 0 && (la < 0 || oa > va || (oa == va && ola < la))) { va = oa; la = ola; }
+    if (olb >= 0 && (lb < 0 || ob > vb || (ob == vb && olb < lb))) { vb = ob; lb = olb; }
+  }
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) { best_a[w] = va; loc_a[w] = la; best_b[w] = vb; loc_b[w] = lb; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    va = 0; vb = 0; la = -1; lb = -1;
+    for (int i = 0; i < int(blockDim.x >> 5); ++i) {
+      if (loc_a[i] >= 0 && (la < 0 || best_a[i] > va || (best_a[i] == va && loc_a[i] < la))) { va = best_a[i]; la = loc_a[i]; }
+      if (loc_b[i] >= 0 && (lb < 0 || best_b[i] > vb || (best_b[i] == vb && loc_b[i] < lb))) { vb = best_b[i]; lb = loc_b[i]; }
+    }
+    out[0] = __longlong_as_double(va);
+    out[1] = double(la);
+    out[2] = __longlong_as_double(vb);
+    out[3] = double(lb);
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_conservation(const ConsPtrs& p, int ncol, int nlev, int64_t ld, double dt, double* maxloc4,
+                                cudaStream_t st) {
+  if (ncol <= 0) return cudaSuccess;
+  const int threads = 256;
+  const long long blocks = (int64_t(ncol) * 32 + threads - 1) / threads;
+  conservation_kernel<<<unsigned(blocks), threads, 0, st>>>(p, ncol, nlev, ld, dt);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || !maxloc4) return e;
+  maxloc_kernel<<<1, 1024, 0, st>>>(p.mass_err, p.energy_err, ncol, maxloc4);
+  return cudaGetLastError();
+}
 
 __global__ void postamble_kernel(const dev::Inst* __restrict__ insts, const dev::WorkItem* __restrict__ work,
                                  int nwork) {

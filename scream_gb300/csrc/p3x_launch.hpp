@@ -132,6 +132,21 @@ cudaError_t launch_interface(const InterfacePtrs& p, int ncol, int nlev, int64_t
 
 cudaError_t launch_selftest(unsigned long long* mismatches_d, cudaStream_t st);
 
+/* Fields of the column mass / energy conservation check (device pointers;
+ * per-level (ncol, ld), winds (ncol, 2, ld), per-column (ncol)). */
+struct ConsPtrs {
+  const double *pd, *T, *qv, *qc, *qi, *qr, *winds, *ps, *phis;
+  const double *vapor_flux, *water_flux, *ice_flux, *heat_flux;
+  double *mass, *energy;                    /* column totals (may be null)   */
+  const double *mass_before, *energy_before; /* null: totals only            */
+  double *mass_err, *energy_err;            /* relative errors (with before) */
+};
+/* Column totals and, with the totals before, relative errors; with maxloc4
+ * (4 doubles, device), also {max mass err, its column, max energy err, its
+ * column}. */
+cudaError_t launch_conservation(const ConsPtrs& p, int ncol, int nlev, int64_t ld, double dt, double* maxloc4,
+                                cudaStream_t st);
+
 cudaError_t launch_budgets(const double* qv, const double* qc, const double* qr, const double* qi,
                            const double* th, const double* dpres, const double* inv_exner, int ncol,
                            int nlev, int64_t ld, double* water, double* energy, cudaStream_t st);

@@ -27,13 +27,25 @@
  * wait for further requests), that instance is rejected instead of waiting
  * for memory that cannot come free.
  *
- * Instance workloads are column slices of synthetic templates (65536
- * standard-atmosphere columns, RH ~ U(0.3, 1.05), per level count), generated once per
- * server and kept on the device: instance `seed` starts at template column
- * seed mod (65536 - ncol + 1), so a request's data does not cross PCIe on the
- * latency path and the same instance has the same data alone and in a mix.
- * Columns are independent, so an instance's result does not depend on what
- * it was batched with.
+ * Requests carry data.  Instance workloads are column slices of synthetic
+ * templates (65536 standard-atmosphere columns, RH ~ U(0.3, 1.05), per level
+ * count) generated once per server into page-locked HOST memory, as a
+ * client's state would be: instance `seed` starts at template column seed
+ * mod (65536 - ncol + 1).  An instance's first step uploads its 23 input
+ * fields from there on the dispatching slot's stream, and every step
+ * downloads its result (the 10 prognostic fields and the two surface
+ * precipitation rates) into the slot's page-locked result buffer before the
+ * slot's completion event, so both copies lie inside the measured latency.
+ * The same instance has the same data alone and in a mix; columns are
+ * independent, so an instance's result does not depend on what it was
+ * batched with.
+ *
+ * Checkpoint / resume: p3x_server_export_instance copies an idle instance's
+ * 23 input fields (the whole state a later step reads) to the host, and
+ * p3x_server_import_instance makes a resident instance from such a copy, so
+ * a run can stop after step N and continue bitwise from N+1 in another
+ * server (the reference carries the same state across restarts, including
+ * qv_prev / T_prev: eamxx_p3_process_interface.cpp:93-94).
  */
 #include <algorithm>
 #include <chrono>
@@ -87,7 +99,21 @@ struct Slot {
   Inst* d_insts = nullptr;
   WorkItem* d_work = nullptr;
   int cap_insts = 0, cap_work = 0;
+  double* h_out = nullptr; /* page-locked results of the dispatch's requests */
+  size_t cap_out = 0;      /* doubles */
 };
+
+/* One completed request: latency and size (for per-class statistics). */
+struct LatRec {
+  double ms;
+  int32_t ncol, nlev, precision;
+};
+
+/* Calibration grid of isolated service times. */
+constexpr int kCalNcol[] = {1, 8, 64, 512, 4096, 32768, 65536};
+constexpr int kCalPoints = int(sizeof(kCalNcol) / sizeof(kCalNcol[0]));
+constexpr int kSizeClasses = 5; /* ncol in [1,10), [10,100), [100,1000), [1000,10000), [10000, 65536] */
+constexpr int kResultFields = 10; /* prognostic fields downloaded per request, plus two surface rates */
 
 }  // namespace
 
@@ -98,16 +124,21 @@ struct p3x_server {
   int64_t resident = 0, peak_resident = 0;
   int32_t peak_inflight = 0;
   cudaMemPool_t pool = nullptr;
-  double* tmpl[2] = {nullptr, nullptr}; /* nlev 72, 128: [P3X_NUM_INPUTS][65536][nlev] */
+  /* page-locked host templates, nlev 72, 128: [P3X_NUM_INPUTS][65536][nlev] */
+  double* tmpl[2] = {nullptr, nullptr};
   std::vector<Slot> slots;
   std::map<int64_t, Instance> inst;
   std::deque<int64_t> admit_fifo;                 /* instances waiting for memory */
   std::multimap<double, int64_t> future;          /* arrivals not yet due: time -> instance */
   Clock::time_point t0;
-  std::vector<double> lat_ms;
+  std::vector<LatRec> lat;
   int64_t completed = 0, rejected = 0;
   double cl_done = 0;
   double first_arrival = -1, last_done = 0;
+  int64_t h2d_bytes = 0, d2h_bytes = 0;
+  /* isolated service time (ms) [precision][nlev 72/128][kCalNcol], 0 until calibrated */
+  double iso_ms[2][2][kCalPoints] = {};
+  bool calibrated = false;
 };
 
 namespace {
@@ -176,41 +207,57 @@ int template_index(int nlev) { return nlev == 72 ? 0 : (nlev == 128 ? 1 : -1); }
 
 int build_template(p3x_server* s, int which, int nlev) {
   const size_t n = size_t(kTemplateCols) * nlev;
-  std::vector<double> host(size_t(P3X_NUM_INPUTS) * n);
+  SRV_CUDA(cudaMallocHost(&s->tmpl[which], size_t(P3X_NUM_INPUTS) * n * sizeof(double)));
   std::vector<double*> fields(P3X_NUM_INPUTS);
-  for (int f = 0; f < P3X_NUM_INPUTS; ++f) fields[f] = host.data() + size_t(f) * n;
-  const int rc = p3x::workload_generate(0, kTemplateSeed, 0, kTemplateCols, nlev, fields.data(), nlev);
-  if (rc) return rc;
-  SRV_CUDA(cudaMalloc(&s->tmpl[which], host.size() * sizeof(double)));
-  SRV_CUDA(cudaMemcpy(s->tmpl[which], host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice));
-  return P3X_OK;
+  for (int f = 0; f < P3X_NUM_INPUTS; ++f) fields[f] = s->tmpl[which] + size_t(f) * n;
+  return p3x::workload_generate(0, kTemplateSeed, 0, kTemplateCols, nlev, fields.data(), nlev);
 }
 
-/* Takes memory for the instance and copies its initial state (template
- * slice) on stream st.  Host-side budget accounting happened already. */
+/* The 23 input fields of an instance, in P3X_F_* order (device pointers). */
+void input_fields(const Instance& I, double* dst[P3X_NUM_INPUTS]) {
+  double* d[P3X_NUM_INPUTS] = {I.in.qc, I.in.nc, I.in.qr, I.in.nr, I.in.qi, I.in.qm, I.in.ni, I.in.bm,
+                               I.in.qv, I.in.th,
+                               const_cast<double*>(I.in.nc_nuceat_tend), const_cast<double*>(I.in.nccn),
+                               const_cast<double*>(I.in.ni_activated), const_cast<double*>(I.in.inv_qc_relvar),
+                               const_cast<double*>(I.in.cld_frac_i), const_cast<double*>(I.in.cld_frac_l),
+                               const_cast<double*>(I.in.cld_frac_r), const_cast<double*>(I.in.pres),
+                               const_cast<double*>(I.in.dz), const_cast<double*>(I.in.dpres),
+                               const_cast<double*>(I.in.inv_exner), const_cast<double*>(I.in.qv_prev),
+                               const_cast<double*>(I.in.t_prev)};
+  for (int f = 0; f < P3X_NUM_INPUTS; ++f) dst[f] = d[f];
+}
+
+/* Takes memory for the instance and uploads its initial state (the template
+ * slice in page-locked host memory) on stream st.  Host-side budget
+ * accounting happened already. */
 int materialise(p3x_server* s, Instance& I, cudaStream_t st) {
   SRV_CUDA(cudaMallocFromPoolAsync(&I.mem, I.bytes, s->pool, st));
   bind_instance(I);
   const int w = template_index(I.nlev);
   const int64_t c0 = int64_t(I.seed % uint64_t(kTemplateCols - I.ncol + 1));
   const size_t n = size_t(kTemplateCols) * I.nlev;
-  double* dst[P3X_NUM_INPUTS] = {I.in.qc, I.in.nc, I.in.qr, I.in.nr, I.in.qi, I.in.qm, I.in.ni, I.in.bm,
-                                 I.in.qv, I.in.th,
-                                 const_cast<double*>(I.in.nc_nuceat_tend), const_cast<double*>(I.in.nccn),
-                                 const_cast<double*>(I.in.ni_activated), const_cast<double*>(I.in.inv_qc_relvar),
-                                 const_cast<double*>(I.in.cld_frac_i), const_cast<double*>(I.in.cld_frac_l),
-                                 const_cast<double*>(I.in.cld_frac_r), const_cast<double*>(I.in.pres),
-                                 const_cast<double*>(I.in.dz), const_cast<double*>(I.in.dpres),
-                                 const_cast<double*>(I.in.inv_exner), const_cast<double*>(I.in.qv_prev),
-                                 const_cast<double*>(I.in.t_prev)};
+  double* dst[P3X_NUM_INPUTS];
+  input_fields(I, dst);
+  const size_t bytes = size_t(I.ncol) * I.nlev * sizeof(double);
   for (int f = 0; f < P3X_NUM_INPUTS; ++f) {
     const double* src = s->tmpl[w] + size_t(f) * n + size_t(c0) * I.nlev;
-    SRV_CUDA(cudaMemcpyAsync(dst[f], src, size_t(I.ncol) * I.nlev * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    SRV_CUDA(cudaMemcpyAsync(dst[f], src, bytes, cudaMemcpyHostToDevice, st));
   }
+  s->h2d_bytes += int64_t(P3X_NUM_INPUTS) * int64_t(bytes);
   return P3X_OK;
 }
 
-int ensure_capacity(Slot& sl, int ninst, int nwork) {
+/* Doubles of one request's downloaded result. */
+size_t result_doubles(const Instance& I) { return size_t(I.ncol) * (size_t(kResultFields) * I.nlev + 2); }
+
+int ensure_capacity(Slot& sl, int ninst, int nwork, size_t nout) {
+  if (nout > sl.cap_out) {
+    if (sl.h_out) cudaFreeHost(sl.h_out);
+    sl.h_out = nullptr;
+    const size_t cap = std::max(nout, 2 * sl.cap_out);
+    SRV_CUDA(cudaMallocHost(&sl.h_out, cap * sizeof(double)));
+    sl.cap_out = cap;
+  }
   if (ninst > sl.cap_insts) {
     if (sl.h_insts) cudaFreeHost(sl.h_insts);
     if (sl.d_insts) cudaFree(sl.d_insts);
@@ -299,13 +346,15 @@ int dispatch(p3x_server* s, Slot& sl) {
     if (I.admitted && !I.busy && !I.arrivals.empty() && I.precision == prec) ready.push_back({I.arrivals.front(), &I});
   }
   std::sort(ready.begin(), ready.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+  size_t nout = 0;
   for (auto& r : ready) {
     if (!take.empty() && cols + r.second->ncol > kBatchColumnCap) break;
     take.push_back(r.second);
     cols += r.second->ncol;
     nlev_max = std::max(nlev_max, r.second->nlev);
+    nout += result_doubles(*r.second);
   }
-  int rc = ensure_capacity(sl, int(take.size()), cols);
+  int rc = ensure_capacity(sl, int(take.size()), cols, nout);
   if (rc) return rc;
   sl.ids.clear();
   sl.arrivals.clear();
@@ -333,6 +382,21 @@ int dispatch(p3x_server* s, Slot& sl) {
   rc = p3x::launch_work(s->ctx, s->rt, prec, sl.d_insts, sl.d_work, w, nlev_max, nullptr, sl.st);
   if (rc) return rc;
   SRV_CUDA(p3x::launch_postamble(sl.d_insts, sl.d_work, w, sl.st));
+  /* each request's result to the host, before the completion event */
+  double* out = sl.h_out;
+  for (Instance* Ip : take) {
+    const Instance& I = *Ip;
+    const size_t nf = size_t(I.ncol) * I.nlev;
+    const double* src[kResultFields] = {I.in.qc, I.in.nc, I.in.qr, I.in.nr, I.in.qi,
+                                        I.in.qm, I.in.ni, I.in.bm, I.in.qv, I.in.th};
+    for (int f = 0; f < kResultFields; ++f, out += nf)
+      SRV_CUDA(cudaMemcpyAsync(out, src[f], nf * sizeof(double), cudaMemcpyDeviceToHost, sl.st));
+    SRV_CUDA(cudaMemcpyAsync(out, I.in.precip_liq_surf, I.ncol * sizeof(double), cudaMemcpyDeviceToHost, sl.st));
+    out += I.ncol;
+    SRV_CUDA(cudaMemcpyAsync(out, I.in.precip_ice_surf, I.ncol * sizeof(double), cudaMemcpyDeviceToHost, sl.st));
+    out += I.ncol;
+    s->d2h_bytes += int64_t(result_doubles(I) * sizeof(double));
+  }
   SRV_CUDA(cudaEventRecord(sl.ev, sl.st));
   sl.busy = true;
   return P3X_OK;
@@ -342,7 +406,7 @@ int dispatch(p3x_server* s, Slot& sl) {
 int complete(p3x_server* s, Slot& sl, double t) {
   for (size_t i = 0; i < sl.ids.size(); ++i) {
     Instance& I = s->inst.at(sl.ids[i]);
-    s->lat_ms.push_back((t - sl.arrivals[i]) * 1e3);
+    s->lat.push_back(LatRec{(t - sl.arrivals[i]) * 1e3, I.ncol, I.nlev, I.precision});
     s->completed += 1;
     s->cl_done += double(I.ncol) * I.nlev;
     I.busy = false;
@@ -443,27 +507,65 @@ double percentile(std::vector<double> v, double q) {
   return i + 1 < v.size() ? v[i] * (1 - f) + v[i + 1] * f : v[i];
 }
 
+int size_class(int ncol) {
+  int c = 0;
+  for (int lim = 10; c < kSizeClasses - 1 && ncol >= lim; lim *= 10) ++c;
+  return c;
+}
+
+/* Isolated service time of a request, log-log interpolated in ncol on the
+ * calibration grid of its precision and level count. */
+double iso_time(const p3x_server* s, const LatRec& r) {
+  const double* t = s->iso_ms[r.precision][r.nlev == 72 ? 0 : 1];
+  int j = 0;
+  while (j + 2 < kCalPoints && r.ncol > kCalNcol[j + 1]) ++j;
+  const double x0 = std::log(double(kCalNcol[j])), x1 = std::log(double(kCalNcol[j + 1]));
+  const double y0 = std::log(t[j]), y1 = std::log(t[j + 1]);
+  const double w = (std::log(double(r.ncol)) - x0) / (x1 - x0);
+  return std::exp(y0 + w * (y1 - y0));
+}
+
 void fill_stats(p3x_server* s, p3x_serve_stats* st, double offered) {
   if (!st) return;
   std::memset(st, 0, sizeof(*st));
+  std::vector<double> ms;
+  ms.reserve(s->lat.size());
+  for (const LatRec& r : s->lat) ms.push_back(r.ms);
   st->completed = s->completed;
   st->rejected = s->rejected;
-  st->p50_ms = percentile(s->lat_ms, 0.50);
-  st->p90_ms = percentile(s->lat_ms, 0.90);
-  st->p99_ms = percentile(s->lat_ms, 0.99);
-  st->max_ms = s->lat_ms.empty() ? 0 : *std::max_element(s->lat_ms.begin(), s->lat_ms.end());
+  st->p50_ms = percentile(ms, 0.50);
+  st->p90_ms = percentile(ms, 0.90);
+  st->p99_ms = percentile(ms, 0.99);
+  st->max_ms = ms.empty() ? 0 : *std::max_element(ms.begin(), ms.end());
   double sum = 0;
-  for (double v : s->lat_ms) sum += v;
-  st->mean_ms = s->lat_ms.empty() ? 0 : sum / s->lat_ms.size();
+  for (double v : ms) sum += v;
+  st->mean_ms = ms.empty() ? 0 : sum / ms.size();
   st->wall_s = s->first_arrival >= 0 ? s->last_done - s->first_arrival : 0;
   st->column_levels_per_s = st->wall_s > 0 ? s->cl_done / st->wall_s : 0;
   st->offered_rate_hz = offered;
   st->peak_bytes = s->peak_resident;
   st->peak_inflight = s->peak_inflight;
+  std::vector<double> cls[kSizeClasses];
+  for (const LatRec& r : s->lat) cls[size_class(r.ncol)].push_back(r.ms);
+  for (int c = 0; c < kSizeClasses; ++c) {
+    st->class_count[c] = int64_t(cls[c].size());
+    st->class_p50_ms[c] = percentile(cls[c], 0.50);
+    st->class_p99_ms[c] = percentile(cls[c], 0.99);
+  }
+  if (s->calibrated && !s->lat.empty()) {
+    std::vector<double> slow;
+    slow.reserve(s->lat.size());
+    for (const LatRec& r : s->lat) slow.push_back(r.ms / iso_time(s, r));
+    st->slowdown_p50 = percentile(slow, 0.50);
+    st->slowdown_p99 = percentile(slow, 0.99);
+  }
+  st->h2d_bytes = s->h2d_bytes;
+  st->d2h_bytes = s->d2h_bytes;
 }
 
 void reset_stats(p3x_server* s) {
-  s->lat_ms.clear();
+  s->lat.clear();
+  s->h2d_bytes = s->d2h_bytes = 0;
   s->completed = s->rejected = 0;
   s->cl_done = 0;
   s->first_arrival = -1;
@@ -553,11 +655,12 @@ int p3x_server_destroy(p3x_server* s) {
     if (sl.st) cudaStreamDestroy(sl.st);
     if (sl.h_insts) cudaFreeHost(sl.h_insts);
     if (sl.h_work) cudaFreeHost(sl.h_work);
+    if (sl.h_out) cudaFreeHost(sl.h_out);
     if (sl.d_insts) cudaFree(sl.d_insts);
     if (sl.d_work) cudaFree(sl.d_work);
   }
   for (double* t : s->tmpl)
-    if (t) cudaFree(t);
+    if (t) cudaFreeHost(t);
   if (s->pool) cudaMemPoolDestroy(s->pool);
   delete s;
   return P3X_OK;
@@ -602,6 +705,107 @@ int p3x_server_run_poisson(p3x_server* s, double rate_hz, int32_t n_requests, in
   rc = run_loop(s);
   fill_stats(s, stats, rate_hz);
   return rc;
+}
+
+int p3x_server_calibrate(p3x_server* s) {
+  if (!s) return P3X_EINVAL;
+  int rc = run_loop(s);
+  if (rc) return rc;
+  const std::vector<LatRec> keep_lat = s->lat;
+  const int64_t keep_done = s->completed, keep_h2d = s->h2d_bytes, keep_d2h = s->d2h_bytes;
+  const double keep_cl = s->cl_done, keep_first = s->first_arrival, keep_last = s->last_done;
+  int64_t id = -1;
+  for (int prec = 0; prec < 2; ++prec)
+    for (int l = 0; l < 2; ++l)
+      for (int j = 0; j < kCalPoints; ++j) {
+        const int nlev = l == 0 ? 72 : 128;
+        const int64_t bytes = int64_t(instance_bytes(kCalNcol[j], nlev));
+        double best = 1e300;
+        if (bytes > s->budget) {
+          s->iso_ms[prec][l][j] = j > 0 ? s->iso_ms[prec][l][j - 1] : 1.0;
+          continue;
+        }
+        /* a fresh instance each time: the first step includes its upload, as
+         * a session's first request does; the best of two */
+        for (int rep = 0; rep < 2; ++rep, --id) {
+          s->lat.clear();
+          rc = enqueue(s, id, kCalNcol[j], nlev, prec, 1, kTemplateSeed + uint64_t(j), 300.0, now_s(s), true);
+          if (rc) return rc;
+          rc = run_loop(s);
+          if (rc) return rc;
+          if (!s->lat.empty()) best = std::min(best, s->lat.back().ms);
+        }
+        s->iso_ms[prec][l][j] = best < 1e300 ? best : 1.0;
+      }
+  s->lat = keep_lat;
+  s->completed = keep_done;
+  s->h2d_bytes = keep_h2d;
+  s->d2h_bytes = keep_d2h;
+  s->cl_done = keep_cl;
+  s->first_arrival = keep_first;
+  s->last_done = keep_last;
+  s->calibrated = true;
+  return P3X_OK;
+}
+
+int p3x_server_isolated_ms(p3x_server* s, int32_t precision, int32_t nlev, int32_t ncol, double* ms) {
+  if (!s || !ms || !s->calibrated || (precision != P3X_FP64 && precision != P3X_FP32_BULK) ||
+      template_index(nlev) < 0 || ncol < 1 || ncol > kTemplateCols)
+    return P3X_EINVAL;
+  *ms = iso_time(s, LatRec{0.0, ncol, nlev, precision});
+  return P3X_OK;
+}
+
+int p3x_server_export_instance(p3x_server* s, int64_t instance_id, double* host_state, int64_t n) {
+  if (!s || !host_state) return P3X_EINVAL;
+  auto it = s->inst.find(instance_id);
+  if (it == s->inst.end() || !it->second.mem || it->second.busy || !it->second.arrivals.empty())
+    return P3X_EINVAL;
+  const Instance& I = it->second;
+  const size_t nf = size_t(I.ncol) * I.nlev;
+  if (n < int64_t(P3X_NUM_INPUTS * nf)) return P3X_EINVAL;
+  double* src[P3X_NUM_INPUTS];
+  input_fields(I, src);
+  SRV_CUDA(cudaDeviceSynchronize());
+  for (int f = 0; f < P3X_NUM_INPUTS; ++f)
+    SRV_CUDA(cudaMemcpy(host_state + size_t(f) * nf, src[f], nf * sizeof(double), cudaMemcpyDeviceToHost));
+  return P3X_OK;
+}
+
+int p3x_server_import_instance(p3x_server* s, int64_t instance_id, int32_t ncol, int32_t nlev, int32_t precision,
+                               double dt, const double* host_state, int64_t n) {
+  if (!s || !host_state || ncol <= 0 || ncol > kTemplateCols || template_index(nlev) < 0 || !(dt > 0) ||
+      (precision != P3X_FP64 && precision != P3X_FP32_BULK))
+    return P3X_EINVAL;
+  const size_t nf = size_t(ncol) * nlev;
+  if (n < int64_t(P3X_NUM_INPUTS * nf)) return P3X_EINVAL;
+  if (s->inst.count(instance_id)) return P3X_EINVAL;
+  int rc = run_loop(s);
+  if (rc) return rc;
+  const size_t bytes = instance_bytes(ncol, nlev);
+  if (int64_t(bytes) > s->budget || !evict_for(s, int64_t(bytes))) return P3X_ENOMEM;
+  Instance I;
+  I.id = instance_id;
+  I.ncol = ncol;
+  I.nlev = nlev;
+  I.precision = precision;
+  I.total_steps = 0; /* evictable when idle, like an explicit instance after its last step */
+  I.dt = dt;
+  I.bytes = bytes;
+  I.admitted = true;
+  cudaStream_t st = s->slots[0].st;
+  SRV_CUDA(cudaMallocFromPoolAsync(&I.mem, I.bytes, s->pool, st));
+  bind_instance(I);
+  double* dst[P3X_NUM_INPUTS];
+  input_fields(I, dst);
+  for (int f = 0; f < P3X_NUM_INPUTS; ++f)
+    SRV_CUDA(cudaMemcpyAsync(dst[f], host_state + size_t(f) * nf, nf * sizeof(double), cudaMemcpyHostToDevice, st));
+  SRV_CUDA(cudaStreamSynchronize(st));
+  s->resident += int64_t(bytes);
+  s->peak_resident = std::max(s->peak_resident, s->resident);
+  I.retired_at = now_s(s);
+  s->inst.emplace(instance_id, std::move(I));
+  return P3X_OK;
 }
 
 int p3x_server_read_field(p3x_server* s, int64_t instance_id, int32_t field, double* host_out, int64_t n) {

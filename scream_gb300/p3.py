@@ -252,6 +252,36 @@ class P3Context:
                                                         C.byref(L.Layout(f.nlev, f.nlev + 1)), float(dt),
                                                         _stream_handle(stream)))
 
+    def _cons(self, fields: Dict[str, "torch.Tensor"]):
+        return L.ConservationFields(*[(_ptr(fields[n]) if fields.get(n) is not None else None)
+                                      for n in L.CONS_FIELDS])
+
+    def column_mass_energy(self, fields: Dict[str, "torch.Tensor"], stream=None):
+        """Column mass and energy of host-model fields (the conservation
+        check's totals before a process); device tensors of shape (ncol,)."""
+        ncol, nlev = fields["qv"].shape
+        m = torch.zeros(ncol, dtype=torch.float64, device=fields["qv"].device)
+        e = torch.zeros_like(m)
+        cf = self._cons(fields)
+        L.check("p3x_column_mass_energy", self.lib.p3x_column_mass_energy(
+            C.byref(cf), ncol, nlev, nlev, _ptr(m), _ptr(e), _stream_handle(stream)))
+        return m, e
+
+    def conservation_check(self, fields: Dict[str, "torch.Tensor"], mass_before, energy_before, dt: float,
+                           mass_tol: float = 1e-10, energy_tol: float = 1e-14, stream=None):
+        """Mass and energy conservation check after a process: (report dict,
+        per-column relative mass errors, per-column relative energy errors).
+        Default tolerances are the reference driver's."""
+        ncol, nlev = fields["qv"].shape
+        me = torch.zeros(ncol, dtype=torch.float64, device=fields["qv"].device)
+        ee = torch.zeros_like(me)
+        rep = L.ConservationReport()
+        cf = self._cons(fields)
+        L.check("p3x_conservation_check", self.lib.p3x_conservation_check(
+            self.h, C.byref(cf), _ptr(mass_before), _ptr(energy_before), ncol, nlev, nlev, float(dt),
+            float(mass_tol), float(energy_tol), _ptr(me), _ptr(ee), C.byref(rep), _stream_handle(stream)))
+        return rep.as_dict(), me, ee
+
     def set_kernel_timing(self, on: bool = True):
         L.check("p3x_set_kernel_timing", self.lib.p3x_set_kernel_timing(self.h, int(bool(on))))
 
@@ -369,6 +399,31 @@ class P3Server:
         L.check("p3x_server_run_poisson", self.ctx.lib.p3x_server_run_poisson(
             self.h, float(rate_hz), int(n_sessions), int(max_ncol), int(seed), C.byref(st)))
         return st.as_dict()
+
+    def calibrate(self):
+        """Isolated service times (p3x_server_calibrate); later stats report slowdowns."""
+        L.check("p3x_server_calibrate", self.ctx.lib.p3x_server_calibrate(self.h))
+
+    def isolated_ms(self, precision: int, nlev: int, ncol: int) -> float:
+        ms = C.c_double(0)
+        L.check("p3x_server_isolated_ms", self.ctx.lib.p3x_server_isolated_ms(
+            self.h, int(precision), int(nlev), int(ncol), C.byref(ms)))
+        return ms.value
+
+    def export_instance(self, instance_id: int, ncol: int, nlev: int) -> np.ndarray:
+        """The instance's 23 input fields, (23, ncol, nlev) float64 (checkpoint)."""
+        out = np.empty((len(L.INPUT_FIELDS), ncol, nlev), dtype=np.float64)
+        L.check("p3x_server_export_instance", self.ctx.lib.p3x_server_export_instance(
+            self.h, int(instance_id), out.ctypes.data_as(C.POINTER(C.c_double)), int(out.size)))
+        return out
+
+    def import_instance(self, instance_id: int, state: np.ndarray, precision: int, dt: float = 300.0):
+        """Makes an instance resident from an exported state (resume)."""
+        st = np.ascontiguousarray(state, dtype=np.float64)
+        _, ncol, nlev = st.shape
+        L.check("p3x_server_import_instance", self.ctx.lib.p3x_server_import_instance(
+            self.h, int(instance_id), int(ncol), int(nlev), int(precision), float(dt),
+            st.ctypes.data_as(C.POINTER(C.c_double)), int(st.size)))
 
     def read_field(self, instance_id: int, field: int, n: int) -> np.ndarray:
         out = np.empty(n, dtype=np.float64)

@@ -120,3 +120,81 @@ def test_preamble_then_postamble_restores_the_wet_state(gpu_ctx):
     for n in SPECIES:
         np.testing.assert_allclose(got[n], inp[n], rtol=1e-15, atol=0, err_msg=n)
     np.testing.assert_allclose(hd["T_atm"].cpu().numpy(), h["T_atm"], rtol=1e-15, err_msg="T_atm")
+
+
+def np_mass_energy(h, s, winds=None, ps=None, phis=None):
+    """compute_total_mass_on_column / compute_total_energy_on_column
+    (mass_and_energy_column_conservation_check.cpp:281-347)."""
+    LV, LF = 2501000.0, 333700.0
+    pd = h["pseudo_density"]
+    m = ((s["qv"] + s["qc"] + s["qi"] + s["qr"]) * pd / G).sum(axis=1)
+    ke = 0.0 if winds is None else 0.5 * (winds[:, 0] ** 2 + winds[:, 1] ** 2)
+    e = ((h["T_atm"] * CP + ke + (LV + LF) * s["qv"] + LF * (s["qc"] + s["qr"])) * pd / G).sum(axis=1)
+    if ps is not None:
+        e = e + phis * ps / G
+    return m, e
+
+
+def _cons_fields(hd, f, extra=None):
+    d = {"pseudo_density": hd["pseudo_density"], "T_mid": hd["T_atm"], "qv": f.t["qv"], "qc": f.t["qc"],
+         "qi": f.t["qi"], "qr": f.t["qr"], "vapor_flux": hd["vapor_flux"], "water_flux": hd["water_flux"],
+         "ice_flux": hd["ice_flux"], "heat_flux": hd["heat_flux"]}
+    d.update(extra or {})
+    return d
+
+
+@pytest.mark.gpu
+def test_conservation_totals_and_maxloc_match_numpy(gpu_ctx):
+    """Column totals (with winds and surface geopotential), relative errors
+    against planted fluxes, and the largest error's column."""
+    import torch
+    import scream_gb300 as p3
+    ncol, nlev, dt = 257, 72, 300.0
+    inp, h = _host_state(ncol, nlev, 5)
+    rng = np.random.default_rng(5)
+    winds = rng.normal(0, 10, (ncol, 2, nlev))
+    ps, phis = rng.uniform(9e4, 1.02e5, ncol), rng.uniform(0, 3e4, ncol)
+    f = p3.P3Fields.from_inputs(inp)
+    hd = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in h.items()}
+    extra = {"horiz_winds": torch.from_numpy(winds).cuda(), "ps": torch.from_numpy(ps).cuda(),
+             "phis": torch.from_numpy(phis).cuda()}
+    m, e = gpu_ctx.column_mass_energy(_cons_fields(hd, f, extra))
+    m_np, e_np = np_mass_energy(h, inp, winds, ps, phis)
+    np.testing.assert_allclose(m.cpu().numpy(), m_np, rtol=1e-13)
+    np.testing.assert_allclose(e.cpu().numpy(), e_np, rtol=1e-13)
+    m0 = m_np * (1 + rng.uniform(-1e-9, 1e-9, ncol))
+    e0 = e_np * (1 + rng.uniform(-1e-9, 1e-9, ncol))
+    m0[101] *= 1 + 3e-6   # the largest mass error
+    e0[17] *= 1 - 5e-7    # the largest energy error
+    rep, me, ee = gpu_ctx.conservation_check(_cons_fields(hd, f, extra), torch.from_numpy(m0).cuda(),
+                                            torch.from_numpy(e0).cuda(), dt, mass_tol=1e-6, energy_tol=1e-6)
+    LV, LF = 2501000.0, 333700.0
+    m_exp = m0 + (h["vapor_flux"] - h["water_flux"] * 1000.0) * dt
+    e_exp = e0 + (h["vapor_flux"] * (LV + LF) - (h["water_flux"] - h["ice_flux"]) * 1000.0 * LF
+                  + h["heat_flux"]) * dt
+    np.testing.assert_allclose(me.cpu().numpy(), np.abs(m_np - m_exp) / m0, rtol=1e-6, atol=1e-15)
+    np.testing.assert_allclose(ee.cpu().numpy(), np.abs(e_np - e_exp) / e0, rtol=1e-6, atol=1e-15)
+    assert rep["mass_col"] == 101 and rep["energy_col"] == 17
+    assert rep["max_mass_err"] == float(me.max()) and not rep["pass"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1])
+def test_process_step_passes_mass_conservation_check(gpu_ctx, precision):
+    """preamble -> p3_main -> postamble (run_impl), then the check with the
+    boundary fluxes the postamble set: column mass closes to round-off
+    (the reference driver's default mass tolerance is 1e-10)."""
+    import torch
+    import scream_gb300 as p3
+    ncol, nlev, dt = 512, 128, 300.0
+    inp, h = _host_state(ncol, nlev, 11)
+    f = p3.P3Fields.from_inputs(inp)
+    hd = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in h.items()}
+    m0, e0 = gpu_ctx.column_mass_energy(_cons_fields(hd, f))
+    gpu_ctx.preamble(hd, f)
+    gpu_ctx.p3_main(f, dt, precision)
+    gpu_ctx.postamble(hd, f, dt)
+    rep, me, ee = gpu_ctx.conservation_check(_cons_fields(hd, f), m0, e0, dt)
+    print("conservation check after one process step, precision", precision, rep)
+    assert rep["max_mass_err"] <= 1e-12, rep
+    assert np.isfinite(rep["max_energy_err"]) and 0 <= rep["energy_col"] < ncol

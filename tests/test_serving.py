@@ -111,3 +111,65 @@ def test_poisson_load_reports_latency(gpu_ctx, server_cls):
         assert st["peak_bytes"] <= 20 * 10**9
     finally:
         srv.close()
+
+
+def test_requests_carry_data_and_report_per_class(gpu_ctx, server_cls):
+    """Every step downloads its result (10 prognostic fields + 2 surface
+    rates) and every session's first step uploads its 23 input fields; the
+    statistics count those bytes, split latency by size class and, after
+    calibration, report slowdowns."""
+    import scream_gb300 as p3
+    srv = server_cls(gpu_ctx, budget_bytes=20 * 10**9, max_inflight=4)
+    try:
+        srv.calibrate()
+        for prec in (p3.P3X_FP64, p3.P3X_FP32_BULK):
+            t_small = srv.isolated_ms(prec, 128, 8)
+            t_big = srv.isolated_ms(prec, 128, 65536)
+            assert 0 < t_small < t_big
+        srv.submit(5, 300, 72, p3.P3X_FP64, total_steps=2, seed=1)
+        srv.submit(5, 300, 72, p3.P3X_FP64, total_steps=2, seed=1)
+        srv.submit(6, 20, 128, p3.P3X_FP32_BULK, total_steps=1, seed=2)
+        st = srv.drain()
+        assert st["completed"] == 3
+        assert st["h2d_bytes"] == 23 * 8 * (300 * 72 + 20 * 128)
+        assert st["d2h_bytes"] == 8 * (2 * 300 * (10 * 72 + 2) + 20 * (10 * 128 + 2))
+        cls = st["by_size_class"]
+        assert cls["10-99"]["count"] == 1 and cls["100-999"]["count"] == 2
+        assert st["slowdown_p50"] > 0
+    finally:
+        srv.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_checkpoint_export_import_resumes_bitwise(gpu_ctx, server_cls, precision):
+    """Step N, export, import into another server, step N+1 .. M: the same
+    bits as M uninterrupted steps."""
+    ncol, nlev, seed, total = 777, 72, 31, 4
+
+    def run(steps, srv, iid=3):
+        for _ in range(steps):
+            srv.submit(iid, ncol, nlev, precision, total_steps=total, seed=seed)
+        srv.drain()
+
+    a = server_cls(gpu_ctx, budget_bytes=4 * 10**9, max_inflight=2)
+    try:
+        run(total, a)
+        ref = read_state(a, 3, ncol, nlev)
+    finally:
+        a.close()
+    b = server_cls(gpu_ctx, budget_bytes=4 * 10**9, max_inflight=2)
+    try:
+        run(2, b)
+        ckpt = b.export_instance(3, ncol, nlev)
+    finally:
+        b.close()
+    c = server_cls(gpu_ctx, budget_bytes=4 * 10**9, max_inflight=2)
+    try:
+        c.import_instance(3, ckpt, precision)
+        np.testing.assert_array_equal(c.export_instance(3, ncol, nlev), ckpt)
+        run(total - 2, c)
+        got = read_state(c, 3, ncol, nlev)
+        for n in ref:
+            assert np.array_equal(got[n], ref[n]), n
+    finally:
+        c.close()
