@@ -181,26 +181,35 @@ __global__ void postamble_kernel(const dev::Inst* __restrict__ insts, const dev:
   }
 }
 
-/* Process-interface preamble and postamble, one thread per column-level
- * (eamxx_p3_process_interface.hpp:63-269; the physics helpers restate
- * share/util/scream_common_physics_functions_impl.hpp:88-426). */
+/* Process-interface preamble and postamble (eamxx_p3_process_interface.hpp:
+ * 63-269; the physics helpers restate
+ * share/util/scream_common_physics_functions_impl.hpp:88-426).  One warp per
+ * column, lanes over its levels (coalesced, no index division).  The
+ * wet <-> dry factor pseudo_density / pseudo_density_dry (or its inverse) is
+ * formed once per level and multiplies the ten mixing ratios, where the
+ * reference divides each of them (x * pd / pdd): one rounding apart, at most
+ * ~2 ulp, for a tenth of the FP64 divisions, which set this kernel's cost
+ * on a part whose FP64 pipe issues a warp instruction every 16 cycles. */
 __global__ void interface_preamble_kernel(InterfacePtrs p, int ncol, int nlev, int64_t ld) {
-  const int64_t n = int64_t(ncol) * nlev;
-  for (int64_t c = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; c < n; c += int64_t(gridDim.x) * blockDim.x) {
-    const int col = int(c / nlev), k = int(c % nlev);
+  const int col = int((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (col >= ncol) return;
+  const double c1 = -1.0 + 1.0 / dev::C::ep_2;
+  const double mincld = 0.0001;
+  for (int k = lane; k < nlev; k += 32) {
     const int64_t o = int64_t(col) * ld + k;
     const double pd = p.pd[o], pdd = p.pdd[o], pmid = p.pmid[o], T = p.T[o];
     const double qv_wet = p.q[8][o];
     /* calculate_dz with the virtual temperature of the wet state */
-    const double c1 = -1.0 + 1.0 / dev::C::ep_2;
     const double Tv = T * (1.0 + c1 * qv_wet);
     p.dz[o] = (dev::C::RD / dev::C::gravit) * pd * Tv / pmid;
-    for (int s = 0; s < 9; ++s) p.q[s][o] = p.q[s][o] * pd / pdd;
-    p.qv_prev[o] = p.qv_prev[o] * pd / pdd;
+    const double wet_to_dry = pd / pdd;
+#pragma unroll
+    for (int s = 0; s < 9; ++s) p.q[s][o] = p.q[s][o] * wet_to_dry;
+    p.qv_prev[o] = p.qv_prev[o] * wet_to_dry;
     const double exner = pow(pmid / dev::C::P0, dev::C::RD * dev::C::INV_CP);
     p.inv_exner[o] = 1.0 / exner;
     p.th[o] = T / exner;
-    const double mincld = 0.0001;
     const double ct = p.cld_t[o];
     const double cl = ct > mincld ? ct : mincld;
     p.cld_l[o] = cl;
@@ -215,44 +224,46 @@ __global__ void interface_preamble_kernel(InterfacePtrs p, int ncol, int nlev, i
 }
 
 __global__ void interface_postamble_kernel(InterfacePtrs p, int ncol, int nlev, int64_t ld, double dt) {
-  const int64_t n = int64_t(ncol) * nlev;
-  for (int64_t c = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; c < n; c += int64_t(gridDim.x) * blockDim.x) {
-    const int col = int(c / nlev), k = int(c % nlev);
+  const int col = int((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (col >= ncol) return;
+  for (int k = lane; k < nlev; k += 32) {
     const int64_t o = int64_t(col) * ld + k;
     const double pd = p.pd[o], pdd = p.pdd[o], pmid = p.pmid[o];
+    const double dry_to_wet = pdd / pd;
     const double T_before = p.T[o];
     const double exner = pow(pmid / dev::C::P0, dev::C::RD * dev::C::INV_CP);
-    double T = (p.th[o] * exner - T_before) * pdd / pd;
+    double T = (p.th[o] * exner - T_before) * dry_to_wet;
     T += T_before;
     p.T[o] = T;
     p.T_prev[o] = T;
-    for (int s = 0; s < 9; ++s) p.q[s][o] = p.q[s][o] * pdd / pd;
+#pragma unroll
+    for (int s = 0; s < 9; ++s) p.q[s][o] = p.q[s][o] * dry_to_wet;
     p.qv_prev[o] = p.q[8][o];
     p.eff_qc[o] *= 1e6;
     p.eff_qi[o] *= 1e6;
     p.eff_qr[o] *= 1e6;
-    if (k == 0) {
-      const double liq = p.liq_surf[col], ice = p.ice_surf[col];
-      if (p.liq_mass) p.liq_mass[col] += liq * dev::C::RHO_H2O * dt;
-      if (p.ice_mass) p.ice_mass[col] += ice * dev::C::RHO_H2O * dt;
-      if (p.vapor_flux) p.vapor_flux[col] = 0.0;
-      if (p.water_flux) p.water_flux[col] = liq + ice;
-      if (p.ice_flux) p.ice_flux[col] = ice;
-      if (p.heat_flux) p.heat_flux[col] = 0.0;
-    }
+  }
+  if (lane == 0) {
+    const double liq = p.liq_surf[col], ice = p.ice_surf[col];
+    if (p.liq_mass) p.liq_mass[col] += liq * dev::C::RHO_H2O * dt;
+    if (p.ice_mass) p.ice_mass[col] += ice * dev::C::RHO_H2O * dt;
+    if (p.vapor_flux) p.vapor_flux[col] = 0.0;
+    if (p.water_flux) p.water_flux[col] = liq + ice;
+    if (p.ice_flux) p.ice_flux[col] = ice;
+    if (p.heat_flux) p.heat_flux[col] = 0.0;
   }
 }
 
 cudaError_t launch_interface(const InterfacePtrs& p, int ncol, int nlev, int64_t ld, bool post, double dt,
                              cudaStream_t st) {
-  const int64_t n = int64_t(ncol) * nlev;
-  if (n <= 0) return cudaSuccess;
-  int blocks = int((n + 255) / 256);
-  if (blocks > 65536) blocks = 65536;
+  if (ncol <= 0 || nlev <= 0) return cudaSuccess;
+  const int threads = 256;
+  const long long blocks = (int64_t(ncol) * 32 + threads - 1) / threads;
   if (post) {
-    interface_postamble_kernel<<<blocks, 256, 0, st>>>(p, ncol, nlev, ld, dt);
+    interface_postamble_kernel<<<unsigned(blocks), threads, 0, st>>>(p, ncol, nlev, ld, dt);
   } else {
-    interface_preamble_kernel<<<blocks, 256, 0, st>>>(p, ncol, nlev, ld);
+    interface_preamble_kernel<<<unsigned(blocks), threads, 0, st>>>(p, ncol, nlev, ld);
   }
   return cudaGetLastError();
 }
