@@ -557,13 +557,13 @@ int p3x_server_read_field(p3x_server* s, int64_t instance_id, int32_t field, dou
 /* Waits until every submitted request has finished. */
 int p3x_server_drain(p3x_server* s, p3x_serve_stats* stats);
 
-/* Measures isolated service times: one request at a time on an otherwise
- * idle server, first steps (upload included) of fresh instances with ncol in
- * {1, 8, 64, 512, 4096, 32768, 65536}, both level counts and both precision
- * forms, best of two.  Later statistics then report the slowdown (latency
- * over the request's isolated time, log-log interpolated in ncol).
- * p3x_server_isolated_ms returns that interpolated time.  No counterpart in
- * the reference. */
+/* Measures isolated service times: two-step sessions alone on an otherwise
+ * idle server, ncol in {1, 8, 64, 512, 4096, 32768, 65536}, both level
+ * counts and both precision forms, best of two; a first step (which uploads
+ * the state) and a later step are timed separately.  Later statistics then
+ * report the slowdown (latency over the isolated time of the same kind of
+ * step, log-log interpolated in ncol).  p3x_server_isolated_ms returns that
+ * interpolated time of a later step.  No counterpart in the reference. */
 int p3x_server_calibrate(p3x_server* s);
 int p3x_server_isolated_ms(p3x_server* s, int32_t precision, int32_t nlev, int32_t ncol, double* ms);
 

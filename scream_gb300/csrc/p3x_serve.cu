@@ -107,6 +107,7 @@ struct Slot {
 struct LatRec {
   double ms;
   int32_t ncol, nlev, precision;
+  int32_t first; /* the instance's first step (it uploads the state) */
 };
 
 /* Calibration grid of isolated service times. */
@@ -136,8 +137,8 @@ struct p3x_server {
   double cl_done = 0;
   double first_arrival = -1, last_done = 0;
   int64_t h2d_bytes = 0, d2h_bytes = 0;
-  /* isolated service time (ms) [precision][nlev 72/128][kCalNcol], 0 until calibrated */
-  double iso_ms[2][2][kCalPoints] = {};
+  /* isolated service time (ms) [first step / later step][precision][nlev 72/128][kCalNcol] */
+  double iso_ms[2][2][2][kCalPoints] = {};
   bool calibrated = false;
 };
 
@@ -406,7 +407,7 @@ int dispatch(p3x_server* s, Slot& sl) {
 int complete(p3x_server* s, Slot& sl, double t) {
   for (size_t i = 0; i < sl.ids.size(); ++i) {
     Instance& I = s->inst.at(sl.ids[i]);
-    s->lat.push_back(LatRec{(t - sl.arrivals[i]) * 1e3, I.ncol, I.nlev, I.precision});
+    s->lat.push_back(LatRec{(t - sl.arrivals[i]) * 1e3, I.ncol, I.nlev, I.precision, I.done == 0 ? 1 : 0});
     s->completed += 1;
     s->cl_done += double(I.ncol) * I.nlev;
     I.busy = false;
@@ -516,7 +517,7 @@ int size_class(int ncol) {
 /* Isolated service time of a request, log-log interpolated in ncol on the
  * calibration grid of its precision and level count. */
 double iso_time(const p3x_server* s, const LatRec& r) {
-  const double* t = s->iso_ms[r.precision][r.nlev == 72 ? 0 : 1];
+  const double* t = s->iso_ms[r.first ? 0 : 1][r.precision][r.nlev == 72 ? 0 : 1];
   int j = 0;
   while (j + 2 < kCalPoints && r.ncol > kCalNcol[j + 1]) ++j;
   const double x0 = std::log(double(kCalNcol[j])), x1 = std::log(double(kCalNcol[j + 1]));
@@ -720,22 +721,24 @@ int p3x_server_calibrate(p3x_server* s) {
       for (int j = 0; j < kCalPoints; ++j) {
         const int nlev = l == 0 ? 72 : 128;
         const int64_t bytes = int64_t(instance_bytes(kCalNcol[j], nlev));
-        double best = 1e300;
+        double best[2] = {1e300, 1e300};
         if (bytes > s->budget) {
-          s->iso_ms[prec][l][j] = j > 0 ? s->iso_ms[prec][l][j - 1] : 1.0;
+          for (int w = 0; w < 2; ++w) s->iso_ms[w][prec][l][j] = j > 0 ? s->iso_ms[w][prec][l][j - 1] : 1.0;
           continue;
         }
-        /* a fresh instance each time: the first step includes its upload, as
-         * a session's first request does; the best of two */
+        /* a fresh two-step session each time, alone on the server: its first
+         * step includes the state upload, as a session's first request does,
+         * and its second (arriving when the first completes) does not; the
+         * best of two sessions */
         for (int rep = 0; rep < 2; ++rep, --id) {
           s->lat.clear();
-          rc = enqueue(s, id, kCalNcol[j], nlev, prec, 1, kTemplateSeed + uint64_t(j), 300.0, now_s(s), true);
+          rc = enqueue(s, id, kCalNcol[j], nlev, prec, 2, kTemplateSeed + uint64_t(j), 300.0, now_s(s), true);
           if (rc) return rc;
           rc = run_loop(s);
           if (rc) return rc;
-          if (!s->lat.empty()) best = std::min(best, s->lat.back().ms);
+          for (const LatRec& r : s->lat) best[r.first ? 0 : 1] = std::min(best[r.first ? 0 : 1], r.ms);
         }
-        s->iso_ms[prec][l][j] = best < 1e300 ? best : 1.0;
+        for (int w = 0; w < 2; ++w) s->iso_ms[w][prec][l][j] = best[w] < 1e300 ? best[w] : 1.0;
       }
   s->lat = keep_lat;
   s->completed = keep_done;
@@ -752,7 +755,7 @@ int p3x_server_isolated_ms(p3x_server* s, int32_t precision, int32_t nlev, int32
   if (!s || !ms || !s->calibrated || (precision != P3X_FP64 && precision != P3X_FP32_BULK) ||
       template_index(nlev) < 0 || ncol < 1 || ncol > kTemplateCols)
     return P3X_EINVAL;
-  *ms = iso_time(s, LatRec{0.0, ncol, nlev, precision});
+  *ms = iso_time(s, LatRec{0.0, ncol, nlev, precision, 0});
   return P3X_OK;
 }
 

@@ -170,8 +170,8 @@ def test_conservation_totals_and_maxloc_match_numpy(gpu_ctx):
     np.testing.assert_allclose(e.cpu().numpy(), e_np, rtol=1e-13)
     m0 = m_np * (1 + rng.uniform(-1e-9, 1e-9, ncol))
     e0 = e_np * (1 + rng.uniform(-1e-9, 1e-9, ncol))
-    m0[101] *= 1 + 3e-6   # the largest mass error
-    e0[17] *= 1 - 5e-7    # the largest energy error
+    m0[101] *= 1 + 0.05   # the largest mass error, far above the flux terms
+    e0[17] *= 1 - 0.05    # the largest energy error
     rep, me, ee = gpu_ctx.conservation_check(_cons_fields(hd, f, extra), torch.from_numpy(m0).cuda(),
                                             torch.from_numpy(e0).cuda(), dt, mass_tol=1e-6, energy_tol=1e-6)
     LV, LF = 2501000.0, 333700.0
