@@ -565,6 +565,17 @@ int p3x_server_drain(p3x_server* s, p3x_serve_stats* stats);
  * step, log-log interpolated in ncol).  p3x_server_isolated_ms returns that
  * interpolated time of a later step.  No counterpart in the reference. */
 int p3x_server_calibrate(p3x_server* s);
+
+/* Dispatch policy (no counterpart in the reference).  on = 1 (the default,
+ * share 0.875): a dispatch holds requests of one size kind (small: at most
+ * 2^19 column-levels); a dispatch of more than 2^20 column-levels takes
+ * large_grid_share of the kernels' resident-block capacity, leaving room on
+ * every SM for other slots; and the last slot (when there is more than one)
+ * takes only small instances, on the highest-priority stream.  Small
+ * requests then wait less behind large steps, at some cost in throughput.
+ * on = 0: every ready request of a precision is packed together, on any
+ * slot, at full capacity.  Waits for running work first. */
+int p3x_server_set_latency_policy(p3x_server* s, int32_t on, double large_grid_share);
 int p3x_server_isolated_ms(p3x_server* s, int32_t precision, int32_t nlev, int32_t ncol, double* ms);
 
 /* Checkpoint / resume of a resident instance (no counterpart in the

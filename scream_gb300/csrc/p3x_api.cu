@@ -1224,11 +1224,13 @@ namespace p3x {
 namespace {
 template <class TR>
 int launch_work_t(p3x_context* ctx, const dev::RuntimeDev& rtd, const LaunchSpec& ls0, const dev::Inst* insts_d,
-                  const dev::WorkItem* work_d, int nwork, int nlev_max, uint32_t* wctr, cudaStream_t st) {
+                  const dev::WorkItem* work_d, int nwork, int nlev_max, uint32_t* wctr, cudaStream_t st,
+                  double grid_frac = 1.0) {
   if (nwork == 0) return P3X_OK;
   const int stride = sm_stride_for(nlev_max);
   const int prec = sizeof(TR) == sizeof(double) ? P3X_FP64 : P3X_FP32_BULK;
-  const LaunchSpec ls = fit_spec(prec, ls0, stride);
+  LaunchSpec ls = fit_spec(prec, ls0, stride);
+  ls.grid_frac = grid_frac;
   if (!spec_fits(prec, ls, stride)) return P3X_EINVAL;
   dev::KParams<TR> kp = make_kparams<TR>(ctx, rtd);
   kp.sm_stride = stride;
@@ -1261,13 +1263,14 @@ void drop_graph(p3x_batch* b) {
 }  // namespace
 
 int launch_work(p3x_context* ctx, const p3x_runtime& rt, int precision, const dev::Inst* insts_d,
-                const dev::WorkItem* work_d, int nwork, int nlev_max, uint32_t* wctr, cudaStream_t st) {
+                const dev::WorkItem* work_d, int nwork, int nlev_max, uint32_t* wctr, cudaStream_t st,
+                double grid_frac) {
   if (!ctx || (precision != P3X_FP64 && precision != P3X_FP32_BULK)) return P3X_EINVAL;
   const dev::RuntimeDev rtd = make_runtime(rt);
   const LaunchSpec ls = spec_of(ctx->cfg[precision]);
   return precision == P3X_FP32_BULK
-             ? launch_work_t<float>(ctx, rtd, ls, insts_d, work_d, nwork, nlev_max, wctr, st)
-             : launch_work_t<double>(ctx, rtd, ls, insts_d, work_d, nwork, nlev_max, wctr, st);
+             ? launch_work_t<float>(ctx, rtd, ls, insts_d, work_d, nwork, nlev_max, wctr, st, grid_frac)
+             : launch_work_t<double>(ctx, rtd, ls, insts_d, work_d, nwork, nlev_max, wctr, st, grid_frac);
 }
 
 }  // namespace p3x

@@ -12,13 +12,19 @@ namespace p3x {
  * after the first one of its shape. */
 template <class TR, class Kern>
 cudaError_t launch_persistent(Kern kern, const dev::Inst& inst0, const dev::KParams<TR>& kp, int threads,
-                              size_t smem, int blocks_per_sm, int num_sms, cudaStream_t stream) {
+                              size_t smem, int blocks_per_sm, int num_sms, cudaStream_t stream,
+                              double grid_frac = 1.0) {
   int per_sm = 0;
   cudaError_t e = kernel_occupancy(reinterpret_cast<const void*>(kern), threads, smem, &per_sm);
   if (e != cudaSuccess) return e;
   if (per_sm <= 0) return cudaErrorInvalidConfiguration;
   if (blocks_per_sm > 0) per_sm = per_sm < blocks_per_sm ? per_sm : blocks_per_sm;
   long long grid = (long long)per_sm * num_sms;
+  /* a share of the capacity leaves room on every SM for other streams' launches */
+  if (grid_frac > 0 && grid_frac < 1) {
+    const long long share = (long long)(double(grid) * grid_frac);
+    grid = share > 0 ? share : 1;
+  }
   const long long need = (kp.nwork + kp.groups_per_block - 1) / kp.groups_per_block;
   if (need < grid) grid = need;
   if (grid <= 0) return cudaSuccess;
@@ -42,21 +48,22 @@ cudaError_t launch_p3_part(const dev::Inst& inst0, const dev::KParams<TR>& kp_in
     }
     if (ls.marks) cudaEventRecord(ls.marks[0], stream);
     e = launch_persistent<TR>(dev::p3_part12_kernel<TR, LANES>, inst0, kp, threads,
-                              p3_smem_bytes<TR>(ls, kp.sm_stride), ls.blocks_per_sm, num_sms, stream);
+                              p3_smem_bytes<TR>(ls, kp.sm_stride), ls.blocks_per_sm, num_sms, stream, ls.grid_frac);
     if (e == cudaSuccess && ls.marks) cudaEventRecord(ls.marks[1], stream);
   } else if (part == kPartK2) {
     if constexpr (LANES == 32) {
       if constexpr (sizeof(TR) == sizeof(float)) {
         e = launch_persistent<TR>(dev::p3_sed_bulk_kernel<LANES>, inst0, kp, threads,
-                                  sed_smem_bytes<TR>(ls, kp.sm_stride), 0, num_sms, stream);
+                                  sed_smem_bytes<TR>(ls, kp.sm_stride), 0, num_sms, stream, ls.grid_frac);
       } else {
         e = launch_persistent<TR>(dev::p3_sed_kernel<TR, LANES>, inst0, kp, threads,
-                                  sed_smem_bytes<TR>(ls, kp.sm_stride), 0, num_sms, stream);
+                                  sed_smem_bytes<TR>(ls, kp.sm_stride), 0, num_sms, stream, ls.grid_frac);
       }
       if (e == cudaSuccess && ls.marks) cudaEventRecord(ls.marks[2], stream);
     }
   } else if (part == kPartK3) {
-    e = launch_persistent<TR>(dev::p3_part3_kernel<TR, LANES>, inst0, kp, threads, 0, 0, num_sms, stream);
+    e = launch_persistent<TR>(dev::p3_part3_kernel<TR, LANES>, inst0, kp, threads, 0, 0, num_sms, stream,
+                              ls.grid_frac);
     if (e == cudaSuccess && ls.marks) cudaEventRecord(ls.marks[3], stream);
   }
   return e;

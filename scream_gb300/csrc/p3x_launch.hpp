@@ -17,6 +17,7 @@ struct LaunchSpec {
   int staged;           /* tables in shared memory */
   int blocks_per_sm;    /* 0: as many as fit */
   cudaEvent_t* marks = nullptr; /* optional: 4 events recorded around K1, K2, K3 */
+  double grid_frac = 1.0;       /* share of the resident-CTA capacity the persistent grid takes */
 };
 
 /* Shared-memory bytes of one CTA of K1 (part1+part2; staged tables plus the
@@ -110,7 +111,8 @@ cudaError_t launch_transpose_to_columns(const double* src, double* dst, int ncol
  * must be bound.  wctr: dev::kWorkCounters device words used by no other
  * launch in flight (zeroed on the stream), or null for a static stride. */
 int launch_work(p3x_context* ctx, const p3x_runtime& rt, int precision, const dev::Inst* insts_d,
-                const dev::WorkItem* work_d, int nwork, int nlev_max, uint32_t* wctr, cudaStream_t st);
+                const dev::WorkItem* work_d, int nwork, int nlev_max, uint32_t* wctr, cudaStream_t st,
+                double grid_frac = 1.0);
 
 /* The state hand-over of the P3 process interface between steps
  * (eamxx_p3_process_interface.hpp:218,237 with dry = wet mixing ratios):

@@ -1409,12 +1409,6 @@ __device__ __forceinline__ void update_prognostics_bulk(const Rates<float>& r, d
                      r.qc2qr_ice_shed_tend + r.qc2qr_accret_tend + r.qc2qr_autoconv_tend - r.qr2qv_evap_tend) * dtf;
   const float dnr = (-r.nr_collect_tend - r.nr2ni_immers_freeze_tend + float(C::nmltratio) * r.ni2nr_melt_tend +
                      r.nr_ice_shed_tend + r.ncshdc + r.ncautr - r.nr_selfcollect_tend - r.nr_evap_tend) * dtf;
-  constexpr float lvs = float((C::LatVap + C::LatIce) * C::INV_CP), lf = float(C::LatIce * C::INV_CP),
-                  lv = float(C::LatVap * C::INV_CP);
-  const float dth = ((r.qv2qi_vapdep_tend - r.qi2qv_sublim_tend + r.qv2qi_nucleat_tend) * lvs +
-                     (r.qr2qi_collect_tend + r.qc2qi_collect_tend + r.qc2qi_hetero_freeze_tend +
-                      r.qr2qi_immers_freeze_tend - r.qi2qr_melt_tend + r.qc2qi_berg_tend) * lf -
-                     r.qr2qv_evap_tend * lv) * dtf;
   /* A reservoir whose conservation limiter engaged has limited sinks equal to
    * its sources, so its new value is exactly the change that later limiters
    * made to its rates (r_lim: the rates right after the conservation
@@ -1447,7 +1441,14 @@ __device__ __forceinline__ void update_prognostics_bulk(const Rates<float>& r, d
   s.qc = s.qc + Dqc;
   s.qr = s.qr + Dqr;
   s.qv = s.qv - (Dqc + Dqr + Dqi);
-  s.th = s.th + inv_exner * f2d(dth);
+  /* Latent heating from the FP64 condensate changes.  The reference heats by
+   * (Lv+Lf)/cp per vapour -> ice, Lf/cp per liquid -> ice and -Lv/cp per
+   * liquid -> vapour (p3_update_prognostics_impl.hpp); with vapour changing
+   * by minus the condensate changes that sum equals
+   * (Lv (Dqc + Dqr) + (Lv+Lf) Dqi) / cp in exact arithmetic.  Formed from the
+   * same FP64 changes as the vapour, the column's energy
+   * cp T + (Lv+Lf) qv + Lf (qc+qr) then closes to FP64 round-off. */
+  s.th = s.th + inv_exner * ((C::LatVap * C::INV_CP) * (Dqc + Dqr) + ((C::LatVap + C::LatIce) * C::INV_CP) * Dqi);
   if (predictNc || prescribedCCN) {
     float dnc = (-r.nc_accret_tend - r.nc2nr_autoconv_tend + r.nc_selfcollect_tend) * dtf;
     if (predictNc) dnc += (-r.nc_collect_tend - r.nc2ni_immers_freeze_tend) * dtf;

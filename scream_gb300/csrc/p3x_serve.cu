@@ -72,6 +72,20 @@ constexpr int kTemplateCols = 65536;
 constexpr uint64_t kTemplateSeed = 5000;   /* seed of the serving workload's templates */
 constexpr int kMidOutputs = 10;             /* 7 per-level diagnostics + 3 history fields */
 constexpr int kBatchColumnCap = 1 << 18;    /* columns per dispatched work list */
+/* Latency policy (the default; p3x_server_set_latency_policy): small
+ * requests must not wait behind large steps (an FP64 step of 65,536 x 128
+ * takes ~130 ms alone).  A dispatch holds requests of one size kind (small:
+ * at most kSmallInstanceCl column-levels); a dispatch of more than
+ * kLargeDispatchCl column-levels takes the policy's share of the
+ * resident-CTA capacity, so every SM keeps room for other slots' launches;
+ * and the last slot (when there is more than one) takes only small
+ * instances, on a stream of the highest priority, so its blocks are
+ * scheduled first as blocks of the large steps retire.  The throughput
+ * policy packs every ready request of a precision together on any slot at
+ * full capacity. */
+constexpr double kLargeDispatchCl = double(1 << 20);
+constexpr double kLargeGridShare = 0.875;
+constexpr int64_t kSmallInstanceCl = int64_t(1) << 19;
 
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
@@ -140,6 +154,8 @@ struct p3x_server {
   /* isolated service time (ms) [first step / later step][precision][nlev 72/128][kCalNcol] */
   double iso_ms[2][2][2][kCalPoints] = {};
   bool calibrated = false;
+  bool latency_policy = true;
+  double large_share = kLargeGridShare;
 };
 
 namespace {
@@ -325,18 +341,30 @@ void admit(p3x_server* s) {
   }
 }
 
-/* Packs every ready request of the oldest ready precision into one work
- * list and launches it on slot sl. */
-int dispatch(p3x_server* s, Slot& sl) {
+/* Packs the ready requests of the oldest ready request's precision and size
+ * kind (small: at most kSmallInstanceCl column-levels) into one work list and
+ * launches it on slot sl, so a small request never rides a large step; with
+ * small_only, only small instances are considered. */
+int dispatch(p3x_server* s, Slot& sl, bool small_only) {
+  const bool by_kind = s->latency_policy;
+  auto is_small = [by_kind](const Instance& I) {
+    return !by_kind || int64_t(I.ncol) * I.nlev <= kSmallInstanceCl;
+  };
+  auto ready_now = [&](const Instance& I) {
+    return I.admitted && !I.busy && !I.arrivals.empty() && (!small_only || is_small(I));
+  };
   int prec = -1;
+  bool small = true;
   double oldest = 1e300;
   for (auto& kv : s->inst) {
     const Instance& I = kv.second;
-    if (I.admitted && !I.busy && !I.arrivals.empty() && I.arrivals.front() < oldest) {
+    if (ready_now(I) && I.arrivals.front() < oldest) {
       oldest = I.arrivals.front();
       prec = I.precision;
+      small = is_small(I);
     }
   }
+  auto eligible = [&](const Instance& I) { return ready_now(I) && is_small(I) == small; };
   if (prec < 0) return 1; /* nothing ready */
   std::vector<Instance*> take;
   int cols = 0, nlev_max = 1;
@@ -344,14 +372,16 @@ int dispatch(p3x_server* s, Slot& sl) {
   std::vector<std::pair<double, Instance*>> ready;
   for (auto& kv : s->inst) {
     Instance& I = kv.second;
-    if (I.admitted && !I.busy && !I.arrivals.empty() && I.precision == prec) ready.push_back({I.arrivals.front(), &I});
+    if (eligible(I) && I.precision == prec) ready.push_back({I.arrivals.front(), &I});
   }
   std::sort(ready.begin(), ready.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
   size_t nout = 0;
+  double cl = 0;
   for (auto& r : ready) {
     if (!take.empty() && cols + r.second->ncol > kBatchColumnCap) break;
     take.push_back(r.second);
     cols += r.second->ncol;
+    cl += double(r.second->ncol) * r.second->nlev;
     nlev_max = std::max(nlev_max, r.second->nlev);
     nout += result_doubles(*r.second);
   }
@@ -380,7 +410,8 @@ int dispatch(p3x_server* s, Slot& sl) {
    * other slots' launches find no free SM until then (measured at 80 % load:
    * p50 1.4 -> 1.75 ms, p90 30 -> 47 ms for 2.5 % more capacity).  With a
    * static stride CTAs retire one by one and the slots interleave. */
-  rc = p3x::launch_work(s->ctx, s->rt, prec, sl.d_insts, sl.d_work, w, nlev_max, nullptr, sl.st);
+  rc = p3x::launch_work(s->ctx, s->rt, prec, sl.d_insts, sl.d_work, w, nlev_max, nullptr, sl.st,
+                        (s->latency_policy && cl > kLargeDispatchCl) ? s->large_share : 1.0);
   if (rc) return rc;
   SRV_CUDA(p3x::launch_postamble(sl.d_insts, sl.d_work, w, sl.st));
   /* each request's result to the host, before the completion event */
@@ -465,7 +496,8 @@ int run_loop(p3x_server* s) {
     admit(s);
     for (auto& sl : s->slots) {
       if (sl.busy) continue;
-      const int rc = dispatch(s, sl);
+      const bool small_only = s->latency_policy && s->slots.size() > 1 && &sl == &s->slots.back();
+      const int rc = dispatch(s, sl, small_only);
       if (rc == 1) break;
       if (rc) return rc;
       ++inflight;
@@ -636,8 +668,11 @@ int p3x_server_create(p3x_context* ctx, const p3x_runtime* rt, int64_t budget_by
     return rc;
   }
   s->slots.resize(max_inflight);
+  int prio_least = 0, prio_greatest = 0;
+  SRV_CUDA(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest));
   for (auto& sl : s->slots) {
-    SRV_CUDA(cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking));
+    const bool small_slot = s->slots.size() > 1 && &sl == &s->slots.back();
+    SRV_CUDA(cudaStreamCreateWithPriority(&sl.st, cudaStreamNonBlocking, small_slot ? prio_greatest : prio_least));
     SRV_CUDA(cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming));
   }
   s->t0 = Clock::now();
@@ -706,6 +741,15 @@ int p3x_server_run_poisson(p3x_server* s, double rate_hz, int32_t n_requests, in
   rc = run_loop(s);
   fill_stats(s, stats, rate_hz);
   return rc;
+}
+
+int p3x_server_set_latency_policy(p3x_server* s, int32_t on, double large_grid_share) {
+  if (!s || !(large_grid_share > 0 && large_grid_share <= 1)) return P3X_EINVAL;
+  const int rc = run_loop(s);
+  if (rc) return rc;
+  s->latency_policy = on != 0;
+  s->large_share = large_grid_share;
+  return P3X_OK;
 }
 
 int p3x_server_calibrate(p3x_server* s) {

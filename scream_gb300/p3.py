@@ -400,6 +400,12 @@ class P3Server:
             self.h, float(rate_hz), int(n_sessions), int(max_ncol), int(seed), C.byref(st)))
         return st.as_dict()
 
+    def set_latency_policy(self, on: bool = True, large_grid_share: float = 0.875):
+        """Dispatch policy (p3x_server_set_latency_policy): on favours small
+        requests' latency, off packs every ready request for throughput."""
+        L.check("p3x_server_set_latency_policy", self.ctx.lib.p3x_server_set_latency_policy(
+            self.h, int(bool(on)), float(large_grid_share)))
+
     def calibrate(self):
         """Isolated service times (p3x_server_calibrate); later stats report slowdowns."""
         L.check("p3x_server_calibrate", self.ctx.lib.p3x_server_calibrate(self.h))

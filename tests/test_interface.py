@@ -205,4 +205,6 @@ def test_process_step_passes_mass_conservation_check(gpu_ctx, precision):
     rep, me, ee = gpu_ctx.conservation_check(_cons_fields(hd, f), m0, e0, dt)
     print("conservation check after one process step, precision", precision, rep)
     assert rep["max_mass_err"] <= 1e-12, rep
-    assert np.isfinite(rep["max_energy_err"]) and 0 <= rep["energy_col"] < ncol
+    # the energy (cp T + (Lv+Lf) qv + Lf (qc+qr)) closes too in both forms: the
+    # FP32-bulk form heats from the same FP64 condensate changes as the vapour
+    assert rep["max_energy_err"] <= 1e-13, rep

@@ -50,12 +50,17 @@ def test_one_step_equals_direct_p3_main(gpu_ctx, server_cls):
         srv.close()
 
 
-def test_result_alone_equals_result_in_mix(gpu_ctx, server_cls):
+@pytest.mark.parametrize("latency_policy", [True, False])
+def test_result_alone_equals_result_in_mix(gpu_ctx, server_cls, latency_policy):
+    """Bitwise the same alone and in a mix, under both dispatch policies (the
+    latency policy also shrinks large steps' grids and reserves a slot)."""
     import scream_gb300 as p3
-    probes = [(7, 300, 72, p3.P3X_FP64, 3, 123), (8, 2000, 128, p3.P3X_FP32_BULK, 4, 456)]
+    probes = [(7, 300, 72, p3.P3X_FP64, 3, 123), (8, 2000, 128, p3.P3X_FP32_BULK, 4, 456),
+              (9, 9000, 128, p3.P3X_FP32_BULK, 2, 789)]
 
     def run(mix):
         srv = server_cls(gpu_ctx, budget_bytes=6 * 10**9, max_inflight=4)
+        srv.set_latency_policy(latency_policy)
         try:
             rng = np.random.default_rng(3)
             if mix:
