@@ -159,24 +159,32 @@ __device__ __forceinline__ T group_max(unsigned mask, T v) {
   for (int o = LANES / 2; o > 0; o >>= 1) v = vmax(v, __shfl_xor_sync(mask, v, o, LANES));
   return v;
 }
-/* maximum over the group of non-negative doubles (dmax_nn) */
+/* Maxima and minima over the group with the warp-reduction instruction
+ * (redux.sync), one instruction instead of log2(LANES) dependent shuffles.
+ * Non-negative floats and doubles order as their bit patterns (as unsigned
+ * integers), so their maximum is the maximum of the patterns; a NaN (a
+ * pattern above +inf) wins and reaches the caller's Courant check. */
+/* maximum over the group of non-negative doubles (dmax_nn): the largest high
+ * word, then the largest low word among the lanes holding it */
 template <int LANES>
 __device__ __forceinline__ double group_max_nn(unsigned mask, double v) {
-#pragma unroll
-  for (int o = LANES / 2; o > 0; o >>= 1) v = dmax_nn(v, __shfl_xor_sync(mask, v, o, LANES));
-  return v;
+  const unsigned hi = unsigned(__double2hiint(v)), lo = unsigned(__double2loint(v));
+  const unsigned mhi = __reduce_max_sync(mask, hi);
+  const unsigned mlo = __reduce_max_sync(mask, hi == mhi ? lo : 0u);
+  return __hiloint2double(int(mhi), int(mlo));
+}
+/* maximum over the group of non-negative floats (Courant numbers) */
+template <int LANES>
+__device__ __forceinline__ float group_max_nn(unsigned mask, float v) {
+  return __uint_as_float(__reduce_max_sync(mask, __float_as_uint(v)));
 }
 template <int LANES>
 __device__ __forceinline__ int group_min_int(unsigned mask, int v) {
-#pragma unroll
-  for (int o = LANES / 2; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(mask, v, o, LANES));
-  return v;
+  return __reduce_min_sync(mask, v);
 }
 template <int LANES>
 __device__ __forceinline__ int group_max_int(unsigned mask, int v) {
-#pragma unroll
-  for (int o = LANES / 2; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(mask, v, o, LANES));
-  return v;
+  return __reduce_max_sync(mask, v);
 }
 
 /* ------------------------------------------------------------------ */
@@ -1397,7 +1405,7 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
       if (k_qxbot < kbot && lane == (k_qxbot + 1 - k_qxtop) % LANES) {
         V12[k_qxbot + 1] = make_float2(0.f, 0.f); /* the cell receiving the leading edge has no fall speed */
       }
-      const float Co_max = group_max<LANES>(mask, lmax) * dt_left;
+      const float Co_max = group_max_nn<LANES>(mask, lmax) * dt_left;
       if (!(Co_max >= 0.0f) || Co_max > 2.0e9f) {
         err |= kErrNumeric;
         break;
