@@ -1473,10 +1473,21 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
 
     /* FP64 state: R_k = B_k + (g / dpres_k) (G_{k-1} - G_k), on the levels
      * from the top to the final leading edge (G is zero elsewhere) */
-    for (int k = k_qxtop + lane; k <= k_qxbot; k += LANES) {
-      for (int f = 0; f < nstate; ++f) {
-        const double gin = k > 0 ? g_value(f, k - 1) : 0.0;
-        Bf[f][co + k] = Bf[f][co + k] + COEF[k] * (gin - g_value(f, k));
+    /* G_{k-1} comes from the lane above (the same value that lane forms for
+     * its own level); above the top it is zero: no flux enters there */
+    double g_in[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int base = k_qxtop; base <= k_qxbot; base += LANES) {
+      const int k = base + lane;
+      const bool act = k <= k_qxbot;
+#pragma unroll
+      for (int f = 0; f < 4; ++f) {
+        if (f < nstate) {
+          const double g = act ? g_value(f, k) : 0.0;
+          double gin = __shfl_up_sync(mask, g, 1, LANES);
+          if (lane == 0) gin = g_in[f];
+          if (act) Bf[f][co + k] = Bf[f][co + k] + COEF[k] * (gin - g);
+          g_in[f] = __shfl_sync(mask, g, LANES - 1, LANES);
+        }
       }
     }
     if (sp == 1) {
