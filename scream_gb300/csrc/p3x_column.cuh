@@ -28,6 +28,8 @@
  */
 #pragma once
 
+#include <type_traits>
+
 #include "p3x_physics.cuh"
 
 namespace p3x {
@@ -1244,8 +1246,10 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
   }
   double precip_liq_surf = 0, precip_ice_surf = 0;
 
-#pragma unroll 1
-  for (int sp = 0; sp < 3; ++sp) {
+  /* The three species, each with its code specialised (field count, tables,
+   * limiters) at compile time. */
+  auto species = [&](auto sp_tag) {
+    constexpr int sp = decltype(sp_tag)::value;
     double* const B0 = sp == 0 ? in.qc : (sp == 1 ? in.qr : in.qi);
     double* const B1 = sp == 0 ? in.nc : (sp == 1 ? in.nr : in.ni);
     double* const B2 = in.qm;
@@ -1266,7 +1270,7 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
 
     const int k_qxtop = sp == 0 ? top_c : (sp == 1 ? top_r : top_i);
     int k_qxbot = sp == 0 ? bot_c : (sp == 1 ? bot_r : bot_i);
-    if (k_qxbot < 0) continue; /* species absent (group-uniform) */
+    if (k_qxbot < 0) return; /* species absent (group-uniform) */
     /* the walk and the rebuild read G one level above the top */
     for (int k = max(k_qxtop - 1, 0) + lane; k < nk; k += LANES) {
       G01[k] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1495,7 +1499,10 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
       for (int k = k_qxtop + 1 + lane; k <= nk; k += LANES) in.precip_liq_flux[ci + k] = dfloat_value(PF[k]);
     }
     __syncwarp(mask);
-  }
+  };
+  species(std::integral_constant<int, 0>{});
+  species(std::integral_constant<int, 1>{});
+  species(std::integral_constant<int, 2>{});
   if (lane == 0) {
     in.precip_liq_surf[col] = precip_liq_surf;
     in.precip_ice_surf[col] = precip_ice_surf;
