@@ -25,6 +25,9 @@ struct p3x_context {
   /* device tables, FP64 and FP32 copies */
   double *d_ice = nullptr, *d_coll = nullptr, *d_vn = nullptr, *d_vm = nullptr, *d_revap = nullptr;
   float *f_ice = nullptr, *f_coll = nullptr, *f_vn = nullptr, *f_vm = nullptr, *f_revap = nullptr;
+  /* FP32 ice-table columns of ice sedimentation only (slots 0-3, 16 bytes a
+   * row): a third of the rows' cache footprint */
+  float* f_ice_sed = nullptr;
   /* Table3 two-column slices for every possible mu index (1..9):
    * [9][3][300][2] */
   double* d_t3slices = nullptr;
@@ -241,6 +244,7 @@ dev::KParams<float> make_kparams<float>(p3x_context* ctx, const dev::RuntimeDev&
   dev::KParams<float> kp{};
   kp.rt = rtd;
   kp.ice = ctx->f_ice;
+  kp.ice_sed = ctx->f_ice_sed;
   kp.collect = ctx->f_coll;
   kp.vn = ctx->f_vn;
   kp.vm = ctx->f_vm;
@@ -565,7 +569,11 @@ int p3x_context_create(const char* table_file, p3x_context** out, int* info) {
   for (size_t row = 0; row < H.ice.size() / dev::kIceCols; ++row)
     for (int s = 0; s < dev::kIceCols; ++s)
       ice_slots[row * dev::kIceCols + s] = H.ice[row * dev::kIceCols + dev::kIceSlotCol[s]];
-  if ((st = upload(&ctx->d_ice, ice_slots)) || (st = upload(&ctx->d_coll, H.collect)) ||
+  std::vector<double> ice_sed(H.ice.size() / dev::kIceCols * dev::kIceSedCols);
+  for (size_t row = 0; row < H.ice.size() / dev::kIceCols; ++row)
+    for (int s = 0; s < dev::kIceSedCols; ++s) ice_sed[row * dev::kIceSedCols + s] = ice_slots[row * dev::kIceCols + s];
+  if ((st = upload(&ctx->d_ice, ice_slots)) || (st = upload(&ctx->f_ice_sed, ice_sed)) ||
+      (st = upload(&ctx->d_coll, H.collect)) ||
       (st = upload(&ctx->d_vn, H.vn)) || (st = upload(&ctx->d_vm, H.vm)) ||
       (st = upload(&ctx->d_revap, H.revap)) || (st = upload(&ctx->f_ice, ice_slots)) ||
       (st = upload(&ctx->f_coll, H.collect)) || (st = upload(&ctx->f_vn, H.vn)) ||
@@ -635,7 +643,7 @@ int p3x_context_create(const char* table_file, p3x_context** out, int* info) {
 
 int p3x_context_destroy(p3x_context* ctx) {
   if (!ctx) return P3X_EINVAL;
-  void* ptrs[] = {ctx->d_ice, ctx->d_coll, ctx->d_vn, ctx->d_vm, ctx->d_revap, ctx->f_ice, ctx->f_coll,
+  void* ptrs[] = {ctx->d_ice, ctx->d_coll, ctx->d_vn, ctx->d_vm, ctx->d_revap, ctx->f_ice, ctx->f_ice_sed, ctx->f_coll,
                   ctx->f_vn, ctx->f_vm, ctx->f_revap, ctx->d_t3slices, ctx->f_t3slices, ctx->d_svp, ctx->d_err,
                   ctx->d_check, ctx->d_maxloc, ctx->fstage};
   for (void* p : ptrs)

@@ -64,6 +64,7 @@ struct KParams {
   RuntimeDev rt;
   /* global tables in the rate precision */
   const TR* ice;
+  const TR* ice_sed; /* FP32-bulk: slots 0-3 of every ice-table row, packed */
   const TR* collect;
   const TR* vn;
   const TR* vm;
@@ -1774,6 +1775,7 @@ __device__ __forceinline__ unsigned char* setup_tables(const KParams<TR>& kp, bo
     uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw + table_smem_bytes<TR>() - 16);
     if (!stage_tables<TR>(kp, s_ice, s_t3, mbar, err)) return nullptr;
     tb.ice = s_ice;
+    tb.ice_stride = kIceCols;
     tb.vn = s_t3;
     tb.vm = s_t3 + 600;
     tb.revap = s_t3 + 1200;
@@ -1782,6 +1784,7 @@ __device__ __forceinline__ unsigned char* setup_tables(const KParams<TR>& kp, bo
     return smem_raw + table_smem_bytes<TR>();
   }
   tb.ice = kp.ice;
+  tb.ice_stride = kIceCols;
   tb.vn = kp.vn;
   tb.vm = kp.vm;
   tb.revap = kp.revap;
@@ -1882,8 +1885,19 @@ template <int LANES>
 __global__ void __maxnreg__(96) p3_sed_bulk_kernel(const Inst inst0, const KParams<float> kp) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint32_t err = 0;
+  /* Compact tables, so that the lookups of the substep walk stay in the L1
+   * data cache beside the CTAs' shared memory: the four ice-table columns of
+   * sedimentation (16 KB) and the two-column Table3 slices of the rain
+   * shape (2.4 KB each) rather than the full tables (48 KB and 12 KB). */
   Tabs<float> tb;
-  setup_tables<float>(kp, false, smem_raw, tb, err);
+  tb.collect = kp.collect;
+  tb.ice = kp.ice_sed;
+  tb.ice_stride = kIceSedCols;
+  tb.vn = kp.t3slice;
+  tb.vm = kp.t3slice + kT3SliceElems / 3;
+  tb.revap = kp.t3slice + 2 * (kT3SliceElems / 3);
+  tb.t3_stride = 2;
+  tb.t3_j0 = kp.rt.t3_dumjj - 1;
   const int g_in_block = threadIdx.x / LANES;
   double* sm = reinterpret_cast<double*>(smem_raw) + size_t(g_in_block) * kSedBulkSlots * kp.sm_stride;
   for_each_work<LANES>(kp.wctr ? kp.wctr + 1 : nullptr, kp.nwork, kp.groups_per_block, [&](int w) {

@@ -366,6 +366,7 @@ __device__ __forceinline__ double qv_sat_dry(double t, double p, bool ice, uint3
 template <class TR>
 struct Tabs {
   const TR* ice;
+  int ice_stride; /* elements per ice-table row: kIceCols, or kIceSedCols in the packed sedimentation copy */
   const TR* collect;
   const TR* vn;
   const TR* vm;
@@ -379,6 +380,7 @@ struct Tabs {
  * (5,11,8,10), so each stage reads a table corner with one or two 16-byte
  * vector loads instead of one scalar load per column. */
 constexpr int kIceSlotCol[kIceCols] = {0, 1, 6, 7, 2, 3, 4, 9, 5, 11, 8, 10};
+constexpr int kIceSedCols = 4;
 
 __device__ __forceinline__ void ld4(const float* p, float o[4]) {
   const float4 v = *reinterpret_cast<const float4*>(p);
@@ -391,7 +393,7 @@ __device__ __forceinline__ void ld4(const double* p, double o[4]) {
 }
 template <class TR>
 __device__ __forceinline__ const TR* ice_row(const Tabs<TR>& t, int jj, int ii, int i) {
-  return t.ice + ((jj * kRimsize + ii) * kIsize + i) * kIceCols;
+  return t.ice + ((jj * kRimsize + ii) * kIsize + i) * t.ice_stride;
 }
 template <class TR>
 __device__ __forceinline__ TR coll_at(const Tabs<TR>& t, int jj, int ii, int i, int j, int idx) {
