@@ -1392,7 +1392,7 @@ __device__ void p3_sed_bulk(const Inst& in, const int col, const KParams<float>&
             TableIce<float> ti;
             lookup_ice<float>(qi_f, ni_l, qm_f, rhop, ti);
             float tv[4];
-            apply_table_ice4<float>(tb, ti, 0, tv); /* columns 0, 1, 6, 7 */
+            ice_table4_f32<kIceSedCols>(tb.ice, ti, 0, tv); /* columns 0, 1, 6, 7, packed copy */
             float n2 = vmin(ni_l, tv[2] * ni_l);
             n2 = vmax(n2, tv[3] * n2);
             if (n2 != ni_plain) {
@@ -1775,7 +1775,6 @@ __device__ __forceinline__ unsigned char* setup_tables(const KParams<TR>& kp, bo
     uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw + table_smem_bytes<TR>() - 16);
     if (!stage_tables<TR>(kp, s_ice, s_t3, mbar, err)) return nullptr;
     tb.ice = s_ice;
-    tb.ice_stride = kIceCols;
     tb.vn = s_t3;
     tb.vm = s_t3 + 600;
     tb.revap = s_t3 + 1200;
@@ -1784,7 +1783,6 @@ __device__ __forceinline__ unsigned char* setup_tables(const KParams<TR>& kp, bo
     return smem_raw + table_smem_bytes<TR>();
   }
   tb.ice = kp.ice;
-  tb.ice_stride = kIceCols;
   tb.vn = kp.vn;
   tb.vm = kp.vm;
   tb.revap = kp.revap;
@@ -1892,7 +1890,6 @@ __global__ void __maxnreg__(96) p3_sed_bulk_kernel(const Inst inst0, const KPara
   Tabs<float> tb;
   tb.collect = kp.collect;
   tb.ice = kp.ice_sed;
-  tb.ice_stride = kIceSedCols;
   tb.vn = kp.t3slice;
   tb.vm = kp.t3slice + kT3SliceElems / 3;
   tb.revap = kp.t3slice + 2 * (kT3SliceElems / 3);

@@ -366,7 +366,6 @@ __device__ __forceinline__ double qv_sat_dry(double t, double p, bool ice, uint3
 template <class TR>
 struct Tabs {
   const TR* ice;
-  int ice_stride; /* elements per ice-table row: kIceCols, or kIceSedCols in the packed sedimentation copy */
   const TR* collect;
   const TR* vn;
   const TR* vm;
@@ -393,7 +392,7 @@ __device__ __forceinline__ void ld4(const double* p, double o[4]) {
 }
 template <class TR>
 __device__ __forceinline__ const TR* ice_row(const Tabs<TR>& t, int jj, int ii, int i) {
-  return t.ice + ((jj * kRimsize + ii) * kIsize + i) * t.ice_stride;
+  return t.ice + ((jj * kRimsize + ii) * kIsize + i) * kIceCols;
 }
 template <class TR>
 __device__ __forceinline__ TR coll_at(const Tabs<TR>& t, int jj, int ii, int i, int j, int idx) {
@@ -499,22 +498,21 @@ __device__ __forceinline__ void apply_table_ice4(const Tabs<TR>& t, const TableI
 }
 
 /* The FP32 form of apply_table_ice4 on packed pairs of columns (s0..s0+1
- * and s0+2..s0+3): the same interpolations in the same order. */
-template <>
-__device__ __forceinline__ void apply_table_ice4<float>(const Tabs<float>& t, const TableIce<float>& tab, int s0,
-                                                       float out[4]) {
+ * and s0+2..s0+3): the same interpolations in the same order.  STRIDE is
+ * the row length of the table copy read (kIceCols, or kIceSedCols for the
+ * packed sedimentation copy), a constant so that the eight corners are one
+ * address plus immediate offsets. */
+template <int STRIDE>
+__device__ __forceinline__ void ice_table4_f32(const float* ice, const TableIce<float>& tab, int s0, float out[4]) {
   const float w1 = tab.dum1 - ival<float>(tab.dumi) - 1.0f;
   const float w4 = tab.dum4 - ival<float>(tab.dumii) - 1.0f;
   const float w5 = tab.dum5 - ival<float>(tab.dumjj) - 1.0f;
   const float2 W1 = f2splat(w1), W4 = f2splat(w4), W5 = f2splat(w5);
-  const float4 a00 = *reinterpret_cast<const float4*>(ice_row(t, tab.dumjj, tab.dumii, tab.dumi) + s0);
-  const float4 a01 = *reinterpret_cast<const float4*>(ice_row(t, tab.dumjj, tab.dumii, tab.dumi + 1) + s0);
-  const float4 a10 = *reinterpret_cast<const float4*>(ice_row(t, tab.dumjj, tab.dumii + 1, tab.dumi) + s0);
-  const float4 a11 = *reinterpret_cast<const float4*>(ice_row(t, tab.dumjj, tab.dumii + 1, tab.dumi + 1) + s0);
-  const float4 b00 = *reinterpret_cast<const float4*>(ice_row(t, tab.dumjj + 1, tab.dumii, tab.dumi) + s0);
-  const float4 b01 = *reinterpret_cast<const float4*>(ice_row(t, tab.dumjj + 1, tab.dumii, tab.dumi + 1) + s0);
-  const float4 b10 = *reinterpret_cast<const float4*>(ice_row(t, tab.dumjj + 1, tab.dumii + 1, tab.dumi) + s0);
-  const float4 b11 = *reinterpret_cast<const float4*>(ice_row(t, tab.dumjj + 1, tab.dumii + 1, tab.dumi + 1) + s0);
+  const float* const r = ice + ((tab.dumjj * kRimsize + tab.dumii) * kIsize + tab.dumi) * STRIDE + s0;
+  constexpr int dI = STRIDE, dR = kIsize * STRIDE, dD = kRimsize * kIsize * STRIDE;
+  auto at = [&](int off) { return *reinterpret_cast<const float4*>(r + off); };
+  const float4 a00 = at(0), a01 = at(dI), a10 = at(dR), a11 = at(dR + dI);
+  const float4 b00 = at(dD), b01 = at(dD + dI), b10 = at(dD + dR), b11 = at(dD + dR + dI);
   auto lo = [](float4 v) { return make_float2(v.x, v.y); };
   auto hi = [](float4 v) { return make_float2(v.z, v.w); };
   const float2 t1l = lerp2(lerp2(lo(a00), lo(a01), W1), lerp2(lo(a10), lo(a11), W1), W4);
@@ -523,6 +521,11 @@ __device__ __forceinline__ void apply_table_ice4<float>(const Tabs<float>& t, co
   const float2 t2h = lerp2(lerp2(hi(b00), hi(b01), W1), lerp2(hi(b10), hi(b11), W1), W4);
   const float2 rl = lerp2(t1l, t2l, W5), rh = lerp2(t1h, t2h, W5);
   out[0] = rl.x; out[1] = rl.y; out[2] = rh.x; out[3] = rh.y;
+}
+template <>
+__device__ __forceinline__ void apply_table_ice4<float>(const Tabs<float>& t, const TableIce<float>& tab, int s0,
+                                                       float out[4]) {
+  ice_table4_f32<kIceCols>(t.ice, tab, s0, out);
 }
 
 /* apply_table_coll, p3_table_ice_impl.hpp:214-297 */
