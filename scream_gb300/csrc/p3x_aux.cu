@@ -291,7 +291,7 @@ __global__ void f2d_selftest_kernel(unsigned long long* mismatches) {
   const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
   for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < (uint64_t(1) << 32); i += stride) {
     const float x = __uint_as_float(uint32_t(i));
-    const double a = dev::f2d(x), b = double(x);
+    const double a = dev::f2d_int(x), b = double(x);
     if (__double_as_longlong(a) != __double_as_longlong(b)) ++bad;
     const int tz = __float2int_rz(x);
     for (const int hi : {4, 5, 20, 30, 50, 300}) {

@@ -1663,8 +1663,8 @@ __device__ void p3_part3(const Inst& in, const int col, const KParams<TR>& kp, c
         const float n_in = float(s.nc) * icl;
         float n_out = n_in, mu_c, lamc;
         get_cloud_dsd2<float>(qc_f, n_out, mu_c, rho_f, lamc);
-        if (n_out != n_in) s.nc = f2d(n_out) * cld_l;
-        eff_qc = f2d(0.5f * (mu_c + 3.0f) / lamc);
+        if (n_out != n_in) s.nc = f2d_int(n_out) * cld_l;
+        eff_qc = f2d_int(0.5f * (mu_c + 3.0f) / lamc);
       } else {
         if (dnz(s.qc)) {
           s.qv = s.qv + s.qc;
@@ -1680,8 +1680,8 @@ __device__ void p3_part3(const Inst& in, const int col, const KParams<TR>& kp, c
         const float n_in = float(s.nr) * icr;
         float n_out = n_in, mu_r = 0, lamr;
         get_rain_dsd2<float>(qr_f, n_out, mu_r, lamr, rt);
-        if (n_out != n_in) s.nr = f2d(n_out) * cld_r;
-        eff_qr = f2d(1.5f / lamr);
+        if (n_out != n_in) s.nr = f2d_int(n_out) * cld_r;
+        eff_qr = f2d_int(1.5f / lamr);
       } else {
         if (dnz(s.qr)) {
           s.qv = s.qv + s.qr;
@@ -1701,8 +1701,8 @@ __device__ void p3_part3(const Inst& in, const int col, const KParams<TR>& kp, c
           const float qm0 = float(s.qm) * ici, bm0 = float(s.bm) * ici;
           float qm_f = qm0, bm_f = bm0;
           const float rhop = calc_bulk_rho_rime<float>(qi_f, qm_f, bm_f, rt);
-          if (qm_f != qm0) s.qm = f2d(qm_f) * cld_i;
-          if (bm_f != bm0) s.bm = f2d(bm_f) * cld_i;
+          if (qm_f != qm0) s.qm = f2d_int(qm_f) * cld_i;
+          if (bm_f != bm0) s.bm = f2d_int(bm_f) * cld_i;
           float ni_f = ni0;
           impose_max_total_ni(ni_f, rt.f.max_total_ni, inv_rho_f);
           TableIce<float> ti;
@@ -1712,9 +1712,9 @@ __device__ void p3_part3(const Inst& in, const int col, const KParams<TR>& kp, c
           apply_table_ice4<float>(tb, ti, 8, te); /* columns 5, 11, 8, 10 */
           ni_f = vmin(ni_f, ta[2] * ni_f);
           ni_f = vmax(ni_f, ta[3] * ni_f);
-          eff_qi = f2d(te[0]);
-          rho_qi = f2d(te[1]);
-          if (ni_f != ni0) s.ni = f2d(ni_f) * cld_i;
+          eff_qi = f2d_int(te[0]);
+          rho_qi = f2d_int(te[1]);
+          if (ni_f != ni0) s.ni = f2d_int(ni_f) * cld_i;
           if (dlt(s.qm, C::QSMALL)) {
             s.qm = 0;
             s.bm = 0;

@@ -135,7 +135,7 @@ __device__ __forceinline__ float m_fabs(float x) { return fabsf(x); }
  * infinities and NaNs take the hardware conversion.  On this part the FP64
  * pipe, which also executes conversions, is the bottleneck of every kernel,
  * while the integer pipes are nearly idle. */
-__device__ __forceinline__ double f2d(float x) {
+__device__ __forceinline__ double f2d_int(float x) {
   const uint32_t u = __float_as_uint(x);
   const uint32_t e = (u >> 23) & 0xffu;
   const uint32_t mag = u & 0x7fffffffu;
@@ -145,6 +145,14 @@ __device__ __forceinline__ double f2d(float x) {
   const uint32_t lo = (m & 7u) << 29;
   return __hiloint2double(int(hi), int(lo));
 }
+
+/* Float -> double where the instruction footprint limits the kernel more than
+ * the FP64 pipe: the FP32-bulk part1+2 and sedimentation kernels are larger
+ * than the SM's instruction cache (instruction fetch is part1+2's top stall at
+ * 65,536 columns), and the hardware conversion is one instruction where
+ * f2d_int inlines a dozen and a branch at each of some 80 call sites.  The
+ * FP64-pipe-bound part3 keeps f2d_int.  Both are exact. */
+__device__ __forceinline__ double f2d(float x) { return double(x); }
 
 /* 1/x for the FP32-bulk form by Newton-Raphson from the FP32 reciprocal:
  * each step r <- r + r (1 - x r) squares the relative error (~2^-22 from
