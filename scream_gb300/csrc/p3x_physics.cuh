@@ -345,9 +345,27 @@ __device__ __forceinline__ TR murphy_koop_svp(TR t, bool ice, uint32_t& err) {
  * error < 1e-12 relative), the formula outside the tabulated range. */
 constexpr double kSvpT0 = 150.0, kSvpInvH = 64.0;
 constexpr int kSvpIntervals = 12800;
+/* The formula outside the table, out of line: it is rarely reached, and its
+ * FP64 divisions would otherwise be inlined at every table call site (about
+ * 6 KB of code each in the FP32-bulk part1+2 kernel, which is larger than the
+ * instruction cache).  The status bits come back with the value. */
+struct SvpValue {
+  double v;
+  uint32_t err;
+};
+static __device__ __noinline__ SvpValue svp_out_of_table(double t, bool ice) {
+  uint32_t e = 0;
+  const double v = murphy_koop_svp<double>(t, ice, e);
+  return SvpValue{v, e};
+}
+
 __device__ __forceinline__ double svp_tabulated(const double* tab, double t, bool ice, uint32_t& err) {
   const double x = fma(t, kSvpInvH, -kSvpT0 * kSvpInvH); /* = (t - T0) * 64, both exact here */
-  if (!(!dneg(x) && dlt(x, double(kSvpIntervals)))) return murphy_koop_svp<double>(t, ice, err);
+  if (!(!dneg(x) && dlt(x, double(kSvpIntervals)))) {
+    const SvpValue r = svp_out_of_table(t, ice);
+    err |= r.err;
+    return r.v;
+  }
   /* floor(x) through the truncated float (exact, see d2f_rz) and its exact
    * double, off the FP64 pipe */
   const int i = ffloor_small(d2f_rz(x));
