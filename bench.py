@@ -108,7 +108,7 @@ def _peaks():
 def _traffic_per_cl(kernel_tag):
     """DRAM bytes per column-level of the column kernel from the committed ncu
     summary (profiles/), or None."""
-    f = ROOT / "profiles" / "p3_step_traffic_4096x128.txt"
+    f = ROOT / "profiles" / "p3_step_traffic_65536x128.txt"
     if not f.exists():
         return None
     for line in f.read_text().splitlines():
