@@ -275,6 +275,79 @@ int p3x_postamble(const p3x_interface_fields* f, const p3x_prognostic_state* pro
                   int32_t nk, const p3x_layout* layout, double dt, void* stream);
 
 /* ------------------------------------------------------------------ */
+/* EAM driver around the step (micro_p3_tend)                          */
+/* ------------------------------------------------------------------ */
+/* Fields of EAM's P3 driver micro_p3_tend
+ * (eam/src/physics/p3/scream/micro_p3_interface.F90:735-1484) on the
+ * device: the physics state it reads, the physics-buffer fields it carries
+ * between steps, the tendencies it returns and its diagnostics.  Per-level
+ * fields are (ncol, nlev) with the layout's ld; zi, flxprc and flxsnw
+ * (nlev+1 interfaces, top first) use ld_int; per-column fields have ncol
+ * entries.  q and ptend_q hold the driver's nine constituents in this
+ * order: qv, cldliq, numliq, rain, numrain, cldice, numice, cldrim, rimvol
+ * (wet mixing ratios, as in state%q).  Diagnostic pointers may be NULL
+ * (not computed); everything else is required. */
+typedef struct p3x_eam_fields {
+  /* physics state (read only) */
+  const double *pmid, *pmiddry, *pdel, *pdeldry, *zi, *t;
+  const double* q[9];
+  /* physics buffer inputs (read only): cloud fraction, activation
+   * tendencies, cloud-liquid relative variance, macrophysics condensation */
+  const double *ast, *npccn, *ni_activated, *relvar, *cmeliq;
+  /* physics buffer carried between steps (in/out): T and wet qv at the end
+   * of the previous step */
+  double *t_prev, *qv_prev;
+  /* tendencies (out): dry static energy and the nine constituents */
+  double* ptend_s;
+  double* ptend_q[9];
+  /* diagnostics (out, optional) */
+  double *qme, *rho, *icimrst, *icwmrst, *icinc, *icwnc, *rel, *rei, *dei, *mu, *lambdac, *nfice, *efcout,
+      *ncout, *freql, *efiout, *niout, *freqi, *aqrain, *anrain, *freqr, *reff_rain, *deff_rain;
+  double *flxprc, *flxsnw;                                  /* interfaces */
+  double *prec_pcw, *snow_pcw, *prec_str, *snow_str, *cdnumc; /* per column */
+  int32_t subgrid_clouds;     /* micro_subgrid_cloud: 0 = all cloud fractions 1 */
+  int32_t precip_frac_method; /* P3X_PRECIP_FRAC_MAX_OVERLAP (the driver's) or _IN_CLOUD */
+} p3x_eam_fields;
+
+#define P3X_PRECIP_FRAC_MAX_OVERLAP 0
+#define P3X_PRECIP_FRAC_IN_CLOUD 1
+
+/* The driver's preparation of the P3 inputs (micro_p3_interface.F90:
+ * 982-1047, get_cloud_fraction :661-732): wet -> dry mixing ratios by
+ * pdel / pdeldry into prog (qv, qc, nc, qr, nr, qi, ni, qm, bm) and qv_prev,
+ * inv_exner = 1 / (pmid 1e-5)^(rair / cp), dz from zi, th = T inv_exner,
+ * pres = pmiddry, dpres = pdeldry, the cloud fractions, nc_nuceat_tend =
+ * npccn, ni_activated, inv_qc_relvar = relvar and t_prev, into din (whose
+ * arrays must be writable; nccn is left to the caller). */
+int p3x_eam_tend_pre(const p3x_eam_fields* e, const p3x_prognostic_state* prog,
+                     const p3x_diagnostic_inputs* din, int32_t nj, int32_t nk, const p3x_layout* layout,
+                     void* stream);
+
+/* The driver's use of the P3 results (micro_p3_interface.F90:1182-1431):
+ * dry -> wet by pdeldry / pdel, the enthalpy-rescaled temperature change,
+ * ptend_s and ptend_q (of the non-negative wet values), t_prev and the wet
+ * qv_prev, qme and vap_liq_exchange += cmeliq (hist), surface precipitation
+ * for export, radiation and COSP diagnostics.  mu and lambdac: the
+ * reference's Fortran p3_main returns the cloud-droplet shape and slope,
+ * which the C++ p3_main replaced here does not; they are written as the
+ * driver's initial values (0) except where ast < 1e-4, where the driver's
+ * convective values apply. */
+int p3x_eam_tend_post(const p3x_eam_fields* e, const p3x_prognostic_state* prog,
+                      const p3x_diagnostic_inputs* din, const p3x_diagnostic_outputs* dout,
+                      const p3x_history_only* hist, int32_t nj, int32_t nk, const p3x_layout* layout,
+                      double dt, void* stream);
+
+/* micro_p3_tend on the device: p3x_eam_tend_pre, the P3 step (p3x_main_async
+ * with infra's dt, it, predictNc and prescribedCCN) and p3x_eam_tend_post on
+ * `stream`, asynchronously.  prog, din, dout and hist are the driver's
+ * working arrays (its local copies of the state). */
+int p3x_eam_micro_p3_tend(p3x_context* ctx, const p3x_runtime* rt, const p3x_eam_fields* e,
+                          const p3x_prognostic_state* prog, const p3x_diagnostic_inputs* din,
+                          const p3x_diagnostic_outputs* dout, const p3x_infrastructure* infra,
+                          const p3x_history_only* hist, int32_t nj, int32_t nk, const p3x_layout* layout,
+                          int32_t precision, void* stream);
+
+/* ------------------------------------------------------------------ */
 /* The step in stages (stage-by-stage checks against a CPU restatement) */
 /* ------------------------------------------------------------------ */
 /* No counterpart in the reference, whose p3_main runs its stages inside one

@@ -98,6 +98,24 @@ class InterfaceFields(C.Structure):
     _fields_ = [(n, C.c_void_p) for n in HOST_MODEL_FIELDS]
 
 
+# EAM driver (micro_p3_tend) fields, in the order of p3x_eam_fields
+EAM_SPECIES = ["qv", "cldliq", "numliq", "rain", "numrain", "cldice", "numice", "cldrim", "rimvol"]
+EAM_STATE = ["pmid", "pmiddry", "pdel", "pdeldry", "zi", "t"]
+EAM_PBUF_IN = ["ast", "npccn", "ni_activated", "relvar", "cmeliq"]
+EAM_DIAG = ["qme", "rho", "icimrst", "icwmrst", "icinc", "icwnc", "rel", "rei", "dei", "mu", "lambdac", "nfice",
+            "efcout", "ncout", "freql", "efiout", "niout", "freqi", "aqrain", "anrain", "freqr", "reff_rain",
+            "deff_rain", "flxprc", "flxsnw", "prec_pcw", "snow_pcw", "prec_str", "snow_str", "cdnumc"]
+PRECIP_FRAC_MAX_OVERLAP, PRECIP_FRAC_IN_CLOUD = 0, 1
+
+
+class EamFields(C.Structure):
+    _fields_ = ([(n, C.c_void_p) for n in EAM_STATE] + [("q", C.c_void_p * 9)] +
+                [(n, C.c_void_p) for n in EAM_PBUF_IN] + [("t_prev", C.c_void_p), ("qv_prev", C.c_void_p),
+                                                         ("ptend_s", C.c_void_p), ("ptend_q", C.c_void_p * 9)] +
+                [(n, C.c_void_p) for n in EAM_DIAG] + [("subgrid_clouds", C.c_int32),
+                                                      ("precip_frac_method", C.c_int32)])
+
+
 class LaunchConfig(C.Structure):
     _fields_ = [("lanes_per_column", C.c_int32), ("columns_per_block", C.c_int32),
                 ("table_staging", C.c_int32), ("blocks_per_sm", C.c_int32)]
@@ -189,6 +207,15 @@ PROTOTYPES = {
                                 C.POINTER(DiagnosticInputs), C.POINTER(DiagnosticOutputs),
                                 C.POINTER(Infrastructure), C.POINTER(HistoryOnly), _I, _I,
                                 C.POINTER(Layout), _I, _I, C.POINTER(C.c_double)]),
+    "p3x_eam_tend_pre": (C.c_int, [C.POINTER(EamFields), C.POINTER(PrognosticState),
+                                   C.POINTER(DiagnosticInputs), _I, _I, C.POINTER(Layout), _V]),
+    "p3x_eam_tend_post": (C.c_int, [C.POINTER(EamFields), C.POINTER(PrognosticState),
+                                    C.POINTER(DiagnosticInputs), C.POINTER(DiagnosticOutputs),
+                                    C.POINTER(HistoryOnly), _I, _I, C.POINTER(Layout), C.c_double, _V]),
+    "p3x_eam_micro_p3_tend": (C.c_int, [_V, C.POINTER(Runtime), C.POINTER(EamFields), C.POINTER(PrognosticState),
+                                        C.POINTER(DiagnosticInputs), C.POINTER(DiagnosticOutputs),
+                                        C.POINTER(Infrastructure), C.POINTER(HistoryOnly), _I, _I,
+                                        C.POINTER(Layout), _I, _V]),
     "p3x_main_async": (C.c_int, [_V, C.POINTER(Runtime), C.POINTER(PrognosticState),
                                  C.POINTER(DiagnosticInputs), C.POINTER(DiagnosticOutputs),
                                  C.POINTER(Infrastructure), C.POINTER(HistoryOnly), _I, _I,

@@ -1136,6 +1136,116 @@ int p3x_postamble(const p3x_interface_fields* f, const p3x_prognostic_state* pro
   return cuda_status(p3x::launch_interface(p, nj, nk, ld, true, dt, static_cast<cudaStream_t>(stream)));
 }
 
+/* EAM driver (micro_p3_tend): pointer checks and the kernels' view. */
+static int eam_ptrs(const p3x_eam_fields* e, const p3x_prognostic_state* prog, const p3x_diagnostic_inputs* din,
+                    const p3x_diagnostic_outputs* dout, const p3x_history_only* hist, bool post,
+                    p3x::EamPtrs& p) {
+  if (!e || !prog || !din) return P3X_EINVAL;
+  if (!e->pmid || !e->pmiddry || !e->pdel || !e->pdeldry || !e->zi || !e->t || !e->ast || !e->npccn ||
+      !e->ni_activated || !e->relvar || !e->t_prev || !e->qv_prev)
+    return P3X_EINVAL;
+  if (e->precip_frac_method != P3X_PRECIP_FRAC_MAX_OVERLAP && e->precip_frac_method != P3X_PRECIP_FRAC_IN_CLOUD)
+    return P3X_EINVAL;
+  p = p3x::EamPtrs{};
+  p.pmid = e->pmid; p.pmiddry = e->pmiddry; p.pdel = e->pdel; p.pdeldry = e->pdeldry; p.zi = e->zi; p.t = e->t;
+  p.ast = e->ast; p.npccn = e->npccn; p.ni_act_in = e->ni_activated; p.relvar = e->relvar; p.cmeliq = e->cmeliq;
+  p.t_prev = e->t_prev; p.qv_prev = e->qv_prev;
+  p.subgrid = e->subgrid_clouds != 0;
+  p.method = e->precip_frac_method;
+  /* the driver's constituents and the P3 state that holds each of them */
+  double* w[9] = {prog->qv, prog->qc, prog->nc, prog->qr, prog->nr, prog->qi, prog->ni, prog->qm, prog->bm};
+  for (int s = 0; s < 9; ++s) {
+    if (!e->q[s] || !w[s]) return P3X_EINVAL;
+    p.q[s] = e->q[s];
+    p.w[s] = w[s];
+  }
+  p.th = prog->th;
+  p.inv_exner = const_cast<double*>(din->inv_exner);
+  p.cld_l = const_cast<double*>(din->cld_frac_l);
+  p.cld_i = const_cast<double*>(din->cld_frac_i);
+  p.cld_r = const_cast<double*>(din->cld_frac_r);
+  if (!p.th || !p.inv_exner || !p.cld_l || !p.cld_i || !p.cld_r) return P3X_EINVAL;
+  if (!post) {
+    p.pres = const_cast<double*>(din->pres);
+    p.dz = const_cast<double*>(din->dz);
+    p.dpres = const_cast<double*>(din->dpres);
+    p.nc_nuceat = const_cast<double*>(din->nc_nuceat_tend);
+    p.ni_act = const_cast<double*>(din->ni_activated);
+    p.inv_relvar = const_cast<double*>(din->inv_qc_relvar);
+    p.qv_prev_dry = const_cast<double*>(din->qv_prev);
+    p.t_prev_p3 = const_cast<double*>(din->t_prev);
+    if (!p.pres || !p.dz || !p.dpres || !p.nc_nuceat || !p.ni_act || !p.inv_relvar || !p.qv_prev_dry ||
+        !p.t_prev_p3)
+      return P3X_EINVAL;
+    return P3X_OK;
+  }
+  if (!dout || !hist || !e->cmeliq || !e->ptend_s || !hist->vap_liq_exchange) return P3X_EINVAL;
+  for (int s = 0; s < 9; ++s) {
+    if (!e->ptend_q[s]) return P3X_EINVAL;
+    p.ptend_q[s] = e->ptend_q[s];
+  }
+  p.ptend_s = e->ptend_s;
+  p.eff_qc = dout->diag_eff_radius_qc; p.eff_qi = dout->diag_eff_radius_qi; p.eff_qr = dout->diag_eff_radius_qr;
+  p.liq_surf = dout->precip_liq_surf; p.ice_surf = dout->precip_ice_surf;
+  p.liq_flux = dout->precip_liq_flux; p.ice_flux = dout->precip_ice_flux; p.depos = dout->qv2qi_depos_tend;
+  if (!p.eff_qc || !p.eff_qi || !p.eff_qr || !p.liq_surf || !p.ice_surf || !p.liq_flux || !p.ice_flux || !p.depos)
+    return P3X_EINVAL;
+  p.vap_liq = hist->vap_liq_exchange;
+  p.qme = e->qme; p.rho = e->rho; p.icimrst = e->icimrst; p.icwmrst = e->icwmrst; p.icinc = e->icinc;
+  p.icwnc = e->icwnc; p.rel = e->rel; p.rei = e->rei; p.dei = e->dei; p.mu = e->mu; p.lambdac = e->lambdac;
+  p.nfice = e->nfice; p.efcout = e->efcout; p.ncout = e->ncout; p.freql = e->freql; p.efiout = e->efiout;
+  p.niout = e->niout; p.freqi = e->freqi; p.aqrain = e->aqrain; p.anrain = e->anrain; p.freqr = e->freqr;
+  p.reff_rain = e->reff_rain; p.deff_rain = e->deff_rain; p.flxprc = e->flxprc; p.flxsnw = e->flxsnw;
+  p.prec_pcw = e->prec_pcw; p.snow_pcw = e->snow_pcw; p.prec_str = e->prec_str; p.snow_str = e->snow_str;
+  p.cdnumc = e->cdnumc;
+  return P3X_OK;
+}
+
+static int eam_layout(const p3x_layout* layout, int32_t nk, int64_t& ld, int64_t& ld_int) {
+  ld = (layout && layout->ld > 0) ? layout->ld : nk;
+  ld_int = (layout && layout->ld_int > 0) ? layout->ld_int : int64_t(nk) + 1;
+  return (ld < nk || ld_int < int64_t(nk) + 1) ? P3X_EINVAL : P3X_OK;
+}
+
+int p3x_eam_tend_pre(const p3x_eam_fields* e, const p3x_prognostic_state* prog, const p3x_diagnostic_inputs* din,
+                     int32_t nj, int32_t nk, const p3x_layout* layout, void* stream) {
+  if (nj < 0 || nk <= 0) return P3X_EINVAL;
+  p3x::EamPtrs p;
+  int st = eam_ptrs(e, prog, din, nullptr, nullptr, false, p);
+  if (st) return st;
+  int64_t ld, ld_int;
+  if ((st = eam_layout(layout, nk, ld, ld_int))) return st;
+  return cuda_status(p3x::launch_eam(p, nj, nk, ld, ld_int, false, 0.0, static_cast<cudaStream_t>(stream)));
+}
+
+int p3x_eam_tend_post(const p3x_eam_fields* e, const p3x_prognostic_state* prog, const p3x_diagnostic_inputs* din,
+                      const p3x_diagnostic_outputs* dout, const p3x_history_only* hist, int32_t nj, int32_t nk,
+                      const p3x_layout* layout, double dt, void* stream) {
+  if (nj < 0 || nk <= 0 || !(dt > 0)) return P3X_EINVAL;
+  p3x::EamPtrs p;
+  int st = eam_ptrs(e, prog, din, dout, hist, true, p);
+  if (st) return st;
+  int64_t ld, ld_int;
+  if ((st = eam_layout(layout, nk, ld, ld_int))) return st;
+  return cuda_status(p3x::launch_eam(p, nj, nk, ld, ld_int, true, dt, static_cast<cudaStream_t>(stream)));
+}
+
+int p3x_eam_micro_p3_tend(p3x_context* ctx, const p3x_runtime* rt, const p3x_eam_fields* e,
+                          const p3x_prognostic_state* prog, const p3x_diagnostic_inputs* din,
+                          const p3x_diagnostic_outputs* dout, const p3x_infrastructure* infra,
+                          const p3x_history_only* hist, int32_t nj, int32_t nk, const p3x_layout* layout,
+                          int32_t precision, void* stream) {
+  if (!ctx || !infra) return P3X_EINVAL;
+  /* both kernels' pointers are checked before anything is launched */
+  p3x::EamPtrs p;
+  int st = eam_ptrs(e, prog, din, dout, hist, false, p);
+  if (!st) st = eam_ptrs(e, prog, din, dout, hist, true, p);
+  if (st) return st;
+  if ((st = p3x_eam_tend_pre(e, prog, din, nj, nk, layout, stream))) return st;
+  if ((st = p3x_main_async(ctx, rt, prog, din, dout, infra, hist, nj, nk, layout, precision, stream))) return st;
+  return p3x_eam_tend_post(e, prog, din, dout, hist, nj, nk, layout, infra->dt, stream);
+}
+
 /* ------------------------------------------------------------------ */
 /* workload / budgets                                                  */
 /* ------------------------------------------------------------------ */

@@ -255,6 +255,193 @@ __global__ void interface_postamble_kernel(InterfacePtrs p, int ncol, int nlev, 
   }
 }
 
+/* EAM's P3 driver micro_p3_tend (eam/src/physics/p3/scream/
+ * micro_p3_interface.F90:661-1431) around the step, one warp per column.
+ * EAM's own constants (share/util/shr_const_mod.F90 through physconst):
+ * R_dry from the gas constant and the molecular weight of dry air, cp_dry
+ * and g; the driver's literal 287.15 in the in-cloud number concentrations
+ * is kept as written. */
+namespace eam {
+constexpr double kRgas = 6.02214e26 * 1.38065e-23;
+constexpr double kRair = kRgas / 28.966, kCpair = 1.00464e3, kGravit = 9.80616;
+constexpr double kMincld = 0.0001, kQsmall = 1.0e-14;
+constexpr double kMucon = 5.3, kDcon = 25.e-6, kDeicon = 50.0;
+__device__ __forceinline__ double fmax_(double a, double b) { return a > b ? a : b; } /* Fortran max for these ranges */
+__device__ __forceinline__ double fmin_(double a, double b) { return a < b ? a : b; }
+}  // namespace eam
+
+/* Preparation of the P3 inputs (micro_p3_interface.F90:982-1047) and the
+ * cloud fractions of get_cloud_fraction (:661-732).  The rain fraction's
+ * recurrence down the column, r_k = c_k ? max(r_{k-1}, m_k) : m_k (m the
+ * floored cloud fraction; c_k: rain or ice above (max overlap) or no cloud
+ * here (in cloud)), is a segmented maximum: a warp scan over each 32-level
+ * chunk with the chunk above carried in.  Same values as the sequential
+ * loop (max is exact). */
+__global__ void eam_pre_kernel(EamPtrs p, int ncol, int nlev, int64_t ld, int64_t ld_int) {
+  const int col = int((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (col >= ncol) return;
+  const double kappa = eam::kRair * (1.0 / eam::kCpair);
+  double carry = 0.0;
+  for (int base = 0; base < nlev; base += 32) {
+    const int k = base + lane;
+    const bool act = k < nlev;
+    double m = 1.0;
+    bool reset = true;
+    if (act) {
+      const int64_t o = int64_t(col) * ld + k;
+      const double ratio = p.pdel[o] / p.pdeldry[o];
+#pragma unroll
+      for (int s = 0; s < 9; ++s) p.w[s][o] = p.q[s][o] * ratio;
+      p.qv_prev_dry[o] = p.qv_prev[o] * ratio;
+      const double inv_exner = 1.0 / pow(p.pmid[o] * 1.e-5, kappa);
+      p.inv_exner[o] = inv_exner;
+      const int64_t oi = int64_t(col) * ld_int + k;
+      p.dz[o] = p.zi[oi] - p.zi[oi + 1];
+      p.th[o] = p.t[o] * inv_exner;
+      p.pres[o] = p.pmiddry[o];
+      p.dpres[o] = p.pdeldry[o];
+      p.nc_nuceat[o] = p.npccn[o];
+      p.ni_act[o] = p.ni_act_in[o];
+      p.inv_relvar[o] = p.relvar[o];
+      p.t_prev_p3[o] = p.t_prev[o];
+      if (p.subgrid) {
+        m = eam::fmax_(p.ast[o], eam::kMincld);
+        if (k > 0) {
+          if (p.method == P3X_PRECIP_FRAC_MAX_OVERLAP) {
+            /* rain or ice mass in the level above (dry mixing ratios) */
+            const double qr_up = p.q[3][o - 1] * (p.pdel[o - 1] / p.pdeldry[o - 1]);
+            const double qi_up = p.q[5][o - 1] * (p.pdel[o - 1] / p.pdeldry[o - 1]);
+            reset = !(qr_up >= eam::kQsmall || qi_up >= eam::kQsmall);
+          } else {
+            reset = !(p.w[1][o] < eam::kQsmall && p.w[5][o] < eam::kQsmall);
+          }
+        }
+        p.cld_l[o] = m;
+        p.cld_i[o] = m;
+      } else {
+        p.cld_l[o] = 1.0;
+        p.cld_i[o] = 1.0;
+        p.cld_r[o] = 1.0;
+      }
+    }
+    if (!p.subgrid) continue;
+    /* inclusive segmented maximum over the chunk: (value, segment closed) */
+    double v = m;
+    bool closed = reset;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const double vu = __shfl_up_sync(0xffffffffu, v, d);
+      const bool cu = __shfl_up_sync(0xffffffffu, closed, d);
+      if (lane >= d && !closed) {
+        v = eam::fmax_(vu, v);
+        closed = cu;
+      }
+    }
+    if (!closed) v = eam::fmax_(carry, v);
+    if (act) p.cld_r[int64_t(col) * ld + k] = v;
+    carry = __shfl_sync(0xffffffffu, v, 31);
+  }
+}
+
+/* Use of the P3 results (micro_p3_interface.F90:1182-1431). */
+__global__ void eam_post_kernel(EamPtrs p, int ncol, int nlev, int64_t ld, int64_t ld_int, double dt) {
+  const int col = int((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (col >= ncol) return;
+  double cdnumc = 0.0;
+  for (int k = lane; k < nlev; k += 32) {
+    const int64_t o = int64_t(col) * ld + k;
+    const double ratio = p.pdeldry[o] / p.pdel[o];
+    double w[9];
+#pragma unroll
+    for (int s = 0; s < 9; ++s) w[s] = p.w[s][o] * ratio;
+    const double t = p.t[o];
+    double dtemp = p.th[o] / p.inv_exner[o] - t;
+    dtemp = __dmul_rn(dtemp, ratio); /* rounded before the sum, as the driver writes it (no fused multiply-add) */
+    const double temp = dtemp + t;
+    p.ptend_s[o] = eam::kCpair * (temp - t) / dt;
+#pragma unroll
+    for (int s = 0; s < 9; ++s) p.ptend_q[s][o] = (eam::fmax_(0.0, w[s]) - p.q[s][o]) / dt;
+    p.t_prev[o] = temp;
+    p.qv_prev[o] = w[0];
+    const double cme = p.cmeliq[o];
+    if (p.qme) p.qme[o] = cme + p.depos[o];
+    p.vap_liq[o] = p.vap_liq[o] + cme;
+    const double pmid = p.pmid[o];
+    if (p.rho) p.rho[o] = pmid / (eam::kRair * temp);
+    const double cl = p.cld_l[o], ci = p.cld_i[o], cr = p.cld_r[o];
+    const double icimr = eam::fmin_(p.q[5][o] / eam::fmax_(eam::kMincld, ci), 0.005);
+    const double icwmr = eam::fmin_(p.q[1][o] / eam::fmax_(eam::kMincld, cl), 0.005);
+    const double icin = p.q[6][o] / eam::fmax_(eam::kMincld, ci) * pmid / (287.15 * t);
+    const double icwn = p.q[2][o] / eam::fmax_(eam::kMincld, cl) * pmid / (287.15 * t);
+    if (p.icimrst) p.icimrst[o] = icimr;
+    if (p.icwmrst) p.icwmrst[o] = icwmr;
+    if (p.icinc) p.icinc[o] = icin;
+    if (p.icwnc) p.icwnc[o] = icwn;
+    const double rel = p.eff_qc[o] * 1e6, rei = p.eff_qi[o] * 1e6;
+    double dei = rei * 2.0, mu = 0.0, lambdac = 0.0;
+    if (p.ast[o] < 1.e-4) {
+      mu = eam::kMucon;
+      lambdac = (eam::kMucon + 1.0) / eam::kDcon;
+      dei = eam::kDeicon;
+    }
+    if (p.rel) p.rel[o] = rel;
+    if (p.rei) p.rei[o] = rei;
+    if (p.dei) p.dei[o] = dei;
+    if (p.mu) p.mu[o] = mu;
+    if (p.lambdac) p.lambdac[o] = lambdac;
+    /* w: 1 cldliq, 2 numliq, 3 rain, 4 numrain, 5 cldice */
+    const double tot = w[3] + w[5] + w[1];
+    if (p.nfice) p.nfice[o] = (w[5] > eam::kQsmall && tot > eam::kQsmall) ? eam::fmin_(w[5] / tot, 1.0) : 0.0;
+    cdnumc = cdnumc + w[2] * p.pdel[o] / eam::kGravit;
+    const bool liq = cl > 0.01 && icwmr > 5.e-5, ice = ci > 0.01 && icimr > 1.e-6;
+    if (p.efcout) p.efcout[o] = liq ? rel * cl : 0.0;
+    if (p.ncout) p.ncout[o] = liq ? icwn * cl : 0.0;
+    if (p.freql) p.freql[o] = liq ? cl : 0.0;
+    if (p.efiout) p.efiout[o] = ice ? rei * ci : 0.0;
+    if (p.niout) p.niout[o] = ice ? icin * ci : 0.0;
+    if (p.freqi) p.freqi[o] = ice ? ci : 0.0;
+    const double reff = p.eff_qr[o];
+    if (p.deff_rain) p.deff_rain[o] = reff * 2.0 * 1.e6;
+    const bool rain = w[3] >= 1.e-7;
+    if (p.aqrain) p.aqrain[o] = rain ? w[3] * cr : 0.0;
+    if (p.anrain) p.anrain[o] = rain ? w[4] * cr : 0.0;
+    if (p.freqr) p.freqr[o] = rain ? cr : 0.0;
+    if (p.reff_rain) p.reff_rain[o] = rain ? reff * 1.e6 : reff;
+  }
+  for (int k = lane; k <= nlev; k += 32) {
+    const int64_t oi = int64_t(col) * ld_int + k;
+    const double lf = p.liq_flux[oi], fi = p.ice_flux[oi];
+    if (p.flxprc) p.flxprc[oi] = lf + fi;
+    if (p.flxsnw) p.flxsnw[oi] = fi;
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) cdnumc += __shfl_xor_sync(0xffffffffu, cdnumc, d);
+  if (lane == 0) {
+    const double liq = p.liq_surf[col], ice = p.ice_surf[col];
+    const double pcw = liq + ice;
+    if (p.prec_pcw) p.prec_pcw[col] = pcw;
+    if (p.prec_str) p.prec_str[col] = pcw + 0.0;
+    if (p.snow_pcw) p.snow_pcw[col] = ice;
+    if (p.snow_str) p.snow_str[col] = ice + 0.0;
+    if (p.cdnumc) p.cdnumc[col] = cdnumc;
+  }
+}
+
+cudaError_t launch_eam(const EamPtrs& p, int ncol, int nlev, int64_t ld, int64_t ld_int, bool post, double dt,
+                       cudaStream_t st) {
+  if (ncol <= 0 || nlev <= 0) return cudaSuccess;
+  const int threads = 256;
+  const long long blocks = (int64_t(ncol) * 32 + threads - 1) / threads;
+  if (post) {
+    eam_post_kernel<<<unsigned(blocks), threads, 0, st>>>(p, ncol, nlev, ld, ld_int, dt);
+  } else {
+    eam_pre_kernel<<<unsigned(blocks), threads, 0, st>>>(p, ncol, nlev, ld, ld_int);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_interface(const InterfacePtrs& p, int ncol, int nlev, int64_t ld, bool post, double dt,
                              cudaStream_t st) {
   if (ncol <= 0 || nlev <= 0) return cudaSuccess;

@@ -132,6 +132,27 @@ struct InterfacePtrs {
 cudaError_t launch_interface(const InterfacePtrs& p, int ncol, int nlev, int64_t ld, bool post, double dt,
                              cudaStream_t st);
 
+/* Device pointers of the EAM driver's pre/post kernels (micro_p3_tend).
+ * Constituent order of q, ptend_q and w: qv, cldliq, numliq, rain, numrain,
+ * cldice, numice, cldrim, rimvol. */
+struct EamPtrs {
+  const double *pmid, *pmiddry, *pdel, *pdeldry, *zi, *t, *q[9], *ast, *npccn, *ni_act_in, *relvar, *cmeliq;
+  double *t_prev, *qv_prev, *ptend_s, *ptend_q[9];
+  double *qme, *rho, *icimrst, *icwmrst, *icinc, *icwnc, *rel, *rei, *dei, *mu, *lambdac, *nfice, *efcout, *ncout,
+      *freql, *efiout, *niout, *freqi, *aqrain, *anrain, *freqr, *reff_rain, *deff_rain, *flxprc, *flxsnw;
+  double *prec_pcw, *snow_pcw, *prec_str, *snow_str, *cdnumc;
+  int subgrid, method;
+  /* the P3 working arrays: prognostic state in constituent order, inputs */
+  double* w[9];
+  double *th, *pres, *dz, *dpres, *inv_exner, *cld_l, *cld_i, *cld_r, *nc_nuceat, *ni_act, *inv_relvar, *qv_prev_dry,
+      *t_prev_p3;
+  /* P3 outputs read by the post kernel */
+  const double *eff_qc, *eff_qi, *eff_qr, *liq_surf, *ice_surf, *liq_flux, *ice_flux, *depos;
+  double* vap_liq;
+};
+cudaError_t launch_eam(const EamPtrs& p, int ncol, int nlev, int64_t ld, int64_t ld_int, bool post, double dt,
+                       cudaStream_t st);
+
 cudaError_t launch_selftest(unsigned long long* mismatches_d, cudaStream_t st);
 
 /* Fields of the column mass / energy conservation check (device pointers;

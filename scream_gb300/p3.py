@@ -252,6 +252,55 @@ class P3Context:
                                                         C.byref(L.Layout(f.nlev, f.nlev + 1)), float(dt),
                                                         _stream_handle(stream)))
 
+    def _eam(self, eam: Dict[str, "torch.Tensor"], subgrid: bool, method: int):
+        def p(n):
+            t = eam.get(n)
+            return _ptr(t) if t is not None else None
+        e = L.EamFields()
+        for n in L.EAM_STATE + L.EAM_PBUF_IN + ["t_prev", "qv_prev", "ptend_s"] + L.EAM_DIAG:
+            setattr(e, n, p(n))
+        for i, s in enumerate(L.EAM_SPECIES):
+            e.q[i] = p(s)
+            e.ptend_q[i] = p("ptend_" + s)
+        e.subgrid_clouds = 1 if subgrid else 0
+        e.precip_frac_method = int(method)
+        return e
+
+    def eam_tend_pre(self, eam: Dict[str, "torch.Tensor"], f: P3Fields, subgrid: bool = True,
+                     method: int = L.PRECIP_FRAC_MAX_OVERLAP, stream=None):
+        """EAM driver preparation (micro_p3_tend): P3 inputs in ``f`` from the
+        EAM state in ``eam`` (device tensors named as in p3x_eam_fields; the
+        nine constituents by their driver names, interfaces (ncol, nlev+1))."""
+        e = self._eam(eam, subgrid, method)
+        L.check("p3x_eam_tend_pre", self.lib.p3x_eam_tend_pre(C.byref(e), C.byref(f.prog()), C.byref(f.din()),
+                                                              f.ncol, f.nlev, C.byref(L.Layout(f.nlev, f.nlev + 1)),
+                                                              _stream_handle(stream)))
+
+    def eam_tend_post(self, eam: Dict[str, "torch.Tensor"], f: P3Fields, dt: float, stream=None):
+        """EAM driver use of the P3 results in ``f``: tendencies, t_prev and
+        qv_prev, diagnostics into ``eam`` (optional ones when present)."""
+        e = self._eam(eam, True, L.PRECIP_FRAC_MAX_OVERLAP)
+        L.check("p3x_eam_tend_post", self.lib.p3x_eam_tend_post(C.byref(e), C.byref(f.prog()), C.byref(f.din()),
+                                                                C.byref(f.dout()), C.byref(f.hist()), f.ncol,
+                                                                f.nlev, C.byref(L.Layout(f.nlev, f.nlev + 1)),
+                                                                float(dt), _stream_handle(stream)))
+
+    def eam_micro_p3_tend(self, eam: Dict[str, "torch.Tensor"], f: P3Fields, dt: float, it: int = 1,
+                          precision: int = L.P3X_FP64, predictNc: bool = True, prescribedCCN: bool = False,
+                          subgrid: bool = True, method: int = L.PRECIP_FRAC_MAX_OVERLAP, runtime=None,
+                          stream=None):
+        """micro_p3_tend on the device: preparation, the P3 step and the use of
+        its results, asynchronously on ``stream`` (``f``: the working arrays)."""
+        e = self._eam(eam, subgrid, method)
+        rt = runtime if runtime is not None else L.default_runtime()
+        infra = L.Infrastructure(float(dt), int(it), 1, f.ncol, 1, f.nlev, int(predictNc), int(prescribedCCN), None)
+        L.check("p3x_eam_micro_p3_tend",
+                self.lib.p3x_eam_micro_p3_tend(self.h, C.byref(rt), C.byref(e), C.byref(f.prog()),
+                                               C.byref(f.din()), C.byref(f.dout()), C.byref(infra),
+                                               C.byref(f.hist()), f.ncol, f.nlev,
+                                               C.byref(L.Layout(f.nlev, f.nlev + 1)), int(precision),
+                                               _stream_handle(stream)))
+
     def _cons(self, fields: Dict[str, "torch.Tensor"]):
         return L.ConservationFields(*[(_ptr(fields[n]) if fields.get(n) is not None else None)
                                       for n in L.CONS_FIELDS])

@@ -58,6 +58,10 @@ def test_struct_layouts_match_header(built):
     assert C.sizeof(L.DiagnosticOutputs) == 11 * 8
     assert C.sizeof(L.HistoryOnly) == 3 * 8
     assert C.sizeof(L.Infrastructure) == 8 + 7 * 4 + 4 + 8
+    # p3x_eam_fields: 62 pointers (state 6, q 9, pbuf 5, t_prev/qv_prev, ptend 10, diagnostics 30), 2 int32
+    assert C.sizeof(L.EamFields) == 62 * 8 + 8
+    assert L.EamFields.ptend_q.offset == 23 * 8
+    assert L.EamFields.subgrid_clouds.offset == 62 * 8
 
 
 def test_invalid_arguments_rejected_without_gpu(built):
@@ -76,6 +80,13 @@ def test_invalid_arguments_rejected_without_gpu(built):
     assert lib.p3x_batch_run(None, None) == L.P3X_EINVAL
     assert lib.p3x_batch_destroy(None) == L.P3X_EINVAL
     assert lib.p3x_server_destroy(None) == L.P3X_EINVAL
+    # EAM driver: missing fields and a bad precipitation-fraction method
+    e = L.EamFields()
+    assert lib.p3x_eam_tend_pre(C.byref(e), C.byref(prog), C.byref(din), 1, 1, C.byref(lay), None) == L.P3X_EINVAL
+    assert lib.p3x_eam_tend_post(C.byref(e), C.byref(prog), C.byref(din), C.byref(dout), C.byref(hist), 1, 1,
+                                 C.byref(lay), 300.0, None) == L.P3X_EINVAL
+    assert lib.p3x_eam_micro_p3_tend(None, C.byref(rt), C.byref(e), C.byref(prog), C.byref(din), C.byref(dout),
+                                     C.byref(infra), C.byref(hist), 1, 1, C.byref(lay), 0, None) == L.P3X_EINVAL
     # workload generator argument checks (host only)
     arr = (C.c_void_p * 23)()
     assert lib.p3x_workload_generate(0, 1, 0, 4, 10, arr, 10) == L.P3X_EINVAL  # null fields
