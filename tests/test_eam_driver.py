@@ -200,3 +200,35 @@ def test_device_driver_end_to_end(gpu_ctx, tables):
         assert r <= 1e-9, (n, r)
     r = rel_l2(got["prec_pcw"] - got["snow_pcw"], want["prec_pcw"] - want["snow_pcw"])
     assert r <= 1e-9, ("liquid surface precipitation", r)
+
+
+@pytest.mark.gpu
+def test_device_driver_fp32_bulk(gpu_ctx, tables):
+    """The driver around the FP32-bulk step: the temperature, vapour and
+    liquid tendencies and the liquid surface precipitation stay within the
+    FP32-bulk form's one-step tolerance of the FP64 oracle chain (1e-4), and
+    the driver's own kernels add nothing to that (its FP64 step agrees to 1e-9
+    in the test above)."""
+    import torch
+    import scream_gb300 as p3
+    from scream_gb300 import _lib as L
+    from oracle import eam_driver as E
+    from oracle import p3_oracle as O
+    inp, e = eam_case(1006)
+    f = p3.P3Fields.from_inputs(inp)
+    eam = _device_state(e, torch)
+    _alloc_outputs(eam, NCOL, NLEV, torch)
+    gpu_ctx.eam_micro_p3_tend(eam, f, DT, precision=L.P3X_FP32_BULK, prescribedCCN=False)
+    torch.cuda.synchronize()
+    pre = E.eam_pre(e)
+    st = oracle_state(inp)
+    for n, v in pre.items():
+        st[n] = v
+    assert O.p3_main(st, tables, DT, prescribedCCN=False)[0] == 0
+    want = E.eam_post(e, st, DT)
+    got = {k: v.cpu().numpy() for k, v in eam.items()}
+    for n in ("ptend_s", "ptend_qv", "ptend_cldliq", "ptend_rain", "t_prev", "qv_prev"):
+        r = rel_l2(got[n], want[n])
+        assert r <= 1e-4, (n, r)
+    r = rel_l2(got["prec_pcw"] - got["snow_pcw"], want["prec_pcw"] - want["snow_pcw"])
+    assert r <= 1e-4, ("liquid surface precipitation", r)
