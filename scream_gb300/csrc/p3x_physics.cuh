@@ -132,9 +132,10 @@ __device__ __forceinline__ float m_fabs(float x) { return fabsf(x); }
 /* Exact float -> double conversion on the integer pipes: a normal float's
  * exponent is re-biased (+896) and its 23-bit significand shifted into the
  * double's 52-bit field; signed zeros map to signed zeros.  Subnormals,
- * infinities and NaNs take the hardware conversion.  On this part the FP64
- * pipe, which also executes conversions, is the bottleneck of every kernel,
- * while the integer pipes are nearly idle. */
+ * infinities and NaNs take the hardware conversion.  For kernels bound by
+ * the FP64 pipe, which also executes the hardware conversion, while their
+ * integer pipes are nearly idle (the FP32-bulk part3; the selftest checks it
+ * against the hardware for every float). */
 __device__ __forceinline__ double f2d_int(float x) {
   const uint32_t u = __float_as_uint(x);
   const uint32_t e = (u >> 23) & 0xffu;
