@@ -156,12 +156,6 @@ template <int LANES>
 __device__ __forceinline__ bool group_any(unsigned mask, bool p) {
   return __ballot_sync(mask, p) != 0u;
 }
-template <int LANES, class T>
-__device__ __forceinline__ T group_max(unsigned mask, T v) {
-#pragma unroll
-  for (int o = LANES / 2; o > 0; o >>= 1) v = vmax(v, __shfl_xor_sync(mask, v, o, LANES));
-  return v;
-}
 /* Maxima and minima over the group with the warp-reduction instruction
  * (redux.sync), one instruction instead of log2(LANES) dependent shuffles.
  * Non-negative floats and doubles order as their bit patterns (as unsigned
