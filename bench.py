@@ -105,16 +105,41 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def _traffic_per_cl(kernel_tag):
-    """DRAM bytes per column-level of the column kernel from the committed ncu
-    summary (profiles/), or None."""
+def _profile_figure(kernel_tag, key):
+    """A per-column-level figure of the step (``dram_bytes_per_cl``,
+    ``fp64_warp_inst_per_cl``) from the committed ncu summary (profiles/), or
+    None."""
     f = ROOT / "profiles" / "p3_step_traffic_65536x128.txt"
     if not f.exists():
         return None
     for line in f.read_text().splitlines():
-        if line.startswith(kernel_tag + " dram_bytes_per_cl"):
+        if line.startswith(kernel_tag + " " + key):
             return float(line.split()[-1])
     return None
+
+
+def _traffic_per_cl(kernel_tag):
+    """DRAM bytes per column-level of the column kernels, or None."""
+    return _profile_figure(kernel_tag, "dram_bytes_per_cl")
+
+
+# FP64-pipe issue rate of one SM on this part: one warp instruction per 16
+# cycles (ncu: sm__pipe_fp64_cycles_active / sm__inst_executed_pipe_fp64)
+FP64_CYCLES_PER_WARP_INST = 16.0
+
+
+def fp64_ceiling(kernel_tag, cl_step, ms_per_step, sm_mhz, num_sms):
+    """The step's floor set by the FP64 pipe alone: FP64-pipe warp
+    instructions per column-level (committed ncu summary) x 16 cycles over
+    the SMs at the sampled SM clock, and the measured step's fraction of it."""
+    ipc = _profile_figure(kernel_tag, "fp64_warp_inst_per_cl")
+    if ipc is None or not sm_mhz or not ms_per_step:
+        return None
+    floor_ms = ipc * FP64_CYCLES_PER_WARP_INST * cl_step / (num_sms * sm_mhz * 1e6) * 1e3
+    return {"fp64_warp_inst_per_cl": ipc, "floor_ms": floor_ms, "frac": floor_ms / ms_per_step,
+            "sm_mhz": sm_mhz, "sms": num_sms,
+            "note": "floor = FP64-pipe warp instructions x 16 cycles / (SMs x SM clock); frac = floor / "
+                    "measured step (1.0 would be an FP64-pipe-bound step with nothing else in the way)"}
 
 
 class ClockSampler:
@@ -535,7 +560,9 @@ def run_gpu(args):
             "kernel": "P3 step <float>: p3_part12_kernel + p3_sed_bulk_kernel + p3_part3_kernel, one launch "
                       "sequence per step; achieved = 360 B/cl x cl / mean event-timed step",
             "alg_bytes_per_cl": ALG_BYTES_PER_CL,
-            "kernels": shares(parts32, names32)}
+            "kernels": shares(parts32, names32),
+            "fp64_pipe": fp64_ceiling("fp32", cl_step, kmean32 * 1e3, (clocks or {}).get("sm_mhz"),
+                                      torch.cuda.get_device_properties(0).multi_processor_count)}
     kmean64 = sum(k64) / len(k64) * 1e-3
     sample = {}
     cb = cpu_baseline(inputs, steps=10, keep=sample) if not args.no_cpu else None
