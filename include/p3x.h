@@ -340,7 +340,9 @@ int p3x_eam_tend_post(const p3x_eam_fields* e, const p3x_prognostic_state* prog,
 /* micro_p3_tend on the device: p3x_eam_tend_pre, the P3 step (p3x_main_async
  * with infra's dt, it, predictNc and prescribedCCN) and p3x_eam_tend_post on
  * `stream`, asynchronously.  prog, din, dout and hist are the driver's
- * working arrays (its local copies of the state). */
+ * working arrays (its local copies of the state).  The arguments of all three
+ * parts are checked before the first launch: P3X_EINVAL leaves every array
+ * as it was. */
 int p3x_eam_micro_p3_tend(p3x_context* ctx, const p3x_runtime* rt, const p3x_eam_fields* e,
                           const p3x_prognostic_state* prog, const p3x_diagnostic_inputs* din,
                           const p3x_diagnostic_outputs* dout, const p3x_infrastructure* infra,

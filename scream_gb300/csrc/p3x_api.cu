@@ -1235,12 +1235,21 @@ int p3x_eam_micro_p3_tend(p3x_context* ctx, const p3x_runtime* rt, const p3x_eam
                           const p3x_diagnostic_outputs* dout, const p3x_infrastructure* infra,
                           const p3x_history_only* hist, int32_t nj, int32_t nk, const p3x_layout* layout,
                           int32_t precision, void* stream) {
-  if (!ctx || !infra) return P3X_EINVAL;
-  /* both kernels' pointers are checked before anything is launched */
+  if (!ctx || !rt || !infra || !valid_runtime(*rt)) return P3X_EINVAL;
+  /* Everything is checked before anything is launched: the preparation
+   * rewrites the state in place (wet to dry), so a call that failed after it
+   * would return with the state half converted. */
   p3x::EamPtrs p;
   int st = eam_ptrs(e, prog, din, dout, hist, false, p);
   if (!st) st = eam_ptrs(e, prog, din, dout, hist, true, p);
   if (st) return st;
+  {
+    /* the step's arguments: sizes, dt, layout, precision, pointers */
+    dev::Inst in;
+    if ((st = fill_inst(prog, din, dout, hist, layout, nj, nk, infra->dt, infra->predictNc, infra->prescribedCCN,
+                        precision, in)))
+      return st;
+  }
   if ((st = p3x_eam_tend_pre(e, prog, din, nj, nk, layout, stream))) return st;
   if ((st = p3x_main_async(ctx, rt, prog, din, dout, infra, hist, nj, nk, layout, precision, stream))) return st;
   return p3x_eam_tend_post(e, prog, din, dout, hist, nj, nk, layout, infra->dt, stream);

@@ -203,6 +203,31 @@ def test_device_driver_end_to_end(gpu_ctx, tables):
 
 
 @pytest.mark.gpu
+def test_device_driver_rejects_before_touching_the_state(gpu_ctx):
+    """An invalid step argument (precision, dt, leading dimension) fails the
+    whole call before the preparation converts the state in place."""
+    import torch
+    import scream_gb300 as p3
+    from scream_gb300 import _lib as L
+    inp, e = eam_case(1007)
+    f = p3.P3Fields.from_inputs(inp)
+    eam = _device_state(e, torch)
+    _alloc_outputs(eam, NCOL, NLEV, torch)
+    before = {k: v.clone() for k, v in eam.items()}
+    before_p3 = {k: v.clone() for k, v in f.t.items()}
+    for kw in ({"precision": 7}, {"dt": 0.0}):
+        args = {"dt": DT, **kw}
+        with pytest.raises(L.P3Error, match="p3x_eam_micro_p3_tend") as err:
+            gpu_ctx.eam_micro_p3_tend(eam, f, args.pop("dt"), **args)
+        assert err.value.code == L.P3X_EINVAL
+    torch.cuda.synchronize()
+    for k in eam:
+        assert torch.equal(eam[k], before[k]), k
+    for k in f.t:
+        assert torch.equal(f.t[k], before_p3[k]), k
+
+
+@pytest.mark.gpu
 def test_device_driver_fp32_bulk(gpu_ctx, tables):
     """The driver around the FP32-bulk step: the temperature, vapour and
     liquid tendencies and the liquid surface precipitation stay within the
