@@ -651,6 +651,20 @@ int p3x_server_calibrate(p3x_server* s);
  * on = 0: every ready request of a precision is packed together, on any
  * slot, at full capacity.  Waits for running work first. */
 int p3x_server_set_latency_policy(p3x_server* s, int32_t on, double large_grid_share);
+
+/* SM partition (no counterpart in the reference).  small_sms > 0 splits the
+ * device's SMs into two green contexts: at least small_sms SMs (rounded up to
+ * the device's partition granularity, 8 on this architecture) for the last
+ * slot, the rest for the other slots.  The last slot then takes only
+ * instances of at most small_max_cl column-levels and the other slots never
+ * take those, so a small request never waits for SMs that a large step holds;
+ * each dispatch's persistent grids are sized to its partition.  small_sms = 0
+ * removes the partition.  Needs max_inflight >= 2.  P3X_ECUDA where the
+ * driver offers no green contexts (the server is then left unpartitioned).
+ * p3x_server_calibrate measures on the whole device either way.  Waits for
+ * running work first.  sms_out (optional, 2 int32): the SMs of the small
+ * partition and of the rest, 0 when unpartitioned. */
+int p3x_server_set_sm_partition(p3x_server* s, int32_t small_sms, int64_t small_max_cl, int32_t* sms_out);
 int p3x_server_isolated_ms(p3x_server* s, int32_t precision, int32_t nlev, int32_t ncol, double* ms);
 
 /* Checkpoint / resume of a resident instance (no counterpart in the

@@ -40,6 +40,15 @@
  * independent, so an instance's result does not depend on what it was
  * batched with.
  *
+ * SM partition (p3x_server_set_sm_partition): the device's SMs are split
+ * into two green contexts.  The last slot's stream lives in the small one and
+ * takes only small instances; the other slots' streams live in the rest and
+ * never take those.  A large step's persistent blocks then never hold the SMs
+ * a small request needs (blocks of different kernels do not fit into each
+ * other's leftovers: an SM running three FP32-bulk part1+2 blocks has no room
+ * for one FP64 part1+2 block).  The green-context calls are the driver's,
+ * resolved through the runtime at run time.
+ *
  * Checkpoint / resume: p3x_server_export_instance copies an idle instance's
  * 23 input fields (the whole state a later step reads) to the host, and
  * p3x_server_import_instance makes a resident instance from such a copy, so
@@ -57,6 +66,8 @@
 #include <random>
 #include <thread>
 #include <vector>
+
+#include <cuda.h> /* driver types of the green-context calls (resolved at run time) */
 
 #include "p3x.h"
 #include "p3x_internal.hpp"
@@ -103,7 +114,9 @@ struct Instance {
 };
 
 struct Slot {
-  cudaStream_t st = nullptr;
+  cudaStream_t st = nullptr;      /* the stream in use: st_full, or st_part under an SM partition */
+  cudaStream_t st_full = nullptr; /* on the whole device */
+  cudaStream_t st_part = nullptr; /* in the slot's green context */
   cudaEvent_t ev = nullptr;
   bool busy = false;
   std::vector<int64_t> ids;     /* instances stepped by this dispatch */
@@ -156,6 +169,13 @@ struct p3x_server {
   bool calibrated = false;
   bool latency_policy = true;
   double large_share = kLargeGridShare;
+  /* SM partition: green contexts {small, rest}, their SM counts, the largest
+   * instance (column-levels) the small one takes */
+  int num_sms = 0;
+  bool part = false;
+  CUgreenCtx gctx[2] = {nullptr, nullptr};
+  int part_sms[2] = {0, 0};
+  int64_t part_small_cl = 0;
 };
 
 namespace {
@@ -171,6 +191,96 @@ int cuda_rc(cudaError_t e) {
   } while (0)
 
 double now_s(const p3x_server* s) { return std::chrono::duration<double>(Clock::now() - s->t0).count(); }
+
+/* The driver's green-context calls, looked up through the runtime so that the
+ * library does not link the driver library. */
+struct GreenApi {
+  CUresult (*device_get)(CUdevice*, int) = nullptr;
+  CUresult (*get_resource)(CUdevice, CUdevResource*, CUdevResourceType) = nullptr;
+  CUresult (*split)(CUdevResource*, unsigned int*, const CUdevResource*, CUdevResource*, unsigned int,
+                    unsigned int) = nullptr;
+  CUresult (*make_desc)(CUdevResourceDesc*, CUdevResource*, unsigned int) = nullptr;
+  CUresult (*create)(CUgreenCtx*, CUdevResourceDesc, CUdevice, unsigned int) = nullptr;
+  CUresult (*destroy)(CUgreenCtx) = nullptr;
+  CUresult (*stream_create)(CUstream*, CUgreenCtx, unsigned int, int) = nullptr;
+  bool ok = false;
+};
+
+template <class F>
+bool driver_entry(const char* name, F& fn) {
+  void* p = nullptr;
+  cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+  if (cudaGetDriverEntryPointByVersion(name, &p, CUDA_VERSION, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !p)
+    return false;
+  fn = reinterpret_cast<F>(p);
+  return true;
+}
+
+const GreenApi& green_api() {
+  static const GreenApi api = [] {
+    GreenApi g;
+    g.ok = driver_entry("cuDeviceGet", g.device_get) && driver_entry("cuDeviceGetDevResource", g.get_resource) &&
+           driver_entry("cuDevSmResourceSplitByCount", g.split) &&
+           driver_entry("cuDevResourceGenerateDesc", g.make_desc) && driver_entry("cuGreenCtxCreate", g.create) &&
+           driver_entry("cuGreenCtxDestroy", g.destroy) && driver_entry("cuGreenCtxStreamCreate", g.stream_create);
+    return g;
+  }();
+  return api;
+}
+
+/* Removes the SM partition: every slot back on its whole-device stream.
+ * The caller has drained the server. */
+void drop_partition(p3x_server* s) {
+  for (auto& sl : s->slots) {
+    sl.st = sl.st_full;
+    if (sl.st_part) cudaStreamDestroy(sl.st_part);
+    sl.st_part = nullptr;
+  }
+  for (CUgreenCtx& g : s->gctx) {
+    if (g && green_api().ok) green_api().destroy(g);
+    g = nullptr;
+  }
+  s->part = false;
+  s->part_sms[0] = s->part_sms[1] = 0;
+}
+
+/* Splits the device into a green context of at least small_sms SMs for the
+ * last slot and one of the remaining SMs for the others. */
+int make_partition(p3x_server* s, int small_sms) {
+  const GreenApi& g = green_api();
+  if (!g.ok) return P3X_ECUDA;
+  int ord = 0;
+  SRV_CUDA(cudaGetDevice(&ord));
+  CUdevice dev;
+  if (g.device_get(&dev, ord) != CUDA_SUCCESS) return P3X_ECUDA;
+  CUdevResource all{}, small{}, rest{};
+  if (g.get_resource(dev, &all, CU_DEV_RESOURCE_TYPE_SM) != CUDA_SUCCESS) return P3X_ECUDA;
+  unsigned int groups = 1;
+  if (g.split(&small, &groups, &all, &rest, 0, unsigned(small_sms)) != CUDA_SUCCESS || groups != 1 ||
+      small.sm.smCount == 0 || rest.sm.smCount == 0)
+    return P3X_EINVAL;
+  CUdevResourceDesc desc[2];
+  if (g.make_desc(&desc[0], &small, 1) != CUDA_SUCCESS || g.make_desc(&desc[1], &rest, 1) != CUDA_SUCCESS)
+    return P3X_ECUDA;
+  for (int i = 0; i < 2; ++i)
+    if (g.create(&s->gctx[i], desc[i], dev, CU_GREEN_CTX_DEFAULT_STREAM) != CUDA_SUCCESS) return P3X_ECUDA;
+  s->part_sms[0] = int(small.sm.smCount);
+  s->part_sms[1] = int(rest.sm.smCount);
+  int prio_least = 0, prio_greatest = 0;
+  SRV_CUDA(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest));
+  for (auto& sl : s->slots) {
+    const bool last = &sl == &s->slots.back();
+    CUstream cs = nullptr;
+    if (g.stream_create(&cs, s->gctx[last ? 0 : 1], CU_STREAM_NON_BLOCKING, last ? prio_greatest : prio_least) !=
+        CUDA_SUCCESS)
+      return P3X_ECUDA;
+    sl.st_part = static_cast<cudaStream_t>(cs);
+  }
+  for (auto& sl : s->slots) sl.st = sl.st_part;
+  s->part = true;
+  return P3X_OK;
+}
 
 size_t instance_bytes(int ncol, int nlev) {
   const size_t mid = align256(size_t(ncol) * nlev * sizeof(double));
@@ -341,17 +451,31 @@ void admit(p3x_server* s) {
   }
 }
 
+/* Which instances a slot takes: any; small ones only (the latency policy's
+ * reserved slot); under an SM partition, those of at most part_small_cl
+ * column-levels (the small partition's slot) or the others. */
+enum Pick { kPickAny, kPickSmall, kPickPartSmall, kPickPartRest };
+
 /* Packs the ready requests of the oldest ready request's precision and size
  * kind (small: at most kSmallInstanceCl column-levels) into one work list and
- * launches it on slot sl, so a small request never rides a large step; with
- * small_only, only small instances are considered. */
-int dispatch(p3x_server* s, Slot& sl, bool small_only) {
+ * launches it on slot sl, so a small request never rides a large step; pick
+ * limits the instances considered. */
+int dispatch(p3x_server* s, Slot& sl, Pick pick) {
   const bool by_kind = s->latency_policy;
   auto is_small = [by_kind](const Instance& I) {
     return !by_kind || int64_t(I.ncol) * I.nlev <= kSmallInstanceCl;
   };
+  auto picked = [&](const Instance& I) {
+    const bool part_small = int64_t(I.ncol) * I.nlev <= s->part_small_cl;
+    switch (pick) {
+      case kPickSmall: return is_small(I);
+      case kPickPartSmall: return part_small;
+      case kPickPartRest: return !part_small;
+      default: return true;
+    }
+  };
   auto ready_now = [&](const Instance& I) {
-    return I.admitted && !I.busy && !I.arrivals.empty() && (!small_only || is_small(I));
+    return I.admitted && !I.busy && !I.arrivals.empty() && picked(I);
   };
   int prec = -1;
   bool small = true;
@@ -410,8 +534,14 @@ int dispatch(p3x_server* s, Slot& sl, bool small_only) {
    * other slots' launches find no free SM until then (measured at 80 % load:
    * p50 1.4 -> 1.75 ms, p90 30 -> 47 ms for 2.5 % more capacity).  With a
    * static stride CTAs retire one by one and the slots interleave. */
-  rc = p3x::launch_work(s->ctx, s->rt, prec, sl.d_insts, sl.d_work, w, nlev_max, nullptr, sl.st,
-                        (s->latency_policy && cl > kLargeDispatchCl) ? s->large_share : 1.0);
+  /* the persistent grids: sized to the slot's SM partition, or the latency
+   * policy's share of the device for a large dispatch */
+  double frac = 1.0;
+  if (s->part && s->num_sms > 0)
+    frac = double(s->part_sms[pick == kPickPartSmall ? 0 : 1]) / double(s->num_sms);
+  else if (s->latency_policy && cl > kLargeDispatchCl)
+    frac = s->large_share;
+  rc = p3x::launch_work(s->ctx, s->rt, prec, sl.d_insts, sl.d_work, w, nlev_max, nullptr, sl.st, frac);
   if (rc) return rc;
   SRV_CUDA(p3x::launch_postamble(sl.d_insts, sl.d_work, w, sl.st));
   /* each request's result to the host, before the completion event */
@@ -496,9 +626,14 @@ int run_loop(p3x_server* s) {
     admit(s);
     for (auto& sl : s->slots) {
       if (sl.busy) continue;
-      const bool small_only = s->latency_policy && s->slots.size() > 1 && &sl == &s->slots.back();
-      const int rc = dispatch(s, sl, small_only);
-      if (rc == 1) break;
+      const bool last = s->slots.size() > 1 && &sl == &s->slots.back();
+      Pick pick = kPickAny;
+      if (s->part)
+        pick = last ? kPickPartSmall : kPickPartRest;
+      else if (s->latency_policy && last)
+        pick = kPickSmall;
+      const int rc = dispatch(s, sl, pick);
+      if (rc == 1) continue; /* nothing ready for this slot */
       if (rc) return rc;
       ++inflight;
       progressed = true;
@@ -640,6 +775,48 @@ int enqueue(p3x_server* s, int64_t id, int32_t ncol, int32_t nlev, int32_t preci
   return P3X_OK;
 }
 
+/* The calibration sessions (p3x_server_calibrate). */
+int calibrate_runs(p3x_server* s) {
+  int rc;
+  const std::vector<LatRec> keep_lat = s->lat;
+  const int64_t keep_done = s->completed, keep_h2d = s->h2d_bytes, keep_d2h = s->d2h_bytes;
+  const double keep_cl = s->cl_done, keep_first = s->first_arrival, keep_last = s->last_done;
+  int64_t id = -1;
+  for (int prec = 0; prec < 2; ++prec)
+    for (int l = 0; l < 2; ++l)
+      for (int j = 0; j < kCalPoints; ++j) {
+        const int nlev = l == 0 ? 72 : 128;
+        const int64_t bytes = int64_t(instance_bytes(kCalNcol[j], nlev));
+        double best[2] = {1e300, 1e300};
+        if (bytes > s->budget) {
+          for (int w = 0; w < 2; ++w) s->iso_ms[w][prec][l][j] = j > 0 ? s->iso_ms[w][prec][l][j - 1] : 1.0;
+          continue;
+        }
+        /* a fresh two-step session each time, alone on the server: its first
+         * step includes the state upload, as a session's first request does,
+         * and its second (arriving when the first completes) does not; the
+         * best of two sessions */
+        for (int rep = 0; rep < 2; ++rep, --id) {
+          s->lat.clear();
+          rc = enqueue(s, id, kCalNcol[j], nlev, prec, 2, kTemplateSeed + uint64_t(j), 300.0, now_s(s), true);
+          if (rc) return rc;
+          rc = run_loop(s);
+          if (rc) return rc;
+          for (const LatRec& r : s->lat) best[r.first ? 0 : 1] = std::min(best[r.first ? 0 : 1], r.ms);
+        }
+        for (int w = 0; w < 2; ++w) s->iso_ms[w][prec][l][j] = best[w] < 1e300 ? best[w] : 1.0;
+      }
+  s->lat = keep_lat;
+  s->completed = keep_done;
+  s->h2d_bytes = keep_h2d;
+  s->d2h_bytes = keep_d2h;
+  s->cl_done = keep_cl;
+  s->first_arrival = keep_first;
+  s->last_done = keep_last;
+  s->calibrated = true;
+  return P3X_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -672,9 +849,12 @@ int p3x_server_create(p3x_context* ctx, const p3x_runtime* rt, int64_t budget_by
   SRV_CUDA(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest));
   for (auto& sl : s->slots) {
     const bool small_slot = s->slots.size() > 1 && &sl == &s->slots.back();
-    SRV_CUDA(cudaStreamCreateWithPriority(&sl.st, cudaStreamNonBlocking, small_slot ? prio_greatest : prio_least));
+    SRV_CUDA(cudaStreamCreateWithPriority(&sl.st_full, cudaStreamNonBlocking,
+                                          small_slot ? prio_greatest : prio_least));
+    sl.st = sl.st_full;
     SRV_CUDA(cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming));
   }
+  SRV_CUDA(cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, dev));
   s->t0 = Clock::now();
   *out = s.release();
   return P3X_OK;
@@ -686,9 +866,10 @@ int p3x_server_destroy(p3x_server* s) {
   for (auto& kv : s->inst)
     if (kv.second.mem) cudaFreeAsync(kv.second.mem, nullptr);
   cudaDeviceSynchronize();
+  drop_partition(s);
   for (auto& sl : s->slots) {
     if (sl.ev) cudaEventDestroy(sl.ev);
-    if (sl.st) cudaStreamDestroy(sl.st);
+    if (sl.st_full) cudaStreamDestroy(sl.st_full);
     if (sl.h_insts) cudaFreeHost(sl.h_insts);
     if (sl.h_work) cudaFreeHost(sl.h_work);
     if (sl.h_out) cudaFreeHost(sl.h_out);
@@ -752,47 +933,40 @@ int p3x_server_set_latency_policy(p3x_server* s, int32_t on, double large_grid_s
   return P3X_OK;
 }
 
+int p3x_server_set_sm_partition(p3x_server* s, int32_t small_sms, int64_t small_max_cl, int32_t* sms_out) {
+  if (!s || small_sms < 0 || (small_sms > 0 && (small_max_cl <= 0 || s->slots.size() < 2))) return P3X_EINVAL;
+  if (small_sms >= s->num_sms) return P3X_EINVAL;
+  int rc = run_loop(s);
+  if (rc) return rc;
+  SRV_CUDA(cudaDeviceSynchronize());
+  drop_partition(s);
+  if (small_sms > 0) {
+    rc = make_partition(s, small_sms);
+    if (rc) {
+      drop_partition(s);
+      return rc;
+    }
+    s->part_small_cl = small_max_cl;
+  }
+  if (sms_out) {
+    sms_out[0] = s->part_sms[0];
+    sms_out[1] = s->part_sms[1];
+  }
+  return P3X_OK;
+}
+
 int p3x_server_calibrate(p3x_server* s) {
   if (!s) return P3X_EINVAL;
   int rc = run_loop(s);
   if (rc) return rc;
-  const std::vector<LatRec> keep_lat = s->lat;
-  const int64_t keep_done = s->completed, keep_h2d = s->h2d_bytes, keep_d2h = s->d2h_bytes;
-  const double keep_cl = s->cl_done, keep_first = s->first_arrival, keep_last = s->last_done;
-  int64_t id = -1;
-  for (int prec = 0; prec < 2; ++prec)
-    for (int l = 0; l < 2; ++l)
-      for (int j = 0; j < kCalPoints; ++j) {
-        const int nlev = l == 0 ? 72 : 128;
-        const int64_t bytes = int64_t(instance_bytes(kCalNcol[j], nlev));
-        double best[2] = {1e300, 1e300};
-        if (bytes > s->budget) {
-          for (int w = 0; w < 2; ++w) s->iso_ms[w][prec][l][j] = j > 0 ? s->iso_ms[w][prec][l][j - 1] : 1.0;
-          continue;
-        }
-        /* a fresh two-step session each time, alone on the server: its first
-         * step includes the state upload, as a session's first request does,
-         * and its second (arriving when the first completes) does not; the
-         * best of two sessions */
-        for (int rep = 0; rep < 2; ++rep, --id) {
-          s->lat.clear();
-          rc = enqueue(s, id, kCalNcol[j], nlev, prec, 2, kTemplateSeed + uint64_t(j), 300.0, now_s(s), true);
-          if (rc) return rc;
-          rc = run_loop(s);
-          if (rc) return rc;
-          for (const LatRec& r : s->lat) best[r.first ? 0 : 1] = std::min(best[r.first ? 0 : 1], r.ms);
-        }
-        for (int w = 0; w < 2; ++w) s->iso_ms[w][prec][l][j] = best[w] < 1e300 ? best[w] : 1.0;
-      }
-  s->lat = keep_lat;
-  s->completed = keep_done;
-  s->h2d_bytes = keep_h2d;
-  s->d2h_bytes = keep_d2h;
-  s->cl_done = keep_cl;
-  s->first_arrival = keep_first;
-  s->last_done = keep_last;
-  s->calibrated = true;
-  return P3X_OK;
+  /* isolated times are those of the whole device, also under an SM partition */
+  const bool part = s->part;
+  for (auto& sl : s->slots) sl.st = sl.st_full;
+  s->part = false;
+  rc = calibrate_runs(s);
+  for (auto& sl : s->slots) sl.st = part ? sl.st_part : sl.st_full;
+  s->part = part;
+  return rc;
 }
 
 int p3x_server_isolated_ms(p3x_server* s, int32_t precision, int32_t nlev, int32_t ncol, double* ms) {

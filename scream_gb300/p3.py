@@ -455,6 +455,16 @@ class P3Server:
         L.check("p3x_server_set_latency_policy", self.ctx.lib.p3x_server_set_latency_policy(
             self.h, int(bool(on)), float(large_grid_share)))
 
+    def set_sm_partition(self, small_sms: int, small_max_cl: int = 1 << 15):
+        """SM partition (p3x_server_set_sm_partition): the last slot on its own
+        green context of at least ``small_sms`` SMs, taking only instances of
+        at most ``small_max_cl`` column-levels; 0 removes it.  Returns the SM
+        counts (small, rest)."""
+        sms = (C.c_int32 * 2)()
+        L.check("p3x_server_set_sm_partition", self.ctx.lib.p3x_server_set_sm_partition(
+            self.h, int(small_sms), int(small_max_cl), sms))
+        return int(sms[0]), int(sms[1])
+
     def calibrate(self):
         """Isolated service times (p3x_server_calibrate); later stats report slowdowns."""
         L.check("p3x_server_calibrate", self.ctx.lib.p3x_server_calibrate(self.h))

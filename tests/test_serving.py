@@ -50,17 +50,22 @@ def test_one_step_equals_direct_p3_main(gpu_ctx, server_cls):
         srv.close()
 
 
-@pytest.mark.parametrize("latency_policy", [True, False])
-def test_result_alone_equals_result_in_mix(gpu_ctx, server_cls, latency_policy):
+@pytest.mark.parametrize("policy", ["latency", "throughput", "latency+partition"])
+def test_result_alone_equals_result_in_mix(gpu_ctx, server_cls, policy):
     """Bitwise the same alone and in a mix, under both dispatch policies (the
-    latency policy also shrinks large steps' grids and reserves a slot)."""
+    latency policy also shrinks large steps' grids and reserves a slot) and
+    under an SM partition (probe 7, 21,600 column-levels, runs on the small
+    partition's green context, the others on the rest of the SMs)."""
     import scream_gb300 as p3
     probes = [(7, 300, 72, p3.P3X_FP64, 3, 123), (8, 2000, 128, p3.P3X_FP32_BULK, 4, 456),
               (9, 9000, 128, p3.P3X_FP32_BULK, 2, 789)]
 
     def run(mix):
         srv = server_cls(gpu_ctx, budget_bytes=6 * 10**9, max_inflight=4)
-        srv.set_latency_policy(latency_policy)
+        srv.set_latency_policy(policy != "throughput")
+        if policy.endswith("partition"):
+            small, rest = srv.set_sm_partition(16, 1 << 15)
+            assert small >= 16 and rest > 0
         try:
             rng = np.random.default_rng(3)
             if mix:
@@ -86,6 +91,37 @@ def test_result_alone_equals_result_in_mix(gpu_ctx, server_cls, latency_policy):
     for iid in alone:
         for n in alone[iid]:
             assert np.array_equal(alone[iid][n], mixed[iid][n]), (iid, n)
+
+
+def test_sm_partition_arguments_and_removal(gpu_ctx, server_cls):
+    """set_sm_partition: argument checks, SM counts that add up to the
+    device's, and removal (0) back to an unpartitioned server that still runs
+    requests."""
+    import torch
+    import scream_gb300 as p3
+    from scream_gb300 import _lib as L
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    srv = server_cls(gpu_ctx, budget_bytes=2 * 10**9, max_inflight=2)
+    try:
+        for bad in ((-1, 1 << 15), (8, 0), (sms, 1 << 15)):
+            with pytest.raises(L.P3Error):
+                srv.set_sm_partition(*bad)
+        small, rest = srv.set_sm_partition(8, 1 << 15)
+        assert small >= 8 and small + rest <= sms
+        srv.submit(1, 16, 72, p3.P3X_FP64, total_steps=1, seed=1)
+        srv.submit(2, 1024, 128, p3.P3X_FP32_BULK, total_steps=1, seed=2)
+        assert srv.drain()["completed"] == 2
+        assert srv.set_sm_partition(0) == (0, 0)
+        srv.submit(3, 16, 72, p3.P3X_FP64, total_steps=1, seed=3)
+        assert srv.drain()["completed"] == 3  # counted since the server started
+    finally:
+        srv.close()
+    one = server_cls(gpu_ctx, budget_bytes=10**9, max_inflight=1)
+    try:
+        with pytest.raises(L.P3Error):  # the partition needs a second slot
+            one.set_sm_partition(8, 1 << 15)
+    finally:
+        one.close()
 
 
 def test_budget_admission_and_rejection(gpu_ctx, server_cls):
