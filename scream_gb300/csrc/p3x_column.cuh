@@ -312,9 +312,18 @@ __device__ __forceinline__ void part2_level_bulk(const Inst& in, const int64_t o
   s.qv = in.qv[o]; s.th = in.th[o];
   const double T = sm[A_TATM * S + k];
   const double qvssi = sm[A_QVSSI * S + k];
-  if (dlt(s.qc, C::QSMALL) && dlt(s.qr, C::QSMALL) && dlt(s.qi, C::QSMALL) && dlt(T, C::T_zerodegc) &&
-      dlt_neg(qvssi, -0.05))
+  const bool dry = dlt(s.qc, C::QSMALL) && dlt(s.qr, C::QSMALL) && dlt(s.qi, C::QSMALL);
+  if (dry && dlt(T, C::T_zerodegc) && dlt_neg(qvssi, -0.05)) return;
+  /* A level without hydrometeors where ice cannot nucleate (nucleation
+   * needs T < Tmelt - 15 and qv_supersat_i >= 0.05; the test below leaves a
+   * margin for the float temperature) has no process rate, so the level keeps
+   * its state and every tendency output is the +0 that part1 wrote, except
+   * vap_liq_exchange = -(+0).  With nc diagnosed (neither predicted nor
+   * prescribed) the update resets nc, so that case goes the whole way. */
+  if (dry && (predictNc || prescribedCCN) && !(dlt(T, C::Tmelt - 14.0) && dge(qvssi, 0.04))) {
+    in.vap_liq_exchange[o] = -0.0;
     return;
+  }
 
   const double cld_i = in.cld_frac_i[o], cld_l = in.cld_frac_l[o], cld_r = in.cld_frac_r[o];
   const double inv_exner = in.inv_exner[o];
