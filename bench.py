@@ -439,7 +439,8 @@ def run_serving(ctx, args):
             "p99_over_p50": st["p99_ms"] / st["p50_ms"] if st["p50_ms"] > 0 else None,
             "isolated_ms": iso,
             "policy": "latency (small requests on their own dispatches and reserved slot, large steps at 87.5 % of "
-                      "the resident-block capacity)",
+                      "the resident-block capacity); both policies launch dispatches in chunks of 2^19 "
+                      "column-levels",
             "throughput_policy": throughput_policy,
             "data": "every request carries data: a session's first step uploads its 23 input fields from "
                     "page-locked host memory, every step downloads 10 prognostic fields + 2 surface rates; "

@@ -265,6 +265,7 @@ PROTOTYPES = {
     "p3x_server_calibrate": (C.c_int, [_V]),
     "p3x_server_set_latency_policy": (C.c_int, [_V, _I, C.c_double]),
     "p3x_server_set_sm_partition": (C.c_int, [_V, _I, C.c_int64, C.POINTER(C.c_int32)]),
+    "p3x_server_set_dispatch_chunk": (C.c_int, [_V, C.c_int64]),
     "p3x_server_isolated_ms": (C.c_int, [_V, _I, _I, _I, _dp]),
     "p3x_server_export_instance": (C.c_int, [_V, C.c_int64, _dp, C.c_int64]),
     "p3x_server_import_instance": (C.c_int, [_V, C.c_int64, _I, _I, _I, C.c_double, _dp, C.c_int64]),

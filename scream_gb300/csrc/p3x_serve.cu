@@ -95,6 +95,10 @@ constexpr int kBatchColumnCap = 1 << 18;    /* columns per dispatched work list 
  * policy packs every ready request of a precision together on any slot at
  * full capacity. */
 constexpr double kLargeDispatchCl = double(1 << 20);
+/* Default dispatch chunk (p3x_server_set_dispatch_chunk): measured at 80 %
+ * load, chunks of 2^19 column-levels cut the slowdown p99 from 33-37 to 8-11
+ * (2^20: 17-20, 2^21: 28-33) at unchanged saturated throughput. */
+constexpr int64_t kDispatchChunkCl = int64_t(1) << 19;
 constexpr double kLargeGridShare = 0.875;
 constexpr int64_t kSmallInstanceCl = int64_t(1) << 19;
 
@@ -176,6 +180,9 @@ struct p3x_server {
   CUgreenCtx gctx[2] = {nullptr, nullptr};
   int part_sms[2] = {0, 0};
   int64_t part_small_cl = 0;
+  /* a dispatch larger than this many column-levels runs as consecutive
+   * launches of at most this size (0: one launch) */
+  int64_t chunk_cl = kDispatchChunkCl;
 };
 
 namespace {
@@ -541,8 +548,18 @@ int dispatch(p3x_server* s, Slot& sl, Pick pick) {
     frac = double(s->part_sms[pick == kPickPartSmall ? 0 : 1]) / double(s->num_sms);
   else if (s->latency_policy && cl > kLargeDispatchCl)
     frac = s->large_share;
-  rc = p3x::launch_work(s->ctx, s->rt, prec, sl.d_insts, sl.d_work, w, nlev_max, nullptr, sl.st, frac);
-  if (rc) return rc;
+  /* In chunks: every kernel of a chunk ends before the next chunk's starts,
+   * so other slots' kernels, launched meanwhile, reach the SMs between them
+   * instead of waiting for a whole large step.  Columns are independent, so
+   * the results are those of one launch. */
+  int per = w;
+  if (s->chunk_cl > 0 && cl > double(s->chunk_cl))
+    per = int(std::max<int64_t>(1, s->chunk_cl / std::max(1, nlev_max)));
+  for (int off = 0; off < w; off += per) {
+    rc = p3x::launch_work(s->ctx, s->rt, prec, sl.d_insts, sl.d_work + off, std::min(per, w - off), nlev_max,
+                          nullptr, sl.st, frac);
+    if (rc) return rc;
+  }
   SRV_CUDA(p3x::launch_postamble(sl.d_insts, sl.d_work, w, sl.st));
   /* each request's result to the host, before the completion event */
   double* out = sl.h_out;
@@ -952,6 +969,14 @@ int p3x_server_set_sm_partition(p3x_server* s, int32_t small_sms, int64_t small_
     sms_out[0] = s->part_sms[0];
     sms_out[1] = s->part_sms[1];
   }
+  return P3X_OK;
+}
+
+int p3x_server_set_dispatch_chunk(p3x_server* s, int64_t max_cl) {
+  if (!s || max_cl < 0) return P3X_EINVAL;
+  const int rc = run_loop(s);
+  if (rc) return rc;
+  s->chunk_cl = max_cl;
   return P3X_OK;
 }
 

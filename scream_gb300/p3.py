@@ -465,6 +465,12 @@ class P3Server:
             self.h, int(small_sms), int(small_max_cl), sms))
         return int(sms[0]), int(sms[1])
 
+    def set_dispatch_chunk(self, max_cl: int):
+        """Dispatch chunking (p3x_server_set_dispatch_chunk): dispatches above
+        ``max_cl`` column-levels run as consecutive launches of at most that
+        size (default 2**19); 0 launches each dispatch at once."""
+        L.check("p3x_server_set_dispatch_chunk", self.ctx.lib.p3x_server_set_dispatch_chunk(self.h, int(max_cl)))
+
     def calibrate(self):
         """Isolated service times (p3x_server_calibrate); later stats report slowdowns."""
         L.check("p3x_server_calibrate", self.ctx.lib.p3x_server_calibrate(self.h))

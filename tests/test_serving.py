@@ -50,12 +50,14 @@ def test_one_step_equals_direct_p3_main(gpu_ctx, server_cls):
         srv.close()
 
 
-@pytest.mark.parametrize("policy", ["latency", "throughput", "latency+partition"])
+@pytest.mark.parametrize("policy", ["latency", "throughput", "latency+partition", "latency+chunks"])
 def test_result_alone_equals_result_in_mix(gpu_ctx, server_cls, policy):
     """Bitwise the same alone and in a mix, under both dispatch policies (the
     latency policy also shrinks large steps' grids and reserves a slot) and
     under an SM partition (probe 7, 21,600 column-levels, runs on the small
-    partition's green context, the others on the rest of the SMs)."""
+    partition's green context, the others on the rest of the SMs) and with
+    dispatches launched in chunks of 2^18 column-levels (probe 9 alone is
+    1.15e6)."""
     import scream_gb300 as p3
     probes = [(7, 300, 72, p3.P3X_FP64, 3, 123), (8, 2000, 128, p3.P3X_FP32_BULK, 4, 456),
               (9, 9000, 128, p3.P3X_FP32_BULK, 2, 789)]
@@ -66,6 +68,8 @@ def test_result_alone_equals_result_in_mix(gpu_ctx, server_cls, policy):
         if policy.endswith("partition"):
             small, rest = srv.set_sm_partition(16, 1 << 15)
             assert small >= 16 and rest > 0
+        if policy.endswith("chunks"):
+            srv.set_dispatch_chunk(1 << 18)
         try:
             rng = np.random.default_rng(3)
             if mix:
