@@ -59,3 +59,21 @@ def test_two_gloo_ranks_max_timing_and_weak_value():
     assert s0 != s1                             # each rank steps its own columns
     assert d0 == (2, 0, 0) and d1 == (2, 1, 1)
     assert rc1 == 0 and out1 == ""              # the reference arm prints on rank 0 only
+
+
+def test_fp64_pipe_floor_from_the_committed_profile():
+    """bench.py's roofline.fp64_pipe: the committed ncu summary's FP64-pipe
+    warp instructions per column-level x 16 cycles over the SMs at the sampled
+    clock, and the measured step's fraction of that floor."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    ipc = bench._profile_figure("fp32", "fp64_warp_inst_per_cl")
+    assert ipc is not None and 1.0 < ipc < 200.0
+    assert bench._traffic_per_cl("fp32") > 360.0  # measured traffic exceeds the algorithmic bytes
+    cl = 345600 * 128
+    got = bench.fp64_ceiling("fp32", cl, 25.0, 2070.0, 152)
+    floor = ipc * 16 * cl / (152 * 2070e6) * 1e3
+    assert got["floor_ms"] == pytest.approx(floor, rel=1e-12)
+    assert got["frac"] == pytest.approx(floor / 25.0, rel=1e-12)
+    assert bench.fp64_ceiling("fp32", cl, 25.0, None, 152) is None  # no clock sample, no floor
+    assert bench.fp64_ceiling("fp64", cl, 400.0, 2070.0, 152)["fp64_warp_inst_per_cl"] > ipc
