@@ -439,7 +439,7 @@ def run_serving(ctx, args):
             "p99_over_p50": st["p99_ms"] / st["p50_ms"] if st["p50_ms"] > 0 else None,
             "isolated_ms": iso,
             "policy": "latency (small requests on their own dispatches and reserved slot, large steps at 87.5 % of "
-                      "the resident-block capacity); both policies launch dispatches in chunks of 2^19 "
+                      "the resident-block capacity); both policies launch dispatches in chunks of 2^18 "
                       "column-levels",
             "throughput_policy": throughput_policy,
             "data": "every request carries data: a session's first step uploads its 23 input fields from "

@@ -670,7 +670,7 @@ int p3x_server_set_sm_partition(p3x_server* s, int32_t small_sms, int64_t small_
  * than max_cl column-levels runs as consecutive launches of at most max_cl
  * column-levels each, so other slots' kernels reach the SMs between them
  * instead of waiting for a whole large step's kernels; 0 launches every
- * dispatch at once.  Default 2^19 (4,096 columns of 128 levels).  Results do
+ * dispatch at once.  Default 2^18 (2,048 columns of 128 levels).  Results do
  * not depend on it.  Waits for running work first. */
 int p3x_server_set_dispatch_chunk(p3x_server* s, int64_t max_cl);
 int p3x_server_isolated_ms(p3x_server* s, int32_t precision, int32_t nlev, int32_t ncol, double* ms);

@@ -96,9 +96,9 @@ constexpr int kBatchColumnCap = 1 << 18;    /* columns per dispatched work list 
  * full capacity. */
 constexpr double kLargeDispatchCl = double(1 << 20);
 /* Default dispatch chunk (p3x_server_set_dispatch_chunk): measured at 80 %
- * load, chunks of 2^19 column-levels cut the slowdown p99 from 33-37 to 8-11
- * (2^20: 17-20, 2^21: 28-33) at unchanged saturated throughput. */
-constexpr int64_t kDispatchChunkCl = int64_t(1) << 19;
+ * load, chunks of 2^18 column-levels cut the slowdown p99 from 33-37 to 5
+ * (2^19: 8-14, 2^20: 17-20, 2^21: 28-33) at unchanged saturated throughput. */
+constexpr int64_t kDispatchChunkCl = int64_t(1) << 18;
 constexpr double kLargeGridShare = 0.875;
 constexpr int64_t kSmallInstanceCl = int64_t(1) << 19;
 

@@ -468,7 +468,7 @@ class P3Server:
     def set_dispatch_chunk(self, max_cl: int):
         """Dispatch chunking (p3x_server_set_dispatch_chunk): dispatches above
         ``max_cl`` column-levels run as consecutive launches of at most that
-        size (default 2**19); 0 launches each dispatch at once."""
+        size (default 2**18); 0 launches each dispatch at once."""
         L.check("p3x_server_set_dispatch_chunk", self.ctx.lib.p3x_server_set_dispatch_chunk(self.h, int(max_cl)))
 
     def calibrate(self):
