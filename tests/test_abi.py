@@ -80,6 +80,8 @@ def test_invalid_arguments_rejected_without_gpu(built):
     assert lib.p3x_batch_run(None, None) == L.P3X_EINVAL
     assert lib.p3x_batch_destroy(None) == L.P3X_EINVAL
     assert lib.p3x_server_destroy(None) == L.P3X_EINVAL
+    assert lib.p3x_server_set_sm_partition(None, 8, 1 << 15, None) == L.P3X_EINVAL
+    assert lib.p3x_server_set_dispatch_chunk(None, 1 << 18) == L.P3X_EINVAL
     # EAM driver: missing fields and a bad precipitation-fraction method
     e = L.EamFields()
     assert lib.p3x_eam_tend_pre(C.byref(e), C.byref(prog), C.byref(din), 1, 1, C.byref(lay), None) == L.P3X_EINVAL
