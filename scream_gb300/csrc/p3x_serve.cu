@@ -15,7 +15,10 @@
  *                 is free, every ready request of one precision (up to a
  *                 column cap) is packed into one work list and stepped by
  *                 the batched kernels (part1+2, sedimentation, part3) plus
- *                 the state hand-over; slots overlap on the device;
+ *                 the state hand-over, in launches of at most a chunk of
+ *                 column-levels (p3x_server_set_dispatch_chunk) so that other
+ *                 slots' kernels reach the SMs between them; slots overlap on
+ *                 the device;
  *   completion -> an event per slot, polled; latency = completion - arrival
  *                 on the host clock; a Poisson session's memory returns to
  *                 the pool after its last step; an instance created by
