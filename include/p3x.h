@@ -637,7 +637,9 @@ int p3x_server_drain(p3x_server* s, p3x_serve_stats* stats);
  * counts and both precision forms, best of two; a first step (which uploads
  * the state) and a later step are timed separately.  Later statistics then
  * report the slowdown (latency over the isolated time of the same kind of
- * step, log-log interpolated in ncol).  p3x_server_isolated_ms returns that
+ * step, log-log interpolated in ncol).  Calibration runs each step as one
+ * launch sequence on the whole device, whatever the SM partition and the
+ * dispatch chunk.  p3x_server_isolated_ms returns that
  * interpolated time of a later step.  No counterpart in the reference. */
 int p3x_server_calibrate(p3x_server* s);
 
@@ -661,7 +663,7 @@ int p3x_server_set_latency_policy(p3x_server* s, int32_t on, double large_grid_s
  * each dispatch's persistent grids are sized to its partition.  small_sms = 0
  * removes the partition.  Needs max_inflight >= 2.  P3X_ECUDA where the
  * driver offers no green contexts (the server is then left unpartitioned).
- * p3x_server_calibrate measures on the whole device either way.  Waits for
+ * Waits for
  * running work first.  sms_out (optional, 2 int32): the SMs of the small
  * partition and of the rest, 0 when unpartitioned. */
 int p3x_server_set_sm_partition(p3x_server* s, int32_t small_sms, int64_t small_max_cl, int32_t* sms_out);

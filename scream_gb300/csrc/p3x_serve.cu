@@ -987,13 +987,17 @@ int p3x_server_calibrate(p3x_server* s) {
   if (!s) return P3X_EINVAL;
   int rc = run_loop(s);
   if (rc) return rc;
-  /* isolated times are those of the whole device, also under an SM partition */
+  /* isolated times are those of one launch sequence on the whole device,
+   * whatever the SM partition and dispatch chunks of the measured runs */
   const bool part = s->part;
+  const int64_t chunk = s->chunk_cl;
   for (auto& sl : s->slots) sl.st = sl.st_full;
   s->part = false;
+  s->chunk_cl = 0;
   rc = calibrate_runs(s);
   for (auto& sl : s->slots) sl.st = part ? sl.st_part : sl.st_full;
   s->part = part;
+  s->chunk_cl = chunk;
   return rc;
 }
 
